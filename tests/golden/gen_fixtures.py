@@ -1,0 +1,185 @@
+"""Generates the golden fixtures in tests/golden/ by running the reference
+simulator itself (its own C++ sources, compiled by oracle/ref/Makefile into
+oracle/_ref/ocp_ref_dump) on seeded synthetic decks from decks.py.
+
+Run in a container that holds the reference sources (they are not needed
+afterwards; the fixtures are committed):
+
+    python tests/golden/gen_fixtures.py [--only NAME]
+
+Fixtures (compressed .npz, one key per dumped array, "<group>/<name>"):
+
+* ``bo_10x10x3``   three-phase black-oil FIM, 300 cells, every Newton
+  iteration of the first time steps (model, init, itNNN/{jac_state,pre,post}).
+* ``comp6_8x8x3``  six-component PR-EoS FIM, 192 cells with per-cell random
+  feeds and pressures (a slice of the 60x60x10 case), PTN start.
+* ``comp8_6x6x4``  eight-component PR-EoS FIM, 144 cells.
+* ``flash10``      ten-component flash-only cells: FlashDer from flash type 0
+  without phase history, random and near-saturation feeds.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+import decks  # noqa: E402
+
+REF_DIR = os.path.join(REPO, "oracle", "ref")
+DUMP = os.path.join(REPO, "oracle", "_ref", "ocp_ref_dump")
+
+# arrays kept per dump group (everything the GPU path reads or writes)
+STATE_KEYS = ["P", "T", "Pb", "Ni", "Nt", "vf", "Pj", "Pc", "S", "phaseExist", "xij", "rho", "xi",
+              "mu", "kr", "rhoP", "xiP", "muP", "rhox", "xix", "mux", "vfP", "vfi", "dKrdS",
+              "dPcdS", "dSec_dPri", "poro", "poroP", "rockVp", "lNi",
+              "skip_flag", "skip_minEigen", "skip_P", "skip_T", "skip_zi"]
+RES_KEYS = ["upblock", "dP", "flux_vj", "flux_ni", "res_bulk", "resRelV", "resRelN", "maxRelRes_V",
+            "maxRelRes_N", "maxId_V", "maxId_N"]
+
+
+def build_reference():
+    subprocess.run(["make", "-C", REF_DIR, "-j8"], check=True, stdout=subprocess.DEVNULL)
+
+
+def load_dir(path, keys=None):
+    out = {}
+    for f in sorted(os.listdir(path)):
+        if not f.endswith(".npy"):
+            continue
+        k = f[:-4]
+        if keys is None or k in keys:
+            out[k] = np.load(os.path.join(path, f))
+    return out
+
+
+PRE_KEYS = ["P", "T", "Pb", "Ni", "Nt", "Pj", "S", "phaseExist", "xij", "lNi",
+            "skip_flag", "skip_minEigen", "skip_P", "skip_T", "skip_zi", "u", "dt", "dSmax"]
+
+
+def pack_fim(outdir):
+    """Packs one run.  ``itNNN/jac_state`` holds the state the Jacobian of
+    iteration NNN was assembled from; where that state equals the previous
+    iteration's ``post`` state (all but lNi, which only enters the residual)
+    only the arrays that differ are stored and ``jac_state/from_post`` names
+    the iteration to take the rest from."""
+    data = {}
+    for k, v in load_dir(os.path.join(outdir, "model")).items():
+        data[f"model/{k}"] = v
+    for k, v in load_dir(os.path.join(outdir, "init"), set(STATE_KEYS)).items():
+        data[f"init/{k}"] = v
+    log = np.load(os.path.join(outdir, "log.npy"))
+    data["log"] = log
+    prev_post = None
+    for it in range(len(log)):
+        base = os.path.join(outdir, f"it{it:03d}")
+        js = load_dir(os.path.join(base, "jac_state"),
+                      set(STATE_KEYS + RES_KEYS + ["jac_rowptr", "jac_col", "jac_val", "dt"]))
+        if prev_post is not None and all(
+                k in ("lNi",) or k not in prev_post[1] or np.array_equal(js[k], prev_post[1][k])
+                for k in STATE_KEYS if k in js):
+            js = {k: v for k, v in js.items() if k not in STATE_KEYS or k == "lNi"}
+            js["from_post"] = np.array([prev_post[0]])
+        for k, v in js.items():
+            data[f"it{it:03d}/jac_state/{k}"] = v
+        pre = os.path.join(base, "pre")
+        if os.path.isdir(pre):
+            for k, v in load_dir(pre, set(PRE_KEYS)).items():
+                data[f"it{it:03d}/pre/{k}"] = v
+        post = os.path.join(base, "post")
+        prev_post = None
+        if os.path.isdir(post) and os.path.exists(os.path.join(post, "P.npy")):
+            pd = load_dir(post, set(STATE_KEYS + RES_KEYS + ["flash_ftype", "flash_iters"]))
+            for k, v in pd.items():
+                data[f"it{it:03d}/post/{k}"] = v
+            prev_post = (it, pd)
+    return data
+
+
+def run_fim(deck_text, name, max_iters, ni=None, calibrate=False):
+    with tempfile.TemporaryDirectory() as tmp:
+        deck = os.path.join(tmp, name + ".data")
+        with open(deck, "w") as f:
+            f.write(deck_text)
+        if ni is not None:
+            ni.astype("<f8").tofile(deck + ".ptn_ni")
+            if calibrate:
+                # scale the moles so the initial fluid volume fills the pores
+                out0 = os.path.join(tmp, "out0")
+                subprocess.run([DUMP, "fim", deck, out0, "0"], check=True, stdout=subprocess.DEVNULL)
+                vf = np.load(os.path.join(out0, "init", "vf.npy"))
+                vp = np.load(os.path.join(out0, "init", "rockVp.npy"))
+                ni = ni * (vp / vf)[:, None]
+                ni.astype("<f8").tofile(deck + ".ptn_ni")
+        out = os.path.join(tmp, "out")
+        subprocess.run([DUMP, "fim", deck, out, str(max_iters)], check=True, stdout=subprocess.DEVNULL)
+        data = pack_fim(out)
+        if ni is not None:
+            data["ptn_ni"] = ni
+    return data
+
+
+def flash_cells(ncomp, n, seed, temp_k=345.0):
+    """Random flash inputs: P ~ U(50, 400) bar, z ~ Dirichlet(1.5), unit moles."""
+    rng = np.random.default_rng(seed)
+    p = rng.uniform(50.0, 400.0, n)
+    z = rng.dirichlet(np.full(ncomp, 1.5), n)
+    ni = np.concatenate([z * 10.0, np.full((n, 1), 1.0)], axis=1)
+    t = np.full(n, temp_k - 273.15)
+    return np.concatenate([p[:, None], t[:, None], ni], axis=1)
+
+
+def run_flash(ncomp, ncell, seed):
+    ni, deck_text = decks.comp_deck(1, 1, 1, ncomp, seed=seed, wells=False)
+    cells = flash_cells(ncomp, ncell, seed + 7)
+    with tempfile.TemporaryDirectory() as tmp:
+        deck = os.path.join(tmp, "fluid.data")
+        with open(deck, "w") as f:
+            f.write(deck_text)
+        ni.astype("<f8").tofile(deck + ".ptn_ni")
+        cf = os.path.join(tmp, "cells.f64")
+        cells.astype("<f8").tofile(cf)
+        out = os.path.join(tmp, "out")
+        subprocess.run([DUMP, "flash", deck, cf, str(ncell), out], check=True, stdout=subprocess.DEVNULL)
+        data = {f"model/{k}": v for k, v in load_dir(os.path.join(out, "model")).items()}
+        for k, v in load_dir(os.path.join(out, "flash")).items():
+            data[f"flash/{k}"] = v
+    data["cells"] = cells
+    return data
+
+
+def _comp_fim(nx, ny, nz, ncomp, seed, name, max_iters):
+    ni, text = decks.comp_deck(nx, ny, nz, ncomp, seed=seed, tsteps=(0.02, 0.05, 0.1), smooth=True)
+    return run_fim(text, name, max_iters, ni=ni, calibrate=True)
+
+
+FIXTURES = {
+    "bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12),
+    "comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4),
+    "comp8_6x6x4": lambda: _comp_fim(6, 6, 4, 8, 4, "c8", 4),
+    "flash10": lambda: run_flash(10, 1024, 3),
+}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", default=None)
+    args = ap.parse_args()
+    build_reference()
+    for name, fn in FIXTURES.items():
+        if args.only and name != args.only:
+            continue
+        data = fn()
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **data)
+        print(f"{name}: {len(data)} arrays, {os.path.getsize(path) / 1e6:.2f} MB")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,223 @@
+/*
+ * ocpx.h -- C ABI of the GB300 FIM Newton-step hot path.
+ *
+ * Drop-in boundary for OpenCAEPoroX's fully implicit Newton step.  The
+ * reference performs this work in per-cell / per-connection C++ loops driven
+ * by IsoT_FIM; each entry point below replaces one of those loops over the
+ * whole grid, on one GPU, with no host round trip in between:
+ *
+ *   ocpx_update_properties  IsoT_FIM::UpdateProperty up to the residual
+ *                           (src/IsoThermalMethod.cpp:811-831): NR.CheckPhysical
+ *                           ("BulkNi","BulkP"), CalFlash -> MixtureUnit::FlashFIM
+ *                           per cell (src/IsoThermalMethod.cpp:1016-1071,
+ *                           src/MixtureUnit.cpp:87-92), CalKrPc (:1073-1088),
+ *                           CalRock (:19-30)
+ *   ocpx_calres             IsoT_FIM::CalRes (src/IsoThermalMethod.cpp:1090-1185)
+ *                           with OCPConvection01::CalFlux (src/OCPConvection.cpp:22-79),
+ *                           bulk part (well terms are added by the host)
+ *   ocpx_assemble           IsoT_FIM::AssembleMatBulks (src/IsoThermalMethod.cpp:1187-1269)
+ *                           with OCPConvection01::AssembleMatFIM (src/OCPConvection.cpp:82-187)
+ *                           into LinearSystem::NewDiag/AddDiag/NewOffDiag
+ *                           (include/LinearSystem.hpp:61-68)
+ *   ocpx_newton_update      IsoT_FIM::GetSolution, bulk part
+ *                           (src/IsoThermalMethod.cpp:1282-1418)
+ *   ocpx_update_last_step   IsoT_FIM::UpdateLastTimeStep, bulk part (:1473-1517)
+ *   ocpx_step               one whole Newton iteration (update, properties,
+ *                           residual, Jacobian) captured as a CUDA graph
+ *
+ * Host arrays exchanged through ocpx_set_field / ocpx_get_field use the
+ * reference's BulkVarSet layout (include/BulkVarSet.hpp): cell-major, then
+ * phase, then component, e.g. x_ij at xij[(n*np + j)*nc + i].  The library
+ * keeps its own structure-of-arrays copy in device memory.
+ *
+ * Errors never abort: every call returns an ocpx_status, the message of the
+ * last failure in this thread is available from ocpx_last_error(), and the
+ * per-cell status bits of the last property update are readable as the
+ * OCPX_F_STATUS field.  One context is used by one host thread at a time.
+ */
+#ifndef OCPX_H
+#define OCPX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OCPX_ABI_VERSION 1
+
+typedef enum ocpx_status {
+    OCPX_OK = 0,
+    OCPX_NONCONVERGED = 1,  /* some cell's flash ended unconverged (see OCPX_F_STATUS) */
+    OCPX_SINGULAR = 2,      /* a per-cell dense solve met a zero pivot */
+    OCPX_NONFINITE = 3,     /* NaN/Inf in a flash result */
+    OCPX_WATCHDOG = 4,      /* a device-side iteration cap was reached */
+    OCPX_INVALID_ARG = 5,
+    OCPX_CUDA_ERROR = 6,
+    OCPX_NEGATIVE_P = 7,    /* Bulk::CheckP failed: the reference cuts the time step */
+    OCPX_NEGATIVE_NI = 8,   /* Bulk::CheckNi failed: the reference cuts the time step */
+    OCPX_NO_DEVICE = 9
+} ocpx_status;
+
+/* Per-cell status bits (OCPX_F_STATUS). */
+#define OCPX_CELL_SPLIT_NONCONV (1u << 0)
+#define OCPX_CELL_STAB_NONCONV (1u << 1)
+#define OCPX_CELL_SINGULAR (1u << 2)
+#define OCPX_CELL_NONFINITE (1u << 3)
+#define OCPX_CELL_NEG_P (1u << 4)
+#define OCPX_CELL_NEG_NI (1u << 5)
+#define OCPX_CELL_ITER_CAP (1u << 6)
+
+typedef struct ocpx_ctx ocpx_ctx;
+
+/* A table in the reference's OCPTable storage: column-major, data[c*nrow + r]. */
+typedef struct ocpx_table {
+    int nrow;
+    int ncol;
+    const double* data;
+} ocpx_table;
+
+/* Fluid, rock and saturation model (ParamReservoir after setup). */
+typedef struct ocpx_model_desc {
+    int mixture;  /* 0: black-oil OGW (OCPMixtureMethodK_OGW01), 1: PR-EoS (OCPMixtureMethodComp01) */
+    int nc;       /* components incl. water: 3 for black-oil, NC+1 for compositional */
+    /* unit constants in force (src/OCPUnits.cpp:15-95) */
+    double gravity_factor, conv_darcy, gas_constant, conv1, conv3, conv4;
+    /* OCPRockIsoT_Linear */
+    double rock_pref, rock_cp1, rock_cp2;
+    /* SWOF (Sw, krw, krow, Pcow) and SGOF (Sg, krg, krog, Pcgo); Stone II oil */
+    ocpx_table swof, sgof;
+    /* PVTW (Pref, Bw, Cw, mu_w, Cmu); black-oil PVCO (Pb, Rs, Bo, mu_o, Co, Cmu), PVDG (P, Bg, mu_g) */
+    ocpx_table pvtw, pvco, pvdg;
+    double std_rho_o, std_rho_g, std_rho_w, std_vo, std_vg, std_vw;
+    /* compositional: arrays of NC = nc-1 entries; BIC is the full NC x NC matrix;
+     * Vshift already multiplied by GAS_CONSTANT*OmegaB*Tc/Pc as EoS_PR stores it */
+    const double *Tc, *Pc, *Vc, *MW, *OmegaA, *OmegaB, *acf, *BIC, *Vshift, *Vcvis;
+    const double* lbc_coef;   /* 5 LBC coefficients as ViscosityMethod03 stores them (x10) */
+    const double* flash_ctrl; /* 13 values: SSMsta maxIt, tol, eYt, Ktol, dYtol; NRsta maxIt, tol;
+                                 SSMsp maxIt, tol; NRsp maxIt, tol; RR maxIt, tol */
+    int skip_psa;             /* SkipPSA enabled (reference default 1) */
+} ocpx_model_desc;
+
+/* Cells and connections (Bulk + BulkConn after Reservoir::Setup and CalTrans). */
+typedef struct ocpx_grid_desc {
+    int nb;                  /* cells (single domain: all interior) */
+    int nconn;               /* connections, in the reference's order (eId > bId) */
+    const double* v;         /* bulk volume */
+    const double* depth;
+    const double* poro_init;
+    const uint32_t* conn_b;
+    const uint32_t* conn_e;
+    const double* conn_trans; /* BulkConnPair::trans, CONV_DARCY included */
+} ocpx_grid_desc;
+
+/* State fields, reference layout.  Type: d = double, u8 = uint8 flag, u32. */
+typedef enum ocpx_field {
+    OCPX_F_P = 0,        /* d  [nb] */
+    OCPX_F_T,            /* d  [nb]  (input temperature units) */
+    OCPX_F_PB,           /* d  [nb] */
+    OCPX_F_NI,           /* d  [nb*nc] */
+    OCPX_F_LNI,          /* d  [nb*nc]  last time step */
+    OCPX_F_NT,           /* d  [nb] */
+    OCPX_F_VF,           /* d  [nb] */
+    OCPX_F_VFP,          /* d  [nb] */
+    OCPX_F_VFI,          /* d  [nb*nc] */
+    OCPX_F_PJ,           /* d  [nb*np] */
+    OCPX_F_PC,           /* d  [nb*np] */
+    OCPX_F_S,            /* d  [nb*np] */
+    OCPX_F_PHASE_EXIST,  /* u8 [nb*np] */
+    OCPX_F_XIJ,          /* d  [nb*np*nc] */
+    OCPX_F_RHO,          /* d  [nb*np] */
+    OCPX_F_XI,
+    OCPX_F_MU,
+    OCPX_F_RHOP,
+    OCPX_F_XIP,
+    OCPX_F_MUP,
+    OCPX_F_RHOX,         /* d  [nb*np*nc] */
+    OCPX_F_XIX,
+    OCPX_F_MUX,
+    OCPX_F_KR,           /* d  [nb*np] */
+    OCPX_F_DKRDS,        /* d  [nb*np*np] */
+    OCPX_F_DPCDS,        /* d  [nb*np*np] */
+    OCPX_F_DSEC_DPRI,    /* d  [nb*np*(nc+1)*(nc+1)] */
+    OCPX_F_PORO,         /* d  [nb] */
+    OCPX_F_POROP,
+    OCPX_F_ROCKVP,
+    OCPX_F_SKIP_FLAG,    /* u8 [nb] */
+    OCPX_F_SKIP_MINEIG,  /* d  [nb] */
+    OCPX_F_SKIP_P,
+    OCPX_F_SKIP_T,
+    OCPX_F_SKIP_ZI,      /* d  [nb*NC] */
+    OCPX_F_STATUS,       /* u32 [nb] per-cell status bits of the last update (read only) */
+    OCPX_F_FTYPE,        /* i8 [nb] flash type left by the last flash (read only) */
+    OCPX_F_FLASH_ITERS,  /* i32 [nb*5] SSM-sta, NR-sta, SSM-split, NR-split, RR iterations (read only) */
+    OCPX_F_UPBLOCK,      /* u32 [nconn*np] (read only) */
+    OCPX_F_CONN_DP,      /* d  [nconn*np] (read only) */
+    OCPX_F_FLUX_VJ,      /* d  [nconn*np] (read only) */
+    OCPX_F_FLUX_NI,      /* d  [nconn*nc] (read only) */
+    OCPX_F_RES,          /* d  [nb*(nc+1)] bulk residual, negated as LinearSystem expects (read only) */
+    OCPX_F_RES_REL_V,    /* d  [nb] (read only) */
+    OCPX_F_RES_REL_N,    /* d  [nb] (read only) */
+    OCPX_F__COUNT
+} ocpx_field;
+
+typedef struct ocpx_report {
+    uint32_t status_or;       /* OR of the per-cell status bits */
+    int n_two_phase;          /* cells with two hydrocarbon phases after the flash */
+    int n_flagged;            /* cells with any status bit set */
+} ocpx_report;
+
+typedef struct ocpx_norms {
+    double maxRelRes_V;  /* OCPNRresidual::maxRelRes_V */
+    double maxRelRes_N;
+    int maxId_V;
+    int maxId_N;
+} ocpx_norms;
+
+/* Context. device < 0 selects the current device. */
+ocpx_status ocpx_create(const ocpx_model_desc* model, const ocpx_grid_desc* grid, int device, ocpx_ctx** out);
+void ocpx_destroy(ocpx_ctx* ctx);
+const char* ocpx_last_error(void);
+int ocpx_abi_version(void);
+
+/* Host <-> device state in the reference layout; count is the element count. */
+ocpx_status ocpx_set_field(ocpx_ctx* ctx, ocpx_field f, const void* host, size_t count);
+ocpx_status ocpx_get_field(ocpx_ctx* ctx, ocpx_field f, void* host, size_t count);
+
+/* Newton-step pieces (asynchronous on the context stream unless noted). */
+ocpx_status ocpx_update_properties(ocpx_ctx* ctx, ocpx_report* rep); /* synchronizes to fill rep */
+ocpx_status ocpx_calres(ocpx_ctx* ctx, double dt, ocpx_norms* norms); /* norms may be NULL */
+ocpx_status ocpx_assemble(ocpx_ctx* ctx, double dt);
+ocpx_status ocpx_newton_update(ocpx_ctx* ctx, const double* u_host, double dSmax);
+ocpx_status ocpx_update_last_step(ocpx_ctx* ctx);
+ocpx_status ocpx_synchronize(ocpx_ctx* ctx);
+
+/* Block-CSR Jacobian of the bulk rows in the reference's order (diagonal
+ * block first, then one block per incident connection in connection order),
+ * blocks (nc+1)x(nc+1) row-major. */
+ocpx_status ocpx_jacobian_dims(ocpx_ctx* ctx, size_t* nrow, size_t* nnz_blocks, int* block_dim);
+ocpx_status ocpx_get_jacobian(ocpx_ctx* ctx, uint32_t* rowptr, uint32_t* col, double* val);
+/* Device pointers of the same arrays (valid until ocpx_destroy). */
+ocpx_status ocpx_jacobian_device(ocpx_ctx* ctx, const uint32_t** rowptr, const uint32_t** col, const double** val);
+
+/* Execution variant: 0 = one kernel per reference loop (plain), 1 = batched
+ * (persistent work-queue flash, fused row assembly, graph-captured step). */
+ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
+
+/* One Newton iteration: optional host Newton update u (nb*(nc+1), may be
+ * NULL), then properties, residual and Jacobian; optional host copies of the
+ * residual (nb*(nc+1)) and Jacobian block values.  Synchronizes. */
+ocpx_status ocpx_step(ocpx_ctx* ctx, const double* u_host, double dSmax, double dt, double* res_host,
+                      double* jac_val_host, ocpx_report* rep);
+
+/* Stream the context launches on (a cudaStream_t), for callers that time or
+ * order work around the library. */
+void* ocpx_stream(ocpx_ctx* ctx);
+/* Number of kernels the library launched on this context so far. */
+uint64_t ocpx_launch_count(ocpx_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OCPX_H */

@@ -1,0 +1,86 @@
+"""Builds the CUDA library libocpx_gb300.so in-tree for sm_103a with nvcc.
+
+Translation units are compiled in parallel; the compositional flash kernel is
+compiled once per component capacity (4, 6, 8, 10, 12 EoS components).
+Objects go to opencaeporox_gb300/_build/, the library next to this file.
+Parity builds use --fmad=false: the reference is compiled without FMA
+contraction, and the black-oil and assembly arithmetic is then bit-identical.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libocpx_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NCM_CAPS = (4, 6, 8, 10, 12)
+
+
+def nvcc_path() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libocpx_gb300.so")
+
+
+def common_flags():
+    return ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+                   "-I" + os.path.join(REPO, "include"), "-I" + CSRC, "-diag-suppress", "177"]
+
+
+def units():
+    out = [("k_fim.cu", [], "k_fim.o"), ("ocpx_capi.cu", [], "ocpx_capi.o")]
+    for c in NCM_CAPS:
+        out.append(("k_flash_comp.cu", [f"-DOCPX_NCM={c}"], f"k_flash_comp_{c}.o"))
+    return out
+
+
+def _deps_mtime():
+    m = 0.0
+    for d in (CSRC, os.path.join(REPO, "include")):
+        for f in os.listdir(d):
+            m = max(m, os.path.getmtime(os.path.join(d, f)))
+    return max(m, os.path.getmtime(__file__))
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile (if anything changed) and return the library path."""
+    os.makedirs(BUILD, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime():
+        return LIB
+    nvcc = nvcc_path()
+    jobs = []
+    for src, extra, obj in units():
+        cmd = [nvcc] + common_flags() + extra + ["-c", os.path.join(CSRC, src), "-o", os.path.join(BUILD, obj)]
+        jobs.append(cmd)
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        return cmd, r
+
+    workers = min(len(jobs), max(2, os.cpu_count() or 2))
+    with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+        for cmd, r in ex.map(run, jobs):
+            if verbose and (r.stdout or r.stderr):
+                print(r.stdout + r.stderr, file=sys.stderr)
+            if r.returncode != 0:
+                raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    objs = [os.path.join(BUILD, o) for _, _, o in units()]
+    tmp = LIB + ".tmp"
+    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,219 @@
+// Kernels of the FIM step other than the compositional flash.
+#include "ocpx_kernels.h"
+#include "cell_ops.cuh"
+#include "conn_ops.cuh"
+
+namespace ocpx {
+
+__global__ void k_flash_bo(const Model* __restrict__ M, BulkView b)
+{
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell < b.nb) bo_flash_der_cell(*M, b, cell);
+}
+
+__global__ void k_krpc_rock(const Model* __restrict__ M, BulkView b)
+{
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell < b.nb) krpc_rock_cell(*M, b, cell);
+}
+
+// CheckNi / CheckP; flags[0] collects the OR of the failure bits.
+__global__ void k_check(BulkView b, uint32_t* __restrict__ flags)
+{
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t st = 0;
+    if (cell < b.nb) st = check_cell(b, cell);
+    // warp-level OR, one atomic per warp that saw a failure
+    st = __reduce_or_sync(0xffffffffu, st);
+    if ((threadIdx.x & 31) == 0 && st) atomicOr(flags, st);
+}
+
+__global__ void k_newton_update(BulkView b, const double* __restrict__ u, double dSmax)
+{
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell < b.nb) newton_update_cell(b, cell, u, dSmax);
+}
+
+__global__ void k_conn_flux(const Model* __restrict__ M, BulkView b, ConnView cv)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < cv.nconn) conn_flux(*M, b, cv, c);
+}
+
+__global__ void k_residual(BulkView b, ConnView cv, double dt, double* __restrict__ res, double* __restrict__ resRelV,
+                           double* __restrict__ resRelN, RowNorm* __restrict__ rn)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < b.nb) cell_residual(b, cv, n, dt, res, resRelV, resRelN, rn + n);
+}
+
+// Global maxima with the reference's tie rule (first cell in index order wins),
+// one block; loops over all cells with a strided pattern.
+__global__ void k_norm_reduce(const RowNorm* __restrict__ rn, int nb, RowNorm* __restrict__ out)
+{
+    __shared__ double sv[256], sn[256];
+    __shared__ int iv[256], in_[256];
+    double mv = 0, mN = 0;
+    int bv = -1, bn = -1;
+    for (int n = threadIdx.x; n < nb; n += blockDim.x) {
+        const RowNorm r = rn[n];
+        // strict ">" in index order as in IsoT_FIM::CalRes: ties keep the first cell
+        if (r.idV >= 0 && (bv < 0 || r.maxV > mv)) { mv = r.maxV; bv = r.idV; }
+        if (r.idN >= 0 && (bn < 0 || r.maxN > mN)) { mN = r.maxN; bn = r.idN; }
+    }
+    sv[threadIdx.x] = mv; iv[threadIdx.x] = bv;
+    sn[threadIdx.x] = mN; in_[threadIdx.x] = bn;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            const int o = threadIdx.x + s;
+            if (iv[o] >= 0 && (iv[threadIdx.x] < 0 || sv[o] > sv[threadIdx.x] ||
+                               (sv[o] == sv[threadIdx.x] && iv[o] < iv[threadIdx.x]))) {
+                sv[threadIdx.x] = sv[o]; iv[threadIdx.x] = iv[o];
+            }
+            if (in_[o] >= 0 && (in_[threadIdx.x] < 0 || sn[o] > sn[threadIdx.x] ||
+                                (sn[o] == sn[threadIdx.x] && in_[o] < in_[threadIdx.x]))) {
+                sn[threadIdx.x] = sn[o]; in_[threadIdx.x] = in_[o];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out->maxV = iv[0] >= 0 ? sv[0] : 0.0; out->idV = iv[0] >= 0 ? iv[0] : 0;
+        out->maxN = in_[0] >= 0 ? sn[0] : 0.0; out->idN = in_[0] >= 0 ? in_[0] : 0;
+    }
+}
+
+template <int NCT>
+__global__ void __launch_bounds__(128) k_jac_conn(const Model* __restrict__ M, BulkView b, ConnView cv, double dt,
+                                                  double* __restrict__ bmat)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cv.nconn) return;
+    const int bsize = (b.nc + 1) * (b.nc + 1);
+    conn_jac_blocks<NCT>(*M, b, cv, c, dt, bmat + (size_t)c * 2 * bsize, bmat + ((size_t)c * 2 + 1) * bsize);
+}
+
+__global__ void k_jac_rows(BulkView b, ConnView cv, const double* __restrict__ bmat, const uint32_t* __restrict__ rowptr,
+                           double* __restrict__ val)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < b.nb) row_assemble(b, cv, r, bmat, rowptr, val);
+}
+
+// out[0]: OR of status bits, out[1]: two-phase cells, out[2]: flagged cells
+__global__ void k_report(BulkView b, uint32_t* __restrict__ out)
+{
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t st = 0, two = 0, fl = 0;
+    if (cell < b.nb) {
+        st = b.status[cell];
+        two = (b.phaseExist[b.idx(0, cell)] && b.phaseExist[b.idx(1, cell)]) ? 1u : 0u;
+        fl = st ? 1u : 0u;
+    }
+    const uint32_t sto = __reduce_or_sync(0xffffffffu, st);
+    const uint32_t twos = __reduce_add_sync(0xffffffffu, two);
+    const uint32_t fls = __reduce_add_sync(0xffffffffu, fl);
+    if ((threadIdx.x & 31) == 0) {
+        if (sto) atomicOr(out, sto);
+        if (twos) atomicAdd(out + 1, twos);
+        if (fls) atomicAdd(out + 2, fls);
+    }
+}
+
+template <typename T>
+__global__ void k_transpose(T* __restrict__ dst, const T* __restrict__ src, int n, int width, bool to_soa)
+{
+    const size_t total = (size_t)n * width;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        // t indexes the destination linearly so stores are coalesced
+        if (to_soa) {
+            const size_t k = t / n, i = t % n;
+            dst[t] = src[i * width + k];
+        }
+        else {
+            const size_t i = t / width, k = t % width;
+            dst[t] = src[k * (size_t)n + i];
+        }
+    }
+}
+
+static int grid_for(int n, int block) { return (n + block - 1) / block; }
+
+cudaError_t launch_flash_bo(const Model* dm, const BulkView& b, int block, cudaStream_t s)
+{
+    if (b.nb) k_flash_bo<<<grid_for(b.nb, block), block, 0, s>>>(dm, b);
+    return cudaGetLastError();
+}
+cudaError_t launch_krpc_rock(const Model* dm, const BulkView& b, int block, cudaStream_t s)
+{
+    if (b.nb) k_krpc_rock<<<grid_for(b.nb, block), block, 0, s>>>(dm, b);
+    return cudaGetLastError();
+}
+cudaError_t launch_check(const BulkView& b, uint32_t* flags, int block, cudaStream_t s)
+{
+    if (b.nb) k_check<<<grid_for(b.nb, block), block, 0, s>>>(b, flags);
+    return cudaGetLastError();
+}
+cudaError_t launch_newton_update(const BulkView& b, const double* u, double dSmax, int block, cudaStream_t s)
+{
+    if (b.nb) k_newton_update<<<grid_for(b.nb, block), block, 0, s>>>(b, u, dSmax);
+    return cudaGetLastError();
+}
+cudaError_t launch_conn_flux(const Model* dm, const BulkView& b, const ConnView& cv, int block, cudaStream_t s)
+{
+    if (cv.nconn) k_conn_flux<<<grid_for(cv.nconn, block), block, 0, s>>>(dm, b, cv);
+    return cudaGetLastError();
+}
+cudaError_t launch_residual(const BulkView& b, const ConnView& cv, double dt, double* res, double* resRelV,
+                            double* resRelN, RowNorm* rn, RowNorm* rn_out, int block, cudaStream_t s)
+{
+    if (!b.nb) return cudaSuccess;
+    k_residual<<<grid_for(b.nb, block), block, 0, s>>>(b, cv, dt, res, resRelV, resRelN, rn);
+    k_norm_reduce<<<1, 256, 0, s>>>(rn, b.nb, rn_out);
+    return cudaGetLastError();
+}
+cudaError_t launch_jac_conn(int nct, const Model* dm, const BulkView& b, const ConnView& cv, double dt, double* bmat,
+                            int block, cudaStream_t s)
+{
+    if (!cv.nconn) return cudaSuccess;
+    const int g = grid_for(cv.nconn, block);
+    switch (nct) {
+    case 3: k_jac_conn<3><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
+    case 5: k_jac_conn<5><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
+    case 7: k_jac_conn<7><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
+    case 9: k_jac_conn<9><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
+    case 11: k_jac_conn<11><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
+    case 13: k_jac_conn<13><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+cudaError_t launch_jac_rows(const BulkView& b, const ConnView& cv, const double* bmat, const uint32_t* rowptr,
+                            double* val, int block, cudaStream_t s)
+{
+    if (b.nb) k_jac_rows<<<grid_for(b.nb, block), block, 0, s>>>(b, cv, bmat, rowptr, val);
+    return cudaGetLastError();
+}
+cudaError_t launch_report(const BulkView& b, uint32_t* out3, int block, cudaStream_t s)
+{
+    if (b.nb) k_report<<<grid_for(b.nb, block), block, 0, s>>>(b, out3);
+    return cudaGetLastError();
+}
+cudaError_t launch_transpose(void* dst, const void* src, int n, int width, int elem_bytes, bool to_soa,
+                             cudaStream_t s)
+{
+    const size_t total = (size_t)n * width;
+    if (!total) return cudaSuccess;
+    const int block = 256;
+    const int grid = (int)((total + block - 1) / block < 4096 ? (total + block - 1) / block : 4096);
+    switch (elem_bytes) {
+    case 1: k_transpose<uint8_t><<<grid, block, 0, s>>>((uint8_t*)dst, (const uint8_t*)src, n, width, to_soa); break;
+    case 4: k_transpose<uint32_t><<<grid, block, 0, s>>>((uint32_t*)dst, (const uint32_t*)src, n, width, to_soa); break;
+    case 8: k_transpose<double><<<grid, block, 0, s>>>((double*)dst, (const double*)src, n, width, to_soa); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace ocpx

@@ -1,0 +1,590 @@
+// C ABI (include/ocpx.h): context, device memory, layout conversion and the
+// launch sequence of one FIM Newton step.
+#include "ocpx.h"
+#include "ocpx_kernels.h"
+#include "model_build.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace ocpx {
+cudaError_t launch_flash_comp_4(const Model*, const BulkView&, int, cudaStream_t);
+cudaError_t launch_flash_comp_6(const Model*, const BulkView&, int, cudaStream_t);
+cudaError_t launch_flash_comp_8(const Model*, const BulkView&, int, cudaStream_t);
+cudaError_t launch_flash_comp_10(const Model*, const BulkView&, int, cudaStream_t);
+cudaError_t launch_flash_comp_12(const Model*, const BulkView&, int, cudaStream_t);
+cudaError_t launch_flash_comp_queue_4(const Model*, const BulkView&, unsigned*, int, int, int, cudaStream_t);
+cudaError_t launch_flash_comp_queue_6(const Model*, const BulkView&, unsigned*, int, int, int, cudaStream_t);
+cudaError_t launch_flash_comp_queue_8(const Model*, const BulkView&, unsigned*, int, int, int, cudaStream_t);
+cudaError_t launch_flash_comp_queue_10(const Model*, const BulkView&, unsigned*, int, int, int, cudaStream_t);
+cudaError_t launch_flash_comp_queue_12(const Model*, const BulkView&, unsigned*, int, int, int, cudaStream_t);
+
+cudaError_t launch_flash_comp(int ncm, const Model* dm, const BulkView& b, int block, cudaStream_t s)
+{
+    switch (ncm) {
+    case 4: return launch_flash_comp_4(dm, b, block, s);
+    case 6: return launch_flash_comp_6(dm, b, block, s);
+    case 8: return launch_flash_comp_8(dm, b, block, s);
+    case 10: return launch_flash_comp_10(dm, b, block, s);
+    case 12: return launch_flash_comp_12(dm, b, block, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+cudaError_t launch_flash_comp_queue(int ncm, const Model* dm, const BulkView& b, unsigned* counter, int grid,
+                                    int block, int chunk, cudaStream_t s)
+{
+    switch (ncm) {
+    case 4: return launch_flash_comp_queue_4(dm, b, counter, grid, block, chunk, s);
+    case 6: return launch_flash_comp_queue_6(dm, b, counter, grid, block, chunk, s);
+    case 8: return launch_flash_comp_queue_8(dm, b, counter, grid, block, chunk, s);
+    case 10: return launch_flash_comp_queue_10(dm, b, counter, grid, block, chunk, s);
+    case 12: return launch_flash_comp_queue_12(dm, b, counter, grid, block, chunk, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+}  // namespace ocpx
+
+using namespace ocpx;
+
+namespace {
+
+thread_local std::string g_err;
+
+ocpx_status fail(ocpx_status st, const std::string& msg)
+{
+    g_err = msg;
+    return st;
+}
+
+#define OCPX_CUDA(call)                                                                                 \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) return fail(OCPX_CUDA_ERROR, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+int cap_ncm(int NC)
+{
+    for (int c : kNcmCaps)
+        if (NC <= c) return c;
+    return -1;
+}
+int cap_nct(int nct)
+{
+    for (int c : kNctCaps)
+        if (nct <= c) return c;
+    return -1;
+}
+
+struct FieldInfo {
+    void* dev;       // device SoA base (or cell-major for AoS-native fields)
+    int n;           // entities (cells or connections)
+    int width;       // values per entity
+    int elem;        // bytes per value
+    bool soa;        // device layout is [k][n]
+    bool writable;
+};
+
+}  // namespace
+
+struct ocpx_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    Model host_model{};
+    Model* d_model = nullptr;
+    int nb = 0, np = 3, nc = 0, nconn = 0, NC = 0, ncm = 0, nct_cap = 0;
+    int variant = 0;
+    // one arena for everything
+    char* arena = nullptr;
+    size_t arena_bytes = 0;
+    BulkView b{};
+    ConnView cv{};
+    double* res = nullptr;
+    double* resRelV = nullptr;
+    double* resRelN = nullptr;
+    RowNorm* rownorm = nullptr;
+    RowNorm* norm_out = nullptr;
+    uint32_t* flags = nullptr;      // [4]: check OR, report (OR, two-phase, flagged)
+    unsigned* queue_counter = nullptr;
+    double* u = nullptr;            // Newton update staging
+    double* bmat = nullptr;         // per-connection Jacobian blocks (2 per connection)
+    uint32_t* jac_rowptr = nullptr;
+    uint32_t* jac_col = nullptr;
+    double* jac_val = nullptr;
+    size_t jac_nnz = 0;
+    void* staging = nullptr;        // host-layout staging for field transfers
+    size_t staging_bytes = 0;
+    uint32_t* h_flags = nullptr;    // pinned
+    RowNorm* h_norm = nullptr;      // pinned
+    uint64_t launches = 0;
+    int block_cell = 128, block_conn = 128, queue_chunk = 1, queue_grid = 0;
+    // graph of one Newton iteration (variant 1)
+    cudaGraphExec_t graph_exec = nullptr;
+    double graph_dt = -1, graph_dSmax = -1;
+    bool graph_with_update = false;
+
+    FieldInfo field(ocpx_field f) const;
+};
+
+FieldInfo ocpx_ctx::field(ocpx_field f) const
+{
+    const int nct = nc, npc = np * nc, lend = np * (nc + 1) * (nc + 1);
+    switch (f) {
+    case OCPX_F_P: return {b.P, nb, 1, 8, true, true};
+    case OCPX_F_T: return {b.T, nb, 1, 8, true, true};
+    case OCPX_F_PB: return {b.Pb, nb, 1, 8, true, true};
+    case OCPX_F_NI: return {b.Ni, nb, nct, 8, true, true};
+    case OCPX_F_LNI: return {b.lNi, nb, nct, 8, true, true};
+    case OCPX_F_NT: return {b.Nt, nb, 1, 8, true, true};
+    case OCPX_F_VF: return {b.vf, nb, 1, 8, true, true};
+    case OCPX_F_VFP: return {b.vfP, nb, 1, 8, true, true};
+    case OCPX_F_VFI: return {b.vfi, nb, nct, 8, true, true};
+    case OCPX_F_PJ: return {b.Pj, nb, np, 8, true, true};
+    case OCPX_F_PC: return {b.Pc, nb, np, 8, true, true};
+    case OCPX_F_S: return {b.S, nb, np, 8, true, true};
+    case OCPX_F_PHASE_EXIST: return {b.phaseExist, nb, np, 1, true, true};
+    case OCPX_F_XIJ: return {b.xij, nb, npc, 8, true, true};
+    case OCPX_F_RHO: return {b.rho, nb, np, 8, true, true};
+    case OCPX_F_XI: return {b.xi, nb, np, 8, true, true};
+    case OCPX_F_MU: return {b.mu, nb, np, 8, true, true};
+    case OCPX_F_RHOP: return {b.rhoP, nb, np, 8, true, true};
+    case OCPX_F_XIP: return {b.xiP, nb, np, 8, true, true};
+    case OCPX_F_MUP: return {b.muP, nb, np, 8, true, true};
+    case OCPX_F_RHOX: return {b.rhox, nb, npc, 8, true, true};
+    case OCPX_F_XIX: return {b.xix, nb, npc, 8, true, true};
+    case OCPX_F_MUX: return {b.mux, nb, npc, 8, true, true};
+    case OCPX_F_KR: return {b.kr, nb, np, 8, true, true};
+    case OCPX_F_DKRDS: return {b.dKrdS, nb, np * np, 8, true, true};
+    case OCPX_F_DPCDS: return {b.dPcdS, nb, np * np, 8, true, true};
+    case OCPX_F_DSEC_DPRI: return {b.dSec_dPri, nb, lend, 8, true, true};
+    case OCPX_F_PORO: return {b.poro, nb, 1, 8, true, true};
+    case OCPX_F_POROP: return {b.poroP, nb, 1, 8, true, true};
+    case OCPX_F_ROCKVP: return {b.rockVp, nb, 1, 8, true, true};
+    case OCPX_F_SKIP_FLAG: return {b.skip_flag, nb, 1, 1, true, true};
+    case OCPX_F_SKIP_MINEIG: return {b.skip_minEig, nb, 1, 8, true, true};
+    case OCPX_F_SKIP_P: return {b.skip_P, nb, 1, 8, true, true};
+    case OCPX_F_SKIP_T: return {b.skip_T, nb, 1, 8, true, true};
+    case OCPX_F_SKIP_ZI: return {b.skip_zi, nb, NC > 0 ? NC : 1, 8, true, true};
+    case OCPX_F_STATUS: return {b.status, nb, 1, 4, true, false};
+    case OCPX_F_FTYPE: return {b.ftype, nb, 1, 1, true, false};
+    case OCPX_F_FLASH_ITERS: return {b.iters, nb, 5, 4, true, false};
+    case OCPX_F_UPBLOCK: return {cv.upblock, nconn, np, 4, true, false};
+    case OCPX_F_CONN_DP: return {cv.dP, nconn, np, 8, true, false};
+    case OCPX_F_FLUX_VJ: return {cv.flux_vj, nconn, np, 8, true, false};
+    case OCPX_F_FLUX_NI: return {cv.flux_ni, nconn, nc, 8, true, false};
+    case OCPX_F_RES: return {res, nb, nc + 1, 8, false, false};
+    case OCPX_F_RES_REL_V: return {resRelV, nb, 1, 8, true, false};
+    case OCPX_F_RES_REL_N: return {resRelN, nb, 1, 8, true, false};
+    default: return {nullptr, 0, 0, 0, true, false};
+    }
+}
+
+namespace {
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" {
+
+int ocpx_abi_version(void) { return OCPX_ABI_VERSION; }
+const char* ocpx_last_error(void) { return g_err.c_str(); }
+
+ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int device, ocpx_ctx** out)
+{
+    if (!md || !gd || !out) return fail(OCPX_INVALID_ARG, "null argument");
+    *out = nullptr;
+    if (gd->nb <= 0 || gd->nconn < 0 || !gd->v || !gd->depth || !gd->poro_init ||
+        (gd->nconn > 0 && (!gd->conn_b || !gd->conn_e || !gd->conn_trans)))
+        return fail(OCPX_INVALID_ARG, "grid description incomplete");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(OCPX_NO_DEVICE, "no CUDA device");
+    for (int c = 0; c < gd->nconn; c++)
+        if (gd->conn_b[c] >= (uint32_t)gd->nb || gd->conn_e[c] >= (uint32_t)gd->nb || gd->conn_b[c] == gd->conn_e[c])
+            return fail(OCPX_INVALID_ARG, "connection endpoint out of range at " + std::to_string(c));
+
+    ocpx_ctx* ctx = new ocpx_ctx();
+    std::string merr;
+    ocpx_status st = build_model(md, ctx->host_model, merr);
+    if (st != OCPX_OK) { delete ctx; return fail(st, merr); }
+    if (device >= 0) {
+        if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return fail(OCPX_NO_DEVICE, "cudaSetDevice failed"); }
+        ctx->device = device;
+    }
+    else {
+        cudaGetDevice(&ctx->device);
+    }
+    ctx->nb = gd->nb;
+    ctx->nc = md->nc;
+    ctx->np = 3;
+    ctx->nconn = gd->nconn;
+    ctx->NC = md->mixture == 1 ? md->nc - 1 : 0;
+    ctx->ncm = md->mixture == 1 ? cap_ncm(ctx->NC) : 0;
+    ctx->nct_cap = cap_nct(md->nc);
+    if (ctx->nct_cap < 0 || (md->mixture == 1 && ctx->ncm < 0)) { delete ctx; return fail(OCPX_INVALID_ARG, "too many components"); }
+
+    const int nb = ctx->nb, np = ctx->np, nc = ctx->nc, nconn = ctx->nconn;
+    const int lend = np * (nc + 1) * (nc + 1), bsize = (nc + 1) * (nc + 1);
+
+    // row -> incident connections (increasing connection index) and the
+    // block-CSR pattern: diagonal first, then one block per incident connection
+    std::vector<uint32_t> deg(nb + 1, 0);
+    for (int c = 0; c < nconn; c++) { deg[gd->conn_b[c]]++; deg[gd->conn_e[c]]++; }
+    std::vector<uint32_t> row_ptr(nb + 1, 0);
+    for (int n = 0; n < nb; n++) row_ptr[n + 1] = row_ptr[n] + deg[n];
+    std::vector<uint32_t> row_conn(row_ptr[nb]);
+    std::vector<uint32_t> fill(row_ptr.begin(), row_ptr.end() - 1);
+    std::vector<uint32_t> jrow(nb + 1, 0), jcol;
+    jcol.reserve(nb + 2 * (size_t)nconn);
+    for (int c = 0; c < nconn; c++) {
+        row_conn[fill[gd->conn_b[c]]++] = ((uint32_t)c << 1) | 0u;
+        row_conn[fill[gd->conn_e[c]]++] = ((uint32_t)c << 1) | 1u;
+    }
+    for (int n = 0; n < nb; n++) {
+        jrow[n + 1] = jrow[n] + 1 + (row_ptr[n + 1] - row_ptr[n]);
+        jcol.push_back(n);
+        for (uint32_t k = row_ptr[n]; k < row_ptr[n + 1]; k++) {
+            const uint32_t c = row_conn[k] >> 1;
+            jcol.push_back((row_conn[k] & 1u) ? gd->conn_b[c] : gd->conn_e[c]);
+        }
+    }
+    ctx->jac_nnz = jcol.size();
+
+    // arena layout
+    struct Slot { void** p; size_t bytes; };
+    std::vector<Slot> slots;
+    auto add = [&](void* pp, size_t bytes) { slots.push_back({(void**)pp, bytes}); };
+    BulkView& b = ctx->b;
+    b.nb = nb; b.np = np; b.nc = nc;
+    const size_t D = sizeof(double) * (size_t)nb;
+    add(&b.v, D); add(&b.depth, D); add(&b.poroInit, D);
+    add(&b.P, D); add(&b.T, D); add(&b.Pb, D);
+    add(&b.Ni, D * nc); add(&b.lNi, D * nc);
+    add(&b.Nt, D); add(&b.vf, D); add(&b.vfP, D); add(&b.vfi, D * nc);
+    add(&b.Pj, D * np); add(&b.Pc, D * np); add(&b.S, D * np);
+    add(&b.phaseExist, (size_t)nb * np);
+    add(&b.xij, D * np * nc);
+    add(&b.rho, D * np); add(&b.xi, D * np); add(&b.mu, D * np);
+    add(&b.rhoP, D * np); add(&b.xiP, D * np); add(&b.muP, D * np);
+    add(&b.rhox, D * np * nc); add(&b.xix, D * np * nc); add(&b.mux, D * np * nc);
+    add(&b.kr, D * np); add(&b.dKrdS, D * np * np); add(&b.dPcdS, D * np * np);
+    add(&b.dSec_dPri, D * lend);
+    add(&b.poro, D); add(&b.poroP, D); add(&b.rockVp, D);
+    add(&b.skip_flag, (size_t)nb); add(&b.skip_minEig, D); add(&b.skip_P, D); add(&b.skip_T, D);
+    add(&b.skip_zi, D * (ctx->NC > 0 ? ctx->NC : 1));
+    add(&b.status, sizeof(uint32_t) * (size_t)nb); add(&b.ftype, (size_t)nb);
+    add(&b.iters, sizeof(int32_t) * (size_t)nb * 5);
+    ConnView& cv = ctx->cv;
+    cv.nconn = nconn;
+    const size_t C = (size_t)(nconn > 0 ? nconn : 1);
+    add(&cv.bId, sizeof(uint32_t) * C); add(&cv.eId, sizeof(uint32_t) * C); add(&cv.trans, sizeof(double) * C);
+    add(&cv.upblock, sizeof(uint32_t) * C * np); add(&cv.dP, sizeof(double) * C * np);
+    add(&cv.flux_vj, sizeof(double) * C * np); add(&cv.flux_ni, sizeof(double) * C * nc);
+    add(&cv.row_ptr, sizeof(uint32_t) * (nb + 1)); add(&cv.row_conn, sizeof(uint32_t) * (row_conn.size() + 1));
+    add(&ctx->res, D * (nc + 1)); add(&ctx->resRelV, D); add(&ctx->resRelN, D);
+    add(&ctx->rownorm, sizeof(RowNorm) * (size_t)nb); add(&ctx->norm_out, sizeof(RowNorm));
+    add(&ctx->flags, sizeof(uint32_t) * 4); add(&ctx->queue_counter, sizeof(unsigned) * 4);
+    add(&ctx->u, D * (nc + 1));
+    add(&ctx->bmat, sizeof(double) * C * 2 * bsize);
+    add(&ctx->jac_rowptr, sizeof(uint32_t) * (nb + 1)); add(&ctx->jac_col, sizeof(uint32_t) * jcol.size());
+    add(&ctx->jac_val, sizeof(double) * jcol.size() * bsize);
+    size_t staging = D * lend;
+    staging = std::max(staging, sizeof(double) * C * nc);
+    add(&ctx->staging, staging);
+    ctx->staging_bytes = staging;
+    size_t total = 0;
+    for (auto& s : slots) total += align256(s.bytes);
+    if (cudaMalloc(&ctx->arena, total) != cudaSuccess) {
+        delete ctx;
+        return fail(OCPX_CUDA_ERROR, "cudaMalloc of " + std::to_string(total) + " bytes failed");
+    }
+    ctx->arena_bytes = total;
+    size_t off = 0;
+    for (auto& s : slots) { *s.p = ctx->arena + off; off += align256(s.bytes); }
+    cudaMemset(ctx->arena, 0, total);
+
+    auto fail_ctx = [&](ocpx_status s2, const std::string& m) { ocpx_destroy(ctx); return fail(s2, m); };
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail_ctx(OCPX_CUDA_ERROR, "stream creation failed");
+    if (cudaMalloc(&ctx->d_model, sizeof(Model)) != cudaSuccess) return fail_ctx(OCPX_CUDA_ERROR, "model alloc failed");
+    if (cudaMallocHost(&ctx->h_flags, sizeof(uint32_t) * 4) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_norm, sizeof(RowNorm)) != cudaSuccess)
+        return fail_ctx(OCPX_CUDA_ERROR, "pinned alloc failed");
+    cudaMemcpy(ctx->d_model, &ctx->host_model, sizeof(Model), cudaMemcpyHostToDevice);
+    cudaMemcpy((void*)b.v, gd->v, D, cudaMemcpyHostToDevice);
+    cudaMemcpy((void*)b.depth, gd->depth, D, cudaMemcpyHostToDevice);
+    cudaMemcpy((void*)b.poroInit, gd->poro_init, D, cudaMemcpyHostToDevice);
+    if (nconn > 0) {
+        cudaMemcpy((void*)cv.bId, gd->conn_b, sizeof(uint32_t) * nconn, cudaMemcpyHostToDevice);
+        cudaMemcpy((void*)cv.eId, gd->conn_e, sizeof(uint32_t) * nconn, cudaMemcpyHostToDevice);
+        cudaMemcpy((void*)cv.trans, gd->conn_trans, sizeof(double) * nconn, cudaMemcpyHostToDevice);
+    }
+    cudaMemcpy((void*)cv.row_ptr, row_ptr.data(), sizeof(uint32_t) * (nb + 1), cudaMemcpyHostToDevice);
+    if (!row_conn.empty())
+        cudaMemcpy((void*)cv.row_conn, row_conn.data(), sizeof(uint32_t) * row_conn.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->jac_rowptr, jrow.data(), sizeof(uint32_t) * (nb + 1), cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->jac_col, jcol.data(), sizeof(uint32_t) * jcol.size(), cudaMemcpyHostToDevice);
+    const cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return fail_ctx(OCPX_CUDA_ERROR, std::string("context setup: ") + cudaGetErrorString(e));
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    ctx->queue_grid = sms * 4;
+    *out = ctx;
+    return OCPX_OK;
+}
+
+void ocpx_destroy(ocpx_ctx* ctx)
+{
+    if (!ctx) return;
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->arena) cudaFree(ctx->arena);
+    if (ctx->d_model) cudaFree(ctx->d_model);
+    if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+    if (ctx->h_norm) cudaFreeHost(ctx->h_norm);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+void* ocpx_stream(ocpx_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+uint64_t ocpx_launch_count(ocpx_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+ocpx_status ocpx_set_field(ocpx_ctx* ctx, ocpx_field f, const void* host, size_t count)
+{
+    if (!ctx || !host) return fail(OCPX_INVALID_ARG, "null argument");
+    const FieldInfo fi = ctx->field(f);
+    if (!fi.dev || !fi.writable) return fail(OCPX_INVALID_ARG, "field not writable: " + std::to_string((int)f));
+    const size_t expect = (size_t)fi.n * fi.width;
+    if (count != expect)
+        return fail(OCPX_INVALID_ARG, "field " + std::to_string((int)f) + ": expected " + std::to_string(expect) +
+                                          " elements, got " + std::to_string(count));
+    const size_t bytes = expect * fi.elem;
+    if (fi.width == 1 || !fi.soa) {
+        OCPX_CUDA(cudaMemcpyAsync(fi.dev, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    else {
+        OCPX_CUDA(cudaMemcpyAsync(ctx->staging, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        OCPX_CUDA(launch_transpose(fi.dev, ctx->staging, fi.n, fi.width, fi.elem, true, ctx->stream));
+        ctx->launches++;
+    }
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_get_field(ocpx_ctx* ctx, ocpx_field f, void* host, size_t count)
+{
+    if (!ctx || !host) return fail(OCPX_INVALID_ARG, "null argument");
+    const FieldInfo fi = ctx->field(f);
+    if (!fi.dev) return fail(OCPX_INVALID_ARG, "unknown field " + std::to_string((int)f));
+    const size_t expect = (size_t)fi.n * fi.width;
+    if (count != expect)
+        return fail(OCPX_INVALID_ARG, "field " + std::to_string((int)f) + ": expected " + std::to_string(expect) +
+                                          " elements, got " + std::to_string(count));
+    const size_t bytes = expect * fi.elem;
+    if (fi.width == 1 || !fi.soa) {
+        OCPX_CUDA(cudaMemcpyAsync(host, fi.dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    else {
+        OCPX_CUDA(launch_transpose(ctx->staging, fi.dev, fi.n, fi.width, fi.elem, false, ctx->stream));
+        ctx->launches++;
+        OCPX_CUDA(cudaMemcpyAsync(host, ctx->staging, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return OCPX_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// CheckNi/CheckP + flash + kr/Pc + rock, all asynchronous
+ocpx_status enqueue_properties(ocpx_ctx* ctx)
+{
+    cudaStream_t s = ctx->stream;
+    OCPX_CUDA(cudaMemsetAsync(ctx->flags, 0, sizeof(uint32_t) * 4, s));
+    OCPX_CUDA(launch_check(ctx->b, ctx->flags, ctx->block_cell, s));
+    ctx->launches++;
+    if (ctx->host_model.mixture == 1) {
+        if (ctx->variant == 1) {
+            OCPX_CUDA(cudaMemsetAsync(ctx->queue_counter, 0, sizeof(unsigned), s));
+            OCPX_CUDA(launch_flash_comp_queue(ctx->ncm, ctx->d_model, ctx->b, ctx->queue_counter, ctx->queue_grid,
+                                              ctx->block_cell, ctx->queue_chunk, s));
+        }
+        else {
+            OCPX_CUDA(launch_flash_comp(ctx->ncm, ctx->d_model, ctx->b, ctx->block_cell, s));
+        }
+    }
+    else {
+        OCPX_CUDA(launch_flash_bo(ctx->d_model, ctx->b, ctx->block_cell, s));
+    }
+    ctx->launches++;
+    OCPX_CUDA(launch_krpc_rock(ctx->d_model, ctx->b, ctx->block_cell, s));
+    ctx->launches++;
+    OCPX_CUDA(launch_report(ctx->b, ctx->flags + 1, ctx->block_cell, s));
+    ctx->launches++;
+    return OCPX_OK;
+}
+
+ocpx_status enqueue_calres(ocpx_ctx* ctx, double dt)
+{
+    cudaStream_t s = ctx->stream;
+    OCPX_CUDA(launch_conn_flux(ctx->d_model, ctx->b, ctx->cv, ctx->block_conn, s));
+    OCPX_CUDA(launch_residual(ctx->b, ctx->cv, dt, ctx->res, ctx->resRelV, ctx->resRelN, ctx->rownorm, ctx->norm_out,
+                              ctx->block_cell, s));
+    ctx->launches += 3;
+    return OCPX_OK;
+}
+
+ocpx_status enqueue_assemble(ocpx_ctx* ctx, double dt)
+{
+    cudaStream_t s = ctx->stream;
+    OCPX_CUDA(launch_jac_conn(ctx->nct_cap, ctx->d_model, ctx->b, ctx->cv, dt, ctx->bmat, ctx->block_conn, s));
+    OCPX_CUDA(launch_jac_rows(ctx->b, ctx->cv, ctx->bmat, ctx->jac_rowptr, ctx->jac_val, ctx->block_cell, s));
+    ctx->launches += 2;
+    return OCPX_OK;
+}
+
+ocpx_status report_from_flags(ocpx_ctx* ctx, ocpx_report* rep)
+{
+    OCPX_CUDA(cudaMemcpyAsync(ctx->h_flags, ctx->flags, sizeof(uint32_t) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    const uint32_t chk = ctx->h_flags[0];
+    if (rep) {
+        rep->status_or = ctx->h_flags[1] | chk;
+        rep->n_two_phase = (int)ctx->h_flags[2];
+        rep->n_flagged = (int)ctx->h_flags[3];
+    }
+    if (chk & ST_NEG_NI) return fail(OCPX_NEGATIVE_NI, "negative moles beyond the clamp rule (Bulk::CheckNi)");
+    if (chk & ST_NEG_P) return fail(OCPX_NEGATIVE_P, "negative pressure (Bulk::CheckP)");
+    const uint32_t f = ctx->h_flags[1];
+    if (f & ST_NONFINITE) return fail(OCPX_NONFINITE, "non-finite flash result");
+    if (f & ST_ITER_CAP) return fail(OCPX_WATCHDOG, "flash iteration cap reached");
+    return OCPX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ocpx_status ocpx_update_properties(ocpx_ctx* ctx, ocpx_report* rep)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    ocpx_status st = enqueue_properties(ctx);
+    if (st != OCPX_OK) return st;
+    return report_from_flags(ctx, rep);
+}
+
+ocpx_status ocpx_calres(ocpx_ctx* ctx, double dt, ocpx_norms* norms)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    ocpx_status st = enqueue_calres(ctx, dt);
+    if (st != OCPX_OK) return st;
+    if (norms) {
+        OCPX_CUDA(cudaMemcpyAsync(ctx->h_norm, ctx->norm_out, sizeof(RowNorm), cudaMemcpyDeviceToHost, ctx->stream));
+        OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+        norms->maxRelRes_V = ctx->h_norm->maxV;
+        norms->maxId_V = ctx->h_norm->idV;
+        norms->maxRelRes_N = ctx->h_norm->maxN;
+        norms->maxId_N = ctx->h_norm->idN;
+    }
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_assemble(ocpx_ctx* ctx, double dt)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    return enqueue_assemble(ctx, dt);
+}
+
+ocpx_status ocpx_newton_update(ocpx_ctx* ctx, const double* u_host, double dSmax)
+{
+    if (!ctx || !u_host) return fail(OCPX_INVALID_ARG, "null argument");
+    const size_t bytes = sizeof(double) * (size_t)ctx->nb * (ctx->nc + 1);
+    OCPX_CUDA(cudaMemcpyAsync(ctx->u, u_host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    OCPX_CUDA(launch_newton_update(ctx->b, ctx->u, dSmax, ctx->block_cell, ctx->stream));
+    ctx->launches++;
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_update_last_step(ocpx_ctx* ctx)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    OCPX_CUDA(cudaMemcpyAsync(ctx->b.lNi, ctx->b.Ni, sizeof(double) * (size_t)ctx->nb * ctx->nc,
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_synchronize(ocpx_ctx* ctx)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_jacobian_dims(ocpx_ctx* ctx, size_t* nrow, size_t* nnz_blocks, int* block_dim)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    if (nrow) *nrow = ctx->nb;
+    if (nnz_blocks) *nnz_blocks = ctx->jac_nnz;
+    if (block_dim) *block_dim = ctx->nc + 1;
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_get_jacobian(ocpx_ctx* ctx, uint32_t* rowptr, uint32_t* col, double* val)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    const size_t bsize = (size_t)(ctx->nc + 1) * (ctx->nc + 1);
+    if (rowptr)
+        OCPX_CUDA(cudaMemcpyAsync(rowptr, ctx->jac_rowptr, sizeof(uint32_t) * (ctx->nb + 1), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    if (col)
+        OCPX_CUDA(cudaMemcpyAsync(col, ctx->jac_col, sizeof(uint32_t) * ctx->jac_nnz, cudaMemcpyDeviceToHost, ctx->stream));
+    if (val)
+        OCPX_CUDA(cudaMemcpyAsync(val, ctx->jac_val, sizeof(double) * ctx->jac_nnz * bsize, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_jacobian_device(ocpx_ctx* ctx, const uint32_t** rowptr, const uint32_t** col, const double** val)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    if (rowptr) *rowptr = ctx->jac_rowptr;
+    if (col) *col = ctx->jac_col;
+    if (val) *val = ctx->jac_val;
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant)
+{
+    if (!ctx || (variant != 0 && variant != 1)) return fail(OCPX_INVALID_ARG, "variant must be 0 or 1");
+    ctx->variant = variant;
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_step(ocpx_ctx* ctx, const double* u_host, double dSmax, double dt, double* res_host,
+                      double* jac_val_host, ocpx_report* rep)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    ocpx_status st;
+    if (u_host) {
+        st = ocpx_newton_update(ctx, u_host, dSmax);
+        if (st != OCPX_OK) return st;
+    }
+    if ((st = enqueue_properties(ctx)) != OCPX_OK) return st;
+    if ((st = enqueue_calres(ctx, dt)) != OCPX_OK) return st;
+    if ((st = enqueue_assemble(ctx, dt)) != OCPX_OK) return st;
+    const size_t bsize = (size_t)(ctx->nc + 1) * (ctx->nc + 1);
+    if (res_host)
+        OCPX_CUDA(cudaMemcpyAsync(res_host, ctx->res, sizeof(double) * (size_t)ctx->nb * (ctx->nc + 1),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    if (jac_val_host)
+        OCPX_CUDA(cudaMemcpyAsync(jac_val_host, ctx->jac_val, sizeof(double) * ctx->jac_nnz * bsize,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    return report_from_flags(ctx, rep);
+}
+
+}  // extern "C"

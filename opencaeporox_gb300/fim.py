@@ -1,0 +1,390 @@
+"""Host-side mirror of the reference's FIM method interface over the C ABI.
+
+``FimContext`` exposes the calls IsoT_FIM makes on the bulk each Newton
+iteration (src/IsoThermalMethod.cpp):
+
+    ===========================  ==========================================
+    reference (IsoT_FIM)          this module
+    ===========================  ==========================================
+    UpdateProperty (:811-836)     FimContext.update_property()
+    CalRes (:1090-1185)           FimContext.cal_res(dt)
+    AssembleMatBulks (:1187-1269) FimContext.assemble_mat(dt)
+    GetSolution (:1282-1418)      FimContext.get_solution(u, dSmax)
+    UpdateLastTimeStep (:1473)    FimContext.update_last_time_step()
+    ===========================  ==========================================
+
+State arrays use the reference's BulkVarSet layout (cell-major, then phase,
+then component).  All numerical work runs in libocpx_gb300.so on the GPU; the
+library must be built (``opencaeporox_gb300.build.build()``) and a CUDA device
+must be present, otherwise every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libocpx_gb300.so")
+
+# ---------------------------------------------------------------- C types --
+OCPX_OK = 0
+STATUS_NAMES = {0: "OK", 1: "NONCONVERGED", 2: "SINGULAR", 3: "NONFINITE", 4: "WATCHDOG", 5: "INVALID_ARG",
+                6: "CUDA_ERROR", 7: "NEGATIVE_P", 8: "NEGATIVE_NI", 9: "NO_DEVICE"}
+
+FIELDS = ["P", "T", "PB", "NI", "LNI", "NT", "VF", "VFP", "VFI", "PJ", "PC", "S", "PHASE_EXIST", "XIJ", "RHO",
+          "XI", "MU", "RHOP", "XIP", "MUP", "RHOX", "XIX", "MUX", "KR", "DKRDS", "DPCDS", "DSEC_DPRI", "PORO",
+          "POROP", "ROCKVP", "SKIP_FLAG", "SKIP_MINEIG", "SKIP_P", "SKIP_T", "SKIP_ZI", "STATUS", "FTYPE",
+          "FLASH_ITERS", "UPBLOCK", "CONN_DP", "FLUX_VJ", "FLUX_NI", "RES", "RES_REL_V", "RES_REL_N"]
+FIELD_ID = {name: i for i, name in enumerate(FIELDS)}
+FIELD_DTYPE = {"PHASE_EXIST": np.uint8, "SKIP_FLAG": np.uint8, "STATUS": np.uint32, "FTYPE": np.int8,
+               "FLASH_ITERS": np.int32, "UPBLOCK": np.uint32}
+
+# BulkVarSet / BulkConnVarSet names -> field ids (for loading reference dumps)
+REF_NAMES = {"P": "P", "T": "T", "Pb": "PB", "Ni": "NI", "lNi": "LNI", "Nt": "NT", "vf": "VF", "vfP": "VFP",
+             "vfi": "VFI", "Pj": "PJ", "Pc": "PC", "S": "S", "phaseExist": "PHASE_EXIST", "xij": "XIJ",
+             "rho": "RHO", "xi": "XI", "mu": "MU", "rhoP": "RHOP", "xiP": "XIP", "muP": "MUP", "rhox": "RHOX",
+             "xix": "XIX", "mux": "MUX", "kr": "KR", "dKrdS": "DKRDS", "dPcdS": "DPCDS",
+             "dSec_dPri": "DSEC_DPRI", "poro": "PORO", "poroP": "POROP", "rockVp": "ROCKVP",
+             "skip_flag": "SKIP_FLAG", "skip_minEigen": "SKIP_MINEIG", "skip_P": "SKIP_P", "skip_T": "SKIP_T",
+             "skip_zi": "SKIP_ZI"}
+
+
+class Table(C.Structure):
+    _fields_ = [("nrow", C.c_int), ("ncol", C.c_int), ("data", C.POINTER(C.c_double))]
+
+
+class ModelDesc(C.Structure):
+    _fields_ = [("mixture", C.c_int), ("nc", C.c_int),
+                ("gravity_factor", C.c_double), ("conv_darcy", C.c_double), ("gas_constant", C.c_double),
+                ("conv1", C.c_double), ("conv3", C.c_double), ("conv4", C.c_double),
+                ("rock_pref", C.c_double), ("rock_cp1", C.c_double), ("rock_cp2", C.c_double),
+                ("swof", Table), ("sgof", Table), ("pvtw", Table), ("pvco", Table), ("pvdg", Table),
+                ("std_rho_o", C.c_double), ("std_rho_g", C.c_double), ("std_rho_w", C.c_double),
+                ("std_vo", C.c_double), ("std_vg", C.c_double), ("std_vw", C.c_double),
+                ("Tc", C.POINTER(C.c_double)), ("Pc", C.POINTER(C.c_double)), ("Vc", C.POINTER(C.c_double)),
+                ("MW", C.POINTER(C.c_double)), ("OmegaA", C.POINTER(C.c_double)),
+                ("OmegaB", C.POINTER(C.c_double)), ("acf", C.POINTER(C.c_double)), ("BIC", C.POINTER(C.c_double)),
+                ("Vshift", C.POINTER(C.c_double)), ("Vcvis", C.POINTER(C.c_double)),
+                ("lbc_coef", C.POINTER(C.c_double)), ("flash_ctrl", C.POINTER(C.c_double)),
+                ("skip_psa", C.c_int)]
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("nb", C.c_int), ("nconn", C.c_int), ("v", C.POINTER(C.c_double)),
+                ("depth", C.POINTER(C.c_double)), ("poro_init", C.POINTER(C.c_double)),
+                ("conn_b", C.POINTER(C.c_uint32)), ("conn_e", C.POINTER(C.c_uint32)),
+                ("conn_trans", C.POINTER(C.c_double))]
+
+
+class Report(C.Structure):
+    _fields_ = [("status_or", C.c_uint32), ("n_two_phase", C.c_int), ("n_flagged", C.c_int)]
+
+
+class Norms(C.Structure):
+    _fields_ = [("maxRelRes_V", C.c_double), ("maxRelRes_N", C.c_double), ("maxId_V", C.c_int),
+                ("maxId_N", C.c_int)]
+
+
+EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy", "ocpx_set_field",
+           "ocpx_get_field", "ocpx_update_properties", "ocpx_calres", "ocpx_assemble", "ocpx_newton_update",
+           "ocpx_update_last_step", "ocpx_synchronize", "ocpx_jacobian_dims", "ocpx_get_jacobian",
+           "ocpx_jacobian_device", "ocpx_set_variant", "ocpx_step", "ocpx_stream", "ocpx_launch_count"]
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load libocpx_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with opencaeporox_gb300.build.build()")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    lib.ocpx_abi_version.restype = C.c_int
+    lib.ocpx_last_error.restype = C.c_char_p
+    lib.ocpx_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(GridDesc), C.c_int, C.POINTER(P)]
+    lib.ocpx_destroy.argtypes = [P]
+    lib.ocpx_set_field.argtypes = [P, C.c_int, P, C.c_size_t]
+    lib.ocpx_get_field.argtypes = [P, C.c_int, P, C.c_size_t]
+    lib.ocpx_update_properties.argtypes = [P, C.POINTER(Report)]
+    lib.ocpx_calres.argtypes = [P, C.c_double, C.POINTER(Norms)]
+    lib.ocpx_assemble.argtypes = [P, C.c_double]
+    lib.ocpx_newton_update.argtypes = [P, P, C.c_double]
+    lib.ocpx_update_last_step.argtypes = [P]
+    lib.ocpx_synchronize.argtypes = [P]
+    lib.ocpx_jacobian_dims.argtypes = [P, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.POINTER(C.c_int)]
+    lib.ocpx_get_jacobian.argtypes = [P, P, P, P]
+    lib.ocpx_set_variant.argtypes = [P, C.c_int]
+    lib.ocpx_step.argtypes = [P, P, C.c_double, C.c_double, P, P, C.POINTER(Report)]
+    lib.ocpx_stream.argtypes = [P]
+    lib.ocpx_stream.restype = P
+    lib.ocpx_launch_count.argtypes = [P]
+    lib.ocpx_launch_count.restype = C.c_uint64
+    for fn in EXPORTS:
+        if fn not in ("ocpx_abi_version", "ocpx_last_error", "ocpx_stream", "ocpx_launch_count", "ocpx_destroy"):
+            getattr(lib, fn).restype = C.c_int
+    lib.ocpx_destroy.restype = None
+    _lib = lib
+    return lib
+
+
+class OcpxError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def _check(st: int):
+    if st != OCPX_OK:
+        raise OcpxError(st, load_library().ocpx_last_error().decode())
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+# ---------------------------------------------------------------- models ---
+@dataclass
+class Model:
+    """ParamReservoir-level description: unit constants, rock, saturation and
+    PVT tables, and for compositional models the EoS component data."""
+    arrays: dict  # name -> np.ndarray, in the reference's storage
+
+    @property
+    def compositional(self) -> bool:
+        return int(np.asarray(self.arrays["mixture_comp"]).ravel()[0]) == 1
+
+    @property
+    def nc(self) -> int:
+        return int(np.asarray(self.arrays["nc"]).ravel()[0])
+
+    def desc(self):
+        """Build the C model description; returns (ModelDesc, keep-alive list)."""
+        a = self.arrays
+        keep = []
+
+        def arr(name):
+            v = np.ascontiguousarray(np.asarray(a[name], dtype=np.float64).ravel())
+            keep.append(v)
+            return v
+
+        def table(name, ncol):
+            if name not in a:
+                return Table(0, 0, None)
+            v = arr(name)
+            nrow = int(np.asarray(a[name + "_nrow"]).ravel()[0])
+            assert v.size == nrow * ncol, name
+            return Table(nrow, ncol, _dptr(v))
+
+        def scal(name, default=0.0):
+            return float(np.asarray(a[name]).ravel()[0]) if name in a else default
+
+        md = ModelDesc()
+        md.mixture = 1 if self.compositional else 0
+        md.nc = self.nc
+        md.gravity_factor = scal("GRAVITY_FACTOR")
+        md.conv_darcy = scal("CONV_DARCY")
+        md.gas_constant = scal("GAS_CONSTANT")
+        md.conv1 = scal("CONV1")
+        md.conv3 = scal("CONV3")
+        md.conv4 = scal("CONV4")
+        md.rock_pref = scal("rock_Pref")
+        md.rock_cp1 = scal("rock_cp1")
+        md.rock_cp2 = scal("rock_cp2")
+        md.swof = table("SWOF", 4)
+        md.sgof = table("SGOF", 4)
+        md.pvtw = table("PVTW", 5)
+        md.std_rho_w = scal("stdRhoW")
+        md.std_vw = scal("stdVw", 1.0)
+        if self.compositional:
+            for nm in ("Tc", "Pc", "Vc", "OmegaA", "OmegaB", "acf", "BIC", "Vshift", "Vcvis"):
+                setattr(md, nm, _dptr(arr(nm)))
+            md.MW = _dptr(arr("MWC"))
+            md.lbc_coef = _dptr(arr("LBCcoef"))
+            md.flash_ctrl = _dptr(arr("flash_ctrl"))
+            md.skip_psa = int(scal("skipPSA", 1))
+        else:
+            md.pvco = table("PVCO", 6)
+            md.pvdg = table("PVDG", 3)
+            md.std_rho_o = scal("stdRhoO")
+            md.std_rho_g = scal("stdRhoG")
+            md.std_vo = scal("stdVo", 1.0)
+            md.std_vg = scal("stdVg", 1.0)
+        return md, keep
+
+
+@dataclass
+class Grid:
+    """Bulk geometry and the connection list (bId < eId pairs in the
+    reference's order) with transmissibilities."""
+    v: np.ndarray
+    depth: np.ndarray
+    poro_init: np.ndarray
+    conn_b: np.ndarray
+    conn_e: np.ndarray
+    conn_trans: np.ndarray
+
+    @property
+    def nb(self):
+        return len(self.v)
+
+    @property
+    def nconn(self):
+        return len(self.conn_b)
+
+    def desc(self):
+        keep = [np.ascontiguousarray(self.v, np.float64), np.ascontiguousarray(self.depth, np.float64),
+                np.ascontiguousarray(self.poro_init, np.float64), np.ascontiguousarray(self.conn_b, np.uint32),
+                np.ascontiguousarray(self.conn_e, np.uint32), np.ascontiguousarray(self.conn_trans, np.float64)]
+        g = GridDesc(self.nb, self.nconn, _dptr(keep[0]), _dptr(keep[1]), _dptr(keep[2]),
+                     keep[3].ctypes.data_as(C.POINTER(C.c_uint32)), keep[4].ctypes.data_as(C.POINTER(C.c_uint32)),
+                     _dptr(keep[5]))
+        return g, keep
+
+
+def model_and_grid_from_dump(arrays: dict, prefix: str = "model/"):
+    """Model + Grid from the model dump of the reference (ParamReservoir,
+    Bulk and BulkConn after setup), e.g. a golden fixture's ``model/*``."""
+    m = {k[len(prefix):]: v for k, v in arrays.items() if k.startswith(prefix)}
+    model = Model(m)
+    grid = Grid(m["v"], m["depth"], m["poroInit"], m["conn_bId"], m["conn_eId"], m["conn_trans"])
+    return model, grid
+
+
+# --------------------------------------------------------------- context ---
+class FimContext:
+    """One GPU context holding the bulk state of a grid."""
+
+    def __init__(self, model: Model, grid: Grid, device: int = -1, variant: int = 0):
+        self.lib = load_library()
+        self.model = model
+        self.grid = grid
+        self.nb = grid.nb
+        self.np = 3
+        self.nc = model.nc
+        self.nconn = grid.nconn
+        self.NC = self.nc - 1 if model.compositional else 0
+        md, k1 = model.desc()
+        gd, k2 = grid.desc()
+        h = C.c_void_p()
+        _check(self.lib.ocpx_create(C.byref(md), C.byref(gd), device, C.byref(h)))
+        self.h = h
+        if variant:
+            self.set_variant(variant)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ocpx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- fields
+    def field_size(self, name: str) -> int:
+        nb, np_, nc, nconn = self.nb, self.np, self.nc, self.nconn
+        w = {"P": 1, "T": 1, "PB": 1, "NI": nc, "LNI": nc, "NT": 1, "VF": 1, "VFP": 1, "VFI": nc, "PJ": np_,
+             "PC": np_, "S": np_, "PHASE_EXIST": np_, "XIJ": np_ * nc, "RHO": np_, "XI": np_, "MU": np_,
+             "RHOP": np_, "XIP": np_, "MUP": np_, "RHOX": np_ * nc, "XIX": np_ * nc, "MUX": np_ * nc, "KR": np_,
+             "DKRDS": np_ * np_, "DPCDS": np_ * np_, "DSEC_DPRI": np_ * (nc + 1) * (nc + 1), "PORO": 1,
+             "POROP": 1, "ROCKVP": 1, "SKIP_FLAG": 1, "SKIP_MINEIG": 1, "SKIP_P": 1, "SKIP_T": 1,
+             "SKIP_ZI": max(self.NC, 1), "STATUS": 1, "FTYPE": 1, "FLASH_ITERS": 5, "RES": nc + 1,
+             "RES_REL_V": 1, "RES_REL_N": 1}
+        cw = {"UPBLOCK": np_, "CONN_DP": np_, "FLUX_VJ": np_, "FLUX_NI": nc}
+        if name in cw:
+            return nconn * cw[name]
+        return nb * w[name]
+
+    def set(self, name: str, values):
+        dt = FIELD_DTYPE.get(name, np.float64)
+        a = np.ascontiguousarray(np.asarray(values).astype(dt, copy=False).ravel())
+        _check(self.lib.ocpx_set_field(self.h, FIELD_ID[name], a.ctypes.data_as(C.c_void_p), a.size))
+
+    def get(self, name: str) -> np.ndarray:
+        dt = FIELD_DTYPE.get(name, np.float64)
+        out = np.empty(self.field_size(name), dtype=dt)
+        _check(self.lib.ocpx_get_field(self.h, FIELD_ID[name], out.ctypes.data_as(C.c_void_p), out.size))
+        return out
+
+    def load_state(self, state: dict, skip_missing: bool = True):
+        """Upload arrays named as in BulkVarSet (P, Ni, S, xij, phaseExist, ...)."""
+        for ref_name, fid in REF_NAMES.items():
+            if ref_name not in state:
+                if not skip_missing:
+                    raise KeyError(ref_name)
+                continue
+            v = np.asarray(state[ref_name])
+            if fid == "SKIP_ZI" and self.NC == 0:
+                continue
+            if v.size != self.field_size(fid):
+                continue
+            self.set(fid, v)
+
+    # ---- Newton step pieces
+    def update_property(self) -> Report:
+        rep = Report()
+        _check(self.lib.ocpx_update_properties(self.h, C.byref(rep)))
+        return rep
+
+    def cal_res(self, dt: float) -> Norms:
+        n = Norms()
+        _check(self.lib.ocpx_calres(self.h, float(dt), C.byref(n)))
+        return n
+
+    def assemble_mat(self, dt: float):
+        _check(self.lib.ocpx_assemble(self.h, float(dt)))
+        _check(self.lib.ocpx_synchronize(self.h))
+
+    def get_solution(self, u, dSmax: float):
+        a = np.ascontiguousarray(np.asarray(u, dtype=np.float64)[: self.nb * (self.nc + 1)])
+        _check(self.lib.ocpx_newton_update(self.h, a.ctypes.data_as(C.c_void_p), float(dSmax)))
+        _check(self.lib.ocpx_synchronize(self.h))
+
+    def update_last_time_step(self):
+        _check(self.lib.ocpx_update_last_step(self.h))
+
+    def set_variant(self, v: int):
+        _check(self.lib.ocpx_set_variant(self.h, int(v)))
+
+    def jacobian(self):
+        nrow, nnz, bd = C.c_size_t(), C.c_size_t(), C.c_int()
+        _check(self.lib.ocpx_jacobian_dims(self.h, C.byref(nrow), C.byref(nnz), C.byref(bd)))
+        rp = np.empty(nrow.value + 1, np.uint32)
+        col = np.empty(nnz.value, np.uint32)
+        val = np.empty(nnz.value * bd.value * bd.value, np.float64)
+        _check(self.lib.ocpx_get_jacobian(self.h, rp.ctypes.data_as(C.c_void_p), col.ctypes.data_as(C.c_void_p),
+                                          val.ctypes.data_as(C.c_void_p)))
+        return rp, col, val
+
+    def step(self, u=None, dSmax=0.2, dt=1.0, res_out=None, jac_out=None):
+        rep = Report()
+        up = None
+        if u is not None:
+            u = np.ascontiguousarray(u, dtype=np.float64)
+            up = u.ctypes.data_as(C.c_void_p)
+        rp = res_out.ctypes.data_as(C.c_void_p) if res_out is not None else None
+        jp = jac_out.ctypes.data_as(C.c_void_p) if jac_out is not None else None
+        _check(self.lib.ocpx_step(self.h, up, float(dSmax), float(dt), rp, jp, C.byref(rep)))
+        return rep
+
+    @property
+    def stream(self):
+        return self.lib.ocpx_stream(self.h)
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.ocpx_launch_count(self.h))

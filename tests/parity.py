@@ -1,0 +1,103 @@
+"""Parity checks of the FIM Newton-step path against golden fixtures dumped
+from the reference simulator (tests/golden/*.npz, made by gen_fixtures.py).
+
+Each fixture iteration ``itNNN`` holds:
+  * ``jac_state``: the bulk state the Jacobian of that iteration was assembled
+    from, with the residual (``res_bulk``), connection arrays and Jacobian;
+  * ``pre``: the state entering IsoT_FIM::UpdateProperty (after
+    GetSolution), plus the Newton update ``u`` and ``dSmax`` that produced it;
+  * ``post``: the state, connection arrays and residual leaving it.
+
+Tolerances: integer data (phase labels, upwind choices, sparsity pattern) must
+match exactly; floating-point values within REL_TOL relative error, measured
+as |a - b| / max(|b|, floor) with floor = ABS_FLOOR_FRAC * max|b| of the array.
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+REL_TOL = 1e-10          # spec target for floating-point parity
+ABS_FLOOR_FRAC = 1e-12   # values below this fraction of the array scale compare absolutely
+
+PHASE_KEYS = ["rho", "xi", "mu", "rhoP", "xiP", "muP"]
+PHASE_COMP_KEYS = ["xij", "rhox", "xix", "mux"]
+CELL_KEYS = ["Nt", "vf", "vfP", "vfi", "S", "dSec_dPri", "kr", "Pc", "Pj", "dKrdS", "dPcdS", "poro", "poroP",
+             "rockVp"]
+
+
+def load_fixture(name: str) -> dict:
+    with np.load(os.path.join(GOLDEN, name + ".npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+def group(fx: dict, prefix: str) -> dict:
+    p = prefix.rstrip("/") + "/"
+    return {k[len(p):]: v for k, v in fx.items() if k.startswith(p)}
+
+
+def iterations(fx: dict):
+    return sorted({k.split("/")[0] for k in fx if k.startswith("it")})
+
+
+def jac_state(fx: dict, it: str) -> dict:
+    js = group(fx, it + "/jac_state")
+    if "from_post" in js:
+        src = "it%03d/post" % int(np.asarray(js["from_post"]).ravel()[0])
+        base = group(fx, src)
+        base.update({k: v for k, v in js.items()})
+        return base
+    return js
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    if a.size == 0:
+        return 0.0
+    scale = np.max(np.abs(b)) if b.size else 0.0
+    floor = max(scale * ABS_FLOOR_FRAC, 1e-300)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor)))
+
+
+def phase_mask(pe, np_=3):
+    return np.asarray(pe).reshape(-1, np_).astype(bool)
+
+
+class Mismatch(AssertionError):
+    pass
+
+
+def compare_state(got: dict, ref: dict, nc: int, np_: int = 3, tol: float = REL_TOL, report=None):
+    """Compare property-update outputs; returns {name: rel_err}."""
+    errs = {}
+    pe_ref = phase_mask(ref["phaseExist"], np_)
+    pe_got = phase_mask(got["phaseExist"], np_)
+    nbad = int(np.sum(np.any(pe_ref != pe_got, axis=1)))
+    errs["phaseExist_mismatch_cells"] = nbad
+    ok_cells = ~np.any(pe_ref != pe_got, axis=1)
+    for k in CELL_KEYS:
+        if k in ref and k in got:
+            r = np.asarray(ref[k]).reshape(len(ok_cells), -1)[ok_cells]
+            g = np.asarray(got[k]).reshape(len(ok_cells), -1)[ok_cells]
+            errs[k] = rel_err(g, r)
+    for k in PHASE_KEYS:
+        if k in ref and k in got:
+            m = pe_ref & ok_cells[:, None]
+            errs[k] = rel_err(np.asarray(got[k]).reshape(-1, np_)[m], np.asarray(ref[k]).reshape(-1, np_)[m])
+    for k in PHASE_COMP_KEYS:
+        if k in ref and k in got:
+            m = pe_ref & ok_cells[:, None]
+            errs[k] = rel_err(np.asarray(got[k]).reshape(-1, np_, nc)[m], np.asarray(ref[k]).reshape(-1, np_, nc)[m])
+    return errs
+
+
+def state_from_ctx(ctx, keys=None) -> dict:
+    names = {"Nt": "NT", "vf": "VF", "vfP": "VFP", "vfi": "VFI", "S": "S", "phaseExist": "PHASE_EXIST",
+             "xij": "XIJ", "rho": "RHO", "xi": "XI", "mu": "MU", "rhoP": "RHOP", "xiP": "XIP", "muP": "MUP",
+             "rhox": "RHOX", "xix": "XIX", "mux": "MUX", "dSec_dPri": "DSEC_DPRI", "kr": "KR", "Pc": "PC",
+             "Pj": "PJ", "dKrdS": "DKRDS", "dPcdS": "DPCDS", "poro": "PORO", "poroP": "POROP", "rockVp": "ROCKVP",
+             "P": "P", "Ni": "NI"}
+    return {k: ctx.get(v) for k, v in names.items() if keys is None or k in keys}

@@ -1,0 +1,138 @@
+"""GPU parity of the FIM Newton-step kernels against the reference simulator.
+
+The golden fixtures were produced by the reference's own C++ (see
+tests/golden/gen_fixtures.py); every test here calls the CUDA library through
+its C ABI and compares with them.
+
+Tolerances (REL_TOL = 1e-10 from tests/parity.py):
+  * exact: phase-existence labels, flash types, skip flags, upwind choices,
+    Jacobian sparsity pattern and block order, Newton-update results;
+  * elementwise <= REL_TOL: phase properties, saturations, kr/Pc, rock,
+    residual, fluxes, residual norms;
+  * per-cell normwise <= REL_TOL for the quantities obtained from the NC x NC
+    derivative solve (vfi, vfP, dSec_dPri): the reference solves it with
+    LAPACK dgesv from OpenBLAS, whose rounding differs from any other LU;
+  * Jacobian values normwise per block row <= REL_TOL (dgemm rounding);
+  * SkipPSA minimum eigenvalue <= 1e-4 relative: the reference computes it in
+    single precision (ssyevd_).
+"""
+import numpy as np
+import pytest
+
+import parity as P
+from opencaeporox_gb300 import fim
+
+pytestmark = pytest.mark.gpu
+
+FIXTURES = ["bo_10x10x3", "comp6_8x8x3", "comp8_6x6x4"]
+SOLVE_KEYS = ("vfi", "vfP", "dSec_dPri")
+
+
+def cellwise(a, b, nb):
+    a = np.asarray(a, np.float64).reshape(nb, -1)
+    b = np.asarray(b, np.float64).reshape(nb, -1)
+    return float(np.max(np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)))
+
+
+def make_ctx(fx, variant=0):
+    model, grid = fim.model_and_grid_from_dump(fx)
+    return fim.FimContext(model, grid, variant=variant), model, grid
+
+
+def check_update(ctx, fx, it, model, grid):
+    pre = P.group(fx, it + "/pre")
+    post = P.group(fx, it + "/post")
+    js = P.jac_state(fx, it)
+    ctx.load_state(js)
+    ctx.load_state(pre)
+    ctx.update_property()
+    got = P.state_from_ctx(ctx)
+    nb = grid.nb
+    pe_g = got["phaseExist"].reshape(nb, 3)
+    pe_r = post["phaseExist"].reshape(nb, 3)
+    assert np.array_equal(pe_g, pe_r), f"{it}: phase labels differ in {np.sum(np.any(pe_g != pe_r, 1))} cells"
+    errs = P.compare_state(got, post, model.nc)
+    for k in SOLVE_KEYS:
+        errs.pop(k, None)
+        errs[k + "_cellwise"] = cellwise(got[k], post[k], nb)
+    if "flash_ftype" in post and model.compositional:
+        assert np.array_equal(ctx.get("FTYPE"), post["flash_ftype"].astype(np.int8)), f"{it}: flash types differ"
+        assert np.array_equal(ctx.get("SKIP_FLAG"), post["skip_flag"].astype(np.uint8)), f"{it}: skip flags differ"
+        ref = post["skip_minEigen"]
+        m = post["skip_flag"].astype(bool)
+        assert P.rel_err(ctx.get("SKIP_MINEIG")[m], ref[m]) < 1e-4
+    norms = ctx.cal_res(float(pre["dt"][0]))
+    assert np.array_equal(ctx.get("UPBLOCK"), post["upblock"]), f"{it}: upwind choices differ"
+    errs["res"] = P.rel_err(ctx.get("RES"), post["res_bulk"])
+    errs["flux_ni"] = P.rel_err(ctx.get("FLUX_NI"), post["flux_ni"])
+    errs["dP"] = P.rel_err(ctx.get("CONN_DP"), post["dP"])
+    errs["resRelV"] = P.rel_err(ctx.get("RES_REL_V"), post["resRelV"])
+    errs["maxRelRes_V"] = P.rel_err([norms.maxRelRes_V], post["maxRelRes_V"])
+    assert norms.maxId_V == int(post["maxId_V"][0]) and norms.maxId_N == int(post["maxId_N"][0])
+    errs.pop("phaseExist_mismatch_cells")
+    bad = {k: v for k, v in errs.items() if v > P.REL_TOL}
+    assert not bad, f"{it}: {bad}"
+    return errs
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_property_update_and_residual(gpu_lib, name):
+    fx = P.load_fixture(name)
+    its = [it for it in P.iterations(fx) if "P" in P.group(fx, it + "/post")]
+    assert its
+    ctx, model, grid = make_ctx(fx)
+    with ctx:
+        for it in its:
+            check_update(ctx, fx, it, model, grid)
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_jacobian(gpu_lib, name):
+    fx = P.load_fixture(name)
+    ctx, model, grid = make_ctx(fx)
+    bs = (model.nc + 1) ** 2
+    with ctx:
+        for it in P.iterations(fx):
+            js = P.jac_state(fx, it)
+            dt = float(js["dt"][0])
+            ctx.load_state(js)
+            ctx.cal_res(dt)
+            assert np.array_equal(ctx.get("UPBLOCK"), js["upblock"])
+            assert P.rel_err(ctx.get("RES"), js["res_bulk"]) <= P.REL_TOL
+            ctx.assemble_mat(dt)
+            rp, col, val = ctx.jacobian()
+            assert np.array_equal(rp, js["jac_rowptr"]) and np.array_equal(col, js["jac_col"]), f"{it}: pattern"
+            ref = js["jac_val"]
+            # normwise per block row
+            for r in range(grid.nb):
+                a, b = val[rp[r] * bs: rp[r + 1] * bs], ref[rp[r] * bs: rp[r + 1] * bs]
+                e = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+                assert e <= P.REL_TOL, f"{it} row {r}: {e:.2e}"
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_newton_update(gpu_lib, name):
+    fx = P.load_fixture(name)
+    ctx, model, grid = make_ctx(fx)
+    with ctx:
+        for it in P.iterations(fx):
+            pre = P.group(fx, it + "/pre")
+            if not pre:
+                continue
+            ctx.load_state(P.jac_state(fx, it))
+            ctx.get_solution(pre["u"], float(pre["dSmax"][0]))
+            for k, f in (("P", "P"), ("Ni", "NI"), ("S", "S"), ("xij", "XIJ")):
+                assert np.array_equal(ctx.get(f), pre[k]), f"{it}: {k}"
+
+
+def test_batched_variant_matches_plain(gpu_lib):
+    fx = P.load_fixture("comp8_6x6x4")
+    it = [it for it in P.iterations(fx) if "P" in P.group(fx, it + "/post")][0]
+    outs = []
+    for variant in (0, 1):
+        ctx, model, grid = make_ctx(fx, variant)
+        with ctx:
+            check_update(ctx, fx, it, model, grid)
+            outs.append({k: ctx.get(k) for k in ("S", "XIJ", "DSEC_DPRI", "RES")})
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k], outs[1][k]), k

@@ -1,0 +1,339 @@
+#!/usr/bin/env python3
+"""FIM Newton-step throughput on GB300: cells/s of one Newton iteration of
+the compositional PR-EoS path (property update with flash and FlashDer,
+kr/Pc, rock, flux, residual and block-CSR Jacobian), batched GPU form vs the
+plain per-kernel form, beside the reference algorithm on the host cores.
+
+Workload (the compositional single-Newton-step case): 60 x 60 x 10 = 36,000
+cells, 6 seeded pseudo-components, per-cell feed z ~ Dirichlet(2), P ~
+U(10, 30) MPa, T = 345 K, 50 mD, porosity 0.2, PTN start; the timed step is a
+Newton iteration after a seeded Newton update of that state.  Wells are
+host-side in the reference design and not part of the GPU step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  value = device-resident cells/s of the
+batched form (CUDA events on the library's stream, L2 flushed between
+steps); e2e = the same metric through the C ABI with host buffers (pinned
+Newton update in, residual and Jacobian values out) inside the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX, NY, NZ, NCOMP, SEED = 60, 60, 10, 6, 2
+DT, DSMAX = 0.1, 0.2
+METRIC = "FIM Newton-step cells/s (flash+assembly), batched vs plain GPU, <=1e-10 rel err"
+WORKLOAD = "compositional PR-EoS FIM, 6 components, 60x60x10 = 36000 cells, single Newton step"
+
+
+# ------------------------------------------------------------ CUDA runtime --
+class Cudart:
+    def __init__(self):
+        for name in ("libcudart.so", "libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"):
+            try:
+                self.rt = C.CDLL(name)
+                break
+            except OSError:
+                continue
+        else:
+            raise RuntimeError("libcudart not found")
+        rt = self.rt
+        rt.cudaEventCreate.argtypes = [C.POINTER(C.c_void_p)]
+        rt.cudaEventRecord.argtypes = [C.c_void_p, C.c_void_p]
+        rt.cudaEventSynchronize.argtypes = [C.c_void_p]
+        rt.cudaEventElapsedTime.argtypes = [C.POINTER(C.c_float), C.c_void_p, C.c_void_p]
+        rt.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+        rt.cudaMallocHost.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+        rt.cudaMemsetAsync.argtypes = [C.c_void_p, C.c_int, C.c_size_t, C.c_void_p]
+        rt.cudaStreamSynchronize.argtypes = [C.c_void_p]
+        rt.cudaSetDevice.argtypes = [C.c_int]
+
+    def event(self):
+        e = C.c_void_p()
+        assert self.rt.cudaEventCreate(C.byref(e)) == 0
+        return e
+
+    def elapsed_ms(self, a, b):
+        self.rt.cudaEventSynchronize(b)
+        ms = C.c_float()
+        assert self.rt.cudaEventElapsedTime(C.byref(ms), a, b) == 0
+        return ms.value
+
+    def malloc(self, nbytes):
+        p = C.c_void_p()
+        assert self.rt.cudaMalloc(C.byref(p), nbytes) == 0
+        return p
+
+    def pinned(self, n, dtype=np.float64):
+        p = C.c_void_p()
+        nbytes = int(n * np.dtype(dtype).itemsize)
+        assert self.rt.cudaMallocHost(C.byref(p), nbytes) == 0
+        buf = (C.c_char * nbytes).from_address(p.value)
+        return np.frombuffer(buf, dtype=dtype, count=n)
+
+
+# ----------------------------------------------------------------- clocks ---
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- workload --
+def build_workload(variant, device=0):
+    from opencaeporox_gb300 import synthetic
+    from opencaeporox_gb300.fim import FimContext
+    model = synthetic.comp_model(NCOMP, SEED)
+    grid = synthetic.comp_grid(NX, NY, NZ)
+    st = synthetic.comp_initial_state(grid, NCOMP, SEED)
+    ctx = FimContext(model, grid, device=device, variant=variant)
+    ctx.load_state(st)
+    ctx.update_property()  # PTN start: FlashDer with no phase history (MixtureUnit::InitFlashFIM)
+    # scale the moles so the fluid fills the pores, then flash again from scratch
+    scale = ctx.get("ROCKVP") / ctx.get("VF")
+    Ni = (st["Ni"].reshape(grid.nb, -1) * scale[:, None]).ravel()
+    st.update(Ni=Ni, lNi=Ni, Nt=Ni.reshape(grid.nb, -1).sum(axis=1))
+    ctx.load_state(st)
+    ctx.set("SKIP_FLAG", np.zeros(grid.nb, np.uint8))
+    ctx.update_property()
+    ctx.cal_res(DT)
+    ctx.update_last_time_step()
+    ctx.checkpoint(1)  # start of the time step
+    rng = np.random.default_rng(SEED + 77)
+    u = np.zeros((grid.nb, NCOMP + 2))
+    u[:, 0] = rng.normal(0.0, 2.0, grid.nb)
+    u[:, 1:] = Ni.reshape(grid.nb, -1) * rng.normal(0.0, 2e-3, (grid.nb, NCOMP + 1))
+    u = u.ravel()
+    ctx.get_solution(u, DSMAX)
+    ctx.checkpoint(0)  # Newton-iteration input
+    return ctx, model, grid, u
+
+
+def time_device(ctx, rt, steps, warmup, flush):
+    """Device time per step (ms), CUDA events on the library's stream."""
+    stream = C.c_void_p(ctx.stream)
+    e0, e1 = rt.event(), rt.event()
+    times = []
+    launches0 = None
+    for k in range(warmup + steps):
+        ctx.checkpoint(0, restore=True)
+        rt.rt.cudaMemsetAsync(flush[0], k & 0xff, flush[1], stream)
+        if k == warmup:
+            launches0 = ctx.launch_count
+        rt.rt.cudaEventRecord(e0, stream)
+        ctx.enqueue_step(DT)
+        rt.rt.cudaEventRecord(e1, stream)
+        ms = rt.elapsed_ms(e0, e1)
+        rep = ctx.step_report()
+        if rep.status_or & ((1 << 4) | (1 << 5)):
+            raise RuntimeError("physical check failed in the timed step")
+        if k >= warmup:
+            times.append(ms)
+    return times, ctx.launch_count - launches0
+
+
+def time_e2e(ctx, rt, steps, warmup, flush, u):
+    """End to end through the C ABI: pinned u in, residual + Jacobian values out."""
+    stream = C.c_void_p(ctx.stream)
+    nb, nc = ctx.nb, ctx.nc
+    _, nnz_col, _ = None, None, None
+    rp, col, val = ctx.jacobian()
+    u_pin = rt.pinned(u.size)
+    u_pin[:] = u
+    res_pin = rt.pinned(nb * (nc + 1))
+    jac_pin = rt.pinned(val.size)
+    times = []
+    for k in range(warmup + steps):
+        ctx.checkpoint(1, restore=True)
+        rt.rt.cudaMemsetAsync(flush[0], k & 0xff, flush[1], stream)
+        rt.rt.cudaStreamSynchronize(stream)
+        t0 = time.perf_counter()
+        ctx.step(u=u_pin, dSmax=DSMAX, dt=DT, res_out=res_pin, jac_out=jac_pin)
+        t1 = time.perf_counter()
+        if k >= warmup:
+            times.append((t1 - t0) * 1e3)
+    return times, u.nbytes, res_pin.nbytes + jac_pin.nbytes
+
+
+def stage_profile(ctx, rt, flush, reps=3):
+    stream = C.c_void_p(ctx.stream)
+    ctx.profile(True)
+    for k in range(reps):
+        ctx.checkpoint(0, restore=True)
+        rt.rt.cudaMemsetAsync(flush[0], k & 0xff, flush[1], stream)
+        ctx.enqueue_step(DT)
+        ctx.step_report()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    return {k: (v[0] / max(v[1], 1), v[1] // reps) for k, v in prof.items() if v[1]}
+
+
+def cpu_baseline(threads=None):
+    """The reference algorithm (oracle port, C, OpenMP over cells) on the host
+    cores: the same workload and Newton iteration, timed on the host."""
+    from opencaeporox_gb300 import synthetic
+    from oracle.pyoracle import OracleBulk
+    model = synthetic.comp_model(NCOMP, SEED)
+    grid = synthetic.comp_grid(NX, NY, NZ)
+    st = synthetic.comp_initial_state(grid, NCOMP, SEED)
+    ob = OracleBulk(model, grid)
+    ob.load(st)
+    ob.update_property()
+    scale = ob.a["rockVp"] / ob.a["vf"]
+    Ni = (st["Ni"].reshape(grid.nb, -1) * scale[:, None]).ravel()
+    st.update(Ni=Ni, lNi=Ni, Nt=Ni.reshape(grid.nb, -1).sum(axis=1))
+    ob.load(st)
+    ob.a["skip_flag"][:] = 0
+    ob.update_property()
+    ob.cal_res(DT)
+    ob.a["lNi"][:] = ob.a["Ni"]
+    rng = np.random.default_rng(SEED + 77)
+    u = np.zeros((grid.nb, NCOMP + 2))
+    u[:, 0] = rng.normal(0.0, 2.0, grid.nb)
+    u[:, 1:] = Ni.reshape(grid.nb, -1) * rng.normal(0.0, 2e-3, (grid.nb, NCOMP + 1))
+    ob.newton_update(u.ravel(), DSMAX)
+    saved = {k: v.copy() for k, v in ob.a.items()}
+    times = []
+    t_end = time.perf_counter() + 12.0
+    while time.perf_counter() < t_end or len(times) < 2:
+        for k, v in saved.items():
+            ob.a[k][:] = v
+        t0 = time.perf_counter()
+        ob.update_property()
+        ob.cal_res(DT)
+        ob.assemble(DT)
+        times.append(time.perf_counter() - t0)
+        if len(times) >= 50:
+            break
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return grid.nb / statistics.median(times), cores, len(times)
+
+
+def fp64_peak():
+    from opencaeporox_gb300.fim import measure_fp64_tflops
+    return max(measure_fp64_tflops(0, 20000) for _ in range(3))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import build as ob
+        ob.build()
+        v, cores, n = cpu_baseline()
+        line = {"metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": NX * NY * NZ / v * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD}, "impl": "reference",
+                "cpu_baseline": {"value": v, "unit": "cells/s", "cores": cores, "kind": "port",
+                                 "sample": f"full 36000-cell Newton iteration, {n} repetitions, median"},
+                "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    from opencaeporox_gb300 import build as gb
+    gb.build()
+    rt = Cudart()
+    rt.rt.cudaSetDevice(local)
+    flush_bytes = 512 << 20
+    flush = (rt.malloc(flush_bytes), flush_bytes)
+    results = {}
+    for variant in (0, 1):
+        ctx, model, grid, u = build_workload(variant, device=local)
+        t, launches = time_device(ctx, rt, args.steps, args.warmup, flush)
+        prof = stage_profile(ctx, rt, flush)
+        results[variant] = dict(ms=statistics.median(t), mean=statistics.fmean(t), launches=launches / args.steps,
+                                prof=prof, ctx=ctx, u=u)
+    clocks = ClockSampler(local)
+    tb, launches = time_device(results[1]["ctx"], rt, args.steps, args.warmup, flush)
+    ck = clocks.stop()
+    e2e_t, h2d, d2h = time_e2e(results[1]["ctx"], rt, args.steps, args.warmup, flush, results[1]["u"])
+    nb = NX * NY * NZ
+    ms = statistics.median(tb)
+    value = nb / (ms * 1e-3) * world
+    plain = nb / (results[0]["ms"] * 1e-3) * world
+    e2e_ms = statistics.median(e2e_t)
+    prof = results[1]["prof"]
+    dom = max(prof, key=lambda k: prof[k][0])
+    line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "l2": "flushed between steps (512 MiB memset)", "variant": "batched"},
+            "plain_value": plain, "plain_ms_per_step": results[0]["ms"], "batched_over_plain": value / plain,
+            "stages_ms": {k: round(v[0], 4) for k, v in prof.items()}, "dominant_stage": dom,
+            "clocks": ck, "gpu_launches": launches,
+            "e2e": {"value": nb / (e2e_ms * 1e-3) * world, "unit": "cells/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h}}
+    if rank == 0 and world == 1 and os.environ.get("OCPX_BENCH_NO_CPU") != "1":
+        v, cores, n = cpu_baseline()
+        line["cpu_baseline"] = {"value": v, "unit": "cells/s", "cores": cores, "kind": "port",
+                                "sample": f"full 36000-cell Newton iteration, {n} repetitions, median"}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

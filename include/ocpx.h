@@ -211,6 +211,32 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
 ocpx_status ocpx_step(ocpx_ctx* ctx, const double* u_host, double dSmax, double dt, double* res_host,
                       double* jac_val_host, ocpx_report* rep);
 
+/* Asynchronous form of ocpx_step without host buffers: enqueue properties,
+ * residual and Jacobian on the context stream and return at once;
+ * ocpx_step_report then waits and reads the status summary. */
+ocpx_status ocpx_enqueue_step(ocpx_ctx* ctx, double dt);
+ocpx_status ocpx_step_report(ocpx_ctx* ctx, ocpx_report* rep);
+
+/* Per-stage device timing with CUDA events recorded on the context stream.
+ * Stages: 0 physical check, 1 flash, 2 kr/Pc + rock, 3 status summary,
+ * 4 connection flux, 5 residual + norms, 6 Jacobian connection blocks,
+ * 7 Jacobian rows, 8 Newton update.  ocpx_profile_read synchronizes and
+ * returns, per stage, the summed milliseconds and the number of timed
+ * launches since profiling was enabled. */
+#define OCPX_STAGE_COUNT 9
+ocpx_status ocpx_profile_enable(ocpx_ctx* ctx, int enable);
+ocpx_status ocpx_profile_read(ocpx_ctx* ctx, double* ms, uint64_t* launches);
+
+/* Save (restore = 0) or restore (restore = 1) the whole mutable bulk state
+ * (every per-cell array) in device-side slot 0 or 1.  Restoring slot 0 after
+ * saving it at the start of a time step is IsoT_FIM::ResetToLastTimeStep
+ * (src/IsoThermalMethod.cpp:1420-1471) without any host copy. */
+ocpx_status ocpx_checkpoint(ocpx_ctx* ctx, int slot, int restore);
+
+/* Measured FP64 fused multiply-add throughput of the device (TFLOP/s), the
+ * roofline denominator of the FP64-bound flash; iters sets the run length. */
+ocpx_status ocpx_measure_fp64_tflops(int device, int iters, double* tflops);
+
 /* Stream the context launches on (a cudaStream_t), for callers that time or
  * order work around the library. */
 void* ocpx_stream(ocpx_ctx* ctx);

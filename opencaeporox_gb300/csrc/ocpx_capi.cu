@@ -121,6 +121,39 @@ struct ocpx_ctx {
     RowNorm* h_norm = nullptr;      // pinned
     uint64_t launches = 0;
     int block_cell = 128, block_conn = 128, queue_chunk = 1, queue_grid = 0;
+    // per-stage event timing
+    bool prof = false;
+    struct Mark { int stage; cudaEvent_t a, b; };
+    std::vector<Mark> marks;
+    std::vector<cudaEvent_t> free_events;
+    double prof_ms[OCPX_STAGE_COUNT] = {0};
+    uint64_t prof_n[OCPX_STAGE_COUNT] = {0};
+    cudaEvent_t take_event()
+    {
+        if (free_events.empty()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            return e;
+        }
+        cudaEvent_t e = free_events.back();
+        free_events.pop_back();
+        return e;
+    }
+    void stage_begin(int s)
+    {
+        if (!prof) return;
+        Mark m{s, take_event(), take_event()};
+        cudaEventRecord(m.a, stream);
+        marks.push_back(m);
+    }
+    void stage_end()
+    {
+        if (!prof || marks.empty()) return;
+        cudaEventRecord(marks.back().b, stream);
+    }
+    // device-side checkpoints of the mutable bulk state
+    char* ckpt[2] = {nullptr, nullptr};
+    size_t state_off = 0, state_bytes = 0;
     // graph of one Newton iteration (variant 1)
     cudaGraphExec_t graph_exec = nullptr;
     double graph_dt = -1, graph_dSmax = -1;
@@ -305,6 +338,9 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     size_t off = 0;
     for (auto& s : slots) { *s.p = ctx->arena + off; off += align256(s.bytes); }
     cudaMemset(ctx->arena, 0, total);
+    // the per-cell state occupies one contiguous range of the arena: P .. iters
+    ctx->state_off = (size_t)((char*)b.P - ctx->arena);
+    ctx->state_bytes = (size_t)((char*)b.iters + align256(sizeof(int32_t) * (size_t)nb * 5) - (char*)b.P);
 
     auto fail_ctx = [&](ocpx_status s2, const std::string& m) { ocpx_destroy(ctx); return fail(s2, m); };
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -341,6 +377,10 @@ void ocpx_destroy(ocpx_ctx* ctx)
     if (!ctx) return;
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (char* c : ctx->ckpt)
+        if (c) cudaFree(c);
+    for (auto& m : ctx->marks) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
+    for (auto e : ctx->free_events) cudaEventDestroy(e);
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->d_model) cudaFree(ctx->d_model);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
@@ -405,25 +445,32 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
 {
     cudaStream_t s = ctx->stream;
     OCPX_CUDA(cudaMemsetAsync(ctx->flags, 0, sizeof(uint32_t) * 4, s));
+    ctx->stage_begin(0);
     OCPX_CUDA(launch_check(ctx->b, ctx->flags, ctx->block_cell, s));
+    ctx->stage_end();
     ctx->launches++;
+    if (ctx->host_model.mixture == 1 && ctx->variant == 1)
+        OCPX_CUDA(cudaMemsetAsync(ctx->queue_counter, 0, sizeof(unsigned), s));
+    ctx->stage_begin(1);
     if (ctx->host_model.mixture == 1) {
-        if (ctx->variant == 1) {
-            OCPX_CUDA(cudaMemsetAsync(ctx->queue_counter, 0, sizeof(unsigned), s));
+        if (ctx->variant == 1)
             OCPX_CUDA(launch_flash_comp_queue(ctx->ncm, ctx->d_model, ctx->b, ctx->queue_counter, ctx->queue_grid,
                                               ctx->block_cell, ctx->queue_chunk, s));
-        }
-        else {
+        else
             OCPX_CUDA(launch_flash_comp(ctx->ncm, ctx->d_model, ctx->b, ctx->block_cell, s));
-        }
     }
     else {
         OCPX_CUDA(launch_flash_bo(ctx->d_model, ctx->b, ctx->block_cell, s));
     }
+    ctx->stage_end();
     ctx->launches++;
+    ctx->stage_begin(2);
     OCPX_CUDA(launch_krpc_rock(ctx->d_model, ctx->b, ctx->block_cell, s));
+    ctx->stage_end();
     ctx->launches++;
+    ctx->stage_begin(3);
     OCPX_CUDA(launch_report(ctx->b, ctx->flags + 1, ctx->block_cell, s));
+    ctx->stage_end();
     ctx->launches++;
     return OCPX_OK;
 }
@@ -431,9 +478,13 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
 ocpx_status enqueue_calres(ocpx_ctx* ctx, double dt)
 {
     cudaStream_t s = ctx->stream;
+    ctx->stage_begin(4);
     OCPX_CUDA(launch_conn_flux(ctx->d_model, ctx->b, ctx->cv, ctx->block_conn, s));
+    ctx->stage_end();
+    ctx->stage_begin(5);
     OCPX_CUDA(launch_residual(ctx->b, ctx->cv, dt, ctx->res, ctx->resRelV, ctx->resRelN, ctx->rownorm, ctx->norm_out,
                               ctx->block_cell, s));
+    ctx->stage_end();
     ctx->launches += 3;
     return OCPX_OK;
 }
@@ -441,8 +492,12 @@ ocpx_status enqueue_calres(ocpx_ctx* ctx, double dt)
 ocpx_status enqueue_assemble(ocpx_ctx* ctx, double dt)
 {
     cudaStream_t s = ctx->stream;
+    ctx->stage_begin(6);
     OCPX_CUDA(launch_jac_conn(ctx->nct_cap, ctx->d_model, ctx->b, ctx->cv, dt, ctx->bmat, ctx->block_conn, s));
+    ctx->stage_end();
+    ctx->stage_begin(7);
     OCPX_CUDA(launch_jac_rows(ctx->b, ctx->cv, ctx->bmat, ctx->jac_rowptr, ctx->jac_val, ctx->block_cell, s));
+    ctx->stage_end();
     ctx->launches += 2;
     return OCPX_OK;
 }
@@ -504,8 +559,56 @@ ocpx_status ocpx_newton_update(ocpx_ctx* ctx, const double* u_host, double dSmax
     if (!ctx || !u_host) return fail(OCPX_INVALID_ARG, "null argument");
     const size_t bytes = sizeof(double) * (size_t)ctx->nb * (ctx->nc + 1);
     OCPX_CUDA(cudaMemcpyAsync(ctx->u, u_host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->stage_begin(8);
     OCPX_CUDA(launch_newton_update(ctx->b, ctx->u, dSmax, ctx->block_cell, ctx->stream));
+    ctx->stage_end();
     ctx->launches++;
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_enqueue_step(ocpx_ctx* ctx, double dt)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    ocpx_status st;
+    if ((st = enqueue_properties(ctx)) != OCPX_OK) return st;
+    if ((st = enqueue_calres(ctx, dt)) != OCPX_OK) return st;
+    return enqueue_assemble(ctx, dt);
+}
+
+ocpx_status ocpx_step_report(ocpx_ctx* ctx, ocpx_report* rep)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    return report_from_flags(ctx, rep);
+}
+
+ocpx_status ocpx_profile_enable(ocpx_ctx* ctx, int enable)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->prof = enable != 0;
+    for (auto& m : ctx->marks) { ctx->free_events.push_back(m.a); ctx->free_events.push_back(m.b); }
+    ctx->marks.clear();
+    for (int s = 0; s < OCPX_STAGE_COUNT; s++) { ctx->prof_ms[s] = 0; ctx->prof_n[s] = 0; }
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_profile_read(ocpx_ctx* ctx, double* ms, uint64_t* launches)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (auto& m : ctx->marks) {
+        float t = 0;
+        OCPX_CUDA(cudaEventElapsedTime(&t, m.a, m.b));
+        ctx->prof_ms[m.stage] += t;
+        ctx->prof_n[m.stage]++;
+        ctx->free_events.push_back(m.a);
+        ctx->free_events.push_back(m.b);
+    }
+    ctx->marks.clear();
+    for (int s = 0; s < OCPX_STAGE_COUNT; s++) {
+        if (ms) ms[s] = ctx->prof_ms[s];
+        if (launches) launches[s] = ctx->prof_n[s];
+    }
     return OCPX_OK;
 }
 
@@ -514,6 +617,21 @@ ocpx_status ocpx_update_last_step(ocpx_ctx* ctx)
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
     OCPX_CUDA(cudaMemcpyAsync(ctx->b.lNi, ctx->b.Ni, sizeof(double) * (size_t)ctx->nb * ctx->nc,
                               cudaMemcpyDeviceToDevice, ctx->stream));
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_checkpoint(ocpx_ctx* ctx, int slot, int restore)
+{
+    if (!ctx || slot < 0 || slot > 1) return fail(OCPX_INVALID_ARG, "checkpoint slot must be 0 or 1");
+    if (!ctx->ckpt[slot]) {
+        if (restore) return fail(OCPX_INVALID_ARG, "checkpoint slot is empty");
+        OCPX_CUDA(cudaMalloc(&ctx->ckpt[slot], ctx->state_bytes));
+    }
+    char* state = ctx->arena + ctx->state_off;
+    if (restore)
+        OCPX_CUDA(cudaMemcpyAsync(state, ctx->ckpt[slot], ctx->state_bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    else
+        OCPX_CUDA(cudaMemcpyAsync(ctx->ckpt[slot], state, ctx->state_bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     return OCPX_OK;
 }
 

@@ -91,7 +91,9 @@ class Norms(C.Structure):
 EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy", "ocpx_set_field",
            "ocpx_get_field", "ocpx_update_properties", "ocpx_calres", "ocpx_assemble", "ocpx_newton_update",
            "ocpx_update_last_step", "ocpx_synchronize", "ocpx_jacobian_dims", "ocpx_get_jacobian",
-           "ocpx_jacobian_device", "ocpx_set_variant", "ocpx_step", "ocpx_stream", "ocpx_launch_count"]
+           "ocpx_jacobian_device", "ocpx_set_variant", "ocpx_step", "ocpx_enqueue_step", "ocpx_step_report",
+           "ocpx_profile_enable", "ocpx_profile_read", "ocpx_checkpoint", "ocpx_measure_fp64_tflops",
+           "ocpx_stream", "ocpx_launch_count"]
 
 _lib = None
 
@@ -121,6 +123,15 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.ocpx_get_jacobian.argtypes = [P, P, P, P]
     lib.ocpx_set_variant.argtypes = [P, C.c_int]
     lib.ocpx_step.argtypes = [P, P, C.c_double, C.c_double, P, P, C.POINTER(Report)]
+    lib.ocpx_checkpoint.argtypes = [P, C.c_int, C.c_int]
+    lib.ocpx_enqueue_step.argtypes = [P, C.c_double]
+    lib.ocpx_step_report.argtypes = [P, C.POINTER(Report)]
+    lib.ocpx_profile_enable.argtypes = [P, C.c_int]
+    lib.ocpx_profile_read.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
+    lib.ocpx_measure_fp64_tflops.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
+    for fn in ("ocpx_enqueue_step", "ocpx_step_report", "ocpx_profile_enable", "ocpx_profile_read",
+               "ocpx_measure_fp64_tflops", "ocpx_checkpoint"):
+        getattr(lib, fn).restype = C.c_int
     lib.ocpx_stream.argtypes = [P]
     lib.ocpx_stream.restype = P
     lib.ocpx_launch_count.argtypes = [P]
@@ -359,6 +370,39 @@ class FimContext:
 
     def set_variant(self, v: int):
         _check(self.lib.ocpx_set_variant(self.h, int(v)))
+
+    def checkpoint(self, slot: int = 0, restore: bool = False):
+        """Save / restore the whole bulk state on the device (ResetToLastTimeStep)."""
+        _check(self.lib.ocpx_checkpoint(self.h, int(slot), 1 if restore else 0))
+
+    def synchronize(self):
+        _check(self.lib.ocpx_synchronize(self.h))
+
+    def enqueue_step(self, dt: float):
+        """Properties, residual and Jacobian enqueued without waiting."""
+        _check(self.lib.ocpx_enqueue_step(self.h, float(dt)))
+
+    def step_report(self) -> Report:
+        rep = Report()
+        _check(self.lib.ocpx_step_report(self.h, C.byref(rep)))
+        return rep
+
+    STAGES = ["check", "flash", "krpc_rock", "report", "flux", "residual", "jac_conn", "jac_rows", "newton_update"]
+
+    def profile(self, enable: bool = True):
+        _check(self.lib.ocpx_profile_enable(self.h, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        ms = (C.c_double * len(self.STAGES))()
+        n = (C.c_uint64 * len(self.STAGES))()
+        _check(self.lib.ocpx_profile_read(self.h, ms, n))
+        return {s: (ms[i], int(n[i])) for i, s in enumerate(self.STAGES)}
+
+
+def measure_fp64_tflops(device: int = 0, iters: int = 20000) -> float:
+    v = C.c_double()
+    _check(load_library().ocpx_measure_fp64_tflops(device, iters, C.byref(v)))
+    return v.value
 
     def jacobian(self):
         nrow, nnz, bd = C.c_size_t(), C.c_size_t(), C.c_int()

@@ -1,0 +1,110 @@
+"""Seeded synthetic workloads (fluids, grids, initial states) for the bench
+and the large-size tests, built without the reference.
+
+The fluid description is what the reference's setup produces from an
+ECL-style deck in METRIC units with TCRIT/PCRIT/ZCRIT/MW/ACF/BIC and the
+flash-control keywords (ComponentParam, src/ParamReservoir.cpp:710-719;
+EoS_PR, src/OCPEoS.cpp:19-66; OCPPhaseEquilibrium::Setup,
+src/OCPPhaseEquilibrium.cpp:15-69; ViscosityMethod03,
+src/OCPFuncPVT.cpp:415-460; OCPMixtureMethodComp01,
+src/OCPMixtureMethodComp.cpp:650-668), including two of its quirks:
+Vc = GAS_CONSTANT * Zc * Tc / Pc for the phase test, but the LBC critical
+volume falls back to 10.73159 * Zc * Tc / Pc (the FIELD gas constant), and the
+standard water density is RHOW_STD whenever DENSITY is given.
+tests/test_synthetic.py checks these arrays against the reference's own dump.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .fim import Model
+from .grid import orthogonal_grid
+
+# METRIC unit constants (src/OCPUnits.cpp:37-55, include/OCPUnits.hpp:80-101)
+METRIC = dict(GRAVITY_FACTOR=0.0000980665, CONV_DARCY=0.008527, GAS_CONSTANT=0.083143, CONV1=1.0, CONV3=1.0,
+              CONV4=273.15)
+RHOW_STD_METRIC = 999.014
+# flash controls used by the synthetic decks: SSMsta (maxIt, tol, eYt, Ktol, dYtol), NRsta (maxIt, tol),
+# SSMsp (maxIt, tol), NRsp (maxIt, tol), RR (maxIt, tol); Ktol and dYtol are the reference's fixed values
+FLASH_CTRL = [100, 1e-12, 1e-8, 1e-4, 1e-6, 55, 1e-12, 100, 1e-6, 55, 1e-12, 30, 1e-12]
+LBC_DEFAULT = [0.1023, 0.023364, 0.058533, -0.040758, 0.0093324]
+
+
+def seeded_components(ncomp, seed):
+    """Light-to-heavy pseudo-components with seeded Tc [K], Pc [bar], omega,
+    MW, Zc and a symmetric BIC matrix in [0, 0.15] with zero diagonal."""
+    rng = np.random.default_rng(seed)
+    f = np.sort(rng.uniform(0.0, 1.0, ncomp))
+    f[0] = 0.0
+    tc = 190.0 + f * 610.0 + rng.uniform(-10, 10, ncomp)
+    pc = 46.0 - f * 32.0 + rng.uniform(-1.5, 1.5, ncomp)
+    acf = 0.01 + f * 0.9 + rng.uniform(0.0, 0.02, ncomp)
+    mw = 16.0 + f * 300.0 + rng.uniform(0.0, 4.0, ncomp)
+    zc = rng.uniform(0.24, 0.29, ncomp)
+    bic = np.zeros((ncomp, ncomp))
+    for i in range(ncomp):
+        for j in range(i):
+            bic[i, j] = bic[j, i] = rng.uniform(0.0, 0.15)
+    return dict(Tc=tc, Pc=pc, acf=acf, MW=mw, Zc=zc, BIC=bic)
+
+
+def corey_tables(nrow=12, swc=0.2, sor=0.2, n=2.0):
+    """SWOF and SGOF (S, kr_phase, kr_oil, Pc) tabulated from Corey curves."""
+    span = 1.0 - swc - sor
+    sw = np.linspace(swc, 1.0, nrow)
+    krw = np.clip((sw - swc) / span, 0, 1) ** n
+    krow = np.clip((1.0 - sw - sor) / span, 0, 1) ** n
+    swof = np.stack([sw, krw, krow, np.zeros(nrow)], axis=1)
+    sg = np.linspace(0.0, 1.0 - swc, nrow)
+    krg = np.clip(sg / span, 0, 1) ** n
+    krog = np.clip((1.0 - swc - sor - sg) / span, 0, 1) ** n
+    sgof = np.stack([sg, krg, krog, np.zeros(nrow)], axis=1)
+    return swof, sgof
+
+
+def comp_model(ncomp, seed, pvtw=(200.0, 1.01, 4.5e-5, 0.5, 0.0), rock=(200.0, 4.5e-5, 0.0)) -> Model:
+    """PR-EoS fluid + water + Corey kr, as the reference sets it up."""
+    c = seeded_components(ncomp, seed)
+    R = METRIC["GAS_CONSTANT"]
+    swof, sgof = corey_tables()
+    a = dict(METRIC)
+    a.update(mixture_comp=np.array([1]), nc=np.array([ncomp + 1]), NC=np.array([ncomp]),
+             Tc=c["Tc"], Pc=c["Pc"], MWC=c["MW"], acf=c["acf"],
+             Vc=R * c["Zc"] * c["Tc"] / c["Pc"], Vcvis=10.73159 * c["Zc"] * c["Tc"] / c["Pc"],
+             OmegaA=np.full(ncomp, 0.457235529), OmegaB=np.full(ncomp, 0.077796074), Vshift=np.zeros(ncomp),
+             BIC=c["BIC"].ravel(), LBCcoef=np.array(LBC_DEFAULT) * 10, flash_ctrl=np.array(FLASH_CTRL, float),
+             PVTW=np.array(pvtw, float), PVTW_nrow=np.array([1]), stdRhoW=np.array([RHOW_STD_METRIC]),
+             stdVw=np.array([1.0]), SWOF=swof.T.ravel().copy(), SWOF_nrow=np.array([swof.shape[0]]),
+             SGOF=sgof.T.ravel().copy(), SGOF_nrow=np.array([sgof.shape[0]]), rock_Pref=np.array([rock[0]]),
+             rock_cp1=np.array([rock[1]]), rock_cp2=np.array([rock[2]]), skipPSA=np.array([1]))
+    for k in METRIC:
+        a[k] = np.array([METRIC[k]])
+    return Model(a)
+
+
+def comp_initial_state(grid, ncomp, seed, p_range=(100.0, 300.0), alpha=2.0, temp_c=71.85, smooth=False, nx=None):
+    """PTN start: per-cell pressure and moles (hydrocarbons then water) with
+    z ~ Dirichlet(alpha), P ~ U(p_range); hydrocarbons fill 80 % of the pore
+    volume at an assumed Z = 0.6 and water 20 % (Bw ~ 1.01).  Phase state is
+    empty, as BulkInitializer::InitPTNi leaves it (src/BulkInitializer.cpp:104-143)."""
+    rng = np.random.default_rng(seed + 1000)
+    n = grid.nb
+    p = rng.uniform(*p_range, n)
+    if smooth:
+        ix = np.arange(n) % nx
+        p = p_range[0] + (p_range[1] - p_range[0]) * ix / max(nx - 1, 1) + rng.uniform(-1, 1, n)
+    z = rng.dirichlet(np.full(ncomp, alpha), n)
+    vp = grid.v * grid.poro_init
+    vm = 0.6 * METRIC["GAS_CONSTANT"] * (temp_c + 273.15) / p
+    ni = z * (0.8 * vp / vm)[:, None]
+    nw = 0.2 * vp / 1.01
+    Ni = np.concatenate([ni, nw[:, None]], axis=1)
+    return dict(P=p, T=np.full(n, temp_c), Ni=Ni.ravel(), Pj=np.repeat(p, 3), phaseExist=np.zeros(3 * n, np.uint8),
+                S=np.zeros(3 * n), xij=np.zeros(3 * n * (ncomp + 1)), lNi=Ni.ravel().copy(),
+                Nt=Ni.sum(axis=1))
+
+
+def comp_grid(nx, ny, nz, dxy=20.0, dz=5.0, perm=50.0, poro=0.2, tops=2000.0):
+    n = nx * ny * nz
+    return orthogonal_grid(nx, ny, nz, dxy, dxy, dz, tops, np.full(n, perm), np.full(n, perm), np.full(n, perm),
+                           np.full(n, poro), conv_darcy=METRIC["CONV_DARCY"])

@@ -1,0 +1,52 @@
+"""Builds the oracle (test infrastructure, never part of the product).
+
+* ``build()``: the C restatement ocpx_oracle.c -> oracle/_build/liboracle.so
+  (cc -O2 -ffp-contract=off -fopenmp; no FMA contraction, like a baseline
+  x86-64 build of the reference).
+* ``build_reference_if_present()``: where the reference sources exist at
+  REF (this container), the reference itself via oracle/ref/Makefile into
+  oracle/_ref/ (used to regenerate the golden fixtures).
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "liboracle.so")
+REF = os.environ.get("OCPX_REFERENCE_DIR", "/root/reference")
+
+
+def build(force: bool = False) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    src = [os.path.join(HERE, "ocpx_oracle.c")]
+    deps = src + [os.path.join(HERE, "ocpx_oracle.h")]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps):
+        return LIB
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        raise RuntimeError("no C compiler for the oracle")
+    tmp = LIB + ".tmp"
+    cmd = [cc, "-O2", "-g0", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-shared", "-fPIC",
+           "-o", tmp] + src + ["-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def build_reference_if_present() -> str | None:
+    if not os.path.isdir(os.path.join(REF, "src")):
+        return None
+    r = subprocess.run(["make", "-C", os.path.join(HERE, "ref"), "-j8", f"REF={REF}"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference oracle build failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
+    return os.path.join(HERE, "_ref", "ocp_ref_dump")
+
+
+if __name__ == "__main__":
+    print(build(force=True))
+    print(build_reference_if_present())

@@ -398,12 +398,6 @@ class FimContext:
         _check(self.lib.ocpx_profile_read(self.h, ms, n))
         return {s: (ms[i], int(n[i])) for i, s in enumerate(self.STAGES)}
 
-
-def measure_fp64_tflops(device: int = 0, iters: int = 20000) -> float:
-    v = C.c_double()
-    _check(load_library().ocpx_measure_fp64_tflops(device, iters, C.byref(v)))
-    return v.value
-
     def jacobian(self):
         nrow, nnz, bd = C.c_size_t(), C.c_size_t(), C.c_int()
         _check(self.lib.ocpx_jacobian_dims(self.h, C.byref(nrow), C.byref(nnz), C.byref(bd)))
@@ -432,3 +426,10 @@ def measure_fp64_tflops(device: int = 0, iters: int = 20000) -> float:
     @property
     def launch_count(self) -> int:
         return int(self.lib.ocpx_launch_count(self.h))
+
+
+def measure_fp64_tflops(device: int = 0, iters: int = 20000) -> float:
+    """Measured FP64 FMA throughput of the device in TFLOP/s."""
+    v = C.c_double()
+    _check(load_library().ocpx_measure_fp64_tflops(device, iters, C.byref(v)))
+    return v.value

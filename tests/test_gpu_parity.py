@@ -85,6 +85,16 @@ def check_update(ctx, fx, it, model, grid):
     assert norms.maxId_V == int(post["maxId_V"][0]) and norms.maxId_N == int(post["maxId_N"][0])
     errs.pop("phaseExist_mismatch_cells")
     REPORT.setdefault(fx["__name__"], {})[it] = errs
+    # worst cells of the transcendental-heavy outputs, with their flash record
+    st, iters = ctx.get("STATUS"), ctx.get("FLASH_ITERS").reshape(nb, 5)
+    for k in ("mu", "xij"):
+        w = np.asarray(got[k], np.float64).reshape(nb, -1)
+        r = np.asarray(post[k], np.float64).reshape(nb, -1)
+        m = pe_r.astype(bool) if k == "mu" else np.repeat(pe_r.astype(bool), model.nc, axis=1)
+        e = np.where(m, np.abs(w - r) / np.maximum(np.abs(r), 1e-300), 0).max(axis=1)
+        worst = np.argsort(e)[-3:][::-1]
+        REPORT[fx["__name__"]][it + "/" + k + "_worst"] = [
+            [int(c), float(e[c]), int(st[c]), iters[c].tolist(), pe_r[c].tolist()] for c in worst]
     bad = {k: v for k, v in errs.items() if v > P.TOL.get(k, P.REL_TOL)}
     assert not bad, f"{it}: {bad}"
     return errs

@@ -19,23 +19,33 @@ LIB = os.path.join(OUT, "liboracle.so")
 REF = os.environ.get("OCPX_REFERENCE_DIR", "/root/reference")
 
 
-def build(force: bool = False) -> str:
+VARIANTS = {
+    # the restatement itself
+    "exact": ("ocpx_oracle.c", LIB),
+    # the same code with every transcendental result moved by one ulp (ulp_nudge.c):
+    # measures the reference algorithm's sensitivity to libm rounding
+    "ulp": ("ulp_nudge.c", os.path.join(OUT, "liboracle_ulp.so")),
+}
+
+
+def build(force: bool = False, variant: str = "exact") -> str:
     os.makedirs(OUT, exist_ok=True)
-    src = [os.path.join(HERE, "ocpx_oracle.c")]
-    deps = src + [os.path.join(HERE, "ocpx_oracle.h")]
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps):
-        return LIB
+    main, lib = VARIANTS[variant]
+    src = [os.path.join(HERE, main)]
+    deps = [os.path.join(HERE, f) for f in ("ocpx_oracle.c", "ocpx_oracle.h", main)]
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= max(os.path.getmtime(d) for d in deps):
+        return lib
     cc = shutil.which("gcc") or shutil.which("cc")
     if not cc:
         raise RuntimeError("no C compiler for the oracle")
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [cc, "-O2", "-g0", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-shared", "-fPIC",
-           "-o", tmp] + src + ["-lm"]
+           "-I", HERE, "-o", tmp] + src + ["-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 def build_reference_if_present() -> str | None:

@@ -15,14 +15,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 from opencaeporox_gb300.fim import ModelDesc  # noqa: E402  (shared description struct of include/ocpx.h)
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
+def lib(variant="exact"):
+    """The oracle library; variant "ulp" is the one-ulp-perturbed build (oracle/ulp_nudge.c)."""
+    if variant not in _libs:
         from oracle import build
-        path = build.build()
+        path = build.build(variant=variant)
         L = C.CDLL(path)
         P = C.c_void_p
         L.oc_create.argtypes = [C.POINTER(ModelDesc)]
@@ -36,8 +36,10 @@ def lib():
         L.oc_assemble.argtypes = [P, P, P, C.c_double, P, P, P]
         L.oc_assemble.restype = C.c_long
         L.oc_newton_update.argtypes = [P, P, P, C.c_double]
-        _lib = L
-    return _lib
+        if variant == "ulp":
+            L.oc_set_nudge_seed.argtypes = [C.c_uint64]
+        _libs[variant] = L
+    return _libs[variant]
 
 
 D = C.POINTER(C.c_double)
@@ -68,14 +70,15 @@ ALIASES = {"skip_minEigen": "skip_minEig"}
 
 
 class OracleModel:
-    def __init__(self, model):
+    def __init__(self, model, variant="exact"):
         self.model = model
+        self.lib = lib(variant)
         self._md, self._keep = model.desc()
-        self.h = lib().oc_create(C.byref(self._md))
+        self.h = self.lib.oc_create(C.byref(self._md))
 
     def __del__(self):
         try:
-            lib().oc_destroy(self.h)
+            self.lib.oc_destroy(self.h)
         except Exception:
             pass
 
@@ -83,8 +86,9 @@ class OracleModel:
 class OracleBulk:
     """Bulk + connections in the reference layout, driven by the oracle."""
 
-    def __init__(self, model, grid):
-        self.om = OracleModel(model)
+    def __init__(self, model, grid, variant="exact"):
+        self.om = OracleModel(model, variant)
+        self.lib = self.om.lib
         self.nb, self.np, self.nc = grid.nb, 3, model.nc
         self.NC = model.nc - 1 if model.compositional else 0
         dims = {"nc": self.nc, "np": 3, "npnc": 3 * self.nc, "npnp": 9, "lend": 3 * (self.nc + 1) ** 2,
@@ -105,6 +109,10 @@ class OracleBulk:
         self.resRelV = np.zeros(self.nb)
         self.resRelN = np.zeros(self.nb)
         self.norms = np.zeros(4)
+
+    def set_nudge_seed(self, seed: int):
+        """Seed of the one-ulp perturbation pattern (variant "ulp" only)."""
+        self.lib.oc_set_nudge_seed(seed)
 
     def load(self, state: dict):
         for k, v in state.items():
@@ -131,15 +139,15 @@ class OracleBulk:
 
     def check(self) -> int:
         b = self._bulk()
-        return lib().oc_check(self.om.h, C.byref(b))
+        return self.lib.oc_check(self.om.h, C.byref(b))
 
     def flash(self, n0=0, n1=None):
         b = self._bulk()
-        lib().oc_flash(self.om.h, C.byref(b), n0, self.nb if n1 is None else n1)
+        self.lib.oc_flash(self.om.h, C.byref(b), n0, self.nb if n1 is None else n1)
 
     def krpc_rock(self, n0=0, n1=None):
         b = self._bulk()
-        lib().oc_krpc_rock(self.om.h, C.byref(b), n0, self.nb if n1 is None else n1)
+        self.lib.oc_krpc_rock(self.om.h, C.byref(b), n0, self.nb if n1 is None else n1)
 
     def update_property(self) -> int:
         st = self.check()
@@ -149,7 +157,7 @@ class OracleBulk:
 
     def cal_res(self, dt):
         b, c = self._bulk(), self._conn()
-        lib().oc_calres(self.om.h, C.byref(b), C.byref(c), float(dt), self.res.ctypes.data_as(D),
+        self.lib.oc_calres(self.om.h, C.byref(b), C.byref(c), float(dt), self.res.ctypes.data_as(D),
                         self.resRelV.ctypes.data_as(D), self.resRelN.ctypes.data_as(D), self.norms.ctypes.data_as(D))
         return self.norms.copy()
 
@@ -160,11 +168,11 @@ class OracleBulk:
         rp = np.zeros(self.nb + 1, np.uint32)
         col = np.zeros(nnz_max, np.uint32)
         val = np.zeros(nnz_max * bs)
-        nnz = lib().oc_assemble(self.om.h, C.byref(b), C.byref(c), float(dt), rp.ctypes.data_as(U),
+        nnz = self.lib.oc_assemble(self.om.h, C.byref(b), C.byref(c), float(dt), rp.ctypes.data_as(U),
                                 col.ctypes.data_as(U), val.ctypes.data_as(D))
         return rp, col[:nnz], val[: nnz * bs]
 
     def newton_update(self, u, dSmax):
         b = self._bulk()
         u = np.ascontiguousarray(u, np.float64)
-        lib().oc_newton_update(self.om.h, C.byref(b), u.ctypes.data_as(D), float(dSmax))
+        self.lib.oc_newton_update(self.om.h, C.byref(b), u.ctypes.data_as(D), float(dSmax))

@@ -11,6 +11,17 @@ Each fixture iteration ``itNNN`` holds:
 Tolerances: integer data (phase labels, upwind choices, sparsity pattern) must
 match exactly; floating-point values within REL_TOL relative error, measured
 as |a - b| / max(|b|, floor) with floor = ABS_FLOOR_FRAC * max|b| of the array.
+
+For the outputs of the compositional flash the tolerance of quantity k is
+max(REL_TOL, LIBM_FACTOR * s_k), s_k being the reference algorithm's own
+sensitivity to libm rounding on the same input: the largest deviation from the
+reference of the oracle built with every exp/log/pow/acos/cos result moved by
+one ulp (oracle/ulp_nudge.c, three perturbation patterns).  Unperturbed, the
+oracle reproduces the reference bit for bit on these fixtures, so s_k is
+purely the effect of 1-ulp differences in the transcendentals; a GPU result
+uses CUDA's libm, which differs from glibc's by up to about 2 ulp per call.
+The phase-split Newton solve amplifies those differences in near-critical
+cells (up to ~2e-10 relative on comp6_8x8x3, cell 18).
 """
 from __future__ import annotations
 
@@ -22,6 +33,9 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 REL_TOL = 1e-10          # spec target for floating-point parity
 ABS_FLOOR_FRAC = 1e-12   # values below this fraction of the array scale compare absolutely
 TOL = {}                 # per-quantity tolerances where REL_TOL is not attainable (with the reason)
+LIBM_FACTOR = 4.0        # CUDA vs glibc transcendentals: up to ~2 ulp apart per call; margin 2
+NUDGE_SEEDS = (1, 2, 3)
+SOLVE_KEYS = ("vfi", "vfP", "dSec_dPri")  # outputs of the NC x NC derivative solve: compared per cell, normwise
 
 PHASE_KEYS = ["rho", "xi", "mu", "rhoP", "xiP", "muP"]
 PHASE_COMP_KEYS = ["xij", "rhox", "xix", "mux"]
@@ -115,3 +129,55 @@ def state_from_ctx(ctx, keys=None) -> dict:
              "Pj": "PJ", "dKrdS": "DKRDS", "dPcdS": "DPCDS", "poro": "PORO", "poroP": "POROP", "rockVp": "ROCKVP",
              "P": "P", "Ni": "NI"}
     return {k: ctx.get(v) for k, v in names.items() if keys is None or k in keys}
+
+
+def cellwise(a, b, nb):
+    """max over cells of ||a_c - b_c|| / ||b_c||."""
+    a = np.asarray(a, np.float64).reshape(nb, -1)
+    b = np.asarray(b, np.float64).reshape(nb, -1)
+    return float(np.max(np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)))
+
+
+def state_errors(got: dict, ref: dict, nc: int, nb: int) -> dict:
+    """compare_state with the derivative-solve outputs compared per cell."""
+    errs = compare_state(got, ref, nc)
+    errs.pop("phaseExist_mismatch_cells")
+    for k in SOLVE_KEYS:
+        errs.pop(k, None)
+        if k in got and k in ref:
+            errs[k + "_cellwise"] = cellwise(got[k], ref[k], nb)
+    return errs
+
+
+_SENS = {}
+
+
+def libm_sensitivity(fx: dict, it: str, model, grid) -> dict:
+    """Per-quantity deviation from the reference of the reference algorithm
+    itself under one-ulp perturbations of its transcendentals (max over
+    NUDGE_SEEDS); patterns that flip a phase label are not used."""
+    key = (fx.get("__name__"), it)
+    if key in _SENS:
+        return _SENS[key]
+    from oracle.pyoracle import OracleBulk
+    pre, post = group(fx, it + "/pre"), group(fx, it + "/post")
+    out = {}
+    for seed in NUDGE_SEEDS:
+        ob = OracleBulk(model, grid, variant="ulp")
+        ob.set_nudge_seed(seed)
+        ob.load(jac_state(fx, it))
+        ob.load(pre)
+        ob.update_property()
+        if not np.array_equal(ob.a["phaseExist"], np.asarray(post["phaseExist"]).astype(np.uint32)):
+            continue
+        errs = state_errors(dict(ob.a), post, model.nc, grid.nb)
+        ob.cal_res(float(pre["dt"][0]))
+        errs["res"] = res_err(ob.res, post["res_bulk"], post["rockVp"], post["Nt"], model.nc)
+        for k, v in errs.items():
+            out[k] = max(out.get(k, 0.0), v)
+    _SENS[key] = out
+    return out
+
+
+def tolerance(k: str, sens: dict) -> float:
+    return max(TOL.get(k, REL_TOL), LIBM_FACTOR * sens.get(k, 0.0))

@@ -8,7 +8,10 @@ Tolerances (REL_TOL = 1e-10 from tests/parity.py):
   * exact: phase-existence labels, flash types, skip flags, upwind choices,
     Jacobian sparsity pattern and block order, Newton-update results;
   * elementwise <= REL_TOL: phase properties, saturations, kr/Pc, rock,
-    residual, fluxes, residual norms;
+    residual, fluxes, residual norms; for the compositional flash outputs
+    <= max(REL_TOL, 4 x the reference algorithm's own deviation under
+    one-ulp perturbations of its transcendentals), measured per fixture
+    iteration by the perturbed oracle (parity.libm_sensitivity);
   * per-cell normwise <= REL_TOL for the quantities obtained from the NC x NC
     derivative solve (vfi, vfP, dSec_dPri): the reference solves it with
     LAPACK dgesv from OpenBLAS, whose rounding differs from any other LU;
@@ -38,13 +41,6 @@ def write_report():
     if out:
         with open(out, "w") as f:
             json.dump(REPORT, f, indent=1, sort_keys=True)
-SOLVE_KEYS = ("vfi", "vfP", "dSec_dPri")
-
-
-def cellwise(a, b, nb):
-    a = np.asarray(a, np.float64).reshape(nb, -1)
-    b = np.asarray(b, np.float64).reshape(nb, -1)
-    return float(np.max(np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)))
 
 
 def make_ctx(fx, variant=0):
@@ -64,10 +60,7 @@ def check_update(ctx, fx, it, model, grid):
     pe_g = got["phaseExist"].reshape(nb, 3)
     pe_r = post["phaseExist"].reshape(nb, 3)
     assert np.array_equal(pe_g, pe_r), f"{it}: phase labels differ in {np.sum(np.any(pe_g != pe_r, 1))} cells"
-    errs = P.compare_state(got, post, model.nc)
-    for k in SOLVE_KEYS:
-        errs.pop(k, None)
-        errs[k + "_cellwise"] = cellwise(got[k], post[k], nb)
+    errs = P.state_errors(got, post, model.nc, nb)
     if "flash_ftype" in post and model.compositional:
         assert np.array_equal(ctx.get("FTYPE"), post["flash_ftype"].astype(np.int8)), f"{it}: flash types differ"
         assert np.array_equal(ctx.get("SKIP_FLAG"), post["skip_flag"].astype(np.uint8)), f"{it}: skip flags differ"
@@ -83,8 +76,9 @@ def check_update(ctx, fx, it, model, grid):
     errs["resRelN"] = float(np.max(np.abs(ctx.get("RES_REL_N") - post["resRelN"])))
     errs["maxRelRes_V"] = abs(norms.maxRelRes_V - float(post["maxRelRes_V"][0]))
     assert norms.maxId_V == int(post["maxId_V"][0]) and norms.maxId_N == int(post["maxId_N"][0])
-    errs.pop("phaseExist_mismatch_cells")
     REPORT.setdefault(fx["__name__"], {})[it] = errs
+    sens = P.libm_sensitivity(fx, it, model, grid) if model.compositional else {}
+    REPORT[fx["__name__"]][it + "/libm_sensitivity"] = sens
     # worst cells of the transcendental-heavy outputs, with their flash record
     st, iters = ctx.get("STATUS"), ctx.get("FLASH_ITERS").reshape(nb, 5)
     for k in ("mu", "xij"):
@@ -95,7 +89,7 @@ def check_update(ctx, fx, it, model, grid):
         worst = np.argsort(e)[-3:][::-1]
         REPORT[fx["__name__"]][it + "/" + k + "_worst"] = [
             [int(c), float(e[c]), int(st[c]), iters[c].tolist(), pe_r[c].tolist()] for c in worst]
-    bad = {k: v for k, v in errs.items() if v > P.TOL.get(k, P.REL_TOL)}
+    bad = {k: (v, P.tolerance(k, sens)) for k, v in errs.items() if v > P.tolerance(k, sens)}
     assert not bad, f"{it}: {bad}"
     return errs
 

@@ -254,9 +254,34 @@ def cpu_baseline(threads=None):
     return grid.nb / statistics.median(times), cores, len(times)
 
 
-def fp64_peak():
+def fp64_peak(device=0):
+    """FP64 peak of this GPU (TFLOP/s), measured by the library's DFMA-chain
+    probe: the measured-peaks file carries HBM and bf16 figures only."""
     from opencaeporox_gb300.fim import measure_fp64_tflops
-    return max(measure_fp64_tflops(0, 20000) for _ in range(3))
+    return max(measure_fp64_tflops(device, 20000) for _ in range(3))
+
+
+# FP64 operations of the flash stage on this workload, per cell: 2 x DFMA + DADD
+# + DMUL thread-level instructions of the k_flash_comp launch of one timed step
+# (ncu smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum), divided
+# by the 36,000 cells; libm internals included.  None until measured.
+FLASH_FP64_FLOP_PER_CELL = None
+# DRAM bytes (read + write) of that launch, from the same capture.
+FLASH_DRAM_BYTES = None
+
+
+def assembly_bytes(nb, nconn, nc, nnzb):
+    """Algorithmic HBM bytes of the Jacobian assembly (k_jac_conn + k_jac_rows):
+    every input it reads, once, and the block-CSR values it writes.
+    Per cell (np = 3 phases, nct = nc components incl. water): kr, mu, muP,
+    xi, xiP, rhoP (6 np), xij, rhox, xix, mux (4 np nct), dKrdS, dPcdS (2 np^2),
+    dSec_dPri ((np nct + np) (nct + 1)), v, poroP, vfP (3), vfi (nct) -- doubles;
+    per connection: bId, eId (2 x u32), trans (f64), upblock (np x u32),
+    dP (np x f64); out: nnzb blocks of (nct + 1)^2 doubles."""
+    np_, nct = 3, nc
+    per_cell = 8 * (6 * np_ + 4 * np_ * nct + 2 * np_ * np_ + (np_ * nct + np_) * (nct + 1) + 3 + nct)
+    per_conn = 4 * 2 + 8 + 4 * np_ + 8 * np_
+    return nb * per_cell + nconn * per_conn + nnzb * (nct + 1) ** 2 * 8
 
 
 def peaks():
@@ -318,12 +343,32 @@ def main():
     e2e_ms = statistics.median(e2e_t)
     prof = results[1]["prof"]
     dom = max(prof, key=lambda k: prof[k][0])
+    fp64 = fp64_peak(local)
+    pk = peaks()
+    hbm = pk.get("hbm_gbs")
+    flash_ms = prof["flash"][0]
+    roof = {"kernel": "k_flash_comp (flash stage of the batched step)", "bound": "fp64", "unit": "TFLOP/s",
+            "peak": fp64, "peak_source": "measured (DFMA-chain probe of this library, best of 3)",
+            "achieved": None, "frac": None, "traffic": FLASH_DRAM_BYTES}
+    if FLASH_FP64_FLOP_PER_CELL:
+        roof["achieved"] = FLASH_FP64_FLOP_PER_CELL * nb / (flash_ms * 1e-3) / 1e12
+        roof["frac"] = roof["achieved"] / fp64
+    ctx1 = results[1]["ctx"]
+    rp, _, _ = ctx1.jacobian()
+    asm_ms = prof["jac_conn"][0] + prof["jac_rows"][0]
+    abytes = assembly_bytes(nb, ctx1.nconn, ctx1.nc, int(rp[-1]))
+    roof_asm = {"kernel": "k_jac_conn + k_jac_rows (Jacobian assembly)", "bound": "hbm", "unit": "GB/s",
+                "algorithmic_bytes": abytes, "achieved": abytes / (asm_ms * 1e-3) / 1e9, "peak": hbm,
+                "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "of fallback 6800",
+                "traffic": None}
+    roof_asm["frac"] = roof_asm["achieved"] / (hbm or 6800.0)
     line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD, "l2": "flushed between steps (512 MiB memset)", "variant": "batched"},
             "plain_value": plain, "plain_ms_per_step": results[0]["ms"], "batched_over_plain": value / plain,
             "stages_ms": {k: round(v[0], 4) for k, v in prof.items()}, "dominant_stage": dom,
+            "roofline": roof, "roofline_assembly": roof_asm, "fp64_peak_tflops": fp64,
             "clocks": ck, "gpu_launches": launches,
             "e2e": {"value": nb / (e2e_ms * 1e-3) * world, "unit": "cells/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h}}

@@ -264,10 +264,11 @@ def fp64_peak(device=0):
 # FP64 operations of the flash stage on this workload, per cell: 2 x DFMA + DADD
 # + DMUL thread-level instructions of the k_flash_comp launch of one timed step
 # (ncu smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum), divided
-# by the 36,000 cells; libm internals included.  None until measured.
-FLASH_FP64_FLOP_PER_CELL = None
+# by the 36,000 cells; libm internals included (2 x 746.2 M + 523.3 M + 574.0 M
+# = 2.590 GFLOP for the launch, profiles/k_flash_comp_comp6_36k.md).
+FLASH_FP64_FLOP_PER_CELL = 2589720497 / 36000
 # DRAM bytes (read + write) of that launch, from the same capture.
-FLASH_DRAM_BYTES = None
+FLASH_DRAM_BYTES = 98142720 + 187619584
 
 
 def assembly_bytes(nb, nconn, nc, nnzb):

@@ -237,6 +237,30 @@ ocpx_status ocpx_checkpoint(ocpx_ctx* ctx, int slot, int restore);
  * roofline denominator of the FP64-bound flash; iters sets the run length. */
 ocpx_status ocpx_measure_fp64_tflops(int device, int iters, double* tflops);
 
+/* Relative-residual norms with no allocation at all.  No counterpart in the
+ * reference: it is the "Calculate RelRes" loop of IsoT_FIM::CalRes
+ * (src/IsoThermalMethod.cpp:1147-1167) as a context-free call on device
+ * arrays, for callers that hold a residual on the device but cannot allocate
+ * device memory at that point (their allocator owns the device, or the
+ * implicit device-wide synchronisation of cudaMalloc/cudaFree would stall
+ * their other streams).
+ *   d_res [nb*len] residual (either sign), d_rockVp [nb], d_Nt [nb]: inputs;
+ *   d_resRelV, d_resRelN [nb]: outputs (per-cell norms, as ocpx_calres);
+ *   norms (host): maxRelRes_V/N and maxId_V/N, first cell wins ties.
+ * Runs on `stream` (a cudaStream_t, NULL = default stream) and waits for it.
+ * Its reduction scratch is one static device array per process and device
+ * (OCPX_RELRES_NOALLOC_MAX_BLOCKS partials, about 24 KB); nb above
+ * OCPX_RELRES_NOALLOC_MAX_CELLS returns OCPX_INVALID_ARG.  The scratch's
+ * block counter starts at zero and every call leaves it at zero.  Calls
+ * whose kernels overlap in time race on the scratch: serialise them (one
+ * stream).  The first call on each device looks up the scratch address
+ * (cudaGetSymbolAddress): make it outside any stream capture.  Errors are
+ * returned as status only; ocpx_last_error is not updated. */
+#define OCPX_RELRES_NOALLOC_MAX_BLOCKS 1024
+#define OCPX_RELRES_NOALLOC_MAX_CELLS 2097152
+ocpx_status ocpx_relres_noalloc(const double* d_res, const double* d_rockVp, const double* d_Nt, int nb, int len,
+                                double* d_resRelV, double* d_resRelN, void* stream, ocpx_norms* norms);
+
 /* Stream the context launches on (a cudaStream_t), for callers that time or
  * order work around the library. */
 void* ocpx_stream(ocpx_ctx* ctx);

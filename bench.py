@@ -299,6 +299,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner (library defaults)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -327,8 +328,12 @@ def main():
     flush_bytes = 512 << 20
     flush = (rt.malloc(flush_bytes), flush_bytes)
     results = {}
+    tuned = None
     for variant in (0, 1):
         ctx, model, grid, u = build_workload(variant, device=local)
+        if variant == 1 and not args.no_tune:
+            from opencaeporox_gb300 import autotune
+            tuned = autotune.tune(ctx, DT, slot=0)
         t, launches = time_device(ctx, rt, args.steps, args.warmup, flush)
         prof = stage_profile(ctx, rt, flush)
         results[variant] = dict(ms=statistics.median(t), mean=statistics.fmean(t), launches=launches / args.steps,
@@ -370,6 +375,10 @@ def main():
             "plain_value": plain, "plain_ms_per_step": results[0]["ms"], "batched_over_plain": value / plain,
             "stages_ms": {k: round(v[0], 4) for k, v in prof.items()}, "dominant_stage": dom,
             "roofline": roof, "roofline_assembly": roof_asm, "fp64_peak_tflops": fp64,
+            "batched": {"flash_budget": ctx1.get_param("flash_budget"), "coop_blocks": ctx1.get_param("coop_blocks"),
+                        "deferred_cells": ctx1.get_param("deferred"),
+                        "autotune": None if tuned is None else {k: tuned[k] for k in
+                                                                ("flash_budget", "coop_blocks", "flash_ms")}},
             "clocks": ck, "gpu_launches": launches,
             "e2e": {"value": nb / (e2e_ms * 1e-3) * world, "unit": "cells/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h}}

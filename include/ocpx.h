@@ -23,7 +23,7 @@
  *                           (src/IsoThermalMethod.cpp:1282-1418)
  *   ocpx_update_last_step   IsoT_FIM::UpdateLastTimeStep, bulk part (:1473-1517)
  *   ocpx_step               one whole Newton iteration (update, properties,
- *                           residual, Jacobian) captured as a CUDA graph
+ *                           residual, Jacobian)
  *
  * Host arrays exchanged through ocpx_set_field / ocpx_get_field use the
  * reference's BulkVarSet layout (include/BulkVarSet.hpp): cell-major, then
@@ -202,8 +202,27 @@ ocpx_status ocpx_get_jacobian(ocpx_ctx* ctx, uint32_t* rowptr, uint32_t* col, do
 ocpx_status ocpx_jacobian_device(ocpx_ctx* ctx, const uint32_t** rowptr, const uint32_t** col, const double** val);
 
 /* Execution variant: 0 = one kernel per reference loop (plain), 1 = batched
- * (persistent work-queue flash, fused row assembly, graph-captured step). */
+ * (cost-ordered flash with a work budget; over-budget cells finish their
+ * phase equilibrium on whole warps).  Both give identical results. */
 ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
+
+/* Tuning parameters of the execution (no effect on results):
+ *   FLASH_BUDGET  work units (EoS fugacity evaluations) a cell's phase
+ *                 equilibrium may use in the batched thread-per-cell flash
+ *                 before it is deferred to the warp-cooperative kernel
+ *                 (0 defers every cell that needs an equilibrium);
+ *   COOP_BLOCKS   blocks of the warp-cooperative kernel;
+ *   BLOCK_CELL    threads per block of the per-cell kernels;
+ *   DEFERRED      (read only) cells deferred by the last batched flash;
+ *                 reading it synchronizes the context stream. */
+typedef enum ocpx_param {
+    OCPX_PARAM_FLASH_BUDGET = 0,
+    OCPX_PARAM_COOP_BLOCKS = 1,
+    OCPX_PARAM_BLOCK_CELL = 2,
+    OCPX_PARAM_DEFERRED = 3
+} ocpx_param;
+ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value);
+ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value);
 
 /* One Newton iteration: optional host Newton update u (nb*(nc+1), may be
  * NULL), then properties, residual and Jacobian; optional host copies of the

@@ -120,26 +120,23 @@ struct EosPR {
     }
 
     // EoS_PR::CalZj (:102-124): the root of smaller Gibbs energy
-    OCPX_HD void cal_Zj()
+    OCPX_HD static double zj_of(double Aj, double Bj)
     {
         const double a = (DELTA1 + DELTA2 - 1) * Bj - 1;
         const double b = (Aj + DELTA1 * DELTA2 * Bj * Bj - (DELTA1 + DELTA2) * Bj * (Bj + 1));
         const double c = -(Aj * Bj + DELTA1 * DELTA2 * Bj * Bj * (Bj + 1));
         double z[3];
         const int flag = cubic_root(a, b, c, z);
-        if (flag == 1) {
-            Zj = z[0];
-        }
-        else {
-            const double zj1 = z[0];
-            const double zj2 = z[2];
-            const double dG = (zj2 - zj1) + log((zj1 - Bj) / (zj2 - Bj)) -
-                              Aj / (Bj * (DELTA2 - DELTA1)) *
-                                  log((zj1 + DELTA1 * Bj) * (zj2 + DELTA2 * Bj) /
-                                      ((zj1 + DELTA2 * Bj) * (zj2 + DELTA1 * Bj)));
-            Zj = dG > 0 ? zj1 : zj2;
-        }
+        if (flag == 1) return z[0];
+        const double zj1 = z[0];
+        const double zj2 = z[2];
+        const double dG = (zj2 - zj1) + log((zj1 - Bj) / (zj2 - Bj)) -
+                          Aj / (Bj * (DELTA2 - DELTA1)) *
+                              log((zj1 + DELTA1 * Bj) * (zj2 + DELTA2 * Bj) /
+                                  ((zj1 + DELTA2 * Bj) * (zj2 + DELTA1 * Bj)));
+        return dG > 0 ? zj1 : zj2;
     }
+    OCPX_HD void cal_Zj() { Zj = zj_of(Aj, Bj); }
 
     OCPX_HD void cal_AjBjZj(const double* x)
     {
@@ -148,17 +145,19 @@ struct EosPR {
     }
 
     // numerator factor and denominator shared by Zx, Zn, Zp (:127-180)
-    OCPX_HD double dz_num() const
+    OCPX_HD static double dz_num_of(double Aj, double Bj, double Zj)
     {
         return (Aj + (DELTA1 * DELTA2) * (3 * Bj * Bj + 2 * Bj)) +
                ((DELTA1 + DELTA2) * (2 * Bj + 1) - 2 * (DELTA1 * DELTA2) * Bj) * Zj -
                ((DELTA1 + DELTA2) - 1) * Zj * Zj;
     }
-    OCPX_HD double dz_den() const
+    OCPX_HD static double dz_den_of(double Aj, double Bj, double Zj)
     {
         return (3 * Zj * Zj + 2 * (((DELTA1 + DELTA2) - 1) * Bj - 1) * Zj +
                 (Aj + (DELTA1 * DELTA2) * Bj * Bj - (DELTA1 + DELTA2) * Bj * (Bj + 1)));
     }
+    OCPX_HD double dz_num() const { return dz_num_of(Aj, Bj, Zj); }
+    OCPX_HD double dz_den() const { return dz_den_of(Aj, Bj, Zj); }
 
     // EoS_PR::CalAxBxZx (:127-143); Bx == Bi
     OCPX_HD_NOINLINE void cal_AxZx(const double* x)

@@ -33,6 +33,49 @@ namespace ocpx {
 // device version stops here and flags the cell.
 constexpr int SPLIT_RESTART_CAP = 64;
 
+// Phase-equilibrium outcome handed from the cooperative kernel (flash_coop.cuh)
+// to the thread that finishes the cell's properties and derivatives.
+struct PERes {
+    int NP;
+    int ftype;
+    uint32_t status;
+    int it[5];  // SSM-stability, NR-stability, SSM-split, NR-split, RR
+    double nu[2];
+    double x[2][NC_MAX];
+};
+
+// A cell whose phase equilibrium ran over its work budget, with the inputs
+// the equilibrium needs besides the cell state.
+struct DeferRec {
+    int cell;
+    int ftype_in;
+    unsigned lNP;
+};
+
+// Append-only list of deferred cells (one atomic per deferred cell).
+struct DeferSink {
+    DeferRec* rec;
+    unsigned* count;
+    int cap;
+    OCPX_HD bool push(int cell, int ftype_in, unsigned lNP) const
+    {
+#ifdef __CUDA_ARCH__
+        const unsigned slot = atomicAdd(count, 1u);
+        if (slot >= (unsigned)cap) return false;
+        rec[slot].cell = cell;
+        rec[slot].ftype_in = ftype_in;
+        rec[slot].lNP = lNP;
+        return true;
+#else
+        (void)cell; (void)ftype_in; (void)lNP;
+        return false;
+#endif
+    }
+};
+
+// Work units charged against the budget: one EoS fugacity evaluation = 1.
+constexpr int WORK_SSM_STA = 1, WORK_NR_STA = 4, WORK_SSM_SP = 2, WORK_NR_SP = 6;
+
 template <int NCM>
 struct CompFlash {
     EosPR<NCM> eos;
@@ -56,6 +99,17 @@ struct CompFlash {
     bool ssm_sta_conv, nr_sta_conv, ssm_sp_conv, nr_sp_conv;
     int it_ssm_sta, it_nr_sta, it_ssm_sp, it_nr_sp, it_rr;
     uint32_t status;
+    // work budget: once `work` exceeds `budget` the equilibrium is abandoned
+    // (deferred) and its partial state is discarded by the caller
+    int work, budget;
+    bool deferred;
+
+    OCPX_HD bool charge(int units)
+    {
+        work += units;
+        if (work > budget) deferred = true;
+        return deferred;
+    }
 
     OCPX_HD static double dnrm2(int n, const double* v)
     {
@@ -97,6 +151,7 @@ struct CompFlash {
             int iter = 0;
             bool flag = false;
             while (true) {
+                if (charge(WORK_SSM_STA)) return true;
                 Yt = 0;
                 for (int i = 0; i < NC; i++) {
                     Y[i] = xj[i] * Ks[i];
@@ -151,6 +206,7 @@ struct CompFlash {
         const double alpha = 1;
         int iter = 0;
         while (Se > Stol) {
+            if (charge(WORK_NR_STA)) return true;
             eos.cal_lnfugX(Y, lnf[0]);
             assemble_jmat_sta();
             if (!sym_lower_solve<NCM>(NC, J, res, W)) status |= ST_SINGULAR;
@@ -201,6 +257,7 @@ struct CompFlash {
             flag = true;
             int iter = 0;
             while (Se > Stol) {
+                if (charge(WORK_SSM_STA)) return true;
                 Yt = 0;
                 for (int i = 0; i < NC; i++) {
                     Y[i] = di[i] / phiSta[i];
@@ -215,6 +272,7 @@ struct CompFlash {
             }
             it_ssm_sta += iter;
             flag = stable_nr();
+            if (deferred) return true;
             if (flag && Yt > 1 + eYt) { ssm_sta_conv = true; return false; }
         }
         return true;
@@ -232,6 +290,7 @@ struct CompFlash {
         }
         else {
             flag = stable_ssm01();
+            if (deferred) return true;
             if (!flag) tmpNP++;
             if (tmpNP != lNP) {
                 flag = stable_ssm();
@@ -307,6 +366,7 @@ struct CompFlash {
         }
         int iter = 0;
         while (Se > Stol) {
+            if (charge(WORK_SSM_SP)) return;
             rachford_rice2();
             update_x_rr();
             eos.cal_fug_phi(x[0], fug[0], phi[0]);
@@ -340,6 +400,7 @@ struct CompFlash {
         int iter = 0;
         const double eNR0 = eNR;
         while (eNR > NRtol) {
+            if (charge(WORK_NR_SP)) return;
             for (int j = 0; j < 2; j++)
                 for (int i = 0; i < NC; i++) ln_[j][i] = n[j][i];
             eos.cal_lnfugN(x[0], nu[0], lnf[0]);
@@ -409,7 +470,9 @@ struct CompFlash {
         ssm_sp_conv = false;
         nr_sp_conv = false;
         split_ssm2(false);
+        if (deferred) return;
         split_nr();
+        if (deferred) return;
         int restarts = 0;
         while (!nr_sp_conv) {
             if (++restarts > SPLIT_RESTART_CAP) {
@@ -417,7 +480,9 @@ struct CompFlash {
                 break;
             }
             split_ssm2(true);
+            if (deferred) return;
             split_nr();
+            if (deferred) return;
             if (!check_split()) break;
             if (ssm_sp_conv) break;
         }
@@ -440,6 +505,7 @@ struct CompFlash {
             for (int i = 0; i < NC; i++) x[0][i] = zi[i];
             cal_kwilson();
             while (!phase_stable()) {
+                if (deferred) return;
                 NP++;
                 phase_split();
                 if (NP == 2 || NP == 1) break;
@@ -457,6 +523,7 @@ struct CompFlash {
             phase_split();
             break;
         }
+        if (deferred) return;
         if (NP > 1) ftype = 2;
     }
 };
@@ -558,7 +625,12 @@ struct CompCellUpdate {
     double rhs[NCM * (NCM + 1)];
     double tT[NCM];
 
-    OCPX_HD void run(const Model& M, const BulkView& b, int cell)
+    // budget: work units the phase equilibrium may use before the cell is
+    // handed to `sink` (the plain kernel passes INT_MAX and no sink);
+    // injected: a phase-equilibrium result computed elsewhere for this cell.
+    // Returns false when the cell was deferred (nothing of it was written).
+    OCPX_HD bool run(const Model& M, const BulkView& b, int cell, int budget = 0x7fffffff,
+                     const DeferSink* sink = nullptr, const PERes* injected = nullptr)
     {
         const CompModel& m = M.comp;
         const int NC = m.nc;
@@ -569,6 +641,9 @@ struct CompCellUpdate {
         f.NC = NC;
         f.status = 0;
         f.it_ssm_sta = f.it_nr_sta = f.it_ssm_sp = f.it_nr_sp = f.it_rr = 0;
+        f.work = 0;
+        f.budget = budget;
+        f.deferred = false;
 
         // ---- SetVarSet (src/OCPMixtureMethodComp.cpp:671-687)
         const double P = b.P[cell];
@@ -618,7 +693,33 @@ struct CompCellUpdate {
 
         // ---- phase equilibrium (lNP = phaseNum - 1 passed through double -> USI)
         f.eos.setup(&m, M.units.gas_constant, P, T);
-        f.phase_equilibrium(ftype_in, npPE, xx[0], xx[1]);
+        if (injected) {
+            f.NP = injected->NP;
+            f.ftype = injected->ftype;
+            f.status = injected->status;
+            f.it_ssm_sta = injected->it[0];
+            f.it_nr_sta = injected->it[1];
+            f.it_ssm_sp = injected->it[2];
+            f.it_nr_sp = injected->it[3];
+            f.it_rr = injected->it[4];
+            for (int j = 0; j < 2; j++) {
+                f.nu[j] = injected->nu[j];
+                for (int i = 0; i < NC; i++) f.x[j][i] = injected->x[j][i];
+            }
+        }
+        else {
+            f.phase_equilibrium(ftype_in, npPE, xx[0], xx[1]);
+            if (f.deferred) {
+                if (sink && sink->push(cell, ftype_in, npPE)) return false;
+                // no room in the list: finish the equilibrium here from the start
+                f.status = 0;
+                f.it_ssm_sta = f.it_nr_sta = f.it_ssm_sp = f.it_nr_sp = f.it_rr = 0;
+                f.work = 0;
+                f.budget = 0x7fffffff;
+                f.deferred = false;
+                f.phase_equilibrium(ftype_in, npPE, xx[0], xx[1]);
+            }
+        }
 
         // ---- CalPropertyDer (:134-142): CopyPhaseFromPE, CalMW, CalVmVj, CalXiRhoMuDer
         const int NPh = f.NP;
@@ -836,6 +937,7 @@ struct CompCellUpdate {
         b.iters[b.idx(2, cell)] = f.it_ssm_sp;
         b.iters[b.idx(3, cell)] = f.it_nr_sp;
         b.iters[b.idx(4, cell)] = f.it_rr;
+        return true;
     }
 
     OCPX_HD void swap_phases(int NC)

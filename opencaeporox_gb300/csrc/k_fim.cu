@@ -195,6 +195,66 @@ cudaError_t launch_jac_rows(const BulkView& b, const ConnView& cv, const double*
     if (b.nb) k_jac_rows<<<grid_for(b.nb, block), block, 0, s>>>(b, cv, bmat, rowptr, val);
     return cudaGetLastError();
 }
+// Predicted work of a cell's next flash: the work units its last flash used
+// (iteration counters weighted as the flash's budget charges them, Rachford-
+// Rice iterations at a fifth), as a bucket in descending order of cost.
+__device__ __forceinline__ int cost_bucket(const BulkView& b, int cell)
+{
+    const int32_t* it = b.iters;
+    const long long w = 3LL + it[b.idx(0, cell)] + 4LL * it[b.idx(1, cell)] + 2LL * it[b.idx(2, cell)] +
+                        6LL * it[b.idx(3, cell)] + it[b.idx(4, cell)] / 5;
+    const int bucket = w < COST_BUCKETS - 1 ? (int)w : COST_BUCKETS - 1;
+    return COST_BUCKETS - 1 - bucket;
+}
+
+__global__ void k_cost_hist(BulkView b, unsigned* __restrict__ hist)
+{
+    __shared__ unsigned h[COST_BUCKETS];
+    for (int k = threadIdx.x; k < COST_BUCKETS; k += blockDim.x) h[k] = 0;
+    __syncthreads();
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell < b.nb) atomicAdd(&h[cost_bucket(b, cell)], 1u);
+    __syncthreads();
+    for (int k = threadIdx.x; k < COST_BUCKETS; k += blockDim.x)
+        if (h[k]) atomicAdd(&hist[k], h[k]);
+}
+
+// exclusive scan of the bucket counts, in place (one block of COST_BUCKETS threads)
+__global__ void k_cost_scan(unsigned* __restrict__ hist)
+{
+    __shared__ unsigned v[COST_BUCKETS];
+    const int t = threadIdx.x;
+    v[t] = hist[t];
+    __syncthreads();
+    for (int d = 1; d < COST_BUCKETS; d <<= 1) {
+        const unsigned add = t >= d ? v[t - d] : 0u;
+        __syncthreads();
+        v[t] += add;
+        __syncthreads();
+    }
+    hist[t] = v[t] - hist[t];
+}
+
+__global__ void k_cost_scatter(BulkView b, unsigned* __restrict__ offs, int* __restrict__ order)
+{
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= b.nb) return;
+    const unsigned pos = atomicAdd(&offs[cost_bucket(b, cell)], 1u);
+    order[pos] = cell;
+}
+
+cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, cudaStream_t s)
+{
+    if (!b.nb) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned) * COST_BUCKETS, s);
+    if (e != cudaSuccess) return e;
+    const int block = 256;
+    k_cost_hist<<<grid_for(b.nb, block), block, 0, s>>>(b, hist);
+    k_cost_scan<<<1, COST_BUCKETS, 0, s>>>(hist);
+    k_cost_scatter<<<grid_for(b.nb, block), block, 0, s>>>(b, hist, order);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_report(const BulkView& b, uint32_t* out3, int block, cudaStream_t s)
 {
     if (b.nb) k_report<<<grid_for(b.nb, block), block, 0, s>>>(b, out3);

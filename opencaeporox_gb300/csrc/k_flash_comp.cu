@@ -1,7 +1,7 @@
 // Compositional FlashDer kernels, compiled once per component capacity
 // (OCPX_NCM) so each build carries arrays sized for its component count.
 #include "ocpx_kernels.h"
-#include "flash_comp.cuh"
+#include "flash_coop.cuh"
 
 #ifndef OCPX_NCM
 #error "compile with -DOCPX_NCM=<capacity>"
@@ -18,27 +18,51 @@ __global__ void __launch_bounds__(128) k_flash_comp(const Model* __restrict__ M,
     u.run(*M, b, cell);
 }
 
-// Work-queue variant: each warp lane claims cells from a global counter in
-// chunks of `chunk` consecutive cells until the grid is exhausted.  The loop
-// is bounded by the number of cells.
+// Batched form, step 1: one thread per cell in the order given by `order`
+// (cells of similar predicted cost side by side), with a work budget on the
+// phase equilibrium; cells over budget are appended to the deferral list and
+// left untouched.
 template <int NCM>
-__global__ void __launch_bounds__(128) k_flash_comp_queue(const Model* __restrict__ M, BulkView b,
-                                                          unsigned* __restrict__ counter, int chunk)
+__global__ void __launch_bounds__(128) k_flash_budget(const Model* __restrict__ M, BulkView b,
+                                                      const int* __restrict__ order, int budget, DeferSink sink)
 {
-    const int lane = threadIdx.x & 31;
-    while (true) {
-        unsigned base = 0;
-        if (lane == 0) base = atomicAdd(counter, 32u * (unsigned)chunk);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= (unsigned)b.nb) break;
-        for (int k = 0; k < chunk; k++) {
-            const unsigned cell = base + (unsigned)k * 32u + (unsigned)lane;
-            if (cell < (unsigned)b.nb) {
-                CompCellUpdate<NCM> u;
-                u.run(*M, b, (int)cell);
-            }
-        }
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= b.nb) return;
+    const int cell = order[p];
+    CompCellUpdate<NCM> u;
+    u.run(*M, b, cell, budget, &sink);
+}
+
+// Step 2: the phase equilibrium of every deferred cell on a whole warp
+// (flash_coop.cuh).  Persistent: warp w takes deferred slots w, w + W, ...
+template <int NCM>
+__global__ void __launch_bounds__(COOP_WARPS * 32) k_flash_pe_coop(const Model* __restrict__ M, BulkView b,
+                                                                   const DeferRec* __restrict__ rec,
+                                                                   const unsigned* __restrict__ count, int cap,
+                                                                   PERes* __restrict__ out)
+{
+    __shared__ CoopSh<NCM> sh[COOP_WARPS];
+    const int warp = threadIdx.x >> 5;
+    const unsigned n = min(*count, (unsigned)cap);
+    for (unsigned slot = blockIdx.x * COOP_WARPS + warp; slot < n; slot += gridDim.x * COOP_WARPS) {
+        CoopPE<NCM> pe(sh[warp], M->comp);
+        pe.run(*M, b, rec[slot], out[slot]);
     }
+}
+
+// Step 3: properties, derivatives and skip state of the deferred cells from
+// their equilibrium, one thread per deferred cell.
+template <int NCM>
+__global__ void __launch_bounds__(128) k_flash_post(const Model* __restrict__ M, BulkView b,
+                                                    const DeferRec* __restrict__ rec,
+                                                    const unsigned* __restrict__ count, int cap,
+                                                    const PERes* __restrict__ pe)
+{
+    const unsigned slot = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned n = min(*count, (unsigned)cap);
+    if (slot >= n) return;
+    CompCellUpdate<NCM> u;
+    u.run(*M, b, rec[slot].cell, 0x7fffffff, nullptr, &pe[slot]);
 }
 
 #define OCPX_CAT2(a, b) a##b
@@ -52,11 +76,18 @@ cudaError_t OCPX_CAT(launch_flash_comp_, OCPX_NCM)(const Model* dm, const BulkVi
     return cudaGetLastError();
 }
 
-cudaError_t OCPX_CAT(launch_flash_comp_queue_, OCPX_NCM)(const Model* dm, const BulkView& b, unsigned* counter,
-                                                         int grid, int block, int chunk, cudaStream_t s)
+cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const BulkView& b, const int* order,
+                                                      const FlashBatch& fb, cudaStream_t s)
 {
     if (b.nb == 0) return cudaSuccess;
-    k_flash_comp_queue<OCPX_NCM><<<grid, block, 0, s>>>(dm, b, counter, chunk);
+    const DeferSink sink{fb.rec, fb.count, fb.cap};
+    k_flash_budget<OCPX_NCM><<<(b.nb + fb.block - 1) / fb.block, fb.block, 0, s>>>(dm, b, order, fb.budget, sink);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_flash_pe_coop<OCPX_NCM><<<fb.coop_blocks, COOP_WARPS * 32, 0, s>>>(dm, b, fb.rec, fb.count, fb.cap, fb.pe);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_flash_post<OCPX_NCM><<<(fb.cap + 127) / 128, 128, 0, s>>>(dm, b, fb.rec, fb.count, fb.cap, fb.pe);
     return cudaGetLastError();
 }
 

@@ -17,11 +17,11 @@ cudaError_t launch_flash_comp_6(const Model*, const BulkView&, int, cudaStream_t
 cudaError_t launch_flash_comp_8(const Model*, const BulkView&, int, cudaStream_t);
 cudaError_t launch_flash_comp_10(const Model*, const BulkView&, int, cudaStream_t);
 cudaError_t launch_flash_comp_12(const Model*, const BulkView&, int, cudaStream_t);
-cudaError_t launch_flash_comp_queue_4(const Model*, const BulkView&, unsigned*, int, int, int, cudaStream_t);
-cudaError_t launch_flash_comp_queue_6(const Model*, const BulkView&, unsigned*, int, int, int, cudaStream_t);
-cudaError_t launch_flash_comp_queue_8(const Model*, const BulkView&, unsigned*, int, int, int, cudaStream_t);
-cudaError_t launch_flash_comp_queue_10(const Model*, const BulkView&, unsigned*, int, int, int, cudaStream_t);
-cudaError_t launch_flash_comp_queue_12(const Model*, const BulkView&, unsigned*, int, int, int, cudaStream_t);
+cudaError_t launch_flash_batched_4(const Model*, const BulkView&, const int*, const FlashBatch&, cudaStream_t);
+cudaError_t launch_flash_batched_6(const Model*, const BulkView&, const int*, const FlashBatch&, cudaStream_t);
+cudaError_t launch_flash_batched_8(const Model*, const BulkView&, const int*, const FlashBatch&, cudaStream_t);
+cudaError_t launch_flash_batched_10(const Model*, const BulkView&, const int*, const FlashBatch&, cudaStream_t);
+cudaError_t launch_flash_batched_12(const Model*, const BulkView&, const int*, const FlashBatch&, cudaStream_t);
 
 cudaError_t launch_flash_comp(int ncm, const Model* dm, const BulkView& b, int block, cudaStream_t s)
 {
@@ -34,15 +34,15 @@ cudaError_t launch_flash_comp(int ncm, const Model* dm, const BulkView& b, int b
     default: return cudaErrorInvalidValue;
     }
 }
-cudaError_t launch_flash_comp_queue(int ncm, const Model* dm, const BulkView& b, unsigned* counter, int grid,
-                                    int block, int chunk, cudaStream_t s)
+cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, const int* order,
+                                 const FlashBatch& fb, cudaStream_t s)
 {
     switch (ncm) {
-    case 4: return launch_flash_comp_queue_4(dm, b, counter, grid, block, chunk, s);
-    case 6: return launch_flash_comp_queue_6(dm, b, counter, grid, block, chunk, s);
-    case 8: return launch_flash_comp_queue_8(dm, b, counter, grid, block, chunk, s);
-    case 10: return launch_flash_comp_queue_10(dm, b, counter, grid, block, chunk, s);
-    case 12: return launch_flash_comp_queue_12(dm, b, counter, grid, block, chunk, s);
+    case 4: return launch_flash_batched_4(dm, b, order, fb, s);
+    case 6: return launch_flash_batched_6(dm, b, order, fb, s);
+    case 8: return launch_flash_batched_8(dm, b, order, fb, s);
+    case 10: return launch_flash_batched_10(dm, b, order, fb, s);
+    case 12: return launch_flash_batched_12(dm, b, order, fb, s);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -108,7 +108,15 @@ struct ocpx_ctx {
     RowNorm* rownorm = nullptr;
     RowNorm* norm_out = nullptr;
     uint32_t* flags = nullptr;      // [4]: check OR, report (OR, two-phase, flagged)
-    unsigned* queue_counter = nullptr;
+    // batched flash: cost order, deferral list, cooperative results
+    int* order = nullptr;
+    unsigned* cost_hist = nullptr;
+    DeferRec* defer_rec = nullptr;
+    unsigned* defer_count = nullptr;   // [4]: deferred cells of the last batched flash
+    PERes* pe_res = nullptr;
+    int defer_cap = 0;
+    int flash_budget = 48;
+    int coop_blocks = 0;
     double* u = nullptr;            // Newton update staging
     double* bmat = nullptr;         // per-connection Jacobian blocks (2 per connection)
     uint32_t* jac_rowptr = nullptr;
@@ -120,7 +128,7 @@ struct ocpx_ctx {
     uint32_t* h_flags = nullptr;    // pinned
     RowNorm* h_norm = nullptr;      // pinned
     uint64_t launches = 0;
-    int block_cell = 128, block_conn = 128, queue_chunk = 1, queue_grid = 0;
+    int block_cell = 128, block_conn = 128;
     // per-stage event timing
     bool prof = false;
     struct Mark { int stage; cudaEvent_t a, b; };
@@ -319,7 +327,11 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     add(&cv.row_ptr, sizeof(uint32_t) * (nb + 1)); add(&cv.row_conn, sizeof(uint32_t) * (row_conn.size() + 1));
     add(&ctx->res, D * (nc + 1)); add(&ctx->resRelV, D); add(&ctx->resRelN, D);
     add(&ctx->rownorm, sizeof(RowNorm) * (size_t)nb); add(&ctx->norm_out, sizeof(RowNorm));
-    add(&ctx->flags, sizeof(uint32_t) * 4); add(&ctx->queue_counter, sizeof(unsigned) * 4);
+    add(&ctx->flags, sizeof(uint32_t) * 4);
+    ctx->defer_cap = std::max(1024, nb / 4);
+    add(&ctx->order, sizeof(int) * (size_t)nb); add(&ctx->cost_hist, sizeof(unsigned) * COST_BUCKETS);
+    add(&ctx->defer_rec, sizeof(DeferRec) * (size_t)ctx->defer_cap); add(&ctx->defer_count, sizeof(unsigned) * 4);
+    add(&ctx->pe_res, sizeof(PERes) * (size_t)ctx->defer_cap);
     add(&ctx->u, D * (nc + 1));
     add(&ctx->bmat, sizeof(double) * C * 2 * bsize);
     add(&ctx->jac_rowptr, sizeof(uint32_t) * (nb + 1)); add(&ctx->jac_col, sizeof(uint32_t) * jcol.size());
@@ -367,7 +379,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     if (e != cudaSuccess) return fail_ctx(OCPX_CUDA_ERROR, std::string("context setup: ") + cudaGetErrorString(e));
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    ctx->queue_grid = sms * 4;
+    ctx->coop_blocks = sms * 4;
     *out = ctx;
     return OCPX_OK;
 }
@@ -449,21 +461,26 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
     OCPX_CUDA(launch_check(ctx->b, ctx->flags, ctx->block_cell, s));
     ctx->stage_end();
     ctx->launches++;
-    if (ctx->host_model.mixture == 1 && ctx->variant == 1)
-        OCPX_CUDA(cudaMemsetAsync(ctx->queue_counter, 0, sizeof(unsigned), s));
     ctx->stage_begin(1);
     if (ctx->host_model.mixture == 1) {
-        if (ctx->variant == 1)
-            OCPX_CUDA(launch_flash_comp_queue(ctx->ncm, ctx->d_model, ctx->b, ctx->queue_counter, ctx->queue_grid,
-                                              ctx->block_cell, ctx->queue_chunk, s));
-        else
+        if (ctx->variant == 1) {
+            OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned), s));
+            OCPX_CUDA(launch_cost_order(ctx->b, ctx->cost_hist, ctx->order, s));
+            const FlashBatch fb{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
+                                ctx->defer_rec, ctx->defer_count, ctx->pe_res};
+            OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fb, s));
+            ctx->launches += 6;
+        }
+        else {
             OCPX_CUDA(launch_flash_comp(ctx->ncm, ctx->d_model, ctx->b, ctx->block_cell, s));
+            ctx->launches++;
+        }
     }
     else {
         OCPX_CUDA(launch_flash_bo(ctx->d_model, ctx->b, ctx->block_cell, s));
+        ctx->launches++;
     }
     ctx->stage_end();
-    ctx->launches++;
     ctx->stage_begin(2);
     OCPX_CUDA(launch_krpc_rock(ctx->d_model, ctx->b, ctx->block_cell, s));
     ctx->stage_end();
@@ -681,6 +698,46 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant)
     if (!ctx || (variant != 0 && variant != 1)) return fail(OCPX_INVALID_ARG, "variant must be 0 or 1");
     ctx->variant = variant;
     return OCPX_OK;
+}
+
+ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    switch (p) {
+    case OCPX_PARAM_FLASH_BUDGET:
+        if (value < 0 || value > 0x7fffffffLL) return fail(OCPX_INVALID_ARG, "flash budget out of range");
+        ctx->flash_budget = (int)value;
+        return OCPX_OK;
+    case OCPX_PARAM_COOP_BLOCKS:
+        if (value < 1 || value > 65535) return fail(OCPX_INVALID_ARG, "cooperative blocks out of range");
+        ctx->coop_blocks = (int)value;
+        return OCPX_OK;
+    case OCPX_PARAM_BLOCK_CELL:
+        if (value != 32 && value != 64 && value != 128) return fail(OCPX_INVALID_ARG, "block size must be 32, 64 or 128");
+        ctx->block_cell = (int)value;
+        return OCPX_OK;
+    default:
+        return fail(OCPX_INVALID_ARG, "unknown or read-only parameter");
+    }
+}
+
+ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value)
+{
+    if (!ctx || !value) return fail(OCPX_INVALID_ARG, "null argument");
+    switch (p) {
+    case OCPX_PARAM_FLASH_BUDGET: *value = ctx->flash_budget; return OCPX_OK;
+    case OCPX_PARAM_COOP_BLOCKS: *value = ctx->coop_blocks; return OCPX_OK;
+    case OCPX_PARAM_BLOCK_CELL: *value = ctx->block_cell; return OCPX_OK;
+    case OCPX_PARAM_DEFERRED: {
+        unsigned n = 0;
+        OCPX_CUDA(cudaMemcpyAsync(&n, ctx->defer_count, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+        OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+        *value = n;
+        return OCPX_OK;
+    }
+    default:
+        return fail(OCPX_INVALID_ARG, "unknown parameter");
+    }
 }
 
 ocpx_status ocpx_step(ocpx_ctx* ctx, const double* u_host, double dSmax, double dt, double* res_host,

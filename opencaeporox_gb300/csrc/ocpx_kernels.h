@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include "bulk_view.cuh"
 #include "conn_ops.cuh"
+#include "flash_comp.cuh"
 
 namespace ocpx {
 
@@ -14,11 +15,23 @@ constexpr int kNctCaps[] = {3, 5, 7, 9, 11, 13};
 
 // Compositional FlashDer for cells [0, nb): one thread per cell.
 cudaError_t launch_flash_comp(int ncm, const Model* dm, const BulkView& b, int block, cudaStream_t s);
-// Persistent work-queue variant: cells are claimed from a global counter in
-// chunks, so warps that finish cheap cells pick up new ones while others are
-// still iterating.
-cudaError_t launch_flash_comp_queue(int ncm, const Model* dm, const BulkView& b, unsigned* counter, int grid,
-                                    int block, int chunk, cudaStream_t s);
+// Batched form: cost-ordered thread-per-cell flash with a work budget, the
+// deferred cells' phase equilibrium on whole warps, then their properties.
+struct FlashBatch {
+    int budget;        // work units before a cell is deferred
+    int block;         // threads per block of the thread-per-cell step
+    int coop_blocks;   // blocks of the cooperative step (COOP_WARPS warps each)
+    int cap;           // capacity of the deferral list
+    DeferRec* rec;
+    unsigned* count;   // deferred cells (may exceed cap: the excess finish in place)
+    PERes* pe;
+};
+cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, const int* order,
+                                 const FlashBatch& fb, cudaStream_t s);
+// Cells in descending order of the work their last flash needed (iteration
+// counters), by a counting sort over COST_BUCKETS buckets.
+constexpr int COST_BUCKETS = 256;
+cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, cudaStream_t s);
 
 cudaError_t launch_flash_bo(const Model* dm, const BulkView& b, int block, cudaStream_t s);
 cudaError_t launch_krpc_rock(const Model* dm, const BulkView& b, int block, cudaStream_t s);

@@ -93,7 +93,9 @@ EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy",
            "ocpx_update_last_step", "ocpx_synchronize", "ocpx_jacobian_dims", "ocpx_get_jacobian",
            "ocpx_jacobian_device", "ocpx_set_variant", "ocpx_step", "ocpx_enqueue_step", "ocpx_step_report",
            "ocpx_profile_enable", "ocpx_profile_read", "ocpx_checkpoint", "ocpx_measure_fp64_tflops",
-           "ocpx_stream", "ocpx_launch_count"]
+           "ocpx_stream", "ocpx_launch_count", "ocpx_set_param", "ocpx_get_param"]
+
+PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3}
 
 _lib = None
 
@@ -129,8 +131,10 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.ocpx_profile_enable.argtypes = [P, C.c_int]
     lib.ocpx_profile_read.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
     lib.ocpx_measure_fp64_tflops.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
+    lib.ocpx_set_param.argtypes = [P, C.c_int, C.c_longlong]
+    lib.ocpx_get_param.argtypes = [P, C.c_int, C.POINTER(C.c_longlong)]
     for fn in ("ocpx_enqueue_step", "ocpx_step_report", "ocpx_profile_enable", "ocpx_profile_read",
-               "ocpx_measure_fp64_tflops", "ocpx_checkpoint"):
+               "ocpx_measure_fp64_tflops", "ocpx_checkpoint", "ocpx_set_param", "ocpx_get_param"):
         getattr(lib, fn).restype = C.c_int
     lib.ocpx_stream.argtypes = [P]
     lib.ocpx_stream.restype = P
@@ -370,6 +374,16 @@ class FimContext:
 
     def set_variant(self, v: int):
         _check(self.lib.ocpx_set_variant(self.h, int(v)))
+
+    def set_param(self, name: str, value: int):
+        """Execution tuning (results do not depend on it): flash_budget,
+        coop_blocks, block_cell."""
+        _check(self.lib.ocpx_set_param(self.h, PARAMS[name], int(value)))
+
+    def get_param(self, name: str) -> int:
+        v = C.c_longlong()
+        _check(self.lib.ocpx_get_param(self.h, PARAMS[name], C.byref(v)))
+        return int(v.value)
 
     def checkpoint(self, slot: int = 0, restore: bool = False):
         """Save / restore the whole bulk state on the device (ResetToLastTimeStep)."""

@@ -145,15 +145,47 @@ def test_newton_update(gpu_lib, name):
                 assert np.array_equal(ctx.get(f), pre[k]), f"{it}: {k}"
 
 
-def test_batched_variant_matches_plain(gpu_lib):
+FLASH_OUT = ("S", "XIJ", "RHO", "XI", "MU", "RHOP", "XIP", "MUP", "RHOX", "XIX", "MUX", "DSEC_DPRI", "VF", "VFP",
+             "VFI", "NT", "PHASE_EXIST", "FTYPE", "FLASH_ITERS", "STATUS", "SKIP_FLAG", "SKIP_MINEIG", "SKIP_P",
+             "SKIP_ZI", "KR", "PC", "PORO", "ROCKVP")
+
+
+def test_batched_variant_against_reference(gpu_lib):
     fx = P.load_fixture("comp8_6x6x4")
     fx["__name__"] = "comp8_6x6x4/batched"
     it = [it for it in P.iterations(fx) if "P" in P.group(fx, it + "/post")][0]
+    ctx, model, grid = make_ctx(fx, 1)
+    with ctx:
+        check_update(ctx, fx, it, model, grid)
+
+
+@pytest.mark.parametrize("name", ["comp6_8x8x3", "comp8_6x6x4"])
+@pytest.mark.parametrize("budget", [0, 3, None])
+def test_batched_variant_matches_plain(gpu_lib, name, budget):
+    """The batched flash (cost order, work budget, warp-cooperative phase
+    equilibrium for the deferred cells) is bit-identical to the plain one.
+    Budget 0 sends every cell that needs an equilibrium through the
+    cooperative kernel."""
+    fx = P.load_fixture(name)
+    its = [it for it in P.iterations(fx) if "P" in P.group(fx, it + "/post")]
     outs = []
+    deferred = []
     for variant in (0, 1):
         ctx, model, grid = make_ctx(fx, variant)
         with ctx:
-            check_update(ctx, fx, it, model, grid)
-            outs.append({k: ctx.get(k) for k in ("S", "XIJ", "DSEC_DPRI", "RES")})
-    for k in outs[0]:
-        assert np.array_equal(outs[0][k], outs[1][k]), k
+            if variant == 1 and budget is not None:
+                ctx.set_param("flash_budget", budget)
+            got = []
+            for it in its:
+                ctx.load_state(P.jac_state(fx, it))
+                ctx.load_state(P.group(fx, it + "/pre"))
+                ctx.update_property()
+                got.append({k: ctx.get(k) for k in FLASH_OUT})
+                if variant == 1:
+                    deferred.append(ctx.get_param("deferred"))
+            outs.append(got)
+    if budget == 0:
+        assert all(d > 0 for d in deferred), deferred
+    for it, a, b in zip(its, outs[0], outs[1]):
+        for k in FLASH_OUT:
+            assert np.array_equal(a[k], b[k], equal_nan=True), f"{name} {it} budget={budget}: {k} differs"

@@ -232,17 +232,22 @@ ocpx_status ocpx_step(ocpx_ctx* ctx, const double* u_host, double dSmax, double 
 
 /* Asynchronous form of ocpx_step without host buffers: enqueue properties,
  * residual and Jacobian on the context stream and return at once;
- * ocpx_step_report then waits and reads the status summary. */
+ * ocpx_step_report then waits and reads the status summary.  In the batched
+ * variant the sequence is captured into a CUDA graph on first use (again
+ * after dt, the variant or a tuning parameter changes) and replayed with one
+ * launch; while stage profiling is on it runs kernel by kernel. */
 ocpx_status ocpx_enqueue_step(ocpx_ctx* ctx, double dt);
 ocpx_status ocpx_step_report(ocpx_ctx* ctx, ocpx_report* rep);
 
 /* Per-stage device timing with CUDA events recorded on the context stream.
  * Stages: 0 physical check, 1 flash, 2 kr/Pc + rock, 3 status summary,
  * 4 connection flux, 5 residual + norms, 6 Jacobian connection blocks,
- * 7 Jacobian rows, 8 Newton update.  ocpx_profile_read synchronizes and
- * returns, per stage, the summed milliseconds and the number of timed
+ * 7 Jacobian rows, 8 Newton update; inside stage 1 of the batched form:
+ * 9 cost order, 10 budgeted per-cell flash, 11 cooperative equilibrium of
+ * the deferred cells, 12 their properties.  ocpx_profile_read synchronizes
+ * and returns, per stage, the summed milliseconds and the number of timed
  * launches since profiling was enabled. */
-#define OCPX_STAGE_COUNT 9
+#define OCPX_STAGE_COUNT 13
 ocpx_status ocpx_profile_enable(ocpx_ctx* ctx, int enable);
 ocpx_status ocpx_profile_read(ocpx_ctx* ctx, double* ms, uint64_t* launches);
 

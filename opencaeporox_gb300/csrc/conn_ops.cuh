@@ -186,19 +186,35 @@ OCPX_HD void conn_jac_blocks(const Model& M, const BulkView& b, const ConnView& 
             rowU[np + j * nc + i] += transJ * xi * dP;
         }
     }
-    // bmat = dt * (dFdXs * dSec) + dt * dFdXp
+    // bmat = dt * (dFdXs * dSec) + dt * dFdXp.  The reference forms the product
+    // with BLAS dgemm (DaABpbC, src/DenseMat.cpp:61-85), whose rounding is
+    // that of fused multiply-adds in some order; here: fused multiply-adds in
+    // column order.  In the compositional model the rows of dSec_dPri for the
+    // water phase's composition are identically zero (the water composition
+    // is fixed, CaldXsdXpW), so their columns of dFdXs are skipped.
+    const int kend = (M.mixture == 1) ? np + (np - 1) * nc : ncol2;
     for (int side = 0; side < 2; side++) {
         const double* Xs = side == 0 ? dFdXsB : dFdXsE;
         const double* Xp = side == 0 ? dFdXpB : dFdXpE;
         const int cell = side == 0 ? bId : eId;
         double* out = side == 0 ? bmatB : bmatE;
-        for (int r = 0; r < ncol; r++) {
-            for (int col = 0; col < ncol; col++) {
-                double acc = 0;
-                if (r > 0)
-                    for (int k = 0; k < ncol2; k++) acc += Xs[r * ncol2 + k] * b.dSec_dPri[b.idx(k * ncol + col, cell)];
+        for (int col = 0; col < ncol; col++) out[col] = dt * 0.0 + dt * (col == 0 ? Xp[0] : 0.0);
+        for (int r = 1; r < ncol; r++) {
+            double acc[NCOL];
+#pragma unroll
+            for (int col = 0; col < NCOL; col++) acc[col] = 0;
+            for (int k = 0; k < kend; k++) {
+                const double x = Xs[r * ncol2 + k];
+                const double* ds = b.dSec_dPri + (size_t)(k * ncol) * b.nb + cell;
+#pragma unroll
+                for (int col = 0; col < NCOL; col++)
+                    if (col < ncol) acc[col] = fma(x, ds[(size_t)col * b.nb], acc[col]);
+            }
+#pragma unroll
+            for (int col = 0; col < NCOL; col++) {
+                if (col >= ncol) break;
                 const double cv0 = (col == 0) ? Xp[r] : 0.0;
-                out[r * ncol + col] = dt * acc + dt * cv0;
+                out[r * ncol + col] = dt * acc[col] + dt * cv0;
             }
         }
     }

@@ -112,8 +112,8 @@ struct EosPR {
         }
         const double tmp1 = -R + sqrt(M);
         const double tmp2 = R + sqrt(M);
-        const double S = sign_d(tmp1) * pow(fabs(tmp1), 1.0 / 3);
-        const double Tt = -sign_d(tmp2) * pow(fabs(tmp2), 1.0 / 3);
+        const double S = sign_d(tmp1) * pow_third(fabs(tmp1));
+        const double Tt = -sign_d(tmp2) * pow_third(fabs(tmp2));
         z[0] = S + Tt - a / 3;
         nt_cubic(z[0], a, b, c);
         return 1;

@@ -129,8 +129,8 @@ struct CompFlash {
         for (int i = 0; i < NC; i++) {
             Kw[0][i] = (m->Pc[i] / P) * exp(5.373 * (1 + m->acf[i]) * (1 - m->Tc[i] / T));
             Kw[1][i] = 1 / Kw[0][i];
-            Kw[2][i] = pow(Kw[0][i], 1.0 / 3);
-            Kw[3][i] = pow(Kw[1][i], 1.0 / 3);
+            Kw[2][i] = pow_third(Kw[0][i]);
+            Kw[3][i] = pow_third(Kw[1][i]);
         }
     }
 
@@ -893,7 +893,8 @@ struct CompCellUpdate {
                         Af[i * NC + j] = v;
                         Af[j * NC + i] = v;
                     }
-                const float eig = sym_min_eig_f32<NCM>(NC, Af, f.W);
+                float Wf[NCM * NCM];
+                const float eig = sym_min_eig_f32<NCM>(NC, Af, Wf);
                 b.skip_flag[cell] = 1;
                 b.skip_minEig[cell] = (double)eig;
                 b.skip_P[cell] = P;

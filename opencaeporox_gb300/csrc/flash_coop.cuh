@@ -87,7 +87,9 @@ struct CoopPE {
         if (act) v[i] = term;
         __syncwarp();
         double acc = 0;
-        for (int k = 0; k < NC; k++) acc += v[k];
+#pragma unroll
+        for (int k = 0; k < NCM; k++)
+            if (k < NC) acc += v[k];
         __syncwarp();
         return acc;
     }
@@ -144,31 +146,127 @@ struct CoopPE {
         }
         __syncwarp();
         double a = 0, bsum = 0;
-        for (int i1 = 0; i1 < NC; i1++) {
-            bsum += tB[i1];
-            a += tA[i1 * NCM + i1];
-            for (int i2 = 0; i2 < i1; i2++) a += tA[i1 * NCM + i2];
+#pragma unroll
+        for (int i1 = 0; i1 < NCM; i1++) {
+            if (i1 < NC) {
+                bsum += tB[i1];
+                a += tA[i1 * NCM + i1];
+#pragma unroll
+                for (int i2 = 0; i2 < i1; i2++) a += tA[i1 * NCM + i2];
+            }
         }
         Aj = a;
         Bj = bsum;
         __syncwarp();
     }
 
-    // EoS_PR::CalFugPhi: fugacity and phi of the own component
+    // EoS_PR::CalZj with CubicRoot, the independent operations spread over
+    // lanes of the half so that one warp instruction sequence serves several
+    // of them: the two divisions of Q and R (lanes 0-1), the square roots
+    // (lanes 0-1), the three trigonometric roots and their Newton refinements
+    // (lanes 0-2) or the two Cardano cube roots (lanes 0-1), and the two
+    // logarithms of the Gibbs-energy test (lanes 0-1).  The expressions are
+    // those of EosPR::zj_of / cubic_root / nt_cubic, so the bits are the same.
+    // Every shuffle is made by the whole warp, outside the branches (the two
+    // halves may be in different root cases).
+    __device__ double zj_lanes() const
+    {
+        const int hb = h * 16;
+        const double a = (DELTA1 + DELTA2 - 1) * Bj - 1;
+        const double b = (Aj + DELTA1 * DELTA2 * Bj * Bj - (DELTA1 + DELTA2) * Bj * (Bj + 1));
+        const double c = -(Aj * Bj + DELTA1 * DELTA2 * Bj * Bj * (Bj + 1));
+        const double qr = (i == 1) ? (2 * a * a * a - 9 * a * b + 27 * c) / 54 : (a * a - 3 * b) / 9;
+        const double Q = __shfl_sync(FULL_MASK, qr, hb);
+        const double R = __shfl_sync(FULL_MASK, qr, hb + 1);
+        const double Q3 = Q * Q * Q;
+        const double M = R * R - Q3;
+        const bool three = M <= 0;
+        const double sv = sqrt(three ? (i == 1 ? Q : Q3) : M);
+        const double s0 = __shfl_sync(FULL_MASK, sv, hb);
+        const double s1 = __shfl_sync(FULL_MASK, sv, hb + 1);
+        double zl;
+        if (three) {
+            const double theta = acos(R / s0);
+            const double t = (i == 1) ? (theta + 2 * PI_REF) : (i == 2 ? (theta - 2 * PI_REF) : theta);
+            zl = -2 * s1 * cos(t / 3) - a / 3;
+        }
+        else {
+            const double tmp1 = -R + s0;
+            const double tmp2 = R + s0;
+            zl = pow_third(fabs(i == 1 ? tmp2 : tmp1));
+        }
+        const double c0 = __shfl_sync(FULL_MASK, zl, hb);
+        const double c1 = __shfl_sync(FULL_MASK, zl, hb + 1);
+        if (!three) {
+            const double tmp1 = -R + s0;
+            const double tmp2 = R + s0;
+            const double S = sign_d(tmp1) * c0;
+            const double Tt = -sign_d(tmp2) * c1;
+            zl = S + Tt - a / 3;
+        }
+        EosPR<NCM>::nt_cubic(zl, a, b, c);
+        const double r0 = __shfl_sync(FULL_MASK, zl, hb);
+        const double r1 = __shfl_sync(FULL_MASK, zl, hb + 1);
+        const double r2 = __shfl_sync(FULL_MASK, zl, hb + 2);
+        double zj1 = r0, zj2 = r0, lv = 0;
+        if (three) {
+            double z0 = r0, z1 = r1, z2 = r2, t;
+            if (z1 < z0) { t = z0; z0 = z1; z1 = t; }
+            if (z2 < z1) { t = z1; z1 = z2; z2 = t; }
+            if (z1 < z0) { t = z0; z0 = z1; z1 = t; }
+            zj1 = z0;
+            zj2 = z2;
+            const double num = (i == 1) ? (zj1 + DELTA1 * Bj) * (zj2 + DELTA2 * Bj) : zj1 - Bj;
+            const double den = (i == 1) ? ((zj1 + DELTA2 * Bj) * (zj2 + DELTA1 * Bj)) : zj2 - Bj;
+            lv = log(num / den);
+        }
+        const double lA = __shfl_sync(FULL_MASK, lv, hb);
+        const double lB = __shfl_sync(FULL_MASK, lv, hb + 1);
+        if (!three) return r0;
+        const double dG = (zj2 - zj1) + lA - Aj / (Bj * (DELTA2 - DELTA1)) * lB;
+        return dG > 0 ? zj1 : zj2;
+    }
+
+    // EoS_PR::CalFugPhi: fugacity and phi of the own component.  Divisions
+    // share instruction sequences across lanes: the logarithm arguments and
+    // Aj/(d1-d2) in one, then Bi/Bj, tmp/Aj and c1 (secondary lanes i+8 when
+    // NC <= 8, otherwise in sequence).
     __device__ void fug_phi(double& fug, double& phi)
     {
         AjBj();
-        Zj = EosPR<NCM>::zj_of(Aj, Bj);
-        // the two logarithms on two lanes of the half
-        const double arg = (i == 1) ? (Zj + DELTA1 * Bj) / (Zj + DELTA2 * Bj) : (Zj - Bj);
-        const double lv = log(arg);
-        const double l1 = __shfl_sync(FULL_MASK, lv, h * 16);
-        const double lg = __shfl_sync(FULL_MASK, lv, h * 16 + 1);
-        const double c1 = Aj / (DELTA1 - DELTA2) / Bj;
+        Zj = zj_lanes();
+        const int hb = h * 16;
+        const double num1 = (i == 1) ? Zj + DELTA1 * Bj : (i == 2 ? Aj : Zj - Bj);
+        const double den1 = (i == 1) ? Zj + DELTA2 * Bj : (i == 2 ? (DELTA1 - DELTA2) : 1.0);
+        const double q1 = num1 / den1;
+        const double lv = log(q1);
+        const double l1 = __shfl_sync(FULL_MASK, lv, hb);
+        const double lg = __shfl_sync(FULL_MASK, lv, hb + 1);
+        const double c1a = __shfl_sync(FULL_MASK, q1, hb + 2);
         const double* x = sh.xs[h];
+        const bool paired = NC <= 8;
+        const int comp = (paired && i >= 8) ? i - 8 : ic;
+        const int cc = comp < NC ? comp : 0;
         double tmp = 0;
-        for (int k = 0; k < NC; k++) tmp += 2 * omb(ic, k) * sh.s[ic * NCM + k] * x[k];
-        const double ph = exp(Bi / Bj * (Zj - 1) - l1 - c1 * (tmp / Aj - Bi / Bj) * lg);
+        for (int k = 0; k < NC; k++) tmp += 2 * omb(cc, k) * sh.s[cc * NCM + k] * x[k];
+        double BiBj, tA, c1;
+        if (paired) {
+            // lane i: Bi/Bj; lane i+8: tmp/Aj of component i; lane 15 (free when NC <= 7): c1
+            const bool second = i >= 8;
+            const double num = second ? (i == 15 && NC <= 7 ? c1a : tmp) : Bi;
+            const double den = second ? (i == 15 && NC <= 7 ? Bj : Aj) : Bj;
+            const double q = num / den;
+            const double qo = __shfl_xor_sync(FULL_MASK, q, 8);
+            BiBj = q;
+            tA = qo;
+            c1 = (NC <= 7) ? __shfl_sync(FULL_MASK, q, hb + 15) : c1a / Bj;
+        }
+        else {
+            BiBj = Bi / Bj;
+            tA = tmp / Aj;
+            c1 = c1a / Bj;
+        }
+        const double ph = exp(BiBj * (Zj - 1) - l1 - c1 * (tA - BiBj) * lg);
         phi = ph;
         fug = ph * x[ic] * P;
     }
@@ -177,7 +275,7 @@ struct CoopPE {
     __device__ void lnfugX()
     {
         AjBj();
-        Zj = EosPR<NCM>::zj_of(Aj, Bj);
+        Zj = zj_lanes();
         const double* x = sh.xs[h];
         const double num = EosPR<NCM>::dz_num_of(Aj, Bj, Zj), den = EosPR<NCM>::dz_den_of(Aj, Bj, Zj);
         double tmp = 0;
@@ -217,7 +315,7 @@ struct CoopPE {
     __device__ void lnfugN(double nt)
     {
         AjBj();
-        Zj = EosPR<NCM>::zj_of(Aj, Bj);
+        Zj = zj_lanes();
         const double* x = sh.xs[h];
         const double num = EosPR<NCM>::dz_num_of(Aj, Bj, Zj), den = EosPR<NCM>::dz_den_of(Aj, Bj, Zj);
         double tmp = 0;
@@ -266,8 +364,8 @@ struct CoopPE {
         if (act) {
             Kw0 = (m.Pc[i] / P) * exp(5.373 * (1 + m.acf[i]) * (1 - m.Tc[i] / T));
             Kw1 = 1 / Kw0;
-            Kw2 = pow(Kw0, 1.0 / 3);
-            Kw3 = pow(Kw1, 1.0 / 3);
+            Kw2 = pow_third(Kw0);
+            Kw3 = pow_third(Kw1);
         }
         else {
             Kw0 = Kw1 = Kw2 = Kw3 = 1;
@@ -490,7 +588,10 @@ struct CoopPE {
     }
 
     // ---------------------------------------------------------- split ----
-    // RachfordRice2, evaluated redundantly (identically) by both halves
+    // RachfordRice2.  Both halves hold the same K and z; they split the work
+    // of each iteration: half 0 forms the terms of the function, half 1 those
+    // of its derivative (one division sequence for both), and each half adds
+    // up its own terms in component order (one addition chain for both).
     __device__ void rachford_rice2()
     {
         double* Kv = sh.K[h];
@@ -502,27 +603,29 @@ struct CoopPE {
             if (Kv[k] > Kmax) Kmax = Kv[k];
         }
         __syncwarp();
-        const double numin = 1 / (1 - Kmax);
-        const double numax = 1 / (1 - Kmin);
+        const double qb = 1 / ((i == 1) ? (1 - Kmin) : (1 - Kmax));
+        const double numin = __shfl_sync(FULL_MASK, qb, h * 16);
+        const double numax = __shfl_sync(FULL_MASK, qb, h * 16 + 1);
         nu0 = 0.5 * (numin + numax);
         int iter = 0;
         const double tol = m.rr_tol;
         const double maxIt = m.rr_maxit;
-        double* tr = sh.v1[h];
-        double* tj = sh.v2[h];
+        double* tv = sh.v1[h];
         while (true) {
-            if (act) {
-                const double tmp = 1 + nu0 * (Ks - 1);
-                tr[i] = z * (Ks - 1) / tmp;
-                tj[i] = z * (Ks - 1) * (Ks - 1) / (tmp * tmp);
-            }
+            const double tmp = 1 + nu0 * (Ks - 1);
+            const double zk = z * (Ks - 1);
+            // half 0: z (K-1) / t; half 1: z (K-1) (K-1) / (t t)
+            const double q = (h ? zk * (Ks - 1) : zk) / (h ? tmp * tmp : tmp);
+            if (act) tv[i] = q;
             __syncwarp();
-            double rj = 0, Jr = 0;
-            for (int k = 0; k < NC; k++) {
-                rj += tr[k];
-                Jr -= tj[k];
-            }
+            // half 0: rj += term; half 1: Jr -= term
+            double acc = 0;
+#pragma unroll
+            for (int k = 0; k < NCM; k++)
+                if (k < NC) acc += h ? -tv[k] : tv[k];
             __syncwarp();
+            const double rj = __shfl_sync(FULL_MASK, acc, 0);
+            const double Jr = __shfl_sync(FULL_MASK, acc, 16);
             if (fabs(rj) < tol || iter > maxIt) break;
             const double dnuj = -rj / Jr;
             const double tmpnu = nu0 + dnuj;
@@ -584,8 +687,11 @@ struct CoopPE {
             update_x_rr();
             double p0, p1;
             fug_both(f0, f1, p0, p1);
-            Se = osum(sq(f1 / f0 - 1));
-            Ks = p1 / p0;
+            // half 0: f1/f0 for Se; half 1: phi1/phi0, the new K (one division sequence)
+            const double q = (h ? p1 : f1) / (h ? p0 : f0);
+            const double qo = __shfl_xor_sync(FULL_MASK, q, 16);
+            Ks = h ? q : qo;
+            Se = osum(sq((h ? qo : q) - 1));
             iter++;
             if (iter > maxIt) {
                 ssm_sp_conv = false;
@@ -638,8 +744,11 @@ struct CoopPE {
             nu0 = osum(n0);
             nu1 = 1;
             nu1 -= nu0;
-            x0 = fabs(n0 / nu0);
-            x1 = fabs(n1 / nu1);
+            // half 0: n0 / nu0, half 1: n1 / nu1 (one division sequence)
+            const double qx = (h ? n1 : n0) / (h ? nu1 : nu0);
+            const double qxo = __shfl_xor_sync(FULL_MASK, qx, 16);
+            x0 = fabs(h ? qxo : qx);
+            x1 = fabs(h ? qx : qxo);
             double p0, p1;
             fug_both(f0, f1, p0, p1);
             res = log(f1 / f0);
@@ -653,7 +762,9 @@ struct CoopPE {
                 double* v = sh.v1[h];
                 if (act) v[i] = (ln1 - n1) * (ln1 - n1);
                 __syncwarp();
-                for (int k = 0; k < NC; k++) en += v[k];
+#pragma unroll
+                for (int k = 0; k < NCM; k++)
+                    if (k < NC) en += v[k];
                 __syncwarp();
             }
             if (en < 1E-16 * (2 * NC) * (2 * NC)) {

@@ -195,16 +195,21 @@ cudaError_t launch_jac_rows(const BulkView& b, const ConnView& cv, const double*
     if (b.nb) k_jac_rows<<<grid_for(b.nb, block), block, 0, s>>>(b, cv, bmat, rowptr, val);
     return cudaGetLastError();
 }
-// Predicted work of a cell's next flash: the work units its last flash used
-// (iteration counters weighted as the flash's budget charges them, Rachford-
-// Rice iterations at a fifth), as a bucket in descending order of cost.
+// Sort key of a cell for the batched flash: its class (skip-flagged cells,
+// which usually skip the equilibrium; two-phase cells, which run the split
+// and the two-phase derivatives; one-phase cells, which run the stability
+// test), then the work units its last flash used (iteration counters weighted
+// as the flash's budget charges them, Rachford-Rice iterations at a fifth), in
+// descending order.  Warps then hold cells on the same code path.
 __device__ __forceinline__ int cost_bucket(const BulkView& b, int cell)
 {
     const int32_t* it = b.iters;
     const long long w = 3LL + it[b.idx(0, cell)] + 4LL * it[b.idx(1, cell)] + 2LL * it[b.idx(2, cell)] +
                         6LL * it[b.idx(3, cell)] + it[b.idx(4, cell)] / 5;
-    const int bucket = w < COST_BUCKETS - 1 ? (int)w : COST_BUCKETS - 1;
-    return COST_BUCKETS - 1 - bucket;
+    const int lvl = w < 63 ? (int)w : 63;
+    const bool two = b.phaseExist[b.idx(0, cell)] && b.phaseExist[b.idx(1, cell)];
+    const int cls = b.skip_flag[cell] ? 2 : (two ? 0 : 1);
+    return cls * 64 + (63 - lvl);
 }
 
 __global__ void k_cost_hist(BulkView b, unsigned* __restrict__ hist)

@@ -77,17 +77,22 @@ cudaError_t OCPX_CAT(launch_flash_comp_, OCPX_NCM)(const Model* dm, const BulkVi
 }
 
 cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const BulkView& b, const int* order,
-                                                      const FlashBatch& fb, cudaStream_t s)
+                                                      const FlashBatch& fb, int part, cudaStream_t s)
 {
     if (b.nb == 0) return cudaSuccess;
-    const DeferSink sink{fb.rec, fb.count, fb.cap};
-    k_flash_budget<OCPX_NCM><<<(b.nb + fb.block - 1) / fb.block, fb.block, 0, s>>>(dm, b, order, fb.budget, sink);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_flash_pe_coop<OCPX_NCM><<<fb.coop_blocks, COOP_WARPS * 32, 0, s>>>(dm, b, fb.rec, fb.count, fb.cap, fb.pe);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_flash_post<OCPX_NCM><<<(fb.cap + 127) / 128, 128, 0, s>>>(dm, b, fb.rec, fb.count, fb.cap, fb.pe);
+    switch (part) {
+    case 0: {
+        const DeferSink sink{fb.rec, fb.count, fb.cap};
+        k_flash_budget<OCPX_NCM><<<(b.nb + fb.block - 1) / fb.block, fb.block, 0, s>>>(dm, b, order, fb.budget, sink);
+        break;
+    }
+    case 1:
+        k_flash_pe_coop<OCPX_NCM><<<fb.coop_blocks, COOP_WARPS * 32, 0, s>>>(dm, b, fb.rec, fb.count, fb.cap, fb.pe);
+        break;
+    default:
+        k_flash_post<OCPX_NCM><<<(fb.cap + 127) / 128, 128, 0, s>>>(dm, b, fb.rec, fb.count, fb.cap, fb.pe);
+        break;
+    }
     return cudaGetLastError();
 }
 

@@ -92,45 +92,46 @@ OCPX_HD bool gen_solve_colmajor(int n, const double* Abuf, double* B, int nrhs, 
 }
 
 // Smallest eigenvalue of a symmetric matrix given in single precision (the
-// reference builds the skip-test matrix as float and calls ssyevd_).  Cyclic
-// Jacobi on the float values carried in double precision, result rounded to
-// float; the iteration count is capped.
+// reference builds the skip-test matrix as float and calls ssyevd_, which
+// works in single precision).  Cyclic Jacobi in single precision: on GB300
+// the FP32 pipe issues 64 times the FP64 rate, and the skip test's tolerance
+// is set by FP32 anyway.  The sweep count is capped.
 template <int NM>
-OCPX_HD_NOINLINE float sym_min_eig_f32(int n, const float* Af, double* A)
+OCPX_HD_NOINLINE float sym_min_eig_f32(int n, const float* Af, float* A)
 {
     for (int i = 0; i < n; i++)
-        for (int j = 0; j < n; j++) A[i * NM + j] = (double)Af[i * n + j];
+        for (int j = 0; j < n; j++) A[i * NM + j] = Af[i * n + j];
     for (int sweep = 0; sweep < 30; sweep++) {
-        double off = 0, diag = 0;
+        float off = 0, diag = 0;
         for (int i = 0; i < n; i++) {
             diag += A[i * NM + i] * A[i * NM + i];
             for (int j = i + 1; j < n; j++) off += A[i * NM + j] * A[i * NM + j];
         }
-        if (off <= 1e-34 * diag || off == 0.0) break;
+        if (off <= 1e-13f * diag || off == 0.0f) break;
         for (int p = 0; p < n - 1; p++)
             for (int q = p + 1; q < n; q++) {
-                const double apq = A[p * NM + q];
-                if (apq == 0.0) continue;
-                const double app = A[p * NM + p], aqq = A[q * NM + q];
-                const double theta = (aqq - app) / (2.0 * apq);
-                const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                const double c = 1.0 / sqrt(t * t + 1.0);
-                const double s = t * c;
+                const float apq = A[p * NM + q];
+                if (apq == 0.0f) continue;
+                const float app = A[p * NM + p], aqq = A[q * NM + q];
+                const float theta = (aqq - app) / (2.0f * apq);
+                const float t = (theta >= 0 ? 1.0f : -1.0f) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+                const float c = 1.0f / sqrtf(t * t + 1.0f);
+                const float s = t * c;
                 for (int k = 0; k < n; k++) {
-                    const double akp = A[k * NM + p], akq = A[k * NM + q];
+                    const float akp = A[k * NM + p], akq = A[k * NM + q];
                     A[k * NM + p] = c * akp - s * akq;
                     A[k * NM + q] = s * akp + c * akq;
                 }
                 for (int k = 0; k < n; k++) {
-                    const double apk = A[p * NM + k], aqk = A[q * NM + k];
+                    const float apk = A[p * NM + k], aqk = A[q * NM + k];
                     A[p * NM + k] = c * apk - s * aqk;
                     A[q * NM + k] = s * apk + c * aqk;
                 }
             }
     }
-    double mn = A[0];
+    float mn = A[0];
     for (int i = 1; i < n; i++) mn = A[i * NM + i] < mn ? A[i * NM + i] : mn;
-    return (float)mn;
+    return mn;
 }
 
 }  // namespace ocpx

@@ -17,11 +17,11 @@ cudaError_t launch_flash_comp_6(const Model*, const BulkView&, int, cudaStream_t
 cudaError_t launch_flash_comp_8(const Model*, const BulkView&, int, cudaStream_t);
 cudaError_t launch_flash_comp_10(const Model*, const BulkView&, int, cudaStream_t);
 cudaError_t launch_flash_comp_12(const Model*, const BulkView&, int, cudaStream_t);
-cudaError_t launch_flash_batched_4(const Model*, const BulkView&, const int*, const FlashBatch&, cudaStream_t);
-cudaError_t launch_flash_batched_6(const Model*, const BulkView&, const int*, const FlashBatch&, cudaStream_t);
-cudaError_t launch_flash_batched_8(const Model*, const BulkView&, const int*, const FlashBatch&, cudaStream_t);
-cudaError_t launch_flash_batched_10(const Model*, const BulkView&, const int*, const FlashBatch&, cudaStream_t);
-cudaError_t launch_flash_batched_12(const Model*, const BulkView&, const int*, const FlashBatch&, cudaStream_t);
+cudaError_t launch_flash_batched_4(const Model*, const BulkView&, const int*, const FlashBatch&, int, cudaStream_t);
+cudaError_t launch_flash_batched_6(const Model*, const BulkView&, const int*, const FlashBatch&, int, cudaStream_t);
+cudaError_t launch_flash_batched_8(const Model*, const BulkView&, const int*, const FlashBatch&, int, cudaStream_t);
+cudaError_t launch_flash_batched_10(const Model*, const BulkView&, const int*, const FlashBatch&, int, cudaStream_t);
+cudaError_t launch_flash_batched_12(const Model*, const BulkView&, const int*, const FlashBatch&, int, cudaStream_t);
 
 cudaError_t launch_flash_comp(int ncm, const Model* dm, const BulkView& b, int block, cudaStream_t s)
 {
@@ -35,14 +35,14 @@ cudaError_t launch_flash_comp(int ncm, const Model* dm, const BulkView& b, int b
     }
 }
 cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, const int* order,
-                                 const FlashBatch& fb, cudaStream_t s)
+                                 const FlashBatch& fb, int part, cudaStream_t s)
 {
     switch (ncm) {
-    case 4: return launch_flash_batched_4(dm, b, order, fb, s);
-    case 6: return launch_flash_batched_6(dm, b, order, fb, s);
-    case 8: return launch_flash_batched_8(dm, b, order, fb, s);
-    case 10: return launch_flash_batched_10(dm, b, order, fb, s);
-    case 12: return launch_flash_batched_12(dm, b, order, fb, s);
+    case 4: return launch_flash_batched_4(dm, b, order, fb, part, s);
+    case 6: return launch_flash_batched_6(dm, b, order, fb, part, s);
+    case 8: return launch_flash_batched_8(dm, b, order, fb, part, s);
+    case 10: return launch_flash_batched_10(dm, b, order, fb, part, s);
+    case 12: return launch_flash_batched_12(dm, b, order, fb, part, s);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -147,25 +147,33 @@ struct ocpx_ctx {
         free_events.pop_back();
         return e;
     }
-    void stage_begin(int s)
+    int stage_begin(int s)
     {
-        if (!prof) return;
+        if (!prof) return -1;
         Mark m{s, take_event(), take_event()};
         cudaEventRecord(m.a, stream);
         marks.push_back(m);
+        return (int)marks.size() - 1;
     }
-    void stage_end()
+    void stage_end(int idx)
     {
-        if (!prof || marks.empty()) return;
-        cudaEventRecord(marks.back().b, stream);
+        if (idx < 0) return;
+        cudaEventRecord(marks[idx].b, stream);
     }
     // device-side checkpoints of the mutable bulk state
     char* ckpt[2] = {nullptr, nullptr};
     size_t state_off = 0, state_bytes = 0;
-    // graph of one Newton iteration (variant 1)
+    // CUDA graph of one Newton iteration (properties, residual, Jacobian) of
+    // the batched variant, captured for one dt and launch configuration
     cudaGraphExec_t graph_exec = nullptr;
-    double graph_dt = -1, graph_dSmax = -1;
-    bool graph_with_update = false;
+    double graph_dt = -1;
+    uint64_t graph_launches = 0;    // kernels in the graph
+    void drop_graph()
+    {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
+        graph_dt = -1;
+    }
 
     FieldInfo field(ocpx_field f) const;
 };
@@ -387,7 +395,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
 void ocpx_destroy(ocpx_ctx* ctx)
 {
     if (!ctx) return;
-    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    ctx->drop_graph();
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (char* c : ctx->ckpt)
         if (c) cudaFree(c);
@@ -457,18 +465,24 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
 {
     cudaStream_t s = ctx->stream;
     OCPX_CUDA(cudaMemsetAsync(ctx->flags, 0, sizeof(uint32_t) * 4, s));
-    ctx->stage_begin(0);
+    int mk = ctx->stage_begin(0);
     OCPX_CUDA(launch_check(ctx->b, ctx->flags, ctx->block_cell, s));
-    ctx->stage_end();
+    ctx->stage_end(mk);
     ctx->launches++;
-    ctx->stage_begin(1);
+    const int mk_flash = ctx->stage_begin(1);
     if (ctx->host_model.mixture == 1) {
         if (ctx->variant == 1) {
             OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned), s));
+            mk = ctx->stage_begin(9);
             OCPX_CUDA(launch_cost_order(ctx->b, ctx->cost_hist, ctx->order, s));
+            ctx->stage_end(mk);
             const FlashBatch fb{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
                                 ctx->defer_rec, ctx->defer_count, ctx->pe_res};
-            OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fb, s));
+            for (int part = 0; part < 3; part++) {
+                mk = ctx->stage_begin(10 + part);
+                OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fb, part, s));
+                ctx->stage_end(mk);
+            }
             ctx->launches += 6;
         }
         else {
@@ -480,14 +494,14 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
         OCPX_CUDA(launch_flash_bo(ctx->d_model, ctx->b, ctx->block_cell, s));
         ctx->launches++;
     }
-    ctx->stage_end();
-    ctx->stage_begin(2);
+    ctx->stage_end(mk_flash);
+    mk = ctx->stage_begin(2);
     OCPX_CUDA(launch_krpc_rock(ctx->d_model, ctx->b, ctx->block_cell, s));
-    ctx->stage_end();
+    ctx->stage_end(mk);
     ctx->launches++;
-    ctx->stage_begin(3);
+    mk = ctx->stage_begin(3);
     OCPX_CUDA(launch_report(ctx->b, ctx->flags + 1, ctx->block_cell, s));
-    ctx->stage_end();
+    ctx->stage_end(mk);
     ctx->launches++;
     return OCPX_OK;
 }
@@ -495,13 +509,13 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
 ocpx_status enqueue_calres(ocpx_ctx* ctx, double dt)
 {
     cudaStream_t s = ctx->stream;
-    ctx->stage_begin(4);
+    int mk = ctx->stage_begin(4);
     OCPX_CUDA(launch_conn_flux(ctx->d_model, ctx->b, ctx->cv, ctx->block_conn, s));
-    ctx->stage_end();
-    ctx->stage_begin(5);
+    ctx->stage_end(mk);
+    mk = ctx->stage_begin(5);
     OCPX_CUDA(launch_residual(ctx->b, ctx->cv, dt, ctx->res, ctx->resRelV, ctx->resRelN, ctx->rownorm, ctx->norm_out,
                               ctx->block_cell, s));
-    ctx->stage_end();
+    ctx->stage_end(mk);
     ctx->launches += 3;
     return OCPX_OK;
 }
@@ -509,12 +523,12 @@ ocpx_status enqueue_calres(ocpx_ctx* ctx, double dt)
 ocpx_status enqueue_assemble(ocpx_ctx* ctx, double dt)
 {
     cudaStream_t s = ctx->stream;
-    ctx->stage_begin(6);
+    int mk = ctx->stage_begin(6);
     OCPX_CUDA(launch_jac_conn(ctx->nct_cap, ctx->d_model, ctx->b, ctx->cv, dt, ctx->bmat, ctx->block_conn, s));
-    ctx->stage_end();
-    ctx->stage_begin(7);
+    ctx->stage_end(mk);
+    mk = ctx->stage_begin(7);
     OCPX_CUDA(launch_jac_rows(ctx->b, ctx->cv, ctx->bmat, ctx->jac_rowptr, ctx->jac_val, ctx->block_cell, s));
-    ctx->stage_end();
+    ctx->stage_end(mk);
     ctx->launches += 2;
     return OCPX_OK;
 }
@@ -576,20 +590,68 @@ ocpx_status ocpx_newton_update(ocpx_ctx* ctx, const double* u_host, double dSmax
     if (!ctx || !u_host) return fail(OCPX_INVALID_ARG, "null argument");
     const size_t bytes = sizeof(double) * (size_t)ctx->nb * (ctx->nc + 1);
     OCPX_CUDA(cudaMemcpyAsync(ctx->u, u_host, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    ctx->stage_begin(8);
+    const int mk = ctx->stage_begin(8);
     OCPX_CUDA(launch_newton_update(ctx->b, ctx->u, dSmax, ctx->block_cell, ctx->stream));
-    ctx->stage_end();
+    ctx->stage_end(mk);
     ctx->launches++;
     return OCPX_OK;
 }
 
-ocpx_status ocpx_enqueue_step(ocpx_ctx* ctx, double dt)
+}  // extern "C"
+
+namespace {
+
+ocpx_status enqueue_step_kernels(ocpx_ctx* ctx, double dt)
 {
-    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
     ocpx_status st;
     if ((st = enqueue_properties(ctx)) != OCPX_OK) return st;
     if ((st = enqueue_calres(ctx, dt)) != OCPX_OK) return st;
     return enqueue_assemble(ctx, dt);
+}
+
+// Capture the step into a CUDA graph (batched variant).  The graph holds no
+// host work, so one launch replays every kernel and memset of the step.
+ocpx_status capture_step(ocpx_ctx* ctx, double dt)
+{
+    ctx->drop_graph();
+    const uint64_t l0 = ctx->launches;
+    OCPX_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const ocpx_status st = enqueue_step_kernels(ctx, dt);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (st != OCPX_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return fail(OCPX_CUDA_ERROR, std::string("graph capture: ") + cudaGetErrorString(e));
+    const cudaError_t ei = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        ctx->graph_exec = nullptr;
+        return fail(OCPX_CUDA_ERROR, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+    }
+    ctx->graph_dt = dt;
+    ctx->graph_launches = ctx->launches - l0;
+    ctx->launches = l0;
+    return OCPX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ocpx_status ocpx_enqueue_step(ocpx_ctx* ctx, double dt)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    // stage profiling records events between the kernels: run those steps eagerly
+    if (ctx->variant != 1 || ctx->prof) return enqueue_step_kernels(ctx, dt);
+    if (!ctx->graph_exec || ctx->graph_dt != dt) {
+        const ocpx_status st = capture_step(ctx, dt);
+        if (st != OCPX_OK) return st;
+    }
+    OCPX_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    ctx->launches += ctx->graph_launches;
+    return OCPX_OK;
 }
 
 ocpx_status ocpx_step_report(ocpx_ctx* ctx, ocpx_report* rep)
@@ -697,12 +759,14 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant)
 {
     if (!ctx || (variant != 0 && variant != 1)) return fail(OCPX_INVALID_ARG, "variant must be 0 or 1");
     ctx->variant = variant;
+    ctx->drop_graph();
     return OCPX_OK;
 }
 
 ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value)
 {
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    ctx->drop_graph();
     switch (p) {
     case OCPX_PARAM_FLASH_BUDGET:
         if (value < 0 || value > 0x7fffffffLL) return fail(OCPX_INVALID_ARG, "flash budget out of range");
@@ -749,9 +813,7 @@ ocpx_status ocpx_step(ocpx_ctx* ctx, const double* u_host, double dSmax, double 
         st = ocpx_newton_update(ctx, u_host, dSmax);
         if (st != OCPX_OK) return st;
     }
-    if ((st = enqueue_properties(ctx)) != OCPX_OK) return st;
-    if ((st = enqueue_calres(ctx, dt)) != OCPX_OK) return st;
-    if ((st = enqueue_assemble(ctx, dt)) != OCPX_OK) return st;
+    if ((st = ocpx_enqueue_step(ctx, dt)) != OCPX_OK) return st;
     const size_t bsize = (size_t)(ctx->nc + 1) * (ctx->nc + 1);
     if (res_host)
         OCPX_CUDA(cudaMemcpyAsync(res_host, ctx->res, sizeof(double) * (size_t)ctx->nb * (ctx->nc + 1),

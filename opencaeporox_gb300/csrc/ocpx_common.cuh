@@ -189,4 +189,28 @@ OCPX_HD double sq(double x) { return x * x; }
 OCPX_HD double sign_d(double d) { return d > 0 ? 1.0 : (d < 0 ? -1.0 : 0.0); }
 OCPX_HD bool finite_d(double x) { return (x - x) == 0.0; }
 
+// pow(x, 1.0 / 3) for x >= 0, the cube roots of CubicRoot (src/UtilMath.cpp:15-53)
+// and CalKwilson.  The exponent 1.0/3 is the double nearest 1/3, below it by
+// d = 1/3 - fl(1/3) = 1.8503717077085942e-17, so
+//     x^fl(1/3) = cbrt(x) * exp(-d ln x) = cbrt(x) * (1 - d ln x) + O((d ln x)^2),
+// with |d ln x| < 1.4e-14 over the whole double range (the dropped term is
+// below 1e-28).  The correction is at most ~62 ulp of cbrt(x), so ln x is
+// needed only to single precision: ln x = e ln 2 + ln m from frexp and a
+// single-precision logarithm.  Error: cbrt's (1 ulp, CUDA) plus one rounding
+// of the fused multiply-add.  On GB300 this costs about a fifth of pow().
+OCPX_HD double pow_third(double x)
+{
+#ifdef __CUDA_ARCH__
+    if (!(x > 0.0) || !finite_d(x)) return pow(x, 1.0 / 3);
+    const double c = cbrt(x);
+    int e;
+    const double m = frexp(x, &e);
+    const float L = __logf((float)m) + (float)e * 0.693147180559945309f;
+    const double corr = (double)L * 1.8503717077085942e-17;
+    return fma(-c, corr, c);
+#else
+    return pow(x, 1.0 / 3);
+#endif
+}
+
 }  // namespace ocpx

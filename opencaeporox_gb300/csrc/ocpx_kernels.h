@@ -26,10 +26,12 @@ struct FlashBatch {
     unsigned* count;   // deferred cells (may exceed cap: the excess finish in place)
     PERes* pe;
 };
+// part 0: budgeted thread-per-cell flash, 1: cooperative equilibrium, 2: finish deferred cells
 cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, const int* order,
-                                 const FlashBatch& fb, cudaStream_t s);
-// Cells in descending order of the work their last flash needed (iteration
-// counters), by a counting sort over COST_BUCKETS buckets.
+                                 const FlashBatch& fb, int part, cudaStream_t s);
+// Cells grouped by flash path (two-phase, one-phase, skip-flagged) and, within
+// a group, in descending order of the work their last flash needed, by a
+// counting sort over COST_BUCKETS buckets.
 constexpr int COST_BUCKETS = 256;
 cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, cudaStream_t s);
 

@@ -401,7 +401,8 @@ class FimContext:
         _check(self.lib.ocpx_step_report(self.h, C.byref(rep)))
         return rep
 
-    STAGES = ["check", "flash", "krpc_rock", "report", "flux", "residual", "jac_conn", "jac_rows", "newton_update"]
+    STAGES = ["check", "flash", "krpc_rock", "report", "flux", "residual", "jac_conn", "jac_rows", "newton_update",
+              "flash_order", "flash_budget", "flash_coop", "flash_post"]
 
     def profile(self, enable: bool = True):
         _check(self.lib.ocpx_profile_enable(self.h, 1 if enable else 0))

@@ -6,8 +6,8 @@ plain per-kernel form, beside the reference algorithm on the host cores.
 
 Workload (the compositional single-Newton-step case): 60 x 60 x 10 = 36,000
 cells, 6 seeded pseudo-components, per-cell feed z ~ Dirichlet(2), P ~
-U(10, 30) MPa, T = 345 K, 50 mD, porosity 0.2, PTN start; the timed step is a
-Newton iteration after a seeded Newton update of that state.  Wells are
+U(10, 30) MPa, T = 345 K, 50 mD, porosity 0.2, PTN start; the timed step is
+the second Newton iteration of the time step (two seeded Newton updates).  Wells are
 host-side in the reference design and not part of the GPU step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
@@ -125,7 +125,22 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- workload --
+def newton_updates(grid, Ni):
+    """Two seeded Newton updates (dP ~ N(0, 2) bar, dNi = Ni N(0, 2e-3))."""
+    out = []
+    for k in range(2):
+        rng = np.random.default_rng(SEED + 77 + k)
+        u = np.zeros((grid.nb, NCOMP + 2))
+        u[:, 0] = rng.normal(0.0, 2.0, grid.nb)
+        u[:, 1:] = Ni.reshape(grid.nb, -1) * rng.normal(0.0, 2e-3, (grid.nb, NCOMP + 1))
+        out.append(u.ravel())
+    return out
+
+
 def build_workload(variant, device=0):
+    """PTN start, pores filled; first Newton iteration of the time step; the
+    timed step is the second Newton iteration (the flash then starts from the
+    phase state and iteration history of the first, as in a simulation)."""
     from opencaeporox_gb300 import synthetic
     from opencaeporox_gb300.fim import FimContext
     model = synthetic.comp_model(NCOMP, SEED)
@@ -143,15 +158,14 @@ def build_workload(variant, device=0):
     ctx.update_property()
     ctx.cal_res(DT)
     ctx.update_last_time_step()
-    ctx.checkpoint(1)  # start of the time step
-    rng = np.random.default_rng(SEED + 77)
-    u = np.zeros((grid.nb, NCOMP + 2))
-    u[:, 0] = rng.normal(0.0, 2.0, grid.nb)
-    u[:, 1:] = Ni.reshape(grid.nb, -1) * rng.normal(0.0, 2e-3, (grid.nb, NCOMP + 1))
-    u = u.ravel()
-    ctx.get_solution(u, DSMAX)
-    ctx.checkpoint(0)  # Newton-iteration input
-    return ctx, model, grid, u
+    u1, u2 = newton_updates(grid, Ni)
+    ctx.get_solution(u1, DSMAX)  # Newton iteration 1
+    ctx.update_property()
+    ctx.cal_res(DT)
+    ctx.checkpoint(1)  # before the second Newton update
+    ctx.get_solution(u2, DSMAX)
+    ctx.checkpoint(0)  # input of the timed Newton iteration
+    return ctx, model, grid, u2
 
 
 def time_device(ctx, rt, steps, warmup, flush):
@@ -232,11 +246,11 @@ def cpu_baseline(threads=None):
     ob.update_property()
     ob.cal_res(DT)
     ob.a["lNi"][:] = ob.a["Ni"]
-    rng = np.random.default_rng(SEED + 77)
-    u = np.zeros((grid.nb, NCOMP + 2))
-    u[:, 0] = rng.normal(0.0, 2.0, grid.nb)
-    u[:, 1:] = Ni.reshape(grid.nb, -1) * rng.normal(0.0, 2e-3, (grid.nb, NCOMP + 1))
-    ob.newton_update(u.ravel(), DSMAX)
+    u1, u2 = newton_updates(grid, Ni)
+    ob.newton_update(u1, DSMAX)
+    ob.update_property()
+    ob.cal_res(DT)
+    ob.newton_update(u2, DSMAX)
     saved = {k: v.copy() for k, v in ob.a.items()}
     times = []
     t_end = time.perf_counter() + 12.0
@@ -346,7 +360,7 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
                 "config": {"workload": WORKLOAD}, "impl": "reference",
                 "cpu_baseline": {"value": v, "unit": "cells/s", "cores": cores, "kind": "port",
-                                 "sample": f"full 36000-cell Newton iteration, {n} repetitions, median"},
+                                 "sample": f"full 36000-cell second Newton iteration, {n} repetitions, median"},
                 "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -416,17 +430,17 @@ def main():
             "roofline": roof, "roofline_assembly": roof_asm, "fp64_peak_tflops": fp64,
             "batched": {"flash_budget": ctx1.get_param("flash_budget"), "coop_blocks": ctx1.get_param("coop_blocks"),
                         "deferred_cells": ctx1.get_param("deferred"),
-                        "block_cell": ctx1.get_param("block_cell"),
+                        "block_cell": ctx1.get_param("block_cell"), "predefer": ctx1.get_param("predefer"),
                         "autotune": None if tuned is None else {k: tuned[k] for k in
                                                                 ("flash_budget", "coop_blocks", "block_cell",
-                                                                 "flash_ms")}},
+                                                                 "predefer", "flash_ms")}},
             "clocks": ck, "gpu_launches": launches,
             "e2e": {"value": nb / (e2e_ms * 1e-3) * world, "unit": "cells/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h}}
     if rank == 0 and world == 1 and os.environ.get("OCPX_BENCH_NO_CPU") != "1":
         v, cores, n = cpu_baseline()
         line["cpu_baseline"] = {"value": v, "unit": "cells/s", "cores": cores, "kind": "port",
-                                "sample": f"full 36000-cell Newton iteration, {n} repetitions, median"}
+                                "sample": f"full 36000-cell second Newton iteration, {n} repetitions, median"}
     if rank == 0:
         print(json.dumps(line))
     ranks.close()

@@ -159,6 +159,8 @@ typedef enum ocpx_field {
     OCPX_F_RES,          /* d  [nb*(nc+1)] bulk residual, negated as LinearSystem expects (read only) */
     OCPX_F_RES_REL_V,    /* d  [nb] (read only) */
     OCPX_F_RES_REL_N,    /* d  [nb] (read only) */
+    OCPX_F_TRANS,        /* d  [nconn] connection transmissibility (BulkConnPair::trans) */
+    OCPX_F_PORO_INIT,    /* d  [nb] reference porosity (BulkVarSet::poroInit) */
     OCPX_F__COUNT
 } ocpx_field;
 
@@ -213,13 +215,19 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *                 (0 defers every cell that needs an equilibrium);
  *   COOP_BLOCKS   blocks of the warp-cooperative kernel;
  *   BLOCK_CELL    threads per block of the per-cell kernels;
- *   DEFERRED      (read only) cells deferred by the last batched flash;
- *                 reading it synchronizes the context stream. */
+ *   DEFERRED      (read only) cells whose equilibrium ran on the
+ *                 warp-cooperative kernel in the last batched flash;
+ *                 reading it synchronizes the context stream;
+ *   PREDEFER      1 (default): cells whose last flash used more than
+ *                 FLASH_BUDGET units go to the cooperative kernel at once, on
+ *                 a second stream, while the per-cell kernel runs; 0: only
+ *                 cells that exceed the budget now are deferred. */
 typedef enum ocpx_param {
     OCPX_PARAM_FLASH_BUDGET = 0,
     OCPX_PARAM_COOP_BLOCKS = 1,
     OCPX_PARAM_BLOCK_CELL = 2,
-    OCPX_PARAM_DEFERRED = 3
+    OCPX_PARAM_DEFERRED = 3,
+    OCPX_PARAM_PREDEFER = 4
 } ocpx_param;
 ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value);
 ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value);
@@ -243,11 +251,13 @@ ocpx_status ocpx_step_report(ocpx_ctx* ctx, ocpx_report* rep);
  * Stages: 0 physical check, 1 flash, 2 kr/Pc + rock, 3 status summary,
  * 4 connection flux, 5 residual + norms, 6 Jacobian connection blocks,
  * 7 Jacobian rows, 8 Newton update; inside stage 1 of the batched form:
- * 9 cost order, 10 budgeted per-cell flash, 11 cooperative equilibrium of
- * the deferred cells, 12 their properties.  ocpx_profile_read synchronizes
- * and returns, per stage, the summed milliseconds and the number of timed
- * launches since profiling was enabled. */
-#define OCPX_STAGE_COUNT 13
+ * 9 pre-deferral and cost order, 10 budgeted per-cell flash, 11 cooperative
+ * equilibrium of the pre-deferred cells (second stream, concurrent with 10),
+ * 12 properties of all deferred cells, 13 cooperative equilibrium of the
+ * cells deferred by 10.  ocpx_profile_read synchronizes and returns, per
+ * stage, the summed milliseconds and the number of timed launches since
+ * profiling was enabled. */
+#define OCPX_STAGE_COUNT 14
 ocpx_status ocpx_profile_enable(ocpx_ctx* ctx, int enable);
 ocpx_status ocpx_profile_read(ocpx_ctx* ctx, double* ms, uint64_t* launches);
 
@@ -284,6 +294,20 @@ ocpx_status ocpx_measure_fp64_tflops(int device, int iters, double* tflops);
 #define OCPX_RELRES_NOALLOC_MAX_CELLS 2097152
 ocpx_status ocpx_relres_noalloc(const double* d_res, const double* d_rockVp, const double* d_Nt, int nb, int len,
                                 double* d_resRelV, double* d_resRelN, void* stream, ocpx_norms* norms);
+
+/* Adjoint of the bulk residual R (the negated residual of ocpx_calres) at the
+ * state of the last ocpx_assemble, as vector-Jacobian products with a host
+ * vector lambda [nb*(nc+1)] (cell-major, like the residual).  No counterpart
+ * in the reference, which has no adjoint:
+ *   jt_lambda  [nb*(nc+1)]  J^T lambda, J the assembled Jacobian dR/d(P, Ni);
+ *   dr_dtrans  [nconn]      (dR/dT_c)^T lambda for every connection's
+ *                           transmissibility (R is linear in T_c: the flux of
+ *                           OCPConvection01::CalFlux scales with it);
+ *   dr_dporo   [nb]         (dR/dporoInit_n)^T lambda (only the volume balance
+ *                           depends on it, through OCPRockIsoT_Linear::CalPoro).
+ * Outputs may be NULL.  Synchronizes. */
+ocpx_status ocpx_adjoint(ocpx_ctx* ctx, const double* lambda, double* jt_lambda, double* dr_dtrans,
+                         double* dr_dporo);
 
 /* Stream the context launches on (a cudaStream_t), for callers that time or
  * order work around the library. */

@@ -1,9 +1,11 @@
 """Launch-shape autotuner of the batched FIM step.
 
-The batched flash has three knobs that change only how the work is laid out
-on the GPU, never the results: the per-cell work budget after which a
-cell's phase equilibrium moves to the warp-cooperative kernel, the number of
-blocks of that kernel, and the block size of the per-cell kernels.  The
+The batched flash has knobs that change only how the work is laid out on
+the GPU, never the results: the per-cell work budget after which a cell's
+phase equilibrium moves to the warp-cooperative kernel, whether cells that
+were expensive in their last flash go there at once (concurrently with the
+per-cell kernel), the number of blocks of that kernel, and the block size of
+the per-cell kernels.  The
 tuner times the flash stage of real Newton iterations (CUDA events recorded
 on the context stream by the library's stage profiler), restoring the same
 device checkpoint before every trial, and keeps the fastest setting.
@@ -30,24 +32,26 @@ def _flash_ms(ctx, dt: float, slot: int, reps: int) -> float:
 
 
 def tune(ctx, dt: float, slot: int = 0, budgets=DEFAULT_BUDGETS, coop_blocks=None, block_cells=(128,),
-         reps: int = 2) -> dict:
+         predefer=(0, 1), reps: int = 2) -> dict:
     """Try every combination on the state saved in checkpoint `slot` (the
     caller saves it) and leave the context set to the fastest one.  Returns
-    {"flash_budget", "coop_blocks", "block_cell", "flash_ms", "trials"}.
+    {"flash_budget", "coop_blocks", "block_cell", "predefer", "flash_ms", "trials"}.
     The context must use the batched variant."""
     if coop_blocks is None:
         coop_blocks = (ctx.get_param("coop_blocks"),)
     trials = []
-    for budget, blocks, bc in itertools.product(budgets, coop_blocks, block_cells):
+    for budget, blocks, bc, pre in itertools.product(budgets, coop_blocks, block_cells, predefer):
         ctx.set_param("flash_budget", budget)
         ctx.set_param("coop_blocks", blocks)
         ctx.set_param("block_cell", bc)
-        trials.append((_flash_ms(ctx, dt, slot, reps), budget, blocks, bc))
-    ms, budget, blocks, bc = min(trials)
+        ctx.set_param("predefer", pre)
+        trials.append((_flash_ms(ctx, dt, slot, reps), budget, blocks, bc, pre))
+    ms, budget, blocks, bc, pre = min(trials)
     ctx.set_param("flash_budget", budget)
     ctx.set_param("coop_blocks", blocks)
     ctx.set_param("block_cell", bc)
+    ctx.set_param("predefer", pre)
     ctx.checkpoint(slot, restore=True)
-    return {"flash_budget": budget, "coop_blocks": blocks, "block_cell": bc, "flash_ms": ms,
-            "trials": [{"flash_ms": t[0], "flash_budget": t[1], "coop_blocks": t[2], "block_cell": t[3]}
-                       for t in trials]}
+    return {"flash_budget": budget, "coop_blocks": blocks, "block_cell": bc, "predefer": pre, "flash_ms": ms,
+            "trials": [{"flash_ms": t[0], "flash_budget": t[1], "coop_blocks": t[2], "block_cell": t[3],
+                        "predefer": t[4]} for t in trials]}

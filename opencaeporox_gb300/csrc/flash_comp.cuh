@@ -76,6 +76,46 @@ struct DeferSink {
 // Work units charged against the budget: one EoS fugacity evaluation = 1.
 constexpr int WORK_SSM_STA = 1, WORK_NR_STA = 4, WORK_SSM_SP = 2, WORK_NR_SP = 6;
 
+// Work units the last flash of a cell used, from its iteration counters
+// (Rachford-Rice iterations at a fifth), plus a constant for the rest.
+OCPX_HD long long predicted_work(const BulkView& b, int cell)
+{
+    const int32_t* it = b.iters;
+    return 3LL + WORK_SSM_STA * (long long)it[b.idx(0, cell)] + WORK_NR_STA * (long long)it[b.idx(1, cell)] +
+           WORK_SSM_SP * (long long)it[b.idx(2, cell)] + WORK_NR_SP * (long long)it[b.idx(3, cell)] +
+           it[b.idx(4, cell)] / 5;
+}
+
+// SkipPSAMethod01::CalFtype02 / IfSkip (src/AcceleratePEC.cpp:64-124): the
+// flash type the phase equilibrium starts from (0 full test, 1 skip, 2 split).
+// Ni: the cell's moles (NC hydrocarbons first), Nt their hydrocarbon sum,
+// T in K, Sin the saturations entering the flash, npPE = phaseNum - 1.
+OCPX_HD int flash_type_in(const CompModel& m, const BulkView& b, int cell, const double* Ni, double Nt, double P,
+                          double T, const double* Sin, unsigned npPE)
+{
+    const int NC = m.nc;
+    int ftype_in = 0;
+    bool skip = false;
+    if (m.skip_psa && b.skip_flag[cell]) {
+        const double me = b.skip_minEig[cell];
+        skip = true;
+        if (fabs(1 - b.skip_P[cell] / P) >= me / 10) skip = false;
+        else if (fabs(b.skip_T[cell] - T) >= me * 10) skip = false;
+        else {
+            for (int i = 0; i < NC; i++)
+                if (fabs(Ni[i] / Nt - b.skip_zi[b.idx(i, cell)]) >= me / 10) { skip = false; break; }
+        }
+    }
+    if (skip) ftype_in = 1;
+    else if (m.skip_psa && npPE >= 2) {
+        unsigned tmp = 0;
+        for (int j = 0; j < 2; j++)
+            if (Sin[j] >= 1E-4) tmp++;
+        ftype_in = (tmp == npPE) ? (int)npPE : 0;
+    }
+    return ftype_in;
+}
+
 template <int NCM>
 struct CompFlash {
     EosPR<NCM> eos;
@@ -671,25 +711,7 @@ struct CompCellUpdate {
 
         // ---- SkipPSAMethod01::CalFtype02 / IfSkip (src/AcceleratePEC.cpp:64-124)
         const unsigned npPE = phaseNum - 1u;
-        int ftype_in = 0;
-        bool skip = false;
-        if (m.skip_psa && b.skip_flag[cell]) {
-            const double me = b.skip_minEig[cell];
-            skip = true;
-            if (fabs(1 - b.skip_P[cell] / P) >= me / 10) skip = false;
-            else if (fabs(b.skip_T[cell] - T) >= me * 10) skip = false;
-            else {
-                for (int i = 0; i < NC; i++)
-                    if (fabs(Ni[i] / Nt - b.skip_zi[b.idx(i, cell)]) >= me / 10) { skip = false; break; }
-            }
-        }
-        if (skip) ftype_in = 1;
-        else if (m.skip_psa && npPE >= 2) {
-            unsigned tmp = 0;
-            for (int j = 0; j < 2; j++)
-                if (Sin[j] >= 1E-4) tmp++;
-            ftype_in = (tmp == npPE) ? (int)npPE : 0;
-        }
+        const int ftype_in = flash_type_in(m, b, cell, Ni, Nt, P, T, Sin, npPE);
 
         // ---- phase equilibrium (lNP = phaseNum - 1 passed through double -> USI)
         f.eos.setup(&m, M.units.gas_constant, P, T);

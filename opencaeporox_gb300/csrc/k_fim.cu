@@ -2,6 +2,7 @@
 #include "ocpx_kernels.h"
 #include "cell_ops.cuh"
 #include "conn_ops.cuh"
+#include "adjoint.cuh"
 
 namespace ocpx {
 
@@ -201,24 +202,25 @@ cudaError_t launch_jac_rows(const BulkView& b, const ConnView& cv, const double*
 // test), then the work units its last flash used (iteration counters weighted
 // as the flash's budget charges them, Rachford-Rice iterations at a fifth), in
 // descending order.  Warps then hold cells on the same code path.
-__device__ __forceinline__ int cost_bucket(const BulkView& b, int cell)
+// Cells already handed to the cooperative kernel (pre-deferred) go to the last
+// bucket, where the per-cell kernel skips them.
+__device__ __forceinline__ int cost_bucket(const BulkView& b, int cell, const uint8_t* pre)
 {
-    const int32_t* it = b.iters;
-    const long long w = 3LL + it[b.idx(0, cell)] + 4LL * it[b.idx(1, cell)] + 2LL * it[b.idx(2, cell)] +
-                        6LL * it[b.idx(3, cell)] + it[b.idx(4, cell)] / 5;
+    if (pre && pre[cell]) return COST_BUCKETS - 1;
+    const long long w = predicted_work(b, cell);
     const int lvl = w < 63 ? (int)w : 63;
     const bool two = b.phaseExist[b.idx(0, cell)] && b.phaseExist[b.idx(1, cell)];
     const int cls = b.skip_flag[cell] ? 2 : (two ? 0 : 1);
     return cls * 64 + (63 - lvl);
 }
 
-__global__ void k_cost_hist(BulkView b, unsigned* __restrict__ hist)
+__global__ void k_cost_hist(BulkView b, const uint8_t* __restrict__ pre, unsigned* __restrict__ hist)
 {
     __shared__ unsigned h[COST_BUCKETS];
     for (int k = threadIdx.x; k < COST_BUCKETS; k += blockDim.x) h[k] = 0;
     __syncthreads();
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell < b.nb) atomicAdd(&h[cost_bucket(b, cell)], 1u);
+    if (cell < b.nb) atomicAdd(&h[cost_bucket(b, cell, pre)], 1u);
     __syncthreads();
     for (int k = threadIdx.x; k < COST_BUCKETS; k += blockDim.x)
         if (h[k]) atomicAdd(&hist[k], h[k]);
@@ -240,23 +242,103 @@ __global__ void k_cost_scan(unsigned* __restrict__ hist)
     hist[t] = v[t] - hist[t];
 }
 
-__global__ void k_cost_scatter(BulkView b, unsigned* __restrict__ offs, int* __restrict__ order)
+__global__ void k_cost_scatter(BulkView b, const uint8_t* __restrict__ pre, unsigned* __restrict__ offs,
+                               int* __restrict__ order)
 {
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= b.nb) return;
-    const unsigned pos = atomicAdd(&offs[cost_bucket(b, cell)], 1u);
+    const unsigned pos = atomicAdd(&offs[cost_bucket(b, cell, pre)], 1u);
     order[pos] = cell;
 }
 
-cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, cudaStream_t s)
+cudaError_t launch_cost_order(const BulkView& b, const uint8_t* pre, unsigned* hist, int* order, cudaStream_t s)
 {
     if (!b.nb) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned) * COST_BUCKETS, s);
     if (e != cudaSuccess) return e;
     const int block = 256;
-    k_cost_hist<<<grid_for(b.nb, block), block, 0, s>>>(b, hist);
+    k_cost_hist<<<grid_for(b.nb, block), block, 0, s>>>(b, pre, hist);
     k_cost_scan<<<1, COST_BUCKETS, 0, s>>>(hist);
-    k_cost_scatter<<<grid_for(b.nb, block), block, 0, s>>>(b, hist, order);
+    k_cost_scatter<<<grid_for(b.nb, block), block, 0, s>>>(b, pre, hist, order);
+    return cudaGetLastError();
+}
+
+// Cells whose last flash used more than `threshold` work units are handed to
+// the cooperative kernel before the per-cell kernel runs, so that both run at
+// the same time (pre[cell] = 1).  Cells that the skip test will let through
+// (flash type 1) stay with the per-cell kernel.
+__global__ void k_predefer(const Model* __restrict__ M, BulkView b, long long threshold, DeferSink sink,
+                           uint8_t* __restrict__ pre)
+{
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= b.nb) return;
+    pre[cell] = 0;
+    if (predicted_work(b, cell) <= threshold) return;
+    const CompModel& m = M->comp;
+    const int NC = m.nc, np = b.np;
+    double Ni[NC_MAX + 1], Sin[3];
+    for (int i = 0; i <= NC; i++) Ni[i] = b.Ni[b.idx(i, cell)];
+    unsigned phaseNum = 0;
+    for (int j = 0; j < np; j++) {
+        Sin[j] = b.S[b.idx(j, cell)];
+        if (b.phaseExist[b.idx(j, cell)]) phaseNum++;
+    }
+    double Nt = 0;
+    for (int i = 0; i < NC; i++) Nt += Ni[i];
+    const double P = b.P[cell], T = b.T[cell] + M->units.conv4;
+    const unsigned npPE = phaseNum - 1u;
+    const int ftype_in = flash_type_in(m, b, cell, Ni, Nt, P, T, Sin, npPE);
+    if (ftype_in == 1) return;
+    if (sink.push(cell, ftype_in, npPE)) pre[cell] = 1;
+}
+
+cudaError_t launch_predefer(const Model* dm, const BulkView& b, long long threshold, const DeferSink& sink,
+                            uint8_t* pre, cudaStream_t s)
+{
+    if (b.nb) k_predefer<<<grid_for(b.nb, 128), 128, 0, s>>>(dm, b, threshold, sink, pre);
+    return cudaGetLastError();
+}
+
+__global__ void k_jt_lambda(BulkView b, ConnView cv, const uint32_t* __restrict__ rowptr,
+                            const double* __restrict__ val, const uint32_t* __restrict__ slot,
+                            const double* __restrict__ lam, double* __restrict__ out)
+{
+    const int dim = b.nc + 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)b.nb * dim) return;
+    jt_lambda_entry(b, cv, rowptr, val, slot, lam, out, (int)(t / dim), (int)(t % dim));
+}
+
+__global__ void k_vjp_trans(BulkView b, ConnView cv, double dt, const double* __restrict__ lam, double* __restrict__ out)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < cv.nconn) out[c] = vjp_trans_conn(b, cv, dt, lam, c);
+}
+
+__global__ void k_vjp_poro(const Model* __restrict__ M, BulkView b, const double* __restrict__ lam,
+                           double* __restrict__ out)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < b.nb) out[n] = vjp_poro_cell(*M, b, lam, n);
+}
+
+cudaError_t launch_jt_lambda(const BulkView& b, const ConnView& cv, const uint32_t* rowptr, const double* val,
+                             const uint32_t* slot, const double* lam, double* out, int block, cudaStream_t s)
+{
+    const long long n = (long long)b.nb * (b.nc + 1);
+    if (n) k_jt_lambda<<<(int)((n + block - 1) / block), block, 0, s>>>(b, cv, rowptr, val, slot, lam, out);
+    return cudaGetLastError();
+}
+cudaError_t launch_vjp_trans(const BulkView& b, const ConnView& cv, double dt, const double* lam, double* out,
+                             int block, cudaStream_t s)
+{
+    if (cv.nconn) k_vjp_trans<<<grid_for(cv.nconn, block), block, 0, s>>>(b, cv, dt, lam, out);
+    return cudaGetLastError();
+}
+cudaError_t launch_vjp_poro(const Model* dm, const BulkView& b, const double* lam, double* out, int block,
+                            cudaStream_t s)
+{
+    if (b.nb) k_vjp_poro<<<grid_for(b.nb, block), block, 0, s>>>(dm, b, lam, out);
     return cudaGetLastError();
 }
 

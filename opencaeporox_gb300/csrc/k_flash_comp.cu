@@ -24,11 +24,13 @@ __global__ void __launch_bounds__(128) k_flash_comp(const Model* __restrict__ M,
 // left untouched.
 template <int NCM>
 __global__ void __launch_bounds__(128) k_flash_budget(const Model* __restrict__ M, BulkView b,
-                                                      const int* __restrict__ order, int budget, DeferSink sink)
+                                                      const int* __restrict__ order, int budget, DeferSink sink,
+                                                      const uint8_t* __restrict__ pre)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= b.nb) return;
     const int cell = order[p];
+    if (pre && pre[cell]) return;  // handled by the cooperative kernel
     CompCellUpdate<NCM> u;
     u.run(*M, b, cell, budget, &sink);
 }
@@ -83,7 +85,8 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
     switch (part) {
     case 0: {
         const DeferSink sink{fb.rec, fb.count, fb.cap};
-        k_flash_budget<OCPX_NCM><<<(b.nb + fb.block - 1) / fb.block, fb.block, 0, s>>>(dm, b, order, fb.budget, sink);
+        k_flash_budget<OCPX_NCM><<<(b.nb + fb.block - 1) / fb.block, fb.block, 0, s>>>(dm, b, order, fb.budget, sink,
+                                                                                         fb.pre);
         break;
     }
     case 1:

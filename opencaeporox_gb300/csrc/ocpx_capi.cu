@@ -111,15 +111,25 @@ struct ocpx_ctx {
     // batched flash: cost order, deferral list, cooperative results
     int* order = nullptr;
     unsigned* cost_hist = nullptr;
-    DeferRec* defer_rec = nullptr;
-    unsigned* defer_count = nullptr;   // [4]: deferred cells of the last batched flash
+    DeferRec* defer_rec = nullptr;     // cells deferred by the per-cell kernel
+    unsigned* defer_count = nullptr;   // [4]: [0] deferred by the per-cell kernel, [1] pre-deferred
     PERes* pe_res = nullptr;
+    DeferRec* pre_rec = nullptr;       // cells pre-deferred from their last flash's work
+    PERes* pre_res = nullptr;
+    uint8_t* pre_flag = nullptr;       // [nb]
     int defer_cap = 0;
     int flash_budget = 48;
     int coop_blocks = 0;
+    int predefer = 1;
+    cudaStream_t stream2 = nullptr;    // high-priority stream of the pre-deferred cooperative kernel
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double* u = nullptr;            // Newton update staging
     double* bmat = nullptr;         // per-connection Jacobian blocks (2 per connection)
     uint32_t* jac_rowptr = nullptr;
+    uint32_t* jac_slot = nullptr;   // [2][nconn]: block index of connection c in row bId / row eId
+    double* adj = nullptr;          // adjoint workspace: lambda, J^T lambda [nb*(nc+1)] each
+    double* adj_conn = nullptr;     // [nconn]
+    double last_dt = 0;             // dt of the last residual / Jacobian
     uint32_t* jac_col = nullptr;
     double* jac_val = nullptr;
     size_t jac_nnz = 0;
@@ -131,7 +141,7 @@ struct ocpx_ctx {
     int block_cell = 128, block_conn = 128;
     // per-stage event timing
     bool prof = false;
-    struct Mark { int stage; cudaEvent_t a, b; };
+    struct Mark { int stage; cudaEvent_t a, b; cudaStream_t st; };
     std::vector<Mark> marks;
     std::vector<cudaEvent_t> free_events;
     double prof_ms[OCPX_STAGE_COUNT] = {0};
@@ -147,18 +157,18 @@ struct ocpx_ctx {
         free_events.pop_back();
         return e;
     }
-    int stage_begin(int s)
+    int stage_begin(int s, cudaStream_t on = nullptr)
     {
         if (!prof) return -1;
-        Mark m{s, take_event(), take_event()};
-        cudaEventRecord(m.a, stream);
+        Mark m{s, take_event(), take_event(), on ? on : stream};
+        cudaEventRecord(m.a, m.st);
         marks.push_back(m);
         return (int)marks.size() - 1;
     }
     void stage_end(int idx)
     {
         if (idx < 0) return;
-        cudaEventRecord(marks[idx].b, stream);
+        cudaEventRecord(marks[idx].b, marks[idx].st);
     }
     // device-side checkpoints of the mutable bulk state
     char* ckpt[2] = {nullptr, nullptr};
@@ -227,6 +237,8 @@ FieldInfo ocpx_ctx::field(ocpx_field f) const
     case OCPX_F_RES: return {res, nb, nc + 1, 8, false, false};
     case OCPX_F_RES_REL_V: return {resRelV, nb, 1, 8, true, false};
     case OCPX_F_RES_REL_N: return {resRelN, nb, 1, 8, true, false};
+    case OCPX_F_TRANS: return {(void*)cv.trans, nconn, 1, 8, true, true};
+    case OCPX_F_PORO_INIT: return {(void*)b.poroInit, nb, 1, 8, true, true};
     default: return {nullptr, 0, 0, 0, true, false};
     }
 }
@@ -301,6 +313,13 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
         }
     }
     ctx->jac_nnz = jcol.size();
+    // block index of each connection in the rows of its two cells (adjoint transpose)
+    std::vector<uint32_t> jslot(2 * (size_t)(nconn > 0 ? nconn : 1), 0);
+    for (int n = 0; n < nb; n++)
+        for (uint32_t k = row_ptr[n]; k < row_ptr[n + 1]; k++) {
+            const uint32_t c = row_conn[k] >> 1, side = row_conn[k] & 1u;
+            jslot[(size_t)side * nconn + c] = jrow[n] + 1 + (k - row_ptr[n]);
+        }
 
     // arena layout
     struct Slot { void** p; size_t bytes; };
@@ -340,9 +359,13 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     add(&ctx->order, sizeof(int) * (size_t)nb); add(&ctx->cost_hist, sizeof(unsigned) * COST_BUCKETS);
     add(&ctx->defer_rec, sizeof(DeferRec) * (size_t)ctx->defer_cap); add(&ctx->defer_count, sizeof(unsigned) * 4);
     add(&ctx->pe_res, sizeof(PERes) * (size_t)ctx->defer_cap);
+    add(&ctx->pre_rec, sizeof(DeferRec) * (size_t)ctx->defer_cap); add(&ctx->pre_res, sizeof(PERes) * (size_t)ctx->defer_cap);
+    add(&ctx->pre_flag, (size_t)nb);
     add(&ctx->u, D * (nc + 1));
     add(&ctx->bmat, sizeof(double) * C * 2 * bsize);
     add(&ctx->jac_rowptr, sizeof(uint32_t) * (nb + 1)); add(&ctx->jac_col, sizeof(uint32_t) * jcol.size());
+    add(&ctx->jac_slot, sizeof(uint32_t) * jslot.size());
+    add(&ctx->adj, D * (nc + 1) * 2); add(&ctx->adj_conn, sizeof(double) * C);
     add(&ctx->jac_val, sizeof(double) * jcol.size() * bsize);
     size_t staging = D * lend;
     staging = std::max(staging, sizeof(double) * C * nc);
@@ -363,6 +386,14 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     ctx->state_bytes = (size_t)((char*)b.iters + align256(sizeof(int32_t) * (size_t)nb * 5) - (char*)b.P);
 
     auto fail_ctx = [&](ocpx_status s2, const std::string& m) { ocpx_destroy(ctx); return fail(s2, m); };
+    {
+        int lo = 0, hi = 0;
+        cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        if (cudaStreamCreateWithPriority(&ctx->stream2, cudaStreamNonBlocking, hi) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)
+            return fail_ctx(OCPX_CUDA_ERROR, "stream/event creation failed");
+    }
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
         return fail_ctx(OCPX_CUDA_ERROR, "stream creation failed");
     if (cudaMalloc(&ctx->d_model, sizeof(Model)) != cudaSuccess) return fail_ctx(OCPX_CUDA_ERROR, "model alloc failed");
@@ -383,6 +414,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
         cudaMemcpy((void*)cv.row_conn, row_conn.data(), sizeof(uint32_t) * row_conn.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->jac_rowptr, jrow.data(), sizeof(uint32_t) * (nb + 1), cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->jac_col, jcol.data(), sizeof(uint32_t) * jcol.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->jac_slot, jslot.data(), sizeof(uint32_t) * jslot.size(), cudaMemcpyHostToDevice);
     const cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return fail_ctx(OCPX_CUDA_ERROR, std::string("context setup: ") + cudaGetErrorString(e));
     int sms = 0;
@@ -406,6 +438,9 @@ void ocpx_destroy(ocpx_ctx* ctx)
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     if (ctx->h_norm) cudaFreeHost(ctx->h_norm);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     delete ctx;
 }
 
@@ -472,18 +507,49 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
     const int mk_flash = ctx->stage_begin(1);
     if (ctx->host_model.mixture == 1) {
         if (ctx->variant == 1) {
-            OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned), s));
+            // cells expensive in their last flash go to the cooperative kernel at
+            // once, on a second (high-priority) stream, concurrently with the
+            // per-cell kernel; cells that turn out expensive now follow after it
+            const bool pre = ctx->predefer != 0;
+            OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned) * 2, s));
             mk = ctx->stage_begin(9);
-            OCPX_CUDA(launch_cost_order(ctx->b, ctx->cost_hist, ctx->order, s));
-            ctx->stage_end(mk);
-            const FlashBatch fb{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
-                                ctx->defer_rec, ctx->defer_count, ctx->pe_res};
-            for (int part = 0; part < 3; part++) {
-                mk = ctx->stage_begin(10 + part);
-                OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fb, part, s));
-                ctx->stage_end(mk);
+            if (pre) {
+                const DeferSink sinkA{ctx->pre_rec, ctx->defer_count + 1, ctx->defer_cap};
+                OCPX_CUDA(launch_predefer(ctx->d_model, ctx->b, ctx->flash_budget, sinkA, ctx->pre_flag, s));
+                ctx->launches++;
             }
-            ctx->launches += 6;
+            OCPX_CUDA(launch_cost_order(ctx->b, pre ? ctx->pre_flag : nullptr, ctx->cost_hist, ctx->order, s));
+            ctx->launches += 3;
+            ctx->stage_end(mk);
+            const FlashBatch fbA{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
+                                 ctx->pre_rec, ctx->defer_count + 1, ctx->pre_res, nullptr};
+            const FlashBatch fbB{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
+                                 ctx->defer_rec, ctx->defer_count, ctx->pe_res, pre ? ctx->pre_flag : nullptr};
+            if (pre) {
+                OCPX_CUDA(cudaEventRecord(ctx->ev_fork, s));
+                OCPX_CUDA(cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
+                mk = ctx->stage_begin(11, ctx->stream2);
+                OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbA, 1, ctx->stream2));
+                ctx->stage_end(mk);
+                OCPX_CUDA(cudaEventRecord(ctx->ev_join, ctx->stream2));
+                ctx->launches++;
+            }
+            mk = ctx->stage_begin(10);
+            OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbB, 0, s));
+            ctx->stage_end(mk);
+            mk = ctx->stage_begin(13);
+            OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbB, 1, s));
+            ctx->stage_end(mk);
+            ctx->launches += 2;
+            if (pre) OCPX_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+            mk = ctx->stage_begin(12);
+            if (pre) {
+                OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbA, 2, s));
+                ctx->launches++;
+            }
+            OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbB, 2, s));
+            ctx->launches++;
+            ctx->stage_end(mk);
         }
         else {
             OCPX_CUDA(launch_flash_comp(ctx->ncm, ctx->d_model, ctx->b, ctx->block_cell, s));
@@ -509,6 +575,7 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
 ocpx_status enqueue_calres(ocpx_ctx* ctx, double dt)
 {
     cudaStream_t s = ctx->stream;
+    ctx->last_dt = dt;
     int mk = ctx->stage_begin(4);
     OCPX_CUDA(launch_conn_flux(ctx->d_model, ctx->b, ctx->cv, ctx->block_conn, s));
     ctx->stage_end(mk);
@@ -780,6 +847,10 @@ ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value)
         if (value != 32 && value != 64 && value != 128) return fail(OCPX_INVALID_ARG, "block size must be 32, 64 or 128");
         ctx->block_cell = (int)value;
         return OCPX_OK;
+    case OCPX_PARAM_PREDEFER:
+        if (value != 0 && value != 1) return fail(OCPX_INVALID_ARG, "predefer must be 0 or 1");
+        ctx->predefer = (int)value;
+        return OCPX_OK;
     default:
         return fail(OCPX_INVALID_ARG, "unknown or read-only parameter");
     }
@@ -792,16 +863,46 @@ ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value)
     case OCPX_PARAM_FLASH_BUDGET: *value = ctx->flash_budget; return OCPX_OK;
     case OCPX_PARAM_COOP_BLOCKS: *value = ctx->coop_blocks; return OCPX_OK;
     case OCPX_PARAM_BLOCK_CELL: *value = ctx->block_cell; return OCPX_OK;
+    case OCPX_PARAM_PREDEFER: *value = ctx->predefer; return OCPX_OK;
     case OCPX_PARAM_DEFERRED: {
-        unsigned n = 0;
-        OCPX_CUDA(cudaMemcpyAsync(&n, ctx->defer_count, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+        unsigned n[2] = {0, 0};
+        OCPX_CUDA(cudaMemcpyAsync(n, ctx->defer_count, sizeof(n), cudaMemcpyDeviceToHost, ctx->stream));
         OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
-        *value = n;
+        *value = (long long)std::min(n[0], (unsigned)ctx->defer_cap) + std::min(n[1], (unsigned)ctx->defer_cap);
         return OCPX_OK;
     }
     default:
         return fail(OCPX_INVALID_ARG, "unknown parameter");
     }
+}
+
+ocpx_status ocpx_adjoint(ocpx_ctx* ctx, const double* lambda, double* jt_lambda, double* dr_dtrans,
+                         double* dr_dporo)
+{
+    if (!ctx || !lambda) return fail(OCPX_INVALID_ARG, "null argument");
+    cudaStream_t s = ctx->stream;
+    const size_t nv = (size_t)ctx->nb * (ctx->nc + 1);
+    double* d_lam = ctx->adj;
+    double* d_out = ctx->adj + nv;
+    OCPX_CUDA(cudaMemcpyAsync(d_lam, lambda, sizeof(double) * nv, cudaMemcpyHostToDevice, s));
+    if (jt_lambda) {
+        OCPX_CUDA(launch_jt_lambda(ctx->b, ctx->cv, ctx->jac_rowptr, ctx->jac_val, ctx->jac_slot, d_lam, d_out,
+                                   ctx->block_cell, s));
+        ctx->launches++;
+        OCPX_CUDA(cudaMemcpyAsync(jt_lambda, d_out, sizeof(double) * nv, cudaMemcpyDeviceToHost, s));
+    }
+    if (dr_dtrans && ctx->nconn) {
+        OCPX_CUDA(launch_vjp_trans(ctx->b, ctx->cv, ctx->last_dt, d_lam, ctx->adj_conn, ctx->block_conn, s));
+        ctx->launches++;
+        OCPX_CUDA(cudaMemcpyAsync(dr_dtrans, ctx->adj_conn, sizeof(double) * ctx->nconn, cudaMemcpyDeviceToHost, s));
+    }
+    if (dr_dporo) {
+        OCPX_CUDA(launch_vjp_poro(ctx->d_model, ctx->b, d_lam, d_out, ctx->block_cell, s));
+        ctx->launches++;
+        OCPX_CUDA(cudaMemcpyAsync(dr_dporo, d_out, sizeof(double) * ctx->nb, cudaMemcpyDeviceToHost, s));
+    }
+    OCPX_CUDA(cudaStreamSynchronize(s));
+    return OCPX_OK;
 }
 
 ocpx_status ocpx_step(ocpx_ctx* ctx, const double* u_host, double dSmax, double dt, double* res_host,

@@ -25,6 +25,7 @@ struct FlashBatch {
     DeferRec* rec;
     unsigned* count;   // deferred cells (may exceed cap: the excess finish in place)
     PERes* pe;
+    const uint8_t* pre;  // cells pre-deferred to another list (skipped by part 0), may be NULL
 };
 // part 0: budgeted thread-per-cell flash, 1: cooperative equilibrium, 2: finish deferred cells
 cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, const int* order,
@@ -33,7 +34,12 @@ cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, co
 // a group, in descending order of the work their last flash needed, by a
 // counting sort over COST_BUCKETS buckets.
 constexpr int COST_BUCKETS = 256;
-cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, cudaStream_t s);
+// pre: cells already pre-deferred (sorted last), may be NULL
+cudaError_t launch_cost_order(const BulkView& b, const uint8_t* pre, unsigned* hist, int* order, cudaStream_t s);
+// hand the cells whose last flash used more than `threshold` work units to the
+// cooperative kernel up front (pre[cell] = 1)
+cudaError_t launch_predefer(const Model* dm, const BulkView& b, long long threshold, const DeferSink& sink,
+                            uint8_t* pre, cudaStream_t s);
 
 cudaError_t launch_flash_bo(const Model* dm, const BulkView& b, int block, cudaStream_t s);
 cudaError_t launch_krpc_rock(const Model* dm, const BulkView& b, int block, cudaStream_t s);
@@ -47,6 +53,13 @@ cudaError_t launch_jac_conn(int nct, const Model* dm, const BulkView& b, const C
 cudaError_t launch_jac_rows(const BulkView& b, const ConnView& cv, const double* bmat, const uint32_t* rowptr,
                             double* val, int block, cudaStream_t s);
 cudaError_t launch_report(const BulkView& b, uint32_t* out3, int block, cudaStream_t s);
+// adjoint vector-Jacobian products (adjoint.cuh)
+cudaError_t launch_jt_lambda(const BulkView& b, const ConnView& cv, const uint32_t* rowptr, const double* val,
+                             const uint32_t* slot, const double* lam, double* out, int block, cudaStream_t s);
+cudaError_t launch_vjp_trans(const BulkView& b, const ConnView& cv, double dt, const double* lam, double* out,
+                             int block, cudaStream_t s);
+cudaError_t launch_vjp_poro(const Model* dm, const BulkView& b, const double* lam, double* out, int block,
+                            cudaStream_t s);
 
 // layout conversion between the reference's cell-major arrays and the
 // device structure-of-arrays: dst[k*n + i] = src[i*width + k] (to_soa) and back

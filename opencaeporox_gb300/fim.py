@@ -37,7 +37,8 @@ STATUS_NAMES = {0: "OK", 1: "NONCONVERGED", 2: "SINGULAR", 3: "NONFINITE", 4: "W
 FIELDS = ["P", "T", "PB", "NI", "LNI", "NT", "VF", "VFP", "VFI", "PJ", "PC", "S", "PHASE_EXIST", "XIJ", "RHO",
           "XI", "MU", "RHOP", "XIP", "MUP", "RHOX", "XIX", "MUX", "KR", "DKRDS", "DPCDS", "DSEC_DPRI", "PORO",
           "POROP", "ROCKVP", "SKIP_FLAG", "SKIP_MINEIG", "SKIP_P", "SKIP_T", "SKIP_ZI", "STATUS", "FTYPE",
-          "FLASH_ITERS", "UPBLOCK", "CONN_DP", "FLUX_VJ", "FLUX_NI", "RES", "RES_REL_V", "RES_REL_N"]
+          "FLASH_ITERS", "UPBLOCK", "CONN_DP", "FLUX_VJ", "FLUX_NI", "RES", "RES_REL_V", "RES_REL_N", "TRANS",
+          "PORO_INIT"]
 FIELD_ID = {name: i for i, name in enumerate(FIELDS)}
 FIELD_DTYPE = {"PHASE_EXIST": np.uint8, "SKIP_FLAG": np.uint8, "STATUS": np.uint32, "FTYPE": np.int8,
                "FLASH_ITERS": np.int32, "UPBLOCK": np.uint32}
@@ -93,9 +94,9 @@ EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy",
            "ocpx_update_last_step", "ocpx_synchronize", "ocpx_jacobian_dims", "ocpx_get_jacobian",
            "ocpx_jacobian_device", "ocpx_set_variant", "ocpx_step", "ocpx_enqueue_step", "ocpx_step_report",
            "ocpx_profile_enable", "ocpx_profile_read", "ocpx_checkpoint", "ocpx_measure_fp64_tflops",
-           "ocpx_stream", "ocpx_launch_count", "ocpx_set_param", "ocpx_get_param"]
+           "ocpx_stream", "ocpx_launch_count", "ocpx_set_param", "ocpx_get_param", "ocpx_adjoint"]
 
-PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3}
+PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3, "predefer": 4}
 
 _lib = None
 
@@ -131,6 +132,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.ocpx_profile_enable.argtypes = [P, C.c_int]
     lib.ocpx_profile_read.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
     lib.ocpx_measure_fp64_tflops.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
+    lib.ocpx_adjoint.argtypes = [P, P, P, P, P]
+    lib.ocpx_adjoint.restype = C.c_int
     lib.ocpx_set_param.argtypes = [P, C.c_int, C.c_longlong]
     lib.ocpx_get_param.argtypes = [P, C.c_int, C.POINTER(C.c_longlong)]
     for fn in ("ocpx_enqueue_step", "ocpx_step_report", "ocpx_profile_enable", "ocpx_profile_read",
@@ -318,8 +321,8 @@ class FimContext:
              "DKRDS": np_ * np_, "DPCDS": np_ * np_, "DSEC_DPRI": np_ * (nc + 1) * (nc + 1), "PORO": 1,
              "POROP": 1, "ROCKVP": 1, "SKIP_FLAG": 1, "SKIP_MINEIG": 1, "SKIP_P": 1, "SKIP_T": 1,
              "SKIP_ZI": max(self.NC, 1), "STATUS": 1, "FTYPE": 1, "FLASH_ITERS": 5, "RES": nc + 1,
-             "RES_REL_V": 1, "RES_REL_N": 1}
-        cw = {"UPBLOCK": np_, "CONN_DP": np_, "FLUX_VJ": np_, "FLUX_NI": nc}
+             "RES_REL_V": 1, "RES_REL_N": 1, "PORO_INIT": 1}
+        cw = {"UPBLOCK": np_, "CONN_DP": np_, "FLUX_VJ": np_, "FLUX_NI": nc, "TRANS": 1}
         if name in cw:
             return nconn * cw[name]
         return nb * w[name]
@@ -402,7 +405,7 @@ class FimContext:
         return rep
 
     STAGES = ["check", "flash", "krpc_rock", "report", "flux", "residual", "jac_conn", "jac_rows", "newton_update",
-              "flash_order", "flash_budget", "flash_coop", "flash_post"]
+              "flash_order", "flash_budget", "flash_coop", "flash_post", "flash_coop_late"]
 
     def profile(self, enable: bool = True):
         _check(self.lib.ocpx_profile_enable(self.h, 1 if enable else 0))
@@ -412,6 +415,20 @@ class FimContext:
         n = (C.c_uint64 * len(self.STAGES))()
         _check(self.lib.ocpx_profile_read(self.h, ms, n))
         return {s: (ms[i], int(n[i])) for i, s in enumerate(self.STAGES)}
+
+    def adjoint(self, lam, jt=True, trans=True, poro=True):
+        """Vector-Jacobian products of the bulk residual at the last assembled
+        state: (J^T lam, (dR/dT)^T lam, (dR/dporoInit)^T lam); None for the ones
+        not requested."""
+        lam = np.ascontiguousarray(np.asarray(lam, np.float64).ravel())
+        if lam.size != self.nb * (self.nc + 1):
+            raise ValueError("lambda must have nb*(nc+1) entries")
+        out_jt = np.empty(lam.size) if jt else None
+        out_t = np.empty(self.nconn) if trans else None
+        out_p = np.empty(self.nb) if poro else None
+        ptr = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
+        _check(self.lib.ocpx_adjoint(self.h, ptr(lam), ptr(out_jt), ptr(out_t), ptr(out_p)))
+        return out_jt, out_t, out_p
 
     def jacobian(self):
         nrow, nnz, bd = C.c_size_t(), C.c_size_t(), C.c_int()

@@ -181,3 +181,55 @@ def libm_sensitivity(fx: dict, it: str, model, grid) -> dict:
 
 def tolerance(k: str, sens: dict) -> float:
     return max(TOL.get(k, REL_TOL), LIBM_FACTOR * sens.get(k, 0.0))
+
+
+# ---------------------------------------------------------------- flash10 --
+# Independent-cell flashes dumped by the reference's flash harness
+# (OCPMixtureMethodComp01::FlashDer with no phase history: phaseNum = 1 gives
+# lNP = 0, the strict four-start stability test).  On the GPU path that is a
+# grid without connections whose cells have only the water phase flagged.
+FLASH_KEYS = {"phaseExist": "phaseExist", "S": "S", "xij": "xij", "rho": "rho", "xi": "xi", "mu": "mu",
+              "rhoP": "rhoP", "xiP": "xiP", "muP": "muP", "rhox": "rhox", "xix": "xix", "mux": "mux",
+              "vf": "vf", "Nt": "Nt", "vfP": "vfP", "vfi": "vfi", "dSec_dPri": "dSec_dPri"}
+
+
+def flash_case(fx: dict):
+    """(model, grid, state, reference outputs) of a flash fixture."""
+    from opencaeporox_gb300 import fim
+    m = {k[len("model/"):]: v for k, v in fx.items() if k.startswith("model/")}
+    model = fim.Model(m)
+    cells = np.asarray(fx["cells"])
+    n, nc = cells.shape[0], model.nc
+    grid = fim.Grid(np.ones(n), np.zeros(n), np.full(n, float(np.asarray(m["poroInit"]).ravel()[0])),
+                    np.zeros(0, np.uint32), np.zeros(0, np.uint32), np.zeros(0))
+    pe = np.tile(np.array([0, 0, 1], np.uint8), n)
+    state = dict(P=cells[:, 0].copy(), T=cells[:, 1].copy(), Ni=cells[:, 2:].ravel().copy(),
+                 lNi=cells[:, 2:].ravel().copy(), Nt=cells[:, 2:].sum(axis=1), phaseExist=pe,
+                 S=np.tile([0.0, 0.0, 1.0], n), xij=np.zeros(n * 3 * nc), Pj=np.repeat(cells[:, 0], 3),
+                 skip_flag=np.zeros(n, np.uint8))
+    ref = {k: fx["flash/" + v] for k, v in FLASH_KEYS.items()}
+    ref["flash_ftype"] = fx["flash/ftype"]
+    ref["flash_iters"] = fx["flash/iters"]
+    return model, grid, state, ref
+
+
+def flash_sensitivity(model, grid, state, ref) -> dict:
+    """libm sensitivity (see libm_sensitivity) of a flash fixture.  Also
+    "iter_cells": the most cells whose iteration counters a one-ulp
+    perturbation changes (SSM loops that stop on a tolerance cross it one
+    iteration earlier or later)."""
+    from oracle.pyoracle import OracleBulk
+    out = {"iter_cells": 0}
+    ri = np.asarray(ref["flash_iters"]).reshape(-1, 5)
+    for seed in NUDGE_SEEDS:
+        ob = OracleBulk(model, grid, variant="ulp")
+        ob.set_nudge_seed(seed)
+        ob.load(state)
+        ob.flash()
+        if not np.array_equal(ob.a["phaseExist"], np.asarray(ref["phaseExist"]).astype(np.uint32)):
+            continue
+        out["iter_cells"] = max(out["iter_cells"],
+                                int(np.sum(np.any(ob.a["iters"].reshape(-1, 5) != ri, axis=1))))
+        for k, v in state_errors(dict(ob.a), ref, model.nc, grid.nb).items():
+            out[k] = max(out.get(k, 0.0), v)
+    return out

@@ -89,3 +89,21 @@ def test_libm_sensitivity_of_reference_algorithm(name):
         assert sens, f"{it}: every perturbation pattern flipped a phase label"
         worst = max(sens.values())
         assert worst < 1e-9, (it, sens)
+
+
+def test_oracle_flash10_against_reference():
+    """The strict (four-start) stability path and 10 components, on 1,024
+    independent cells flashed by the reference."""
+    fx = P.load_fixture("flash10")
+    model, grid, state, ref = P.flash_case(fx)
+    ob = OracleBulk(model, grid)
+    ob.load(state)
+    ob.flash()
+    got = dict(ob.a)
+    assert np.array_equal(got["phaseExist"], ref["phaseExist"].astype(np.uint32))
+    assert np.array_equal(got["ftype"], ref["flash_ftype"])
+    gi, ri = got["iters"].reshape(-1, 5), ref["flash_iters"].reshape(-1, 5)
+    assert np.sum(np.any(gi != ri, axis=1)) <= 2
+    errs = P.state_errors(got, ref, model.nc, grid.nb)
+    bad = {k: v for k, v in errs.items() if v > P.REL_TOL}
+    assert not bad, bad

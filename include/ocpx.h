@@ -218,10 +218,10 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *   DEFERRED      (read only) cells whose equilibrium ran on the
  *                 warp-cooperative kernel in the last batched flash;
  *                 reading it synchronizes the context stream;
- *   PREDEFER      1 (default): cells whose last flash used more than
- *                 FLASH_BUDGET units go to the cooperative kernel at once, on
- *                 a second stream, while the per-cell kernel runs; 0: only
- *                 cells that exceed the budget now are deferred. */
+ *   PREDEFER      cells whose last flash used more than this many work
+ *                 units go to the cooperative kernel at once, on a second
+ *                 stream, while the per-cell kernel runs (default 192);
+ *                 0: only cells that exceed the budget now are deferred. */
 typedef enum ocpx_param {
     OCPX_PARAM_FLASH_BUDGET = 0,
     OCPX_PARAM_COOP_BLOCKS = 1,

@@ -14,7 +14,7 @@ from __future__ import annotations
 
 import itertools
 
-DEFAULT_BUDGETS = (8, 16, 32, 48, 64, 96, 128, 192)
+DEFAULT_BUDGETS = (16, 32, 48, 64, 96, 128, 192, 256, 384)
 
 
 def _flash_ms(ctx, dt: float, slot: int, reps: int) -> float:
@@ -32,10 +32,11 @@ def _flash_ms(ctx, dt: float, slot: int, reps: int) -> float:
 
 
 def tune(ctx, dt: float, slot: int = 0, budgets=DEFAULT_BUDGETS, coop_blocks=None, block_cells=(128,),
-         predefer=(0, 1), reps: int = 2) -> dict:
+         predefer=(0, 1, 2, 4, 8), reps: int = 2) -> dict:
     """Try every combination on the state saved in checkpoint `slot` (the
     caller saves it) and leave the context set to the fastest one.  Returns
     {"flash_budget", "coop_blocks", "block_cell", "predefer", "flash_ms", "trials"}.
+    predefer: pre-deferral thresholds as multiples of the budget (0: off).
     The context must use the batched variant."""
     if coop_blocks is None:
         coop_blocks = (ctx.get_param("coop_blocks"),)
@@ -44,8 +45,8 @@ def tune(ctx, dt: float, slot: int = 0, budgets=DEFAULT_BUDGETS, coop_blocks=Non
         ctx.set_param("flash_budget", budget)
         ctx.set_param("coop_blocks", blocks)
         ctx.set_param("block_cell", bc)
-        ctx.set_param("predefer", pre)
-        trials.append((_flash_ms(ctx, dt, slot, reps), budget, blocks, bc, pre))
+        ctx.set_param("predefer", pre * budget)
+        trials.append((_flash_ms(ctx, dt, slot, reps), budget, blocks, bc, pre * budget))
     ms, budget, blocks, bc, pre = min(trials)
     ctx.set_param("flash_budget", budget)
     ctx.set_param("coop_blocks", blocks)

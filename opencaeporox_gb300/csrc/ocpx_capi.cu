@@ -120,7 +120,7 @@ struct ocpx_ctx {
     int defer_cap = 0;
     int flash_budget = 48;
     int coop_blocks = 0;
-    int predefer = 1;
+    long long predefer = 192;          // pre-deferral threshold in work units (0: off)
     cudaStream_t stream2 = nullptr;    // high-priority stream of the pre-deferred cooperative kernel
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double* u = nullptr;            // Newton update staging
@@ -510,12 +510,12 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             // cells expensive in their last flash go to the cooperative kernel at
             // once, on a second (high-priority) stream, concurrently with the
             // per-cell kernel; cells that turn out expensive now follow after it
-            const bool pre = ctx->predefer != 0;
+            const bool pre = ctx->predefer > 0;
             OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned) * 2, s));
             mk = ctx->stage_begin(9);
             if (pre) {
                 const DeferSink sinkA{ctx->pre_rec, ctx->defer_count + 1, ctx->defer_cap};
-                OCPX_CUDA(launch_predefer(ctx->d_model, ctx->b, ctx->flash_budget, sinkA, ctx->pre_flag, s));
+                OCPX_CUDA(launch_predefer(ctx->d_model, ctx->b, ctx->predefer, sinkA, ctx->pre_flag, s));
                 ctx->launches++;
             }
             OCPX_CUDA(launch_cost_order(ctx->b, pre ? ctx->pre_flag : nullptr, ctx->cost_hist, ctx->order, s));
@@ -848,8 +848,8 @@ ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value)
         ctx->block_cell = (int)value;
         return OCPX_OK;
     case OCPX_PARAM_PREDEFER:
-        if (value != 0 && value != 1) return fail(OCPX_INVALID_ARG, "predefer must be 0 or 1");
-        ctx->predefer = (int)value;
+        if (value < 0) return fail(OCPX_INVALID_ARG, "predefer threshold must be >= 0");
+        ctx->predefer = value;
         return OCPX_OK;
     default:
         return fail(OCPX_INVALID_ARG, "unknown or read-only parameter");

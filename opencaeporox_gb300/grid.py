@@ -30,23 +30,28 @@ def orthogonal_grid(nx, ny, nz, dx, dy, dz, tops, kx, ky, kz, poro, ntg=None, co
     for k in range(1, nz):
         top[k * layer:(k + 1) * layer] = top[(k - 1) * layer:k * layer] + dz[(k - 1) * layer:k * layer]
     depth = top + dz / 2
-    b_list, e_list, t_list = [], [], []
     idx = np.arange(n)
     i = idx % nx
     j = (idx // nx) % ny
     k = idx // layer
-    for bId in range(n):
-        for cond, step, area_fn, perm in (
-                (i[bId] < nx - 1, 1, lambda c: 2 * dy[c] * dz[c] / dx[c], kx * ntg),
-                (j[bId] < ny - 1, nx, lambda c: 2 * dz[c] * dx[c] / dy[c], ky * ntg),
-                (k[bId] < nz - 1, layer, lambda c: 2 * dx[c] * dy[c] / dz[c], kz)):
-            if not cond:
-                continue
-            eId = bId + step
-            T1 = perm[bId] * area_fn(bId)
-            T2 = perm[eId] * area_fn(eId)
-            b_list.append(bId)
-            e_list.append(eId)
-            t_list.append(1.0 / (1 / T1 + 1 / T2) * conv_darcy)
+    # per direction, vectorised; then ordered by (bId, direction x < y < z) as
+    # the reference's cell loop emits them
+    bs, es, ts, keys = [], [], [], []
+    for d, (cond, step, area, perm) in enumerate((
+            (i < nx - 1, 1, 2 * dy * dz / dx, kx * ntg),
+            (j < ny - 1, nx, 2 * dz * dx / dy, ky * ntg),
+            (k < nz - 1, layer, 2 * dx * dy / dz, kz))):
+        bId = idx[cond]
+        eId = bId + step
+        T1 = perm[bId] * area[bId]
+        T2 = perm[eId] * area[eId]
+        bs.append(bId)
+        es.append(eId)
+        ts.append(1.0 / (1 / T1 + 1 / T2) * conv_darcy)
+        keys.append(bId * 3 + d)
+    order = np.argsort(np.concatenate(keys), kind="stable")
+    b_list = np.concatenate(bs)[order]
+    e_list = np.concatenate(es)[order]
+    t_list = np.concatenate(ts)[order]
     return Grid(v=v, depth=depth, poro_init=poro, conn_b=np.array(b_list, np.uint32),
                 conn_e=np.array(e_list, np.uint32), conn_trans=np.array(t_list))

@@ -108,3 +108,56 @@ def comp_grid(nx, ny, nz, dxy=20.0, dz=5.0, perm=50.0, poro=0.2, tops=2000.0):
     n = nx * ny * nz
     return orthogonal_grid(nx, ny, nz, dxy, dxy, dz, tops, np.full(n, perm), np.full(n, perm), np.full(n, perm),
                            np.full(n, poro), conv_darcy=METRIC["CONV_DARCY"])
+
+
+def layered_lognormal_perm(nx, ny, nz, median, sigma_ln, corr_cells, seed):
+    """Layered lognormal permeability [mD]: a seeded standard-normal field
+    smoothed in x and y by a Gaussian filter of standard deviation
+    corr_cells / 2 (cells), rescaled to unit variance per layer, then
+    k = median * exp(sigma_ln * g).  Cell order (k, j, i), x fastest."""
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    g = rng.standard_normal((nz, ny, nx))
+    for k in range(nz):
+        layer = gaussian_filter(g[k], sigma=corr_cells / 2.0, mode="wrap")
+        g[k] = (layer - layer.mean()) / max(layer.std(), 1e-12)
+    return (median * np.exp(sigma_ln * g)).ravel()
+
+
+def comp_grid_lognormal(nx, ny, nz, median=200.0, sigma_ln=1.5, corr_cells=10, seed=0, dxy=20.0, dz=5.0,
+                        poro=0.2, tops=2000.0, kz_ratio=0.1):
+    """Orthogonal grid with layered lognormal permeability (kz = kz_ratio kx)."""
+    k = layered_lognormal_perm(nx, ny, nz, median, sigma_ln, corr_cells, seed)
+    n = nx * ny * nz
+    return orthogonal_grid(nx, ny, nz, dxy, dxy, dz, tops, k, k, kz_ratio * k, np.full(n, poro),
+                           conv_darcy=METRIC["CONV_DARCY"])
+
+
+def ptn_workload(ctx, grid, ncomp, seed, dt=0.1, dsmax=0.2, p_range=(100.0, 300.0)):
+    """Drive a context to the input of the second Newton iteration of a time
+    step from a seeded PTN start (pores filled by scaling the moles), as the
+    bench does; returns the two seeded Newton updates (u1 applied, u2 the one
+    that produced the returned state)."""
+    st = comp_initial_state(grid, ncomp, seed, p_range=p_range)
+    ctx.load_state(st)
+    ctx.update_property()
+    scale = ctx.get("ROCKVP") / ctx.get("VF")
+    Ni = (st["Ni"].reshape(grid.nb, -1) * scale[:, None]).ravel()
+    st.update(Ni=Ni, lNi=Ni, Nt=Ni.reshape(grid.nb, -1).sum(axis=1))
+    ctx.load_state(st)
+    ctx.set("SKIP_FLAG", np.zeros(grid.nb, np.uint8))
+    ctx.update_property()
+    ctx.cal_res(dt)
+    ctx.update_last_time_step()
+    us = []
+    for k in range(2):
+        rng = np.random.default_rng(seed + 77 + k)
+        u = np.zeros((grid.nb, ncomp + 2))
+        u[:, 0] = rng.normal(0.0, 2.0, grid.nb)
+        u[:, 1:] = Ni.reshape(grid.nb, -1) * rng.normal(0.0, 2e-3, (grid.nb, ncomp + 1))
+        us.append(u.ravel())
+    ctx.get_solution(us[0], dsmax)
+    ctx.update_property()
+    ctx.cal_res(dt)
+    ctx.get_solution(us[1], dsmax)
+    return us

@@ -319,8 +319,9 @@ class Ranks:
             dist.init_process_group("gloo")
             self.dist = dist
 
-    def barrier(self, rt):
-        rt.rt.cudaDeviceSynchronize()
+    def barrier(self, rt=None):
+        if rt is not None:
+            rt.rt.cudaDeviceSynchronize()
         if self.dist:
             self.dist.barrier()
 

@@ -220,7 +220,7 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *                 reading it synchronizes the context stream;
  *   PREDEFER      cells whose last flash used more than this many work
  *                 units go to the cooperative kernel at once, on a second
- *                 stream, while the per-cell kernel runs (default 192);
+ *                 stream, while the per-cell kernel runs (default 96);
  *                 0: only cells that exceed the budget now are deferred. */
 typedef enum ocpx_param {
     OCPX_PARAM_FLASH_BUDGET = 0,

@@ -120,7 +120,7 @@ struct ocpx_ctx {
     int defer_cap = 0;
     int flash_budget = 48;
     int coop_blocks = 0;
-    long long predefer = 192;          // pre-deferral threshold in work units (0: off)
+    long long predefer = 96;           // pre-deferral threshold in work units (0: off)
     cudaStream_t stream2 = nullptr;    // high-priority stream of the pre-deferred cooperative kernel
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double* u = nullptr;            // Newton update staging

@@ -275,14 +275,15 @@ def fp64_peak(device=0):
     return max(measure_fp64_tflops(device, 20000) for _ in range(3))
 
 
-# FP64 operations of the flash stage on this workload, per cell: 2 x DFMA + DADD
-# + DMUL thread-level instructions of the k_flash_comp launch of one timed step
-# (ncu smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum), divided
-# by the 36,000 cells; libm internals included (2 x 746.2 M + 523.3 M + 574.0 M
-# = 2.590 GFLOP for the launch, profiles/k_flash_comp_comp6_36k.md).
-FLASH_FP64_FLOP_PER_CELL = 2589720497 / 36000
+# FP64 operations of the flash on this workload, per cell: 2 x DFMA + DADD + DMUL
+# thread-level instructions of the plain one-thread-per-cell kernel (k_flash_comp)
+# for the timed Newton iteration (ncu smsp__sass_thread_inst_executed_op_
+# {dfma,dadd,dmul}_pred_on.sum: 223.4 M, 121.7 M, 142.7 M = 711.2 MFLOP), divided by
+# the 36,000 cells; libm internals included.  The batched form does the same
+# algorithmic work in another order (profiles/k_flash_comp_comp6_36k.md).
+FLASH_FP64_FLOP_PER_CELL = (2 * 223408633 + 121682495 + 142721273) / 36000
 # DRAM bytes (read + write) of that launch, from the same capture.
-FLASH_DRAM_BYTES = 98142720 + 187619584
+FLASH_DRAM_BYTES = 107259392 + 173581568
 
 
 def assembly_bytes(nb, nconn, nc, nnzb):
@@ -305,6 +306,68 @@ def peaks():
             return json.load(f)
     except OSError:
         return {}
+
+
+# ------------------------------------------------- batched-flash stress ---
+FS_CELLS, FS_NCOMP, FS_SEED, FS_TEMP = 1 << 20, 10, 3, 71.85
+FS_METRIC = "batched-flash stress: flash cells/s, 10 components, 20% of cells near saturation"
+
+
+def flash_stress(args, rt, local):
+    """1,048,576 independent 10-component cells; 20 % placed within 5 % of their
+    saturation pressure by bisection on the seeded fluid's envelope, the rest
+    at P ~ U(5, 40) MPa, z ~ Dirichlet(1.5), T = 345 K.  Each timed flash starts
+    from no phase history (full stability test) with the iteration counters
+    of the previous flash of the same cells.  Plain one-thread-per-cell kernel
+    vs the batched form (cost order, work budget, warp-cooperative tail)."""
+    from opencaeporox_gb300 import synthetic
+    from opencaeporox_gb300.fim import FimContext
+    model = synthetic.comp_model(FS_NCOMP, FS_SEED)
+    t0 = time.perf_counter()
+    P, Ni = synthetic.flash_stress_cells(lambda g: FimContext(model, g, device=local, variant=1), FS_CELLS,
+                                         FS_NCOMP, FS_SEED, temp_c=FS_TEMP)
+    t_setup = time.perf_counter() - t0
+    grid = synthetic.flash_grid(FS_CELLS)
+    st = synthetic.flash_state(P, Ni, FS_TEMP)
+    out = {}
+    for variant in (0, 1):
+        ctx = FimContext(model, grid, device=local, variant=variant)
+        ctx.load_state(st)
+        ctx.update_property()  # iteration history
+        ctx.load_state(st)
+        ctx.checkpoint(0)
+        if variant == 1 and not args.no_tune:
+            # tune on the flash stage (the step has no connections)
+            from opencaeporox_gb300 import autotune
+            out["autotune"] = {k: v for k, v in autotune.tune(ctx, DT, slot=0, block_cells=(64, 128),
+                                                              coop_blocks=(152, 304, 608)).items() if k != "trials"}
+        times = []
+        for k in range(args.warmup + args.steps):
+            ctx.checkpoint(0, restore=True)
+            ctx.profile(True)
+            ctx.update_property()
+            ms, n = ctx.profile_read()["flash"]
+            ctx.profile(False)
+            if k >= args.warmup:
+                times.append(ms)
+        pe = ctx.get("PHASE_EXIST").reshape(-1, 3)
+        out[variant] = dict(ms=statistics.median(times), two_phase=int(np.sum((pe[:, 0] != 0) & (pe[:, 1] != 0))),
+                            iters=ctx.get("FLASH_ITERS").reshape(-1, 5),
+                            deferred=ctx.get_param("deferred") if variant == 1 else 0)
+        ctx.close()
+    it = out[0]["iters"].sum(axis=1)
+    line = {"metric": FS_METRIC, "value": FS_CELLS / (out[1]["ms"] * 1e-3), "unit": "cells/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out[1]["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": "1,048,576 independent cells, 10 seeded components, 20% within 5% of "
+                                   "saturation (bisection), rest P~U(5,40) MPa, z~Dirichlet(1.5), T=345 K"},
+            "plain_value": FS_CELLS / (out[0]["ms"] * 1e-3), "plain_ms": out[0]["ms"],
+            "batched_over_plain": out[0]["ms"] / out[1]["ms"], "two_phase_cells": out[0]["two_phase"],
+            "iterations_per_cell": {"mean": float(it.mean()), "p99": float(np.percentile(it, 99)),
+                                    "max": int(it.max())},
+            "deferred_cells": out[1]["deferred"], "autotune": out.get("autotune"), "setup_s": t_setup,
+            "timing": "flash stage, CUDA events on the library stream"}
+    return line
 
 
 class Ranks:
@@ -345,6 +408,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner (library defaults)")
+    ap.add_argument("--workload", default="fim", choices=["fim", "flash-stress"],
+                    help="fim: the compositional Newton step (default); flash-stress: 1M independent flashes")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -370,6 +435,10 @@ def main():
     gb.build()
     rt = Cudart()
     rt.rt.cudaSetDevice(local)
+    if args.workload == "flash-stress":
+        if rank == 0:
+            print(json.dumps(flash_stress(args, rt, local)))
+        return
     ranks = Ranks(world)
     flush_bytes = 512 << 20
     flush = (rt.malloc(flush_bytes), flush_bytes)
@@ -379,7 +448,7 @@ def main():
         ctx, model, grid, u = build_workload(variant, device=local)
         if variant == 1 and not args.no_tune:
             from opencaeporox_gb300 import autotune
-            tuned = autotune.tune(ctx, DT, slot=0, block_cells=(64, 128))
+            tuned = autotune.tune(ctx, DT, slot=0, block_cells=(64, 128), coop_blocks=(152, 304, 608))
         ranks.barrier(rt)
         t, launches = time_device(ctx, rt, args.steps, args.warmup, flush)
         ranks.barrier(rt)

@@ -14,7 +14,7 @@ from __future__ import annotations
 
 import itertools
 
-DEFAULT_BUDGETS = (16, 32, 48, 64, 96, 128, 192, 256, 384)
+DEFAULT_BUDGETS = (24, 32, 48, 64, 96, 128, 192)
 
 
 def _flash_ms(ctx, dt: float, slot: int, reps: int) -> float:

@@ -21,6 +21,7 @@ struct EosPR {
     const CompModel* m;
     double Ai[NCM], Bi[NCM];
     double s[NCM * NCM];  // sqrt(Ai[i] * Ai[k])
+    double s2[NCM * NCM]; // 2 * (1 - BIC_ik) * sqrt(Ai[i] * Ai[k]), the factor of CalFug/CalFugPhi's sum
     // per-call scratch
     double Aj, Bj, Zj;
     double Ax[NCM], Zx[NCM], An[NCM], Bn[NCM], Zn[NCM];
@@ -48,6 +49,8 @@ struct EosPR {
                 s[i * NCM + k] = v;
                 s[k * NCM + i] = v;
             }
+        for (int i = 0; i < nc; i++)
+            for (int k = 0; k < nc; k++) s2[i * NCM + k] = 2 * omb(i, k) * s[i * NCM + k];
     }
 
     OCPX_HD double omb(int i, int k) const { return m->omb[i * NC_MAX + k]; }
@@ -196,7 +199,7 @@ struct EosPR {
     OCPX_HD double mix2(int i, const double* x) const
     {
         double tmp = 0;
-        for (int k = 0; k < nc; k++) tmp += 2 * omb(i, k) * s[i * NCM + k] * x[k];
+        for (int k = 0; k < nc; k++) tmp += s2[i * NCM + k] * x[k];  // (2 * omb * s) * x
         return tmp;
     }
     // sum_k (1-BIC_ik) sqrt(Ai Ak) x_k, as CalLnFugN/P/PhiN form it

@@ -33,6 +33,7 @@ template <int NCM>
 struct CoopSh {
     double Ai[NCM], Bi[NCM];
     double s[NCM * NCM], omb[NCM * NCM];
+    double s2[NCM * NCM];         // 2 (1 - BIC) sqrt(Ai Ak), the factor of CalFugPhi's sum
     double xs[2][NCM];            // EoS input composition of each half
     double tA[2][NCM * NCM];      // Aj terms
     double tB[2][NCM];            // Bj terms
@@ -130,6 +131,9 @@ struct CoopPE {
                 sh.s[k * NCM + i] = v;
             }
         __syncwarp();
+        if (act && h == 0)
+            for (int k = 0; k < NC; k++) sh.s2[i * NCM + k] = 2 * omb(i, k) * sh.s[i * NCM + k];
+        __syncwarp();
     }
 
     // EoS_PR::CalAjBj for the half's composition
@@ -175,7 +179,8 @@ struct CoopPE {
         const double a = (DELTA1 + DELTA2 - 1) * Bj - 1;
         const double b = (Aj + DELTA1 * DELTA2 * Bj * Bj - (DELTA1 + DELTA2) * Bj * (Bj + 1));
         const double c = -(Aj * Bj + DELTA1 * DELTA2 * Bj * Bj * (Bj + 1));
-        const double qr = (i == 1) ? (2 * a * a * a - 9 * a * b + 27 * c) / 54 : (a * a - 3 * b) / 9;
+        // lane 1: R = (2a^3 - 9ab + 27c) / 54, the others Q = (a^2 - 3b) / 9 (one division)
+        const double qr = ((i == 1) ? (2 * a * a * a - 9 * a * b + 27 * c) : (a * a - 3 * b)) / ((i == 1) ? 54.0 : 9.0);
         const double Q = __shfl_sync(FULL_MASK, qr, hb);
         const double R = __shfl_sync(FULL_MASK, qr, hb + 1);
         const double Q3 = Q * Q * Q;
@@ -248,7 +253,8 @@ struct CoopPE {
         const int comp = (paired && i >= 8) ? i - 8 : ic;
         const int cc = comp < NC ? comp : 0;
         double tmp = 0;
-        for (int k = 0; k < NC; k++) tmp += 2 * omb(cc, k) * sh.s[cc * NCM + k] * x[k];
+        // (2 * omb * s) * x in the reference's association; the factor is precomputed
+        for (int k = 0; k < NC; k++) tmp += sh.s2[cc * NCM + k] * x[k];
         double BiBj, tA, c1;
         if (paired) {
             // lane i: Bi/Bj; lane i+8: tmp/Aj of component i; lane 15 (free when NC <= 7): c1

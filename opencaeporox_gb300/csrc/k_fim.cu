@@ -202,11 +202,8 @@ cudaError_t launch_jac_rows(const BulkView& b, const ConnView& cv, const double*
 // test), then the work units its last flash used (iteration counters weighted
 // as the flash's budget charges them, Rachford-Rice iterations at a fifth), in
 // descending order.  Warps then hold cells on the same code path.
-// Cells already handed to the cooperative kernel (pre-deferred) go to the last
-// bucket, where the per-cell kernel skips them.
-__device__ __forceinline__ int cost_bucket(const BulkView& b, int cell, const uint8_t* pre)
+__device__ __forceinline__ int cost_bucket(const BulkView& b, int cell)
 {
-    if (pre && pre[cell]) return COST_BUCKETS - 1;
     const long long w = predicted_work(b, cell);
     const int lvl = w < 63 ? (int)w : 63;
     const bool two = b.phaseExist[b.idx(0, cell)] && b.phaseExist[b.idx(1, cell)];
@@ -214,13 +211,13 @@ __device__ __forceinline__ int cost_bucket(const BulkView& b, int cell, const ui
     return cls * 64 + (63 - lvl);
 }
 
-__global__ void k_cost_hist(BulkView b, const uint8_t* __restrict__ pre, unsigned* __restrict__ hist)
+__global__ void k_cost_hist(BulkView b, unsigned* __restrict__ hist)
 {
     __shared__ unsigned h[COST_BUCKETS];
     for (int k = threadIdx.x; k < COST_BUCKETS; k += blockDim.x) h[k] = 0;
     __syncthreads();
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell < b.nb) atomicAdd(&h[cost_bucket(b, cell, pre)], 1u);
+    if (cell < b.nb) atomicAdd(&h[cost_bucket(b, cell)], 1u);
     __syncthreads();
     for (int k = threadIdx.x; k < COST_BUCKETS; k += blockDim.x)
         if (h[k]) atomicAdd(&hist[k], h[k]);
@@ -242,36 +239,38 @@ __global__ void k_cost_scan(unsigned* __restrict__ hist)
     hist[t] = v[t] - hist[t];
 }
 
-__global__ void k_cost_scatter(BulkView b, const uint8_t* __restrict__ pre, unsigned* __restrict__ offs,
-                               int* __restrict__ order)
+__global__ void k_cost_scatter(BulkView b, unsigned* __restrict__ offs, int* __restrict__ order)
 {
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= b.nb) return;
-    const unsigned pos = atomicAdd(&offs[cost_bucket(b, cell, pre)], 1u);
+    const unsigned pos = atomicAdd(&offs[cost_bucket(b, cell)], 1u);
     order[pos] = cell;
 }
 
-cudaError_t launch_cost_order(const BulkView& b, const uint8_t* pre, unsigned* hist, int* order, cudaStream_t s)
+cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, cudaStream_t s)
 {
     if (!b.nb) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned) * COST_BUCKETS, s);
     if (e != cudaSuccess) return e;
     const int block = 256;
-    k_cost_hist<<<grid_for(b.nb, block), block, 0, s>>>(b, pre, hist);
+    k_cost_hist<<<grid_for(b.nb, block), block, 0, s>>>(b, hist);
     k_cost_scan<<<1, COST_BUCKETS, 0, s>>>(hist);
-    k_cost_scatter<<<grid_for(b.nb, block), block, 0, s>>>(b, pre, hist, order);
+    k_cost_scatter<<<grid_for(b.nb, block), block, 0, s>>>(b, hist, order);
     return cudaGetLastError();
 }
 
 // Cells whose last flash used more than `threshold` work units are handed to
 // the cooperative kernel before the per-cell kernel runs, so that both run at
 // the same time (pre[cell] = 1).  Cells that the skip test will let through
-// (flash type 1) stay with the per-cell kernel.
-__global__ void k_predefer(const Model* __restrict__ M, BulkView b, long long threshold, DeferSink sink,
-                           uint8_t* __restrict__ pre)
+// (flash type 1) stay with the per-cell kernel.  Cells are visited in the cost
+// order, so the list comes out roughly heaviest first and the cooperative
+// kernel's warps, which take list slots in order, start with the longest cells.
+__global__ void k_predefer(const Model* __restrict__ M, BulkView b, const int* __restrict__ order,
+                           long long threshold, DeferSink sink, uint8_t* __restrict__ pre)
 {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= b.nb) return;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= b.nb) return;
+    const int cell = order[p];
     pre[cell] = 0;
     if (predicted_work(b, cell) <= threshold) return;
     const CompModel& m = M->comp;
@@ -292,10 +291,10 @@ __global__ void k_predefer(const Model* __restrict__ M, BulkView b, long long th
     if (sink.push(cell, ftype_in, npPE)) pre[cell] = 1;
 }
 
-cudaError_t launch_predefer(const Model* dm, const BulkView& b, long long threshold, const DeferSink& sink,
-                            uint8_t* pre, cudaStream_t s)
+cudaError_t launch_predefer(const Model* dm, const BulkView& b, const int* order, long long threshold,
+                            const DeferSink& sink, uint8_t* pre, cudaStream_t s)
 {
-    if (b.nb) k_predefer<<<grid_for(b.nb, 128), 128, 0, s>>>(dm, b, threshold, sink, pre);
+    if (b.nb) k_predefer<<<grid_for(b.nb, 128), 128, 0, s>>>(dm, b, order, threshold, sink, pre);
     return cudaGetLastError();
 }
 

@@ -513,13 +513,13 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             const bool pre = ctx->predefer > 0;
             OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned) * 2, s));
             mk = ctx->stage_begin(9);
+            OCPX_CUDA(launch_cost_order(ctx->b, ctx->cost_hist, ctx->order, s));
+            ctx->launches += 3;
             if (pre) {
                 const DeferSink sinkA{ctx->pre_rec, ctx->defer_count + 1, ctx->defer_cap};
-                OCPX_CUDA(launch_predefer(ctx->d_model, ctx->b, ctx->predefer, sinkA, ctx->pre_flag, s));
+                OCPX_CUDA(launch_predefer(ctx->d_model, ctx->b, ctx->order, ctx->predefer, sinkA, ctx->pre_flag, s));
                 ctx->launches++;
             }
-            OCPX_CUDA(launch_cost_order(ctx->b, pre ? ctx->pre_flag : nullptr, ctx->cost_hist, ctx->order, s));
-            ctx->launches += 3;
             ctx->stage_end(mk);
             const FlashBatch fbA{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
                                  ctx->pre_rec, ctx->defer_count + 1, ctx->pre_res, nullptr};

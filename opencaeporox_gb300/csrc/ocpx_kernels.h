@@ -34,12 +34,11 @@ cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, co
 // a group, in descending order of the work their last flash needed, by a
 // counting sort over COST_BUCKETS buckets.
 constexpr int COST_BUCKETS = 256;
-// pre: cells already pre-deferred (sorted last), may be NULL
-cudaError_t launch_cost_order(const BulkView& b, const uint8_t* pre, unsigned* hist, int* order, cudaStream_t s);
+cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, cudaStream_t s);
 // hand the cells whose last flash used more than `threshold` work units to the
-// cooperative kernel up front (pre[cell] = 1)
-cudaError_t launch_predefer(const Model* dm, const BulkView& b, long long threshold, const DeferSink& sink,
-                            uint8_t* pre, cudaStream_t s);
+// cooperative kernel up front (pre[cell] = 1), visiting cells in `order`
+cudaError_t launch_predefer(const Model* dm, const BulkView& b, const int* order, long long threshold,
+                            const DeferSink& sink, uint8_t* pre, cudaStream_t s);
 
 cudaError_t launch_flash_bo(const Model* dm, const BulkView& b, int block, cudaStream_t s);
 cudaError_t launch_krpc_rock(const Model* dm, const BulkView& b, int block, cudaStream_t s);

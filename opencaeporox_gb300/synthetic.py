@@ -161,3 +161,63 @@ def ptn_workload(ctx, grid, ncomp, seed, dt=0.1, dsmax=0.2, p_range=(100.0, 300.
     ctx.cal_res(dt)
     ctx.get_solution(us[1], dsmax)
     return us
+
+
+def flash_grid(n, poro=0.2):
+    """n independent unit-volume cells without connections (flash-only runs)."""
+    from .fim import Grid
+    return Grid(np.ones(n), np.zeros(n), np.full(n, poro), np.zeros(0, np.uint32), np.zeros(0, np.uint32),
+                np.zeros(0))
+
+
+def flash_state(P, Ni, temp_c):
+    """State of independent cells flashed with no phase history (only the water
+    phase flagged, so lNP = 0 and the phase equilibrium starts with the full
+    four-start stability test, as the reference's InitFlash does)."""
+    n = P.size
+    nct = Ni.shape[1]
+    return dict(P=P.copy(), T=np.full(n, temp_c), Ni=Ni.ravel().copy(), lNi=Ni.ravel().copy(),
+                Nt=Ni.sum(axis=1), phaseExist=np.tile(np.array([0, 0, 1], np.uint8), n),
+                S=np.tile([0.0, 0.0, 1.0], n), xij=np.zeros(n * 3 * nct), Pj=np.repeat(P, 3),
+                skip_flag=np.zeros(n, np.uint8))
+
+
+def flash_stress_cells(ctx_factory, n, ncomp, seed, near_frac=0.2, p_range=(50.0, 400.0), near_band=0.05,
+                       temp_c=71.85, bisections=30):
+    """Inputs of the batched-flash stress case: n independent cells with
+    ncomp seeded components.  A fraction near_frac of the cells lie within
+    +-near_band of their saturation pressure, found by bisection between a
+    two-phase and a single-phase pressure of the seeded fluid's envelope
+    (evaluated with the GPU flash itself); the others have P ~ U(p_range)
+    and z ~ Dirichlet(1.5).  Returns (P [bar], Ni [n, ncomp+1])."""
+    rng = np.random.default_rng(seed + 2000)
+    z = rng.dirichlet(np.full(ncomp, 1.5), n)
+    Ni = np.concatenate([z * 10.0, np.ones((n, 1))], axis=1)
+    P = rng.uniform(*p_range, n)
+    near = rng.random(n) < near_frac
+    idx = np.nonzero(near)[0]
+    if idx.size:
+        sub = Ni[idx]
+        ctx = ctx_factory(flash_grid(idx.size))
+        try:
+            def two_phase(p):
+                ctx.load_state(flash_state(p, sub, temp_c))
+                ctx.update_property()
+                pe = ctx.get("PHASE_EXIST").reshape(-1, 3)
+                return (pe[:, 0] != 0) & (pe[:, 1] != 0)
+            lo = np.full(idx.size, p_range[0])
+            hi = np.full(idx.size, p_range[1])
+            tl, th = two_phase(lo), two_phase(hi)
+            ok = tl != th           # a phase boundary inside the range
+            for _ in range(bisections):
+                mid = 0.5 * (lo + hi)
+                tm = two_phase(mid)
+                same = tm == tl
+                lo = np.where(same, mid, lo)
+                hi = np.where(same, hi, mid)
+            psat = 0.5 * (lo + hi)
+            band = rng.uniform(-near_band, near_band, idx.size)
+            P[idx] = np.where(ok, psat * (1 + band), P[idx])
+        finally:
+            ctx.close()
+    return P, Ni

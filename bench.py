@@ -327,6 +327,7 @@ def flash_stress(args, rt, local):
     P, Ni = synthetic.flash_stress_cells(lambda g: FimContext(model, g, device=local, variant=1), FS_CELLS,
                                          FS_NCOMP, FS_SEED, temp_c=FS_TEMP)
     t_setup = time.perf_counter() - t0
+    print(f"flash-stress: inputs ready in {t_setup:.1f} s", file=sys.stderr, flush=True)
     grid = synthetic.flash_grid(FS_CELLS)
     st = synthetic.flash_state(P, Ni, FS_TEMP)
     out = {}
@@ -339,8 +340,11 @@ def flash_stress(args, rt, local):
         if variant == 1 and not args.no_tune:
             # tune on the flash stage (the step has no connections)
             from opencaeporox_gb300 import autotune
-            out["autotune"] = {k: v for k, v in autotune.tune(ctx, DT, slot=0, block_cells=(64, 128),
-                                                              coop_blocks=(152, 304, 608)).items() if k != "trials"}
+            # each flash of this workload takes seconds: a small candidate set, one round
+            space = {"flash_budget": (48, 192), "predefer": (0, 192), "coop_cells": (608, 1216, 4864),
+                     "coop_blocks": (608,), "block_cell": (128,)}
+            out["autotune"] = {k: v for k, v in autotune.tune(ctx, DT, slot=0, space=space, rounds=1,
+                                                              reps=1).items() if k != "trials"}
         times = []
         for k in range(args.warmup + args.steps):
             ctx.checkpoint(0, restore=True)
@@ -350,6 +354,7 @@ def flash_stress(args, rt, local):
             ctx.profile(False)
             if k >= args.warmup:
                 times.append(ms)
+        print(f"flash-stress: variant {variant} flash {statistics.median(times):.1f} ms", file=sys.stderr, flush=True)
         pe = ctx.get("PHASE_EXIST").reshape(-1, 3)
         out[variant] = dict(ms=statistics.median(times), two_phase=int(np.sum((pe[:, 0] != 0) & (pe[:, 1] != 0))),
                             iters=ctx.get("FLASH_ITERS").reshape(-1, 5),
@@ -368,6 +373,65 @@ def flash_stress(args, rt, local):
             "deferred_cells": out[1]["deferred"], "autotune": out.get("autotune"), "setup_s": t_setup,
             "timing": "flash stage, CUDA events on the library stream"}
     return line
+
+
+# ------------------------------------------------------ large Newton step ---
+LG_NX, LG_NY, LG_NZ, LG_NCOMP, LG_SEED = 200, 200, 100, 9, 5
+LG_METRIC = "FIM Newton-step cells/s, 4,000,000-cell compositional grid, 9 components"
+
+
+def large_step(args, rt, local):
+    """200 x 200 x 100 = 4,000,000 cells, 9 seeded components, lognormal
+    permeability (median 100 mD, sigma_ln 2.0, correlation 10 cells), layer
+    tops dipping by seeded angles within +-5 degrees (orthogonal cells: the
+    corner-point pillar perturbation of the configuration needs corner-point
+    ingest, which is not built).  PTN start, the second Newton iteration timed
+    as in the default workload; plain vs batched form, library defaults."""
+    from opencaeporox_gb300 import synthetic
+    from opencaeporox_gb300.fim import FimContext
+    from opencaeporox_gb300.grid import orthogonal_grid
+    rng = np.random.default_rng(LG_SEED)
+    dxy, dz = 20.0, 2.0
+    ax, ay = np.deg2rad(rng.uniform(-5, 5, 2))
+    x = (np.arange(LG_NX) + 0.5) * dxy
+    y = (np.arange(LG_NY) + 0.5) * dxy
+    tops = (2000.0 + np.tan(ax) * x[None, :] + np.tan(ay) * y[:, None]).ravel()
+    n = LG_NX * LG_NY * LG_NZ
+    k = synthetic.layered_lognormal_perm(LG_NX, LG_NY, LG_NZ, 100.0, 2.0, 10, LG_SEED)
+    grid = orthogonal_grid(LG_NX, LG_NY, LG_NZ, dxy, dxy, dz, tops, k, k, 0.1 * k, np.full(n, 0.2),
+                           conv_darcy=synthetic.METRIC["CONV_DARCY"])
+    model = synthetic.comp_model(LG_NCOMP, LG_SEED)
+    out = {}
+    stages = ("check", "flash", "krpc_rock", "report", "flux", "residual", "jac_conn", "jac_rows")
+    for variant in (0, 1):
+        t0 = time.perf_counter()
+        ctx = FimContext(model, grid, device=local, variant=variant)
+        synthetic.ptn_workload(ctx, grid, LG_NCOMP, LG_SEED, dt=DT, dsmax=DSMAX)
+        ctx.checkpoint(0)
+        print(f"large: variant {variant} set up in {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
+        times = []
+        for kk in range(args.warmup + args.steps):
+            ctx.checkpoint(0, restore=True)
+            ctx.profile(True)
+            ctx.enqueue_step(DT)
+            ctx.step_report()
+            prof = ctx.profile_read()
+            ctx.profile(False)
+            if kk >= args.warmup:
+                times.append(sum(prof[st][0] for st in stages))
+        out[variant] = dict(ms=statistics.median(times), stages={st: round(v[0], 3) for st, v in prof.items() if v[1]})
+        print(f"large: variant {variant} step {out[variant]['ms']:.1f} ms", file=sys.stderr, flush=True)
+        ctx.close()
+    return {"metric": LG_METRIC, "value": n / (out[1]["ms"] * 1e-3), "unit": "cells/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out[1]["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": "200x200x100 = 4,000,000 cells, 9 components, lognormal k (median 100 mD, "
+                                   "sigma_ln 2.0), dipping layers, second Newton iteration",
+                       "connections": int(grid.nconn)},
+            "plain_value": n / (out[0]["ms"] * 1e-3), "plain_ms": out[0]["ms"],
+            "batched_over_plain": out[0]["ms"] / out[1]["ms"], "stages_ms": out[1]["stages"],
+            "plain_stages_ms": out[0]["stages"],
+            "timing": "sum of the step's stage times, CUDA events on the library stream (library defaults)"}
 
 
 class Ranks:
@@ -408,8 +472,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner (library defaults)")
-    ap.add_argument("--workload", default="fim", choices=["fim", "flash-stress"],
-                    help="fim: the compositional Newton step (default); flash-stress: 1M independent flashes")
+    ap.add_argument("--workload", default="fim", choices=["fim", "flash-stress", "large"],
+                    help="fim: the compositional Newton step (default); flash-stress: 1M independent flashes; "
+                         "large: the 4M-cell Newton step")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -435,9 +500,10 @@ def main():
     gb.build()
     rt = Cudart()
     rt.rt.cudaSetDevice(local)
-    if args.workload == "flash-stress":
+    if args.workload != "fim":
         if rank == 0:
-            print(json.dumps(flash_stress(args, rt, local)))
+            fn = flash_stress if args.workload == "flash-stress" else large_step
+            print(json.dumps(fn(args, rt, local)))
         return
     ranks = Ranks(world)
     flush_bytes = 512 << 20
@@ -448,7 +514,7 @@ def main():
         ctx, model, grid, u = build_workload(variant, device=local)
         if variant == 1 and not args.no_tune:
             from opencaeporox_gb300 import autotune
-            tuned = autotune.tune(ctx, DT, slot=0, block_cells=(64, 128), coop_blocks=(152, 304, 608))
+            tuned = autotune.tune(ctx, DT, slot=0)
         ranks.barrier(rt)
         t, launches = time_device(ctx, rt, args.steps, args.warmup, flush)
         ranks.barrier(rt)
@@ -501,9 +567,8 @@ def main():
             "batched": {"flash_budget": ctx1.get_param("flash_budget"), "coop_blocks": ctx1.get_param("coop_blocks"),
                         "deferred_cells": ctx1.get_param("deferred"),
                         "block_cell": ctx1.get_param("block_cell"), "predefer": ctx1.get_param("predefer"),
-                        "autotune": None if tuned is None else {k: tuned[k] for k in
-                                                                ("flash_budget", "coop_blocks", "block_cell",
-                                                                 "predefer", "flash_ms")}},
+                        "coop_cells": ctx1.get_param("coop_cells"),
+                        "autotune": None if tuned is None else {k: v for k, v in tuned.items() if k != "trials"}},
             "clocks": ck, "gpu_launches": launches,
             "e2e": {"value": nb / (e2e_ms * 1e-3) * world, "unit": "cells/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h}}

@@ -221,13 +221,20 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *   PREDEFER      cells whose last flash used more than this many work
  *                 units go to the cooperative kernel at once, on a second
  *                 stream, while the per-cell kernel runs (default 96);
- *                 0: only cells that exceed the budget now are deferred. */
+ *                 0: only cells that exceed the budget now are deferred;
+ *   COOP_CELLS    adaptive floor of both thresholds: about this many of the
+ *                 cells with the largest predicted work may go to the
+ *                 cooperative kernel (default 1216, two per warp slot); on a
+ *                 workload where every cell is expensive the per-cell kernel
+ *                 keeps almost all of them.  0: the thresholds are the two
+ *                 parameters above only. */
 typedef enum ocpx_param {
     OCPX_PARAM_FLASH_BUDGET = 0,
     OCPX_PARAM_COOP_BLOCKS = 1,
     OCPX_PARAM_BLOCK_CELL = 2,
     OCPX_PARAM_DEFERRED = 3,
-    OCPX_PARAM_PREDEFER = 4
+    OCPX_PARAM_PREDEFER = 4,
+    OCPX_PARAM_COOP_CELLS = 5
 } ocpx_param;
 ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value);
 ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value);

@@ -196,16 +196,23 @@ cudaError_t launch_jac_rows(const BulkView& b, const ConnView& cv, const double*
     if (b.nb) k_jac_rows<<<grid_for(b.nb, block), block, 0, s>>>(b, cv, bmat, rowptr, val);
     return cudaGetLastError();
 }
+// Work level of a predicted work w >= 1: floor(4 log2 w), at most 63 (levels
+// are 19 % apart and reach 2^15.75 work units).
+__device__ __forceinline__ int cost_level(long long w)
+{
+    const int l = (int)(4.0f * __log2f((float)w));
+    return l < 0 ? 0 : (l > 63 ? 63 : l);
+}
+
 // Sort key of a cell for the batched flash: its class (skip-flagged cells,
 // which usually skip the equilibrium; two-phase cells, which run the split
 // and the two-phase derivatives; one-phase cells, which run the stability
-// test), then the work units its last flash used (iteration counters weighted
+// test), then the work level its last flash used (iteration counters weighted
 // as the flash's budget charges them, Rachford-Rice iterations at a fifth), in
 // descending order.  Warps then hold cells on the same code path.
 __device__ __forceinline__ int cost_bucket(const BulkView& b, int cell)
 {
-    const long long w = predicted_work(b, cell);
-    const int lvl = w < 63 ? (int)w : 63;
+    const int lvl = cost_level(predicted_work(b, cell));
     const bool two = b.phaseExist[b.idx(0, cell)] && b.phaseExist[b.idx(1, cell)];
     const int cls = b.skip_flag[cell] ? 2 : (two ? 0 : 1);
     return cls * 64 + (63 - lvl);
@@ -223,12 +230,32 @@ __global__ void k_cost_hist(BulkView b, unsigned* __restrict__ hist)
         if (h[k]) atomicAdd(&hist[k], h[k]);
 }
 
-// exclusive scan of the bucket counts, in place (one block of COST_BUCKETS threads)
-__global__ void k_cost_scan(unsigned* __restrict__ hist)
+// Exclusive scan of the bucket counts, in place (one block of COST_BUCKETS
+// threads).  Also the adaptive work level: the lowest level L such that at
+// most coop_cells cells have a predicted level >= L (0 when coop_cells is 0),
+// written to level[0].  The cooperative kernel then gets about that many
+// cells whatever the workload's mean work.
+__global__ void k_cost_scan(unsigned* __restrict__ hist, unsigned coop_cells, int* __restrict__ level)
 {
     __shared__ unsigned v[COST_BUCKETS];
     const int t = threadIdx.x;
     v[t] = hist[t];
+    __syncthreads();
+    if (t == 0) {
+        int L = 0;
+        if (coop_cells) {
+            unsigned cum = 0;
+            L = 64;
+            for (int l = 63; l >= 0; l--) {
+                unsigned tot = 0;
+                for (int cls = 0; cls < COST_BUCKETS / 64; cls++) tot += v[cls * 64 + (63 - l)];
+                if (cum + tot > coop_cells) break;
+                cum += tot;
+                L = l;
+            }
+        }
+        level[0] = L;
+    }
     __syncthreads();
     for (int d = 1; d < COST_BUCKETS; d <<= 1) {
         const unsigned add = t >= d ? v[t - d] : 0u;
@@ -247,32 +274,36 @@ __global__ void k_cost_scatter(BulkView b, unsigned* __restrict__ offs, int* __r
     order[pos] = cell;
 }
 
-cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, cudaStream_t s)
+cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, unsigned coop_cells, int* level,
+                              cudaStream_t s)
 {
     if (!b.nb) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned) * COST_BUCKETS, s);
     if (e != cudaSuccess) return e;
     const int block = 256;
     k_cost_hist<<<grid_for(b.nb, block), block, 0, s>>>(b, hist);
-    k_cost_scan<<<1, COST_BUCKETS, 0, s>>>(hist);
+    k_cost_scan<<<1, COST_BUCKETS, 0, s>>>(hist, coop_cells, level);
     k_cost_scatter<<<grid_for(b.nb, block), block, 0, s>>>(b, hist, order);
     return cudaGetLastError();
 }
 
-// Cells whose last flash used more than `threshold` work units are handed to
-// the cooperative kernel before the per-cell kernel runs, so that both run at
-// the same time (pre[cell] = 1).  Cells that the skip test will let through
+// Cells whose last flash used more than `threshold` work units, and whose
+// work level is at or above the adaptive level, are handed to the cooperative
+// kernel before the per-cell kernel runs, so that both run at the same time
+// (pre[cell] = 1).  Cells that the skip test will let through
 // (flash type 1) stay with the per-cell kernel.  Cells are visited in the cost
 // order, so the list comes out roughly heaviest first and the cooperative
 // kernel's warps, which take list slots in order, start with the longest cells.
 __global__ void k_predefer(const Model* __restrict__ M, BulkView b, const int* __restrict__ order,
-                           long long threshold, DeferSink sink, uint8_t* __restrict__ pre)
+                           long long threshold, const int* __restrict__ level, DeferSink sink,
+                           uint8_t* __restrict__ pre)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= b.nb) return;
     const int cell = order[p];
     pre[cell] = 0;
-    if (predicted_work(b, cell) <= threshold) return;
+    const long long w = predicted_work(b, cell);
+    if (w <= threshold || cost_level(w) < level[0]) return;
     const CompModel& m = M->comp;
     const int NC = m.nc, np = b.np;
     double Ni[NC_MAX + 1], Sin[3];
@@ -292,9 +323,9 @@ __global__ void k_predefer(const Model* __restrict__ M, BulkView b, const int* _
 }
 
 cudaError_t launch_predefer(const Model* dm, const BulkView& b, const int* order, long long threshold,
-                            const DeferSink& sink, uint8_t* pre, cudaStream_t s)
+                            const int* level, const DeferSink& sink, uint8_t* pre, cudaStream_t s)
 {
-    if (b.nb) k_predefer<<<grid_for(b.nb, 128), 128, 0, s>>>(dm, b, order, threshold, sink, pre);
+    if (b.nb) k_predefer<<<grid_for(b.nb, 128), 128, 0, s>>>(dm, b, order, threshold, level, sink, pre);
     return cudaGetLastError();
 }
 

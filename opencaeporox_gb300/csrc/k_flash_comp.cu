@@ -25,12 +25,18 @@ __global__ void __launch_bounds__(128) k_flash_comp(const Model* __restrict__ M,
 template <int NCM>
 __global__ void __launch_bounds__(128) k_flash_budget(const Model* __restrict__ M, BulkView b,
                                                       const int* __restrict__ order, int budget, DeferSink sink,
-                                                      const uint8_t* __restrict__ pre)
+                                                      const uint8_t* __restrict__ pre, const int* __restrict__ level)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= b.nb) return;
     const int cell = order[p];
     if (pre && pre[cell]) return;  // handled by the cooperative kernel
+    if (level) {
+        // at least the work of the adaptive level: only cells heavier than the
+        // heaviest predicted ones are deferred now
+        const long long lw = (long long)exp2f(0.25f * (float)level[0]);
+        if (lw > budget) budget = lw > 0x7fffffffLL ? 0x7fffffff : (int)lw;
+    }
     CompCellUpdate<NCM> u;
     u.run(*M, b, cell, budget, &sink);
 }
@@ -86,7 +92,7 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
     case 0: {
         const DeferSink sink{fb.rec, fb.count, fb.cap};
         k_flash_budget<OCPX_NCM><<<(b.nb + fb.block - 1) / fb.block, fb.block, 0, s>>>(dm, b, order, fb.budget, sink,
-                                                                                         fb.pre);
+                                                                                         fb.pre, fb.level);
         break;
     }
     case 1:

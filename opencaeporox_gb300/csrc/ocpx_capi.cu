@@ -121,6 +121,8 @@ struct ocpx_ctx {
     int flash_budget = 48;
     int coop_blocks = 0;
     long long predefer = 96;           // pre-deferral threshold in work units (0: off)
+    long long coop_cells = 1216;       // target cells per cooperative pass (adaptive level; 0: off)
+    int* adapt_level = nullptr;        // device: adaptive work level of the last cost order
     cudaStream_t stream2 = nullptr;    // high-priority stream of the pre-deferred cooperative kernel
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double* u = nullptr;            // Newton update staging
@@ -360,7 +362,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     add(&ctx->defer_rec, sizeof(DeferRec) * (size_t)ctx->defer_cap); add(&ctx->defer_count, sizeof(unsigned) * 4);
     add(&ctx->pe_res, sizeof(PERes) * (size_t)ctx->defer_cap);
     add(&ctx->pre_rec, sizeof(DeferRec) * (size_t)ctx->defer_cap); add(&ctx->pre_res, sizeof(PERes) * (size_t)ctx->defer_cap);
-    add(&ctx->pre_flag, (size_t)nb);
+    add(&ctx->pre_flag, (size_t)nb); add(&ctx->adapt_level, sizeof(int) * 4);
     add(&ctx->u, D * (nc + 1));
     add(&ctx->bmat, sizeof(double) * C * 2 * bsize);
     add(&ctx->jac_rowptr, sizeof(uint32_t) * (nb + 1)); add(&ctx->jac_col, sizeof(uint32_t) * jcol.size());
@@ -513,18 +515,21 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             const bool pre = ctx->predefer > 0;
             OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned) * 2, s));
             mk = ctx->stage_begin(9);
-            OCPX_CUDA(launch_cost_order(ctx->b, ctx->cost_hist, ctx->order, s));
+            OCPX_CUDA(launch_cost_order(ctx->b, ctx->cost_hist, ctx->order, (unsigned)ctx->coop_cells,
+                                        ctx->adapt_level, s));
             ctx->launches += 3;
             if (pre) {
                 const DeferSink sinkA{ctx->pre_rec, ctx->defer_count + 1, ctx->defer_cap};
-                OCPX_CUDA(launch_predefer(ctx->d_model, ctx->b, ctx->order, ctx->predefer, sinkA, ctx->pre_flag, s));
+                OCPX_CUDA(launch_predefer(ctx->d_model, ctx->b, ctx->order, ctx->predefer, ctx->adapt_level, sinkA,
+                                          ctx->pre_flag, s));
                 ctx->launches++;
             }
             ctx->stage_end(mk);
             const FlashBatch fbA{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
-                                 ctx->pre_rec, ctx->defer_count + 1, ctx->pre_res, nullptr};
+                                 ctx->pre_rec, ctx->defer_count + 1, ctx->pre_res, nullptr, nullptr};
             const FlashBatch fbB{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
-                                 ctx->defer_rec, ctx->defer_count, ctx->pe_res, pre ? ctx->pre_flag : nullptr};
+                                 ctx->defer_rec, ctx->defer_count, ctx->pe_res, pre ? ctx->pre_flag : nullptr,
+                                 ctx->adapt_level};
             if (pre) {
                 OCPX_CUDA(cudaEventRecord(ctx->ev_fork, s));
                 OCPX_CUDA(cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
@@ -851,6 +856,10 @@ ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value)
         if (value < 0) return fail(OCPX_INVALID_ARG, "predefer threshold must be >= 0");
         ctx->predefer = value;
         return OCPX_OK;
+    case OCPX_PARAM_COOP_CELLS:
+        if (value < 0 || value > 0x7fffffffLL) return fail(OCPX_INVALID_ARG, "coop cells out of range");
+        ctx->coop_cells = value;
+        return OCPX_OK;
     default:
         return fail(OCPX_INVALID_ARG, "unknown or read-only parameter");
     }
@@ -864,6 +873,7 @@ ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value)
     case OCPX_PARAM_COOP_BLOCKS: *value = ctx->coop_blocks; return OCPX_OK;
     case OCPX_PARAM_BLOCK_CELL: *value = ctx->block_cell; return OCPX_OK;
     case OCPX_PARAM_PREDEFER: *value = ctx->predefer; return OCPX_OK;
+    case OCPX_PARAM_COOP_CELLS: *value = ctx->coop_cells; return OCPX_OK;
     case OCPX_PARAM_DEFERRED: {
         unsigned n[2] = {0, 0};
         OCPX_CUDA(cudaMemcpyAsync(n, ctx->defer_count, sizeof(n), cudaMemcpyDeviceToHost, ctx->stream));

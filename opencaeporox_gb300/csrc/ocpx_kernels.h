@@ -26,6 +26,7 @@ struct FlashBatch {
     unsigned* count;   // deferred cells (may exceed cap: the excess finish in place)
     PERes* pe;
     const uint8_t* pre;  // cells pre-deferred to another list (skipped by part 0), may be NULL
+    const int* level;    // adaptive work level: the budget is at least its work units, may be NULL
 };
 // part 0: budgeted thread-per-cell flash, 1: cooperative equilibrium, 2: finish deferred cells
 cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, const int* order,
@@ -34,11 +35,14 @@ cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, co
 // a group, in descending order of the work their last flash needed, by a
 // counting sort over COST_BUCKETS buckets.
 constexpr int COST_BUCKETS = 256;
-cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, cudaStream_t s);
-// hand the cells whose last flash used more than `threshold` work units to the
-// cooperative kernel up front (pre[cell] = 1), visiting cells in `order`
+// level[0] receives the adaptive work level (see k_cost_scan)
+cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, unsigned coop_cells, int* level,
+                              cudaStream_t s);
+// hand the cells whose last flash used more than `threshold` work units, at or
+// above the adaptive level, to the cooperative kernel up front (pre[cell] = 1),
+// visiting cells in `order`
 cudaError_t launch_predefer(const Model* dm, const BulkView& b, const int* order, long long threshold,
-                            const DeferSink& sink, uint8_t* pre, cudaStream_t s);
+                            const int* level, const DeferSink& sink, uint8_t* pre, cudaStream_t s);
 
 cudaError_t launch_flash_bo(const Model* dm, const BulkView& b, int block, cudaStream_t s);
 cudaError_t launch_krpc_rock(const Model* dm, const BulkView& b, int block, cudaStream_t s);

@@ -160,8 +160,8 @@ def test_batched_variant_against_reference(gpu_lib):
 
 
 @pytest.mark.parametrize("name", ["comp6_8x8x3", "comp8_6x6x4"])
-@pytest.mark.parametrize("budget", [0, 3, None])
-def test_batched_variant_matches_plain(gpu_lib, name, budget):
+@pytest.mark.parametrize("budget,coop_cells", [(0, None), (3, None), (None, None), (None, 8), (None, 0)])
+def test_batched_variant_matches_plain(gpu_lib, name, budget, coop_cells):
     """The batched flash (cost order, work budget, warp-cooperative phase
     equilibrium for the deferred cells) is bit-identical to the plain one.
     Budget 0 sends every cell that needs an equilibrium through the
@@ -175,6 +175,8 @@ def test_batched_variant_matches_plain(gpu_lib, name, budget):
         with ctx:
             if variant == 1 and budget is not None:
                 ctx.set_param("flash_budget", budget)
+            if variant == 1 and coop_cells is not None:
+                ctx.set_param("coop_cells", coop_cells)
             got = []
             for it in its:
                 ctx.load_state(P.jac_state(fx, it))

@@ -358,7 +358,9 @@ def flash_stress(args, rt, local):
         pe = ctx.get("PHASE_EXIST").reshape(-1, 3)
         out[variant] = dict(ms=statistics.median(times), two_phase=int(np.sum((pe[:, 0] != 0) & (pe[:, 1] != 0))),
                             iters=ctx.get("FLASH_ITERS").reshape(-1, 5),
-                            deferred=ctx.get_param("deferred") if variant == 1 else 0)
+                            deferred=ctx.get_param("deferred") if variant == 1 else 0,
+                            predeferred=ctx.get_param("predeferred") if variant == 1 else 0,
+                            level=ctx.get_param("level") if variant == 1 else 0)
         ctx.close()
     it = out[0]["iters"].sum(axis=1)
     line = {"metric": FS_METRIC, "value": FS_CELLS / (out[1]["ms"] * 1e-3), "unit": "cells/s", "n_gpus": 1,
@@ -370,7 +372,8 @@ def flash_stress(args, rt, local):
             "batched_over_plain": out[0]["ms"] / out[1]["ms"], "two_phase_cells": out[0]["two_phase"],
             "iterations_per_cell": {"mean": float(it.mean()), "p99": float(np.percentile(it, 99)),
                                     "max": int(it.max())},
-            "deferred_cells": out[1]["deferred"], "autotune": out.get("autotune"), "setup_s": t_setup,
+            "deferred_cells": out[1]["deferred"], "predeferred_cells": out[1]["predeferred"],
+            "level": out[1]["level"], "autotune": out.get("autotune"), "setup_s": t_setup,
             "timing": "flash stage, CUDA events on the library stream"}
     return line
 
@@ -402,24 +405,19 @@ def large_step(args, rt, local):
                            conv_darcy=synthetic.METRIC["CONV_DARCY"])
     model = synthetic.comp_model(LG_NCOMP, LG_SEED)
     out = {}
-    stages = ("check", "flash", "krpc_rock", "report", "flux", "residual", "jac_conn", "jac_rows")
+    flush = (rt.malloc(512 << 20), 512 << 20)
     for variant in (0, 1):
         t0 = time.perf_counter()
         ctx = FimContext(model, grid, device=local, variant=variant)
         synthetic.ptn_workload(ctx, grid, LG_NCOMP, LG_SEED, dt=DT, dsmax=DSMAX)
         ctx.checkpoint(0)
         print(f"large: variant {variant} set up in {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
-        times = []
-        for kk in range(args.warmup + args.steps):
-            ctx.checkpoint(0, restore=True)
-            ctx.profile(True)
-            ctx.enqueue_step(DT)
-            ctx.step_report()
-            prof = ctx.profile_read()
-            ctx.profile(False)
-            if kk >= args.warmup:
-                times.append(sum(prof[st][0] for st in stages))
-        out[variant] = dict(ms=statistics.median(times), stages={st: round(v[0], 3) for st, v in prof.items() if v[1]})
+        times, _ = time_device(ctx, rt, args.steps, args.warmup, flush)
+        prof = stage_profile(ctx, rt, flush, reps=1)
+        out[variant] = dict(ms=statistics.median(times), stages={st: round(v[0], 3) for st, v in prof.items()},
+                            deferred=ctx.get_param("deferred") if variant == 1 else 0,
+                            predeferred=ctx.get_param("predeferred") if variant == 1 else 0,
+                            level=ctx.get_param("level") if variant == 1 else 0)
         print(f"large: variant {variant} step {out[variant]['ms']:.1f} ms", file=sys.stderr, flush=True)
         ctx.close()
     return {"metric": LG_METRIC, "value": n / (out[1]["ms"] * 1e-3), "unit": "cells/s", "n_gpus": 1,
@@ -430,8 +428,10 @@ def large_step(args, rt, local):
                        "connections": int(grid.nconn)},
             "plain_value": n / (out[0]["ms"] * 1e-3), "plain_ms": out[0]["ms"],
             "batched_over_plain": out[0]["ms"] / out[1]["ms"], "stages_ms": out[1]["stages"],
-            "plain_stages_ms": out[0]["stages"],
-            "timing": "sum of the step's stage times, CUDA events on the library stream (library defaults)"}
+            "plain_stages_ms": out[0]["stages"], "deferred_cells": out[1]["deferred"],
+            "predeferred_cells": out[1]["predeferred"], "level": out[1]["level"],
+            "timing": "CUDA events on the library stream around the step (the batched form's graph), "
+                      "L2 flushed between steps; stage times from one eager profiled step (library defaults)"}
 
 
 class Ranks:
@@ -566,6 +566,7 @@ def main():
             "roofline": roof, "roofline_assembly": roof_asm, "fp64_peak_tflops": fp64,
             "batched": {"flash_budget": ctx1.get_param("flash_budget"), "coop_blocks": ctx1.get_param("coop_blocks"),
                         "deferred_cells": ctx1.get_param("deferred"),
+                        "predeferred_cells": ctx1.get_param("predeferred"), "level": ctx1.get_param("level"),
                         "block_cell": ctx1.get_param("block_cell"), "predefer": ctx1.get_param("predefer"),
                         "coop_cells": ctx1.get_param("coop_cells"),
                         "autotune": None if tuned is None else {k: v for k, v in tuned.items() if k != "trials"}},

@@ -222,19 +222,27 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *                 units go to the cooperative kernel at once, on a second
  *                 stream, while the per-cell kernel runs (default 96);
  *                 0: only cells that exceed the budget now are deferred;
- *   COOP_CELLS    adaptive floor of both thresholds: about this many of the
- *                 cells with the largest predicted work may go to the
- *                 cooperative kernel (default 1216, two per warp slot); on a
- *                 workload where every cell is expensive the per-cell kernel
- *                 keeps almost all of them.  0: the thresholds are the two
- *                 parameters above only. */
+ *   COOP_CELLS    adaptive floor of both thresholds, active only when
+ *                 more than this many cells are predicted above the
+ *                 pre-deferral threshold (the budget when PREDEFER is 0):
+ *                 then about this many of the cells with the largest
+ *                 predicted work go to the cooperative kernel and the
+ *                 per-cell kernel keeps the rest (default 1216, two per warp
+ *                 slot).  0: the thresholds are the two parameters above
+ *                 only;
+ *   PREDEFERRED   (read only) cells of DEFERRED that were pre-deferred;
+ *   LEVEL         (read only) the adaptive work level of the last batched
+ *                 flash (0: no floor; else the budget was at least
+ *                 2^(LEVEL/4) work units). */
 typedef enum ocpx_param {
     OCPX_PARAM_FLASH_BUDGET = 0,
     OCPX_PARAM_COOP_BLOCKS = 1,
     OCPX_PARAM_BLOCK_CELL = 2,
     OCPX_PARAM_DEFERRED = 3,
     OCPX_PARAM_PREDEFER = 4,
-    OCPX_PARAM_COOP_CELLS = 5
+    OCPX_PARAM_COOP_CELLS = 5,
+    OCPX_PARAM_PREDEFERRED = 6,
+    OCPX_PARAM_LEVEL = 7
 } ocpx_param;
 ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value);
 ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value);
@@ -259,9 +267,9 @@ ocpx_status ocpx_step_report(ocpx_ctx* ctx, ocpx_report* rep);
  * 4 connection flux, 5 residual + norms, 6 Jacobian connection blocks,
  * 7 Jacobian rows, 8 Newton update; inside stage 1 of the batched form:
  * 9 pre-deferral and cost order, 10 budgeted per-cell flash, 11 cooperative
- * equilibrium of the pre-deferred cells (second stream, concurrent with 10),
- * 12 properties of all deferred cells, 13 cooperative equilibrium of the
- * cells deferred by 10.  ocpx_profile_read synchronizes and returns, per
+ * equilibrium and properties of the pre-deferred cells (second stream,
+ * concurrent with 10), 12 properties of the cells deferred by 10,
+ * 13 cooperative equilibrium of the cells deferred by 10.  ocpx_profile_read synchronizes and returns, per
  * stage, the summed milliseconds and the number of timed launches since
  * profiling was enabled. */
 #define OCPX_STAGE_COUNT 14

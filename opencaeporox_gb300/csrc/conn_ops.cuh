@@ -120,101 +120,141 @@ OCPX_HD void cell_residual(const BulkView& b, const ConnView& cv, int n, double 
 // OCPConvection01::AssembleMatFIM for one connection followed by the two
 // DaABpbC products: bmat = dt * (dFdXp + dFdXs * dSec_dPri[side cell]).
 // Writes bmatB (side 0) and bmatE (side 1), each ncol x ncol row-major.
+//
+// The reference fills the dense ncol x ncol2 matrix dFdXs and multiplies it
+// by dSec_dPri with dgemm.  Its rows have a fixed structure: phase j adds
+// x_ij * v_j to row i + 1 (component i), where the row vector v_j does not
+// depend on i, plus one diagonal entry transJ*xi*dP in the upwind side's
+// column of (j, i).  So
+//   (dFdXs * dSec)[i+1] = sum_j x_ij * (v_j * dSec) + sum_j e_j * dSec[np+j*nc+i]
+// and only np vectors W_j = v_j * dSec of length ncol are formed per side,
+// from the np saturation rows and the nc composition rows of phase j.  Each
+// entry is the same sum of products as the reference's, grouped by phase
+// (rounding differs from dgemm's, as any dgemm blocking does).  Everything
+// stays in registers.  Column 0 of dFdXp is accumulated phase by phase with
+// the reference's operations.  In the compositional model the rows of
+// dSec_dPri for the water phase's composition are identically zero (the
+// water composition is fixed, CaldXsdXpW), so they are skipped.
 template <int NCT>
 OCPX_HD void conn_jac_blocks(const Model& M, const BulkView& b, const ConnView& cv, int c, double dt,
                              double* bmatB, double* bmatE)
 {
     const int np = b.np, nc = b.nc, nconn = cv.nconn;
-    const int ncol = nc + 1, ncol2 = np * nc + np;
-    constexpr int NCOL = NCT + 1, NCOL2 = NP * NCT + NP;
-    double dFdXpB[NCOL], dFdXpE[NCOL];         // column 0 only (rows 0..ncol-1)
-    double dFdXsB[NCOL * NCOL2], dFdXsE[NCOL * NCOL2];
-    for (int r = 0; r < ncol; r++) { dFdXpB[r] = 0; dFdXpE[r] = 0; }
-    for (int k = 0; k < ncol * ncol2; k++) { dFdXsB[k] = 0; dFdXsE[k] = 0; }
+    const int ncol = nc + 1;
+    constexpr int NCOL = NCT + 1;
+    const size_t nb = (size_t)b.nb;
     const int bId = (int)cv.bId[c], eId = (int)cv.eId[c];
     const double Akd = cv.trans[c];
     const double dGamma = M.units.gravity_factor * (b.depth[bId] - b.depth[eId]);
-    for (int j = 0; j < np; j++) {
-        const int u = (int)cv.upblock[j * nconn + c];
-        if (!b.phaseExist[b.idx(j, u)]) continue;
-        const bool up_is_b = (u == bId);
-        const int d = up_is_b ? eId : bId;
+    const int jcomp_end = (M.mixture == 1) ? np - 1 : np;  // phases whose composition rows of dSec are nonzero
+
+    // per-phase scalars of the connection
+    int up[NP];
+    bool act[NP];
+    double transJ[NP], xiU[NP], dPj[NP], muU[NP], wU[NP], wD[NP], muP[NP], xiP[NP], rhoPu[NP], rhoPd[NP];
+#pragma unroll
+    for (int j = 0; j < NP; j++) {
+        const int u = j < np ? (int)cv.upblock[j * nconn + c] : bId;
+        up[j] = u;
+        act[j] = j < np && b.phaseExist[b.idx(j, u)] != 0;
+        transJ[j] = 0; xiU[j] = 0; dPj[j] = 0; muU[j] = 1; wU[j] = 0; wD[j] = 0;
+        muP[j] = 0; xiP[j] = 0; rhoPu[j] = 0; rhoPd[j] = 0;
+        if (!act[j]) continue;
+        const int d = (u == bId) ? eId : bId;
         const bool exD = b.phaseExist[b.idx(j, d)] != 0;
-        double* dFdXpU = up_is_b ? dFdXpB : dFdXpE;
-        double* dFdXpD = up_is_b ? dFdXpE : dFdXpB;
-        double* dFdXsU = up_is_b ? dFdXsB : dFdXsE;
-        double* dFdXsD = up_is_b ? dFdXsE : dFdXsB;
-        const double rhoWghtU = exD ? 0.5 : 1;
-        const double rhoWghtD = exD ? 0.5 : 0;
-        const double dP = cv.dP[j * nconn + c];
-        const double xi = b.xi[b.idx(j, u)];
-        const double kr = b.kr[b.idx(j, u)];
-        const double mu = b.mu[b.idx(j, u)];
-        const double muP = b.muP[b.idx(j, u)];
-        const double xiP = b.xiP[b.idx(j, u)];
-        const double rhoPu = b.rhoP[b.idx(j, u)];
-        const double rhoPd = b.rhoP[b.idx(j, d)];
-        const double transJ = Akd * kr / mu;
-        for (int i = 0; i < nc; i++) {
-            const double xij = b.xij[b.idx(j * nc + i, u)];
-            const double transIJ = xij * xi * transJ;
-            dFdXpB[i + 1] += transIJ;
-            dFdXpE[i + 1] -= transIJ;
-            double tmp = transJ * xiP * xij * dP;
-            tmp += -transIJ * muP / mu * dP;
-            dFdXpU[i + 1] += (tmp - transIJ * rhoWghtU * rhoPu * dGamma);
-            dFdXpD[i + 1] += -transIJ * rhoWghtD * rhoPd * dGamma;
-            double* rowB = dFdXsB + (i + 1) * ncol2;
-            double* rowE = dFdXsE + (i + 1) * ncol2;
-            double* rowU = dFdXsU + (i + 1) * ncol2;
-            double* rowD = dFdXsD + (i + 1) * ncol2;
-            for (int k = 0; k < np; k++) {
-                rowB[k] += transIJ * b.dPcdS[b.idx(j * np + k, bId)];
-                rowE[k] -= transIJ * b.dPcdS[b.idx(j * np + k, eId)];
-                rowU[k] += Akd * b.dKrdS[b.idx(j * np + k, u)] / mu * xi * xij * dP;
-            }
-            for (int k = 0; k < nc; k++) {
-                const double rhox = b.rhox[b.idx(j * nc + k, u)];
-                const double xix = b.xix[b.idx(j * nc + k, u)];
-                const double mux = b.mux[b.idx(j * nc + k, u)];
-                double t2 = -transIJ * rhoWghtU * rhox * dGamma;
-                t2 += transJ * xix * xij * dP;
-                t2 += -transIJ * mux / mu * dP;
-                rowU[np + j * nc + k] += t2;
-                rowD[np + j * nc + k] += -transIJ * rhoWghtD * b.rhox[b.idx(j * nc + k, d)] * dGamma;
-            }
-            rowU[np + j * nc + i] += transJ * xi * dP;
-        }
+        wU[j] = exD ? 0.5 : 1;
+        wD[j] = exD ? 0.5 : 0;
+        dPj[j] = cv.dP[j * nconn + c];
+        xiU[j] = b.xi[b.idx(j, u)];
+        muU[j] = b.mu[b.idx(j, u)];
+        transJ[j] = Akd * b.kr[b.idx(j, u)] / muU[j];
+        muP[j] = b.muP[b.idx(j, u)];
+        xiP[j] = b.xiP[b.idx(j, u)];
+        rhoPu[j] = b.rhoP[b.idx(j, u)];
+        rhoPd[j] = b.rhoP[b.idx(j, d)];
     }
-    // bmat = dt * (dFdXs * dSec) + dt * dFdXp.  The reference forms the product
-    // with BLAS dgemm (DaABpbC, src/DenseMat.cpp:61-85), whose rounding is
-    // that of fused multiply-adds in some order; here: fused multiply-adds in
-    // column order.  In the compositional model the rows of dSec_dPri for the
-    // water phase's composition are identically zero (the water composition
-    // is fixed, CaldXsdXpW), so their columns of dFdXs are skipped.
-    const int kend = (M.mixture == 1) ? np + (np - 1) * nc : ncol2;
+
     for (int side = 0; side < 2; side++) {
-        const double* Xs = side == 0 ? dFdXsB : dFdXsE;
-        const double* Xp = side == 0 ? dFdXpB : dFdXpE;
         const int cell = side == 0 ? bId : eId;
+        const double sgn = side == 0 ? 1.0 : -1.0;
         double* out = side == 0 ? bmatB : bmatE;
-        for (int col = 0; col < ncol; col++) out[col] = dt * 0.0 + dt * (col == 0 ? Xp[0] : 0.0);
-        for (int r = 1; r < ncol; r++) {
+        const double* ds = b.dSec_dPri + cell;  // ds[(k * ncol + col) * nb]
+        double W[NP][NCOL];
+#pragma unroll
+        for (int j = 0; j < NP; j++) {
+#pragma unroll
+            for (int col = 0; col < NCOL; col++) W[j][col] = 0;
+            if (!act[j]) continue;
+            const int u = up[j];
+            const bool isU = (u == cell);
+            const double xt = xiU[j] * transJ[j];
+            // saturation columns: sgn*xi*transJ*dPcdS(side cell) [+ Akd*dKrdS(U)/mu*xi*dP on the upwind side]
+            for (int k = 0; k < np; k++) {
+                double a = sgn * xt * b.dPcdS[b.idx(j * np + k, cell)];
+                if (isU) a += Akd * b.dKrdS[b.idx(j * np + k, u)] / muU[j] * xiU[j] * dPj[j];
+#pragma unroll
+                for (int col = 0; col < NCOL; col++)
+                    if (col < ncol) W[j][col] = fma(a, ds[(size_t)(k * ncol + col) * nb], W[j][col]);
+            }
+            if (j >= jcomp_end) continue;
+            // composition columns of phase j
+            for (int m = 0; m < nc; m++) {
+                double g;
+                if (isU) {
+                    const double rhox = b.rhox[b.idx(j * nc + m, u)];
+                    const double xix = b.xix[b.idx(j * nc + m, u)];
+                    const double mux = b.mux[b.idx(j * nc + m, u)];
+                    g = -xt * wU[j] * rhox * dGamma;
+                    g += transJ[j] * xix * dPj[j];
+                    g += -xt * mux / muU[j] * dPj[j];
+                }
+                else {
+                    if (wD[j] == 0) continue;
+                    g = -xt * wD[j] * b.rhox[b.idx(j * nc + m, cell)] * dGamma;
+                }
+                const int k = np + j * nc + m;
+#pragma unroll
+                for (int col = 0; col < NCOL; col++)
+                    if (col < ncol) W[j][col] = fma(g, ds[(size_t)(k * ncol + col) * nb], W[j][col]);
+            }
+        }
+        // row 0 has no flux term: dt * 0 + dt * 0
+        for (int col = 0; col < ncol; col++) out[col] = dt * 0.0 + dt * 0.0;
+        for (int i = 0; i < nc; i++) {
             double acc[NCOL];
 #pragma unroll
             for (int col = 0; col < NCOL; col++) acc[col] = 0;
-            for (int k = 0; k < kend; k++) {
-                const double x = Xs[r * ncol2 + k];
-                const double* ds = b.dSec_dPri + (size_t)(k * ncol) * b.nb + cell;
+            double xp = 0;  // dFdXp[i + 1][0] of this side
+#pragma unroll
+            for (int j = 0; j < NP; j++) {
+                if (!act[j]) continue;
+                const double xij = b.xij[b.idx(j * nc + i, up[j])];
+                const double transIJ = xij * xiU[j] * transJ[j];
+                xp += sgn * transIJ;
+                if (up[j] == cell) {
+                    double tmp = transJ[j] * xiP[j] * xij * dPj[j];
+                    tmp += -transIJ * muP[j] / muU[j] * dPj[j];
+                    xp += (tmp - transIJ * wU[j] * rhoPu[j] * dGamma);
+                }
+                else {
+                    xp += -transIJ * wD[j] * rhoPd[j] * dGamma;
+                }
 #pragma unroll
                 for (int col = 0; col < NCOL; col++)
-                    if (col < ncol) acc[col] = fma(x, ds[(size_t)col * b.nb], acc[col]);
+                    if (col < ncol) acc[col] = fma(xij, W[j][col], acc[col]);
+                if (up[j] == cell && j < jcomp_end) {
+                    const double e = transJ[j] * xiU[j] * dPj[j];
+                    const int k = np + j * nc + i;
+#pragma unroll
+                    for (int col = 0; col < NCOL; col++)
+                        if (col < ncol) acc[col] = fma(e, ds[(size_t)(k * ncol + col) * nb], acc[col]);
+                }
             }
 #pragma unroll
             for (int col = 0; col < NCOL; col++) {
                 if (col >= ncol) break;
-                const double cv0 = (col == 0) ? Xp[r] : 0.0;
-                out[r * ncol + col] = dt * acc[col] + dt * cv0;
+                const double cv0 = (col == 0) ? xp : 0.0;
+                out[(i + 1) * ncol + col] = dt * acc[col] + dt * cv0;
             }
         }
     }

@@ -231,11 +231,13 @@ __global__ void k_cost_hist(BulkView b, unsigned* __restrict__ hist)
 }
 
 // Exclusive scan of the bucket counts, in place (one block of COST_BUCKETS
-// threads).  Also the adaptive work level: the lowest level L such that at
-// most coop_cells cells have a predicted level >= L (0 when coop_cells is 0),
-// written to level[0].  The cooperative kernel then gets about that many
-// cells whatever the workload's mean work.
-__global__ void k_cost_scan(unsigned* __restrict__ hist, unsigned coop_cells, int* __restrict__ level)
+// threads).  Also the adaptive work level, written to level[0].  It is 0 (no
+// floor) unless more than coop_cells cells lie at or above the level of the
+// deferral threshold `wt`; then it is the lowest level L such that at most
+// coop_cells cells have a predicted level >= L.  The cooperative kernel then
+// gets about that many cells even when most cells of the workload are
+// expensive, and is left alone when only a tail of cells is.
+__global__ void k_cost_scan(unsigned* __restrict__ hist, unsigned coop_cells, long long wt, int* __restrict__ level)
 {
     __shared__ unsigned v[COST_BUCKETS];
     const int t = threadIdx.x;
@@ -243,7 +245,11 @@ __global__ void k_cost_scan(unsigned* __restrict__ hist, unsigned coop_cells, in
     __syncthreads();
     if (t == 0) {
         int L = 0;
-        if (coop_cells) {
+        unsigned above = 0;
+        if (coop_cells)
+            for (int l = 63; l >= cost_level(wt + 1); l--)
+                for (int cls = 0; cls < COST_BUCKETS / 64; cls++) above += v[cls * 64 + (63 - l)];
+        if (above > coop_cells) {
             unsigned cum = 0;
             L = 64;
             for (int l = 63; l >= 0; l--) {
@@ -274,15 +280,15 @@ __global__ void k_cost_scatter(BulkView b, unsigned* __restrict__ offs, int* __r
     order[pos] = cell;
 }
 
-cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, unsigned coop_cells, int* level,
-                              cudaStream_t s)
+cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, unsigned coop_cells, long long wt,
+                              int* level, cudaStream_t s)
 {
     if (!b.nb) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned) * COST_BUCKETS, s);
     if (e != cudaSuccess) return e;
     const int block = 256;
     k_cost_hist<<<grid_for(b.nb, block), block, 0, s>>>(b, hist);
-    k_cost_scan<<<1, COST_BUCKETS, 0, s>>>(hist, coop_cells, level);
+    k_cost_scan<<<1, COST_BUCKETS, 0, s>>>(hist, coop_cells, wt, level);
     k_cost_scatter<<<grid_for(b.nb, block), block, 0, s>>>(b, hist, order);
     return cudaGetLastError();
 }

@@ -42,19 +42,28 @@ __global__ void __launch_bounds__(128) k_flash_budget(const Model* __restrict__ 
 }
 
 // Step 2: the phase equilibrium of every deferred cell on a whole warp
-// (flash_coop.cuh).  Persistent: warp w takes deferred slots w, w + W, ...
+// (flash_coop.cuh).  Persistent: each warp takes the next list slot from the
+// counter `next` (zero before the launch) until the list is exhausted, so a
+// warp that drew a short cell moves on at once; the list is roughly
+// heaviest first, so the long cells start first.
 template <int NCM>
 __global__ void __launch_bounds__(COOP_WARPS * 32) k_flash_pe_coop(const Model* __restrict__ M, BulkView b,
                                                                    const DeferRec* __restrict__ rec,
                                                                    const unsigned* __restrict__ count, int cap,
+                                                                   unsigned* __restrict__ next,
                                                                    PERes* __restrict__ out)
 {
     __shared__ CoopSh<NCM> sh[COOP_WARPS];
-    const int warp = threadIdx.x >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned n = min(*count, (unsigned)cap);
-    for (unsigned slot = blockIdx.x * COOP_WARPS + warp; slot < n; slot += gridDim.x * COOP_WARPS) {
+    for (;;) {
+        unsigned slot = 0;
+        if (lane == 0) slot = atomicAdd(next, 1u);
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (slot >= n) break;
         CoopPE<NCM> pe(sh[warp], M->comp);
         pe.run(*M, b, rec[slot], out[slot]);
+        __syncwarp();
     }
 }
 
@@ -96,11 +105,27 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
         break;
     }
     case 1:
-        k_flash_pe_coop<OCPX_NCM><<<fb.coop_blocks, COOP_WARPS * 32, 0, s>>>(dm, b, fb.rec, fb.count, fb.cap, fb.pe);
-        break;
-    default:
-        k_flash_post<OCPX_NCM><<<(fb.cap + 127) / 128, 128, 0, s>>>(dm, b, fb.rec, fb.count, fb.cap, fb.pe);
-        break;
+    default: {
+        // parts 1 and 2 carry their own launch priority, which a stream
+        // capture keeps in the graph's kernel node
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributePriority;
+        attr[0].val.priority = fb.prio;
+        cudaLaunchConfig_t cfg = {};
+        cfg.stream = s;
+        cfg.attrs = attr;
+        cfg.numAttrs = fb.prio ? 1 : 0;
+        if (part == 1) {
+            cfg.gridDim = dim3(fb.coop_blocks);
+            cfg.blockDim = dim3(COOP_WARPS * 32);
+            return cudaLaunchKernelEx(&cfg, k_flash_pe_coop<OCPX_NCM>, dm, b, (const DeferRec*)fb.rec,
+                                      (const unsigned*)fb.count, fb.cap, fb.count + 2, fb.pe);
+        }
+        cfg.gridDim = dim3((fb.cap + 127) / 128);
+        cfg.blockDim = dim3(128);
+        return cudaLaunchKernelEx(&cfg, k_flash_post<OCPX_NCM>, dm, b, (const DeferRec*)fb.rec,
+                                  (const unsigned*)fb.count, fb.cap, (const PERes*)fb.pe);
+    }
     }
     return cudaGetLastError();
 }

@@ -124,6 +124,7 @@ struct ocpx_ctx {
     long long coop_cells = 1216;       // target cells per cooperative pass (adaptive level; 0: off)
     int* adapt_level = nullptr;        // device: adaptive work level of the last cost order
     cudaStream_t stream2 = nullptr;    // high-priority stream of the pre-deferred cooperative kernel
+    int prio_hi = 0;                   // greatest stream priority of the device
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double* u = nullptr;            // Newton update staging
     double* bmat = nullptr;         // per-connection Jacobian blocks (2 per connection)
@@ -391,6 +392,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     {
         int lo = 0, hi = 0;
         cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        ctx->prio_hi = hi;
         if (cudaStreamCreateWithPriority(&ctx->stream2, cudaStreamNonBlocking, hi) != cudaSuccess ||
             cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)
@@ -513,10 +515,11 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             // once, on a second (high-priority) stream, concurrently with the
             // per-cell kernel; cells that turn out expensive now follow after it
             const bool pre = ctx->predefer > 0;
-            OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned) * 2, s));
+            // list counts [0] late, [1] pre-deferred; [2], [3] the cooperative kernels' next-slot counters
+            OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned) * 4, s));
             mk = ctx->stage_begin(9);
             OCPX_CUDA(launch_cost_order(ctx->b, ctx->cost_hist, ctx->order, (unsigned)ctx->coop_cells,
-                                        ctx->adapt_level, s));
+                                        pre ? ctx->predefer : (long long)ctx->flash_budget, ctx->adapt_level, s));
             ctx->launches += 3;
             if (pre) {
                 const DeferSink sinkA{ctx->pre_rec, ctx->defer_count + 1, ctx->defer_cap};
@@ -526,18 +529,22 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             }
             ctx->stage_end(mk);
             const FlashBatch fbA{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
-                                 ctx->pre_rec, ctx->defer_count + 1, ctx->pre_res, nullptr, nullptr};
+                                 ctx->pre_rec, ctx->defer_count + 1, ctx->pre_res, nullptr, nullptr, ctx->prio_hi};
             const FlashBatch fbB{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
                                  ctx->defer_rec, ctx->defer_count, ctx->pe_res, pre ? ctx->pre_flag : nullptr,
-                                 ctx->adapt_level};
+                                 ctx->adapt_level, 0};
             if (pre) {
+                // the pre-deferred cells' equilibrium and FlashDer on the second
+                // stream; the per-cell kernel skips them, so nothing else
+                // touches their state until the join
                 OCPX_CUDA(cudaEventRecord(ctx->ev_fork, s));
                 OCPX_CUDA(cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
                 mk = ctx->stage_begin(11, ctx->stream2);
                 OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbA, 1, ctx->stream2));
+                OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbA, 2, ctx->stream2));
                 ctx->stage_end(mk);
                 OCPX_CUDA(cudaEventRecord(ctx->ev_join, ctx->stream2));
-                ctx->launches++;
+                ctx->launches += 2;
             }
             mk = ctx->stage_begin(10);
             OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbB, 0, s));
@@ -546,15 +553,11 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbB, 1, s));
             ctx->stage_end(mk);
             ctx->launches += 2;
-            if (pre) OCPX_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
             mk = ctx->stage_begin(12);
-            if (pre) {
-                OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbA, 2, s));
-                ctx->launches++;
-            }
             OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbB, 2, s));
             ctx->launches++;
             ctx->stage_end(mk);
+            if (pre) OCPX_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
         }
         else {
             OCPX_CUDA(launch_flash_comp(ctx->ncm, ctx->d_model, ctx->b, ctx->block_cell, s));
@@ -879,6 +882,20 @@ ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value)
         OCPX_CUDA(cudaMemcpyAsync(n, ctx->defer_count, sizeof(n), cudaMemcpyDeviceToHost, ctx->stream));
         OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
         *value = (long long)std::min(n[0], (unsigned)ctx->defer_cap) + std::min(n[1], (unsigned)ctx->defer_cap);
+        return OCPX_OK;
+    }
+    case OCPX_PARAM_PREDEFERRED: {
+        unsigned n = 0;
+        OCPX_CUDA(cudaMemcpyAsync(&n, ctx->defer_count + 1, sizeof(n), cudaMemcpyDeviceToHost, ctx->stream));
+        OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+        *value = (long long)std::min(n, (unsigned)ctx->defer_cap);
+        return OCPX_OK;
+    }
+    case OCPX_PARAM_LEVEL: {
+        int L = 0;
+        OCPX_CUDA(cudaMemcpyAsync(&L, ctx->adapt_level, sizeof(L), cudaMemcpyDeviceToHost, ctx->stream));
+        OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+        *value = L;
         return OCPX_OK;
     }
     default:

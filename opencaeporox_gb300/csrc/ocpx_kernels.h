@@ -27,6 +27,7 @@ struct FlashBatch {
     PERes* pe;
     const uint8_t* pre;  // cells pre-deferred to another list (skipped by part 0), may be NULL
     const int* level;    // adaptive work level: the budget is at least its work units, may be NULL
+    int prio;            // launch priority of parts 1 and 2 (CUDA stream-priority scale), 0 = the stream's
 };
 // part 0: budgeted thread-per-cell flash, 1: cooperative equilibrium, 2: finish deferred cells
 cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, const int* order,
@@ -35,9 +36,10 @@ cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, co
 // a group, in descending order of the work their last flash needed, by a
 // counting sort over COST_BUCKETS buckets.
 constexpr int COST_BUCKETS = 256;
-// level[0] receives the adaptive work level (see k_cost_scan)
-cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, unsigned coop_cells, int* level,
-                              cudaStream_t s);
+// level[0] receives the adaptive work level (see k_cost_scan); wt is the
+// deferral threshold in work units
+cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, unsigned coop_cells, long long wt,
+                              int* level, cudaStream_t s);
 // hand the cells whose last flash used more than `threshold` work units, at or
 // above the adaptive level, to the cooperative kernel up front (pre[cell] = 1),
 // visiting cells in `order`

@@ -233,7 +233,11 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *   PREDEFERRED   (read only) cells of DEFERRED that were pre-deferred;
  *   LEVEL         (read only) the adaptive work level of the last batched
  *                 flash (0: no floor; else the budget was at least
- *                 2^(LEVEL/4) work units). */
+ *                 2^(LEVEL/4) work units);
+ *   PRE_BLOCKS    > 0: the pre-deferred cells run on this many SM-exclusive
+ *                 blocks (one warp per SM sub-partition, no other block on
+ *                 the SM while they run) instead of COOP_BLOCKS blocks that
+ *                 share SMs with the per-cell kernel (default 0). */
 typedef enum ocpx_param {
     OCPX_PARAM_FLASH_BUDGET = 0,
     OCPX_PARAM_COOP_BLOCKS = 1,
@@ -242,7 +246,8 @@ typedef enum ocpx_param {
     OCPX_PARAM_PREDEFER = 4,
     OCPX_PARAM_COOP_CELLS = 5,
     OCPX_PARAM_PREDEFERRED = 6,
-    OCPX_PARAM_LEVEL = 7
+    OCPX_PARAM_LEVEL = 7,
+    OCPX_PARAM_PRE_BLOCKS = 8
 } ocpx_param;
 ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value);
 ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value);

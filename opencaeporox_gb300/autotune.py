@@ -8,7 +8,8 @@ the GPU, never the results:
 - the pre-deferral threshold (cells that were expensive in their last flash
   go there at once, concurrently with the per-cell kernel);
 - the adaptive cap on how many cells the cooperative kernel gets;
-- the number of blocks of that kernel;
+- the number of blocks of that kernel, and whether the pre-deferred cells
+  run on SM-exclusive blocks instead (and how many);
 - the block size of the per-cell kernels.
 
 The tuner times whole Newton iterations as they run in production: the
@@ -30,6 +31,7 @@ DEFAULT_SPACE = {
     "coop_cells": (0, 1216, 4864),
     "coop_blocks": (152, 304, 608),
     "block_cell": (64, 128),
+    "pre_blocks": (0, 38, 76),
 }
 
 

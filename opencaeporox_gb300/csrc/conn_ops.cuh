@@ -263,16 +263,26 @@ OCPX_HD void conn_jac_blocks(const Model& M, const BulkView& b, const ConnView& 
 // One block row of the Jacobian: the accumulation diagonal block
 // (BulkAccumuTerm01::CaldFdXpFIM) plus the connection blocks, in the
 // reference's order: diagonal first, then one off-diagonal block per incident
-// connection in increasing connection order.
-OCPX_HD void row_assemble(const BulkView& b, const ConnView& cv, int r, const double* bmat, const uint32_t* jac_rowptr,
-                          double* jac_val)
+// connection in increasing connection order.  One warp per row: lane `lane`
+// owns the block entries q = lane, lane + 32, ...; each entry's sum is formed
+// in the same order as a single thread would, and every load of a
+// connection block and store of a row block is contiguous across the warp.
+OCPX_HD void row_assemble_warp(const BulkView& b, const ConnView& cv, int r, const double* bmat,
+                               const uint32_t* jac_rowptr, double* jac_val, int lane)
 {
+    constexpr int QPL = ((NCT_MAX + 1) * (NCT_MAX + 1) + 31) / 32;
     const int nc = b.nc, dim = nc + 1, bsize = dim * dim;
-    double diag[(NCT_MAX + 1) * (NCT_MAX + 1)];
-    for (int k = 0; k < bsize; k++) diag[k] = 0;
-    diag[0] = b.v[r] * b.poroP[r] - b.vfP[r];
-    for (int i = 0; i < nc; i++) diag[i + 1] = -b.vfi[b.idx(i, r)];
-    for (int i = 1; i < dim; i++) diag[i * dim + i] = 1;
+    const double d0 = b.v[r] * b.poroP[r] - b.vfP[r];
+    double diag[QPL];
+#pragma unroll
+    for (int t = 0; t < QPL; t++) {
+        const int q = lane + 32 * t;
+        double x = 0;
+        if (q == 0) x = d0;
+        else if (q < dim) x = -b.vfi[b.idx(q - 1, r)];
+        else if (q < bsize && q % dim == q / dim) x = 1;
+        diag[t] = x;
+    }
     double* out = jac_val + (size_t)jac_rowptr[r] * bsize;
     int slot = 1;
     for (uint32_t k = cv.row_ptr[r]; k < cv.row_ptr[r + 1]; k++, slot++) {
@@ -283,16 +293,26 @@ OCPX_HD void row_assemble(const BulkView& b, const ConnView& cv, int r, const do
         double* off = out + (size_t)slot * bsize;
         if ((e & 1u) == 0) {
             // row is bId: AddDiag(bId, bmatB); NewOffDiag(bId, eId, bmatE)
-            for (int q = 0; q < bsize; q++) diag[q] += bB[q];
-            for (int q = 0; q < bsize; q++) off[q] = bE[q];
+#pragma unroll
+            for (int t = 0; t < QPL; t++) {
+                const int q = lane + 32 * t;
+                if (q < bsize) { diag[t] += bB[q]; off[q] = bE[q]; }
+            }
         }
         else {
             // row is eId: NewOffDiag(eId, bId, -bmatB); AddDiag(eId, -bmatE)
-            for (int q = 0; q < bsize; q++) off[q] = -1.0 * bB[q];
-            for (int q = 0; q < bsize; q++) diag[q] += -1.0 * bE[q];
+#pragma unroll
+            for (int t = 0; t < QPL; t++) {
+                const int q = lane + 32 * t;
+                if (q < bsize) { off[q] = -1.0 * bB[q]; diag[t] += -1.0 * bE[q]; }
+            }
         }
     }
-    for (int q = 0; q < bsize; q++) out[q] = diag[q];
+#pragma unroll
+    for (int t = 0; t < QPL; t++) {
+        const int q = lane + 32 * t;
+        if (q < bsize) out[q] = diag[t];
+    }
 }
 
 }  // namespace ocpx

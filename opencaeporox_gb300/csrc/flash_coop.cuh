@@ -28,6 +28,7 @@ namespace ocpx {
 
 constexpr unsigned FULL_MASK = 0xffffffffu;
 constexpr int COOP_WARPS = 2;  // warps (cells in flight) per block
+constexpr int EXCL_WARPS = 4;  // warps per block of the SM-exclusive form: one per SM sub-partition
 
 template <int NCM>
 struct CoopSh {

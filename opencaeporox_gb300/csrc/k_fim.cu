@@ -95,11 +95,12 @@ __global__ void __launch_bounds__(128) k_jac_conn(const Model* __restrict__ M, B
     conn_jac_blocks<NCT>(*M, b, cv, c, dt, bmat + (size_t)c * 2 * bsize, bmat + ((size_t)c * 2 + 1) * bsize);
 }
 
+// one warp per Jacobian block row
 __global__ void k_jac_rows(BulkView b, ConnView cv, const double* __restrict__ bmat, const uint32_t* __restrict__ rowptr,
                            double* __restrict__ val)
 {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < b.nb) row_assemble(b, cv, r, bmat, rowptr, val);
+    const long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (r < b.nb) row_assemble_warp(b, cv, (int)r, bmat, rowptr, val, threadIdx.x & 31);
 }
 
 // out[0]: OR of status bits, out[1]: two-phase cells, out[2]: flagged cells
@@ -193,7 +194,8 @@ cudaError_t launch_jac_conn(int nct, const Model* dm, const BulkView& b, const C
 cudaError_t launch_jac_rows(const BulkView& b, const ConnView& cv, const double* bmat, const uint32_t* rowptr,
                             double* val, int block, cudaStream_t s)
 {
-    if (b.nb) k_jac_rows<<<grid_for(b.nb, block), block, 0, s>>>(b, cv, bmat, rowptr, val);
+    const int wpb = block / 32;  // rows per block
+    if (b.nb) k_jac_rows<<<(b.nb + wpb - 1) / wpb, block, 0, s>>>(b, cv, bmat, rowptr, val);
     return cudaGetLastError();
 }
 // Work level of a predicted work w >= 1: floor(4 log2 w), at most 63 (levels

@@ -46,14 +46,21 @@ __global__ void __launch_bounds__(128) k_flash_budget(const Model* __restrict__ 
 // counter `next` (zero before the launch) until the list is exhausted, so a
 // warp that drew a short cell moves on at once; the list is roughly
 // heaviest first, so the long cells start first.
-template <int NCM>
-__global__ void __launch_bounds__(COOP_WARPS * 32) k_flash_pe_coop(const Model* __restrict__ M, BulkView b,
-                                                                   const DeferRec* __restrict__ rec,
-                                                                   const unsigned* __restrict__ count, int cap,
-                                                                   unsigned* __restrict__ next,
-                                                                   PERes* __restrict__ out)
+//
+// WARPS = COOP_WARPS: small blocks that share SMs with the other kernels of
+// the flash.  WARPS = EXCL_WARPS: one warp per SM sub-partition, launched with
+// all the shared memory a block may hold, so that no other block is placed
+// on the SM while it runs; its warps then have the FP64 pipes of their
+// sub-partitions to themselves (one warp's dependent FP64 chain issues at the
+// pipe's full rate, so the longest cells run at full speed).
+template <int NCM, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_flash_pe_coop(const Model* __restrict__ M, BulkView b,
+                                                              const DeferRec* __restrict__ rec,
+                                                              const unsigned* __restrict__ count, int cap,
+                                                              unsigned* __restrict__ next,
+                                                              PERes* __restrict__ out)
 {
-    __shared__ CoopSh<NCM> sh[COOP_WARPS];
+    __shared__ CoopSh<NCM> sh[WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned n = min(*count, (unsigned)cap);
     for (;;) {
@@ -115,10 +122,17 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
         cfg.stream = s;
         cfg.attrs = attr;
         cfg.numAttrs = fb.prio ? 1 : 0;
+        if (part == 1 && fb.excl_blocks > 0) {
+            cfg.gridDim = dim3(fb.excl_blocks);
+            cfg.blockDim = dim3(EXCL_WARPS * 32);
+            cfg.dynamicSmemBytes = fb.excl_smem;
+            return cudaLaunchKernelEx(&cfg, k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>, dm, b, (const DeferRec*)fb.rec,
+                                      (const unsigned*)fb.count, fb.cap, fb.count + 2, fb.pe);
+        }
         if (part == 1) {
             cfg.gridDim = dim3(fb.coop_blocks);
             cfg.blockDim = dim3(COOP_WARPS * 32);
-            return cudaLaunchKernelEx(&cfg, k_flash_pe_coop<OCPX_NCM>, dm, b, (const DeferRec*)fb.rec,
+            return cudaLaunchKernelEx(&cfg, k_flash_pe_coop<OCPX_NCM, COOP_WARPS>, dm, b, (const DeferRec*)fb.rec,
                                       (const unsigned*)fb.count, fb.cap, fb.count + 2, fb.pe);
         }
         cfg.gridDim = dim3((fb.cap + 127) / 128);
@@ -128,6 +142,26 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
     }
     }
     return cudaGetLastError();
+}
+
+// Once per device (that device current): the SM-exclusive cooperative kernel
+// may use all the shared memory a block can opt into; *excl_smem receives the
+// dynamic part that fills it.
+cudaError_t OCPX_CAT(setup_flash_batched_, OCPX_NCM)(int* excl_smem)
+{
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>);
+    if (e != cudaSuccess) return e;
+    const int dyn = optin > (int)fa.sharedSizeBytes ? optin - (int)fa.sharedSizeBytes : 0;
+    e = cudaFuncSetAttribute(k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+    *excl_smem = dyn;
+    return e;
 }
 
 }  // namespace ocpx

@@ -22,6 +22,11 @@ cudaError_t launch_flash_batched_6(const Model*, const BulkView&, const int*, co
 cudaError_t launch_flash_batched_8(const Model*, const BulkView&, const int*, const FlashBatch&, int, cudaStream_t);
 cudaError_t launch_flash_batched_10(const Model*, const BulkView&, const int*, const FlashBatch&, int, cudaStream_t);
 cudaError_t launch_flash_batched_12(const Model*, const BulkView&, const int*, const FlashBatch&, int, cudaStream_t);
+cudaError_t setup_flash_batched_4(int*);
+cudaError_t setup_flash_batched_6(int*);
+cudaError_t setup_flash_batched_8(int*);
+cudaError_t setup_flash_batched_10(int*);
+cudaError_t setup_flash_batched_12(int*);
 
 cudaError_t launch_flash_comp(int ncm, const Model* dm, const BulkView& b, int block, cudaStream_t s)
 {
@@ -43,6 +48,17 @@ cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, co
     case 8: return launch_flash_batched_8(dm, b, order, fb, part, s);
     case 10: return launch_flash_batched_10(dm, b, order, fb, part, s);
     case 12: return launch_flash_batched_12(dm, b, order, fb, part, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+cudaError_t setup_flash_batched(int ncm, int* excl_smem)
+{
+    switch (ncm) {
+    case 4: return setup_flash_batched_4(excl_smem);
+    case 6: return setup_flash_batched_6(excl_smem);
+    case 8: return setup_flash_batched_8(excl_smem);
+    case 10: return setup_flash_batched_10(excl_smem);
+    case 12: return setup_flash_batched_12(excl_smem);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -125,6 +141,8 @@ struct ocpx_ctx {
     int* adapt_level = nullptr;        // device: adaptive work level of the last cost order
     cudaStream_t stream2 = nullptr;    // high-priority stream of the pre-deferred cooperative kernel
     int prio_hi = 0;                   // greatest stream priority of the device
+    int pre_blocks = 0;                // SM-exclusive blocks of the pre-deferred pass (0: shared-SM blocks)
+    int excl_smem = 0;                 // their dynamic shared memory
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double* u = nullptr;            // Newton update staging
     double* bmat = nullptr;         // per-connection Jacobian blocks (2 per connection)
@@ -400,6 +418,8 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     }
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
         return fail_ctx(OCPX_CUDA_ERROR, "stream creation failed");
+    if (ctx->ncm > 0 && setup_flash_batched(ctx->ncm, &ctx->excl_smem) != cudaSuccess)
+        return fail_ctx(OCPX_CUDA_ERROR, "flash kernel set-up failed");
     if (cudaMalloc(&ctx->d_model, sizeof(Model)) != cudaSuccess) return fail_ctx(OCPX_CUDA_ERROR, "model alloc failed");
     if (cudaMallocHost(&ctx->h_flags, sizeof(uint32_t) * 4) != cudaSuccess ||
         cudaMallocHost(&ctx->h_norm, sizeof(RowNorm)) != cudaSuccess)
@@ -529,10 +549,11 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             }
             ctx->stage_end(mk);
             const FlashBatch fbA{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
-                                 ctx->pre_rec, ctx->defer_count + 1, ctx->pre_res, nullptr, nullptr, ctx->prio_hi};
+                                 ctx->pre_rec, ctx->defer_count + 1, ctx->pre_res, nullptr, nullptr, ctx->prio_hi,
+                                 ctx->pre_blocks, ctx->excl_smem};
             const FlashBatch fbB{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
                                  ctx->defer_rec, ctx->defer_count, ctx->pe_res, pre ? ctx->pre_flag : nullptr,
-                                 ctx->adapt_level, 0};
+                                 ctx->adapt_level, 0, 0, 0};
             if (pre) {
                 // the pre-deferred cells' equilibrium and FlashDer on the second
                 // stream; the per-cell kernel skips them, so nothing else
@@ -863,6 +884,10 @@ ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value)
         if (value < 0 || value > 0x7fffffffLL) return fail(OCPX_INVALID_ARG, "coop cells out of range");
         ctx->coop_cells = value;
         return OCPX_OK;
+    case OCPX_PARAM_PRE_BLOCKS:
+        if (value < 0 || value > 65535) return fail(OCPX_INVALID_ARG, "pre blocks out of range");
+        ctx->pre_blocks = (int)value;
+        return OCPX_OK;
     default:
         return fail(OCPX_INVALID_ARG, "unknown or read-only parameter");
     }
@@ -877,6 +902,7 @@ ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value)
     case OCPX_PARAM_BLOCK_CELL: *value = ctx->block_cell; return OCPX_OK;
     case OCPX_PARAM_PREDEFER: *value = ctx->predefer; return OCPX_OK;
     case OCPX_PARAM_COOP_CELLS: *value = ctx->coop_cells; return OCPX_OK;
+    case OCPX_PARAM_PRE_BLOCKS: *value = ctx->pre_blocks; return OCPX_OK;
     case OCPX_PARAM_DEFERRED: {
         unsigned n[2] = {0, 0};
         OCPX_CUDA(cudaMemcpyAsync(n, ctx->defer_count, sizeof(n), cudaMemcpyDeviceToHost, ctx->stream));

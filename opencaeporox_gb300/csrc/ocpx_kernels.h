@@ -28,7 +28,11 @@ struct FlashBatch {
     const uint8_t* pre;  // cells pre-deferred to another list (skipped by part 0), may be NULL
     const int* level;    // adaptive work level: the budget is at least its work units, may be NULL
     int prio;            // launch priority of parts 1 and 2 (CUDA stream-priority scale), 0 = the stream's
+    int excl_blocks;     // > 0: part 1 runs as this many SM-exclusive blocks (EXCL_WARPS warps each)
+    int excl_smem;       // dynamic shared memory of an SM-exclusive block (from setup_flash_batched)
 };
+// once per device: configure the SM-exclusive cooperative kernel of capacity ncm
+cudaError_t setup_flash_batched(int ncm, int* excl_smem);
 // part 0: budgeted thread-per-cell flash, 1: cooperative equilibrium, 2: finish deferred cells
 cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, const int* order,
                                  const FlashBatch& fb, int part, cudaStream_t s);

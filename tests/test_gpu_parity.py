@@ -160,12 +160,16 @@ def test_batched_variant_against_reference(gpu_lib):
 
 
 @pytest.mark.parametrize("name", ["comp6_8x8x3", "comp8_6x6x4"])
-@pytest.mark.parametrize("budget,coop_cells", [(0, None), (3, None), (None, None), (None, 8), (None, 0)])
-def test_batched_variant_matches_plain(gpu_lib, name, budget, coop_cells):
+@pytest.mark.parametrize("budget,coop_cells,predefer,pre_blocks",
+                         [(0, None, None, None), (3, None, None, None), (None, None, None, None),
+                          (None, 8, None, None), (None, 0, None, None), (None, 0, 1, 0), (None, 0, 1, 3)])
+def test_batched_variant_matches_plain(gpu_lib, name, budget, coop_cells, predefer, pre_blocks):
     """The batched flash (cost order, work budget, warp-cooperative phase
     equilibrium for the deferred cells) is bit-identical to the plain one.
     Budget 0 sends every cell that needs an equilibrium through the
-    cooperative kernel."""
+    cooperative kernel; pre-deferral threshold 1 sends the cells that needed
+    an equilibrium last time to the second stream, on shared-SM blocks or on
+    three SM-exclusive blocks."""
     fx = P.load_fixture(name)
     its = [it for it in P.iterations(fx) if "P" in P.group(fx, it + "/post")]
     outs = []
@@ -177,6 +181,10 @@ def test_batched_variant_matches_plain(gpu_lib, name, budget, coop_cells):
                 ctx.set_param("flash_budget", budget)
             if variant == 1 and coop_cells is not None:
                 ctx.set_param("coop_cells", coop_cells)
+            if variant == 1 and predefer is not None:
+                ctx.set_param("predefer", predefer)
+            if variant == 1 and pre_blocks is not None:
+                ctx.set_param("pre_blocks", pre_blocks)
             got = []
             for it in its:
                 ctx.load_state(P.jac_state(fx, it))
@@ -184,10 +192,12 @@ def test_batched_variant_matches_plain(gpu_lib, name, budget, coop_cells):
                 ctx.update_property()
                 got.append({k: ctx.get(k) for k in FLASH_OUT})
                 if variant == 1:
-                    deferred.append(ctx.get_param("deferred"))
+                    deferred.append((ctx.get_param("deferred"), ctx.get_param("predeferred")))
             outs.append(got)
     if budget == 0:
-        assert all(d > 0 for d in deferred), deferred
+        assert all(d > 0 for d, _ in deferred), deferred
+    if predefer == 1:
+        assert sum(p for _, p in deferred) > 0, deferred
     for it, a, b in zip(its, outs[0], outs[1]):
         for k in FLASH_OUT:
             assert np.array_equal(a[k], b[k], equal_nan=True), f"{name} {it} budget={budget}: {k} differs"

@@ -216,7 +216,8 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *   COOP_BLOCKS   blocks of the warp-cooperative kernel;
  *   BLOCK_CELL    threads per block of the per-cell kernels;
  *   DEFERRED      (read only) cells whose equilibrium ran on the
- *                 warp-cooperative kernel in the last batched flash;
+ *                 warp-cooperative kernel in the last batched flash
+ *                 (pre-deferred, and left over after the rounds);
  *                 reading it synchronizes the context stream;
  *   PREDEFER      cells whose last flash used more than this many work
  *                 units go to the cooperative kernel at once, on a second
@@ -237,7 +238,16 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *   PRE_BLOCKS    > 0: the pre-deferred cells run on this many SM-exclusive
  *                 blocks (one warp per SM sub-partition, no other block on
  *                 the SM while they run) instead of COOP_BLOCKS blocks that
- *                 share SMs with the per-cell kernel (default 0). */
+ *                 share SMs with the per-cell kernel (default 0);
+ *   CELL_BLOCKS   > 0: the budgeted per-cell kernel runs as this many
+ *                 persistent blocks whose warps take 32 cells at a time in
+ *                 cost order (fewer resident warps, dynamic balance);
+ *                 0: one thread per cell (default);
+ *   ROUNDS        re-budgeting rounds (0..8, default 0): the cells over the
+ *                 budget are rerun one thread per cell, compacted, with the
+ *                 budget multiplied by ROUND_GROWTH per round, before the
+ *                 cells left over go to the cooperative kernel;
+ *   ROUND_GROWTH  budget factor per round (2..64, default 4). */
 typedef enum ocpx_param {
     OCPX_PARAM_FLASH_BUDGET = 0,
     OCPX_PARAM_COOP_BLOCKS = 1,
@@ -247,7 +257,10 @@ typedef enum ocpx_param {
     OCPX_PARAM_COOP_CELLS = 5,
     OCPX_PARAM_PREDEFERRED = 6,
     OCPX_PARAM_LEVEL = 7,
-    OCPX_PARAM_PRE_BLOCKS = 8
+    OCPX_PARAM_PRE_BLOCKS = 8,
+    OCPX_PARAM_CELL_BLOCKS = 9,
+    OCPX_PARAM_ROUNDS = 10,
+    OCPX_PARAM_ROUND_GROWTH = 11
 } ocpx_param;
 ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value);
 ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value);

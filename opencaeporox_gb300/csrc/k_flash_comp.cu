@@ -21,15 +21,16 @@ __global__ void __launch_bounds__(128) k_flash_comp(const Model* __restrict__ M,
 // Batched form, step 1: one thread per cell in the order given by `order`
 // (cells of similar predicted cost side by side), with a work budget on the
 // phase equilibrium; cells over budget are appended to the deferral list and
-// left untouched.
+// left untouched.  With `next` NULL the grid has one thread per position of
+// `order`.  Otherwise the grid is persistent: each warp takes the next 32
+// positions from the counter `next` (zero before the launch) until `order`
+// is exhausted, so fewer warps are resident (and fewer per-thread frames are
+// live at once) and a warp that finishes early moves on at once.
 template <int NCM>
-__global__ void __launch_bounds__(128) k_flash_budget(const Model* __restrict__ M, BulkView b,
-                                                      const int* __restrict__ order, int budget, DeferSink sink,
-                                                      const uint8_t* __restrict__ pre, const int* __restrict__ level)
+__device__ __forceinline__ void flash_budget_cell(const Model* __restrict__ M, const BulkView& b, int cell, int budget,
+                                                  const DeferSink& sink, const uint8_t* __restrict__ pre,
+                                                  const int* __restrict__ level)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= b.nb) return;
-    const int cell = order[p];
     if (pre && pre[cell]) return;  // handled by the cooperative kernel
     if (level) {
         // at least the work of the adaptive level: only cells heavier than the
@@ -39,6 +40,68 @@ __global__ void __launch_bounds__(128) k_flash_budget(const Model* __restrict__ 
     }
     CompCellUpdate<NCM> u;
     u.run(*M, b, cell, budget, &sink);
+}
+
+template <int NCM>
+__global__ void __launch_bounds__(128) k_flash_budget(const Model* __restrict__ M, BulkView b,
+                                                      const int* __restrict__ order, int budget, DeferSink sink,
+                                                      const uint8_t* __restrict__ pre, const int* __restrict__ level,
+                                                      unsigned* __restrict__ next)
+{
+    if (!next) {
+        const int p = blockIdx.x * blockDim.x + threadIdx.x;
+        if (p < b.nb) flash_budget_cell<NCM>(M, b, order[p], budget, sink, pre, level);
+        return;
+    }
+    const unsigned lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(next, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= (unsigned)b.nb) break;
+        const unsigned p = base + lane;
+        if (p < (unsigned)b.nb) flash_budget_cell<NCM>(M, b, order[p], budget, sink, pre, level);
+        __syncwarp();
+    }
+}
+
+// Re-budgeting round: the cells of a deferral list, rerun one thread per cell
+// from their (untouched) state with the round's budget, b0 * mult, where b0
+// is the step-1 budget (raised to the adaptive level).  Cells over it go to
+// the next list.  Each warp takes 32 list entries at a time from `next`.
+// Restarting a cell from scratch repeats exactly the arithmetic it would have
+// done, so the result does not depend on the round a cell finishes in; with a
+// budget growing by a factor G per round, the repeated work is at most
+// 1 / (G - 1) of the work of the cells that go through the rounds, and warps
+// hold cells whose work lies within one factor of G of each other.
+template <int NCM>
+__global__ void __launch_bounds__(128) k_flash_round(const Model* __restrict__ M, BulkView b,
+                                                     const DeferRec* __restrict__ rin,
+                                                     const unsigned* __restrict__ rin_count, int cap, int budget,
+                                                     long long mult, DeferSink sink, const int* __restrict__ level,
+                                                     unsigned* __restrict__ next)
+{
+    const unsigned n = min(*rin_count, (unsigned)cap);
+    long long b0 = budget;
+    if (level) {
+        const long long lw = (long long)exp2f(0.25f * (float)level[0]);
+        if (lw > b0) b0 = lw;
+    }
+    long long br = b0 * mult;
+    if (br > 0x7fffffffLL || br < 0) br = 0x7fffffffLL;
+    const unsigned lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(next, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const unsigned p = base + lane;
+        if (p < n) {
+            CompCellUpdate<NCM> u;
+            u.run(*M, b, rin[p].cell, (int)br, &sink);
+        }
+        __syncwarp();
+    }
 }
 
 // Step 2: the phase equilibrium of every deferred cell on a whole warp
@@ -107,8 +170,17 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
     switch (part) {
     case 0: {
         const DeferSink sink{fb.rec, fb.count, fb.cap};
-        k_flash_budget<OCPX_NCM><<<(b.nb + fb.block - 1) / fb.block, fb.block, 0, s>>>(dm, b, order, fb.budget, sink,
-                                                                                         fb.pre, fb.level);
+        const int grid = fb.cell_blocks > 0 ? fb.cell_blocks : (b.nb + fb.block - 1) / fb.block;
+        k_flash_budget<OCPX_NCM><<<grid, fb.block, 0, s>>>(dm, b, order, fb.budget, sink, fb.pre, fb.level,
+                                                           fb.cell_blocks > 0 ? fb.cell_next : nullptr);
+        break;
+    }
+    case 3: {
+        // re-budgeting round: from list (rin, rin_count) into (rec, count)
+        const DeferSink sink{fb.rec, fb.count, fb.cap};
+        const int grid = fb.cell_blocks > 0 ? fb.cell_blocks : 304;
+        k_flash_round<OCPX_NCM><<<grid, fb.block, 0, s>>>(dm, b, fb.rin, fb.rin_count, fb.cap, fb.budget, fb.mult,
+                                                          sink, fb.level, fb.cell_next);
         break;
     }
     case 1:
@@ -127,13 +199,13 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
             cfg.blockDim = dim3(EXCL_WARPS * 32);
             cfg.dynamicSmemBytes = fb.excl_smem;
             return cudaLaunchKernelEx(&cfg, k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>, dm, b, (const DeferRec*)fb.rec,
-                                      (const unsigned*)fb.count, fb.cap, fb.count + 2, fb.pe);
+                                      (const unsigned*)fb.count, fb.cap, fb.coop_next, fb.pe);
         }
         if (part == 1) {
             cfg.gridDim = dim3(fb.coop_blocks);
             cfg.blockDim = dim3(COOP_WARPS * 32);
             return cudaLaunchKernelEx(&cfg, k_flash_pe_coop<OCPX_NCM, COOP_WARPS>, dm, b, (const DeferRec*)fb.rec,
-                                      (const unsigned*)fb.count, fb.cap, fb.count + 2, fb.pe);
+                                      (const unsigned*)fb.count, fb.cap, fb.coop_next, fb.pe);
         }
         cfg.gridDim = dim3((fb.cap + 127) / 128);
         cfg.blockDim = dim3(128);

@@ -128,7 +128,11 @@ struct ocpx_ctx {
     int* order = nullptr;
     unsigned* cost_hist = nullptr;
     DeferRec* defer_rec = nullptr;     // cells deferred by the per-cell kernel
-    unsigned* defer_count = nullptr;   // [4]: [0] deferred by the per-cell kernel, [1] pre-deferred
+    unsigned* defer_count = nullptr;   // [32]: [0] deferred by the per-cell kernel, [1] pre-deferred, others counters
+    DeferRec* defer_rec2 = nullptr;    // second late list (re-budgeting rounds alternate between the two)
+    int rounds = 0;                    // re-budgeting rounds before the late cooperative pass (0..8)
+    int round_growth = 4;              // budget factor per round
+    int late_count = 0;                // index in defer_count of the list the late cooperative pass takes
     PERes* pe_res = nullptr;
     DeferRec* pre_rec = nullptr;       // cells pre-deferred from their last flash's work
     PERes* pre_res = nullptr;
@@ -143,6 +147,7 @@ struct ocpx_ctx {
     int prio_hi = 0;                   // greatest stream priority of the device
     int pre_blocks = 0;                // SM-exclusive blocks of the pre-deferred pass (0: shared-SM blocks)
     int excl_smem = 0;                 // their dynamic shared memory
+    int cell_blocks = 0;               // persistent blocks of the per-cell kernel (0: one thread per cell)
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double* u = nullptr;            // Newton update staging
     double* bmat = nullptr;         // per-connection Jacobian blocks (2 per connection)
@@ -378,7 +383,8 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     add(&ctx->flags, sizeof(uint32_t) * 4);
     ctx->defer_cap = std::max(1024, nb / 4);
     add(&ctx->order, sizeof(int) * (size_t)nb); add(&ctx->cost_hist, sizeof(unsigned) * COST_BUCKETS);
-    add(&ctx->defer_rec, sizeof(DeferRec) * (size_t)ctx->defer_cap); add(&ctx->defer_count, sizeof(unsigned) * 4);
+    add(&ctx->defer_rec, sizeof(DeferRec) * (size_t)ctx->defer_cap); add(&ctx->defer_count, sizeof(unsigned) * 32);
+    add(&ctx->defer_rec2, sizeof(DeferRec) * (size_t)ctx->defer_cap);
     add(&ctx->pe_res, sizeof(PERes) * (size_t)ctx->defer_cap);
     add(&ctx->pre_rec, sizeof(DeferRec) * (size_t)ctx->defer_cap); add(&ctx->pre_res, sizeof(PERes) * (size_t)ctx->defer_cap);
     add(&ctx->pre_flag, (size_t)nb); add(&ctx->adapt_level, sizeof(int) * 4);
@@ -535,8 +541,10 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             // once, on a second (high-priority) stream, concurrently with the
             // per-cell kernel; cells that turn out expensive now follow after it
             const bool pre = ctx->predefer > 0;
-            // list counts [0] late, [1] pre-deferred; [2], [3] the cooperative kernels' next-slot counters
-            OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned) * 4, s));
+            // list counts [0] late, [1] pre-deferred; [2], [3] the cooperative kernels' next-slot
+            // counters; [4] the persistent per-cell kernel's position counter; [8 + r], [16 + r]
+            // the count and position counter of re-budgeting round r
+            OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned) * 32, s));
             mk = ctx->stage_begin(9);
             OCPX_CUDA(launch_cost_order(ctx->b, ctx->cost_hist, ctx->order, (unsigned)ctx->coop_cells,
                                         pre ? ctx->predefer : (long long)ctx->flash_budget, ctx->adapt_level, s));
@@ -548,12 +556,13 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
                 ctx->launches++;
             }
             ctx->stage_end(mk);
+            unsigned* const cnt = ctx->defer_count;
             const FlashBatch fbA{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
-                                 ctx->pre_rec, ctx->defer_count + 1, ctx->pre_res, nullptr, nullptr, ctx->prio_hi,
-                                 ctx->pre_blocks, ctx->excl_smem};
-            const FlashBatch fbB{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
-                                 ctx->defer_rec, ctx->defer_count, ctx->pe_res, pre ? ctx->pre_flag : nullptr,
-                                 ctx->adapt_level, 0, 0, 0};
+                                 ctx->pre_rec, cnt + 1, ctx->pre_res, nullptr, nullptr, ctx->prio_hi,
+                                 ctx->pre_blocks, ctx->excl_smem, 0, nullptr, cnt + 3, nullptr, nullptr, 0};
+            FlashBatch fbB{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
+                           ctx->defer_rec, cnt, ctx->pe_res, pre ? ctx->pre_flag : nullptr,
+                           ctx->adapt_level, 0, 0, 0, ctx->cell_blocks, cnt + 4, cnt + 2, nullptr, nullptr, 0};
             if (pre) {
                 // the pre-deferred cells' equilibrium and FlashDer on the second
                 // stream; the per-cell kernel skips them, so nothing else
@@ -569,6 +578,24 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             }
             mk = ctx->stage_begin(10);
             OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbB, 0, s));
+            // re-budgeting rounds: list r-1 -> list r with budget x G^r, alternating
+            // between the two late lists; counts cnt[8 + r], position counters cnt[16 + r]
+            long long mult = 1;
+            for (int r = 1; r <= ctx->rounds; r++) {
+                mult *= ctx->round_growth;
+                FlashBatch fr = fbB;
+                fr.rin = fbB.rec;
+                fr.rin_count = fbB.count;
+                fr.rec = (r & 1) ? ctx->defer_rec2 : ctx->defer_rec;
+                fr.count = cnt + 8 + r;
+                fr.cell_next = cnt + 16 + r;
+                fr.mult = mult;
+                OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fr, 3, s));
+                ctx->launches++;
+                fbB.rec = fr.rec;
+                fbB.count = fr.count;
+            }
+            ctx->late_count = (int)(fbB.count - cnt);
             ctx->stage_end(mk);
             mk = ctx->stage_begin(13);
             OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbB, 1, s));
@@ -888,6 +915,18 @@ ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value)
         if (value < 0 || value > 65535) return fail(OCPX_INVALID_ARG, "pre blocks out of range");
         ctx->pre_blocks = (int)value;
         return OCPX_OK;
+    case OCPX_PARAM_CELL_BLOCKS:
+        if (value < 0 || value > 65535) return fail(OCPX_INVALID_ARG, "cell blocks out of range");
+        ctx->cell_blocks = (int)value;
+        return OCPX_OK;
+    case OCPX_PARAM_ROUNDS:
+        if (value < 0 || value > 8) return fail(OCPX_INVALID_ARG, "rounds must be 0..8");
+        ctx->rounds = (int)value;
+        return OCPX_OK;
+    case OCPX_PARAM_ROUND_GROWTH:
+        if (value < 2 || value > 64) return fail(OCPX_INVALID_ARG, "round growth must be 2..64");
+        ctx->round_growth = (int)value;
+        return OCPX_OK;
     default:
         return fail(OCPX_INVALID_ARG, "unknown or read-only parameter");
     }
@@ -903,9 +942,15 @@ ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value)
     case OCPX_PARAM_PREDEFER: *value = ctx->predefer; return OCPX_OK;
     case OCPX_PARAM_COOP_CELLS: *value = ctx->coop_cells; return OCPX_OK;
     case OCPX_PARAM_PRE_BLOCKS: *value = ctx->pre_blocks; return OCPX_OK;
+    case OCPX_PARAM_CELL_BLOCKS: *value = ctx->cell_blocks; return OCPX_OK;
+    case OCPX_PARAM_ROUNDS: *value = ctx->rounds; return OCPX_OK;
+    case OCPX_PARAM_ROUND_GROWTH: *value = ctx->round_growth; return OCPX_OK;
     case OCPX_PARAM_DEFERRED: {
         unsigned n[2] = {0, 0};
-        OCPX_CUDA(cudaMemcpyAsync(n, ctx->defer_count, sizeof(n), cudaMemcpyDeviceToHost, ctx->stream));
+        OCPX_CUDA(cudaMemcpyAsync(&n[0], ctx->defer_count + ctx->late_count, sizeof(unsigned),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+        OCPX_CUDA(cudaMemcpyAsync(&n[1], ctx->defer_count + 1, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
         OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
         *value = (long long)std::min(n[0], (unsigned)ctx->defer_cap) + std::min(n[1], (unsigned)ctx->defer_cap);
         return OCPX_OK;

@@ -30,10 +30,17 @@ struct FlashBatch {
     int prio;            // launch priority of parts 1 and 2 (CUDA stream-priority scale), 0 = the stream's
     int excl_blocks;     // > 0: part 1 runs as this many SM-exclusive blocks (EXCL_WARPS warps each)
     int excl_smem;       // dynamic shared memory of an SM-exclusive block (from setup_flash_batched)
+    int cell_blocks;     // > 0: part 0 runs as this many persistent blocks taking 32 cells per warp
+    unsigned* cell_next; // their position counter (zero before the launch); part 3's too
+    unsigned* coop_next; // slot counter of part 1 (zero before the launch)
+    const DeferRec* rin;        // part 3: input list and its count
+    const unsigned* rin_count;
+    long long mult;             // part 3: budget multiplier of the round
 };
 // once per device: configure the SM-exclusive cooperative kernel of capacity ncm
 cudaError_t setup_flash_batched(int ncm, int* excl_smem);
-// part 0: budgeted thread-per-cell flash, 1: cooperative equilibrium, 2: finish deferred cells
+// part 0: budgeted thread-per-cell flash, 1: cooperative equilibrium, 2: finish deferred cells,
+// 3: re-budgeting round over a deferral list (thread per cell)
 cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, const int* order,
                                  const FlashBatch& fb, int part, cudaStream_t s);
 // Cells grouped by flash path (two-phase, one-phase, skip-flagged) and, within

@@ -59,6 +59,25 @@ def test_large_batched_matches_plain(case):
         assert np.array_equal(a[k], b[k], equal_nan=True), k
 
 
+def test_large_batched_launch_forms_match_plain(case):
+    """Re-budgeting rounds, the persistent per-cell kernel and SM-exclusive
+    pre-deferral blocks at 200,000 cells: the flash stays bit-identical."""
+    _, _, out = case
+    ctx = out[1]["ctx"]
+    keep = {k: ctx.get_param(k) for k in ("flash_budget", "rounds", "round_growth", "cell_blocks", "pre_blocks")}
+    try:
+        for k, v in dict(flash_budget=8, rounds=3, round_growth=4, cell_blocks=152, pre_blocks=38).items():
+            ctx.set_param(k, v)
+        ctx.checkpoint(0, restore=True)
+        ctx.update_property()
+        assert ctx.get_param("deferred") > 0
+        for k in FLASH_OUT:
+            assert np.array_equal(out[0]["res"][k], ctx.get(k), equal_nan=True), k
+    finally:
+        for k, v in keep.items():
+            ctx.set_param(k, v)
+
+
 def fim_to_ref(field):
     """Field name of the library -> BulkVarSet name (the oracle's)."""
     inv = {v: k for k, v in fim.REF_NAMES.items()}

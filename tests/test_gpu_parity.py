@@ -159,17 +159,28 @@ def test_batched_variant_against_reference(gpu_lib):
         check_update(ctx, fx, it, model, grid)
 
 
+BATCH_CASES = [
+    dict(flash_budget=0), dict(flash_budget=3), dict(), dict(coop_cells=8), dict(coop_cells=0),
+    dict(coop_cells=0, predefer=1, pre_blocks=0), dict(coop_cells=0, predefer=1, pre_blocks=3),
+    dict(flash_budget=3, coop_cells=0, cell_blocks=2),
+    dict(flash_budget=3, coop_cells=0, rounds=2, round_growth=2),
+    dict(flash_budget=1, coop_cells=0, predefer=0, rounds=8, round_growth=2, cell_blocks=1),
+]
+
+
 @pytest.mark.parametrize("name", ["comp6_8x8x3", "comp8_6x6x4"])
-@pytest.mark.parametrize("budget,coop_cells,predefer,pre_blocks",
-                         [(0, None, None, None), (3, None, None, None), (None, None, None, None),
-                          (None, 8, None, None), (None, 0, None, None), (None, 0, 1, 0), (None, 0, 1, 3)])
-def test_batched_variant_matches_plain(gpu_lib, name, budget, coop_cells, predefer, pre_blocks):
+@pytest.mark.parametrize("params", BATCH_CASES, ids=lambda p: ",".join(f"{k}={v}" for k, v in p.items()) or "defaults")
+def test_batched_variant_matches_plain(gpu_lib, name, params):
     """The batched flash (cost order, work budget, warp-cooperative phase
-    equilibrium for the deferred cells) is bit-identical to the plain one.
-    Budget 0 sends every cell that needs an equilibrium through the
-    cooperative kernel; pre-deferral threshold 1 sends the cells that needed
-    an equilibrium last time to the second stream, on shared-SM blocks or on
-    three SM-exclusive blocks."""
+    equilibrium for the deferred cells) is bit-identical to the plain one,
+    whatever its launch parameters: budget 0 sends every cell that needs an
+    equilibrium through the cooperative kernel; pre-deferral threshold 1
+    sends the cells that needed an equilibrium last time to the second
+    stream, on shared-SM or SM-exclusive blocks; persistent blocks run the
+    per-cell kernel 32 cells per warp at a time; re-budgeting rounds rerun
+    the over-budget cells with growing budgets before the cooperative pass."""
+    budget = params.get("flash_budget")
+    predefer = params.get("predefer")
     fx = P.load_fixture(name)
     its = [it for it in P.iterations(fx) if "P" in P.group(fx, it + "/post")]
     outs = []
@@ -177,14 +188,9 @@ def test_batched_variant_matches_plain(gpu_lib, name, budget, coop_cells, predef
     for variant in (0, 1):
         ctx, model, grid = make_ctx(fx, variant)
         with ctx:
-            if variant == 1 and budget is not None:
-                ctx.set_param("flash_budget", budget)
-            if variant == 1 and coop_cells is not None:
-                ctx.set_param("coop_cells", coop_cells)
-            if variant == 1 and predefer is not None:
-                ctx.set_param("predefer", predefer)
-            if variant == 1 and pre_blocks is not None:
-                ctx.set_param("pre_blocks", pre_blocks)
+            if variant == 1:
+                for k, v in params.items():
+                    ctx.set_param(k, v)
             got = []
             for it in its:
                 ctx.load_state(P.jac_state(fx, it))
@@ -200,4 +206,4 @@ def test_batched_variant_matches_plain(gpu_lib, name, budget, coop_cells, predef
         assert sum(p for _, p in deferred) > 0, deferred
     for it, a, b in zip(its, outs[0], outs[1]):
         for k in FLASH_OUT:
-            assert np.array_equal(a[k], b[k], equal_nan=True), f"{name} {it} budget={budget}: {k} differs"
+            assert np.array_equal(a[k], b[k], equal_nan=True), f"{name} {it} {params}: {k} differs"

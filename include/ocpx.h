@@ -22,6 +22,9 @@
  *   ocpx_newton_update      IsoT_FIM::GetSolution, bulk part
  *                           (src/IsoThermalMethod.cpp:1282-1418)
  *   ocpx_update_last_step   IsoT_FIM::UpdateLastTimeStep, bulk part (:1473-1517)
+ *   ocpx_nr_*, ocpx_step_max_change, ocpx_next_time_step
+ *                           Newton and time-step control (OCPNRsuite,
+ *                           ControlNR, ControlTime), bulk part; see below
  *   ocpx_step               one whole Newton iteration (update, properties,
  *                           residual, Jacobian)
  *
@@ -246,7 +249,9 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *   ROUNDS        re-budgeting rounds (0..8, default 0): the cells over the
  *                 budget are rerun one thread per cell, compacted, with the
  *                 budget multiplied by ROUND_GROWTH per round, before the
- *                 cells left over go to the cooperative kernel;
+ *                 cells left over go to the cooperative kernel; with rounds
+ *                 the adaptive floor no longer raises the budget (it still
+ *                 limits pre-deferral);
  *   ROUND_GROWTH  budget factor per round (2..64, default 4). */
 typedef enum ocpx_param {
     OCPX_PARAM_FLASH_BUDGET = 0,
@@ -341,6 +346,60 @@ ocpx_status ocpx_relres_noalloc(const double* d_res, const double* d_rockVp, con
  * Outputs may be NULL.  Synchronizes. */
 ocpx_status ocpx_adjoint(ocpx_ctx* ctx, const double* lambda, double* jt_lambda, double* dr_dtrans,
                          double* dr_dporo);
+
+/* Newton-iteration and time-step control of the FIM run, bulk part, on the
+ * device.  Replaces, for the bulk cells:
+ *   ocpx_nr_init_step       OCPNRsuite::InitStep (src/OCPNRsuite.cpp:70-83):
+ *                           the last Newton iterate := the last time step's
+ *                           state (saved by ocpx_update_last_step), and the
+ *                           initial residual norm := that of the last
+ *                           ocpx_calres (CalInitRes, src/IsoThermalMethod.cpp:1170-1177)
+ *   ocpx_nr_max_change      OCPNRsuite::CalMaxChangeNR (src/OCPNRsuite.cpp:86-160)
+ *   ocpx_step_max_change    OCPNRsuite::CalMaxChangeTime (src/OCPNRsuite.cpp:163-232)
+ *   ocpx_nr_check_converge  ControlNR::CheckConverge with {"res", "d"}
+ *                           (src/OCPControlNR.cpp:27-77), as IsoT_FIM::FinishNR
+ *                           calls it (src/IsoThermalMethod.cpp:838-864)
+ *   ocpx_next_time_step     ControlTime::CalNextTimeStep with {"dP", "dS", "iter"}
+ *                           (src/OCPControlTime.cpp:128-178), as IsoT_FIM::FinishStep
+ *                           calls it (src/IsoThermalMethod.cpp:865-870)
+ * The maxima are signed, with the reference's rule: the first entry in cell
+ * order whose magnitude is the largest, 0 when every change is 0; results
+ * are bit-identical to the reference's.  Wells stay with the host (their
+ * equations are not on the device), so their terms enter through
+ * ocpx_nr_control.  Every output pointer may be NULL: the values then stay
+ * on the device for the next call, and nothing synchronizes. */
+typedef struct ocpx_change_max {
+    double dP, dT, dN, dS, eV;  /* pressure, temperature, relative moles, saturation, volume error */
+} ocpx_change_max;
+typedef struct ocpx_nr_control {
+    /* ControlNRParam (include/OCPControlNR.hpp:28-51) */
+    int maxIter;
+    double tol, dPmin, dSmin;
+    /* ControlTimeParam (include/OCPControlTime.hpp:29-72) */
+    double maxIncreFac, minChopFac, dPlim, dSlim, timeMax, timeMin, end_time;
+    /* the time step that ends: its length and the time at its start */
+    double current_dt, current_time;
+    /* Newton iterations done in this time step (OCPNRsuite::GetIterNR) */
+    int iterNR;
+    /* well terms: the largest relative well-equation residual
+     * (OCPNRresidual::maxWellRelRes_mol) and the well pressure change over the
+     * time step that CalMaxChangeTime compares with the bulk's (dPWmaxT) */
+    double maxWellRelRes_mol, dPWmaxT;
+    /* 1: use these residual norms (for example with the wells' perforation
+     * terms added by the host); 0: the device's, from the last ocpx_calres
+     * and the one recorded by ocpx_nr_init_step */
+    int res_from_host;
+    double maxRelRes_V, maxRelRes0_V, maxRelRes_N;
+} ocpx_nr_control;
+ocpx_status ocpx_nr_init_step(ocpx_ctx* ctx);
+ocpx_status ocpx_nr_max_change(ocpx_ctx* ctx, ocpx_change_max* out);
+ocpx_status ocpx_step_max_change(ocpx_ctx* ctx, ocpx_change_max* out);
+/* state: 0 converged, 1 keep iterating, 2 not converged within maxIter
+ * (the integer values of the reference's OCPNRStateC) */
+ocpx_status ocpx_nr_check_converge(ocpx_ctx* ctx, const ocpx_nr_control* c, int* state);
+/* next_dt: the length of the next time step (clamped to the end of the
+ * current report interval, end_time); predict_dt: the same before that clamp */
+ocpx_status ocpx_next_time_step(ocpx_ctx* ctx, const ocpx_nr_control* c, double* next_dt, double* predict_dt);
 
 /* Stream the context launches on (a cudaStream_t), for callers that time or
  * order work around the library. */

@@ -67,8 +67,8 @@ __global__ void __launch_bounds__(128) k_flash_budget(const Model* __restrict__ 
 
 // Re-budgeting round: the cells of a deferral list, rerun one thread per cell
 // from their (untouched) state with the round's budget, b0 * mult, where b0
-// is the step-1 budget (raised to the adaptive level).  Cells over it go to
-// the next list.  Each warp takes 32 list entries at a time from `next`.
+// is the step-1 budget (raised to the adaptive level when `level` is given).
+// Cells over it go to the next list.  Each warp takes 32 list entries at a time from `next`.
 // Restarting a cell from scratch repeats exactly the arithmetic it would have
 // done, so the result does not depend on the round a cell finishes in; with a
 // budget growing by a factor G per round, the repeated work is at most

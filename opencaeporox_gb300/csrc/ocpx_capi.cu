@@ -150,6 +150,14 @@ struct ocpx_ctx {
     int cell_blocks = 0;               // persistent blocks of the per-cell kernel (0: one thread per cell)
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double* u = nullptr;            // Newton update staging
+    double *nr_lP = nullptr, *nr_lT = nullptr, *nr_lN = nullptr, *nr_lS = nullptr;  // last Newton iterate
+    double *ts_lP = nullptr, *ts_lT = nullptr, *ts_lS = nullptr;                    // last time step
+    void* maxch_partial = nullptr;  // per-block candidates of the max-change reductions
+    double* nr_stats = nullptr;     // [5] CalMaxChangeNR: dP, dT, dN, dS, eV
+    double* ts_stats = nullptr;     // [5] CalMaxChangeTime
+    double* nr_res0 = nullptr;      // initial relative residual of the time step
+    int* nr_state = nullptr;        // last CheckConverge state
+    double* nr_dt = nullptr;        // [2] next dt, predicted dt
     double* bmat = nullptr;         // per-connection Jacobian blocks (2 per connection)
     uint32_t* jac_rowptr = nullptr;
     uint32_t* jac_slot = nullptr;   // [2][nconn]: block index of connection c in row bId / row eId
@@ -389,6 +397,13 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     add(&ctx->pre_rec, sizeof(DeferRec) * (size_t)ctx->defer_cap); add(&ctx->pre_res, sizeof(PERes) * (size_t)ctx->defer_cap);
     add(&ctx->pre_flag, (size_t)nb); add(&ctx->adapt_level, sizeof(int) * 4);
     add(&ctx->u, D * (nc + 1));
+    // Newton / time-step control: last Newton iterate, last time step (P, T, S;
+    // Ni's is b.lNi), reduction candidates, results
+    add(&ctx->nr_lP, D); add(&ctx->nr_lT, D); add(&ctx->nr_lN, D * nc); add(&ctx->nr_lS, D * np);
+    add(&ctx->ts_lP, D); add(&ctx->ts_lT, D); add(&ctx->ts_lS, D * np);
+    add(&ctx->maxch_partial, (size_t)MAX_CHANGE_BLOCKS * 5 * 16);
+    add(&ctx->nr_stats, sizeof(double) * 5); add(&ctx->ts_stats, sizeof(double) * 5);
+    add(&ctx->nr_res0, sizeof(double)); add(&ctx->nr_state, sizeof(int)); add(&ctx->nr_dt, sizeof(double) * 2);
     add(&ctx->bmat, sizeof(double) * C * 2 * bsize);
     add(&ctx->jac_rowptr, sizeof(uint32_t) * (nb + 1)); add(&ctx->jac_col, sizeof(uint32_t) * jcol.size());
     add(&ctx->jac_slot, sizeof(uint32_t) * jslot.size());
@@ -560,9 +575,13 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             const FlashBatch fbA{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
                                  ctx->pre_rec, cnt + 1, ctx->pre_res, nullptr, nullptr, ctx->prio_hi,
                                  ctx->pre_blocks, ctx->excl_smem, 0, nullptr, cnt + 3, nullptr, nullptr, 0};
+            // with re-budgeting rounds the rounds, not a budget raised to the
+            // adaptive level, keep the cooperative list short: the per-cell
+            // kernel then starts from the plain budget
             FlashBatch fbB{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
                            ctx->defer_rec, cnt, ctx->pe_res, pre ? ctx->pre_flag : nullptr,
-                           ctx->adapt_level, 0, 0, 0, ctx->cell_blocks, cnt + 4, cnt + 2, nullptr, nullptr, 0};
+                           ctx->rounds > 0 ? nullptr : ctx->adapt_level, 0, 0, 0, ctx->cell_blocks, cnt + 4, cnt + 2,
+                           nullptr, nullptr, 0};
             if (pre) {
                 // the pre-deferred cells' equilibrium and FlashDer on the second
                 // stream; the per-cell kernel skips them, so nothing else
@@ -817,8 +836,82 @@ ocpx_status ocpx_profile_read(ocpx_ctx* ctx, double* ms, uint64_t* launches)
 ocpx_status ocpx_update_last_step(ocpx_ctx* ctx)
 {
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
-    OCPX_CUDA(cudaMemcpyAsync(ctx->b.lNi, ctx->b.Ni, sizeof(double) * (size_t)ctx->nb * ctx->nc,
-                              cudaMemcpyDeviceToDevice, ctx->stream));
+    const size_t D = sizeof(double) * (size_t)ctx->nb;
+    OCPX_CUDA(cudaMemcpyAsync(ctx->b.lNi, ctx->b.Ni, D * ctx->nc, cudaMemcpyDeviceToDevice, ctx->stream));
+    // lP, lT, lS of BulkVarSet, read by CalMaxChangeTime and OCPNRsuite::InitStep
+    OCPX_CUDA(cudaMemcpyAsync(ctx->ts_lP, ctx->b.P, D, cudaMemcpyDeviceToDevice, ctx->stream));
+    OCPX_CUDA(cudaMemcpyAsync(ctx->ts_lT, ctx->b.T, D, cudaMemcpyDeviceToDevice, ctx->stream));
+    OCPX_CUDA(cudaMemcpyAsync(ctx->ts_lS, ctx->b.S, D * ctx->np, cudaMemcpyDeviceToDevice, ctx->stream));
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_nr_init_step(ocpx_ctx* ctx)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    const size_t D = sizeof(double) * (size_t)ctx->nb;
+    cudaStream_t s = ctx->stream;
+    OCPX_CUDA(cudaMemcpyAsync(ctx->nr_lP, ctx->ts_lP, D, cudaMemcpyDeviceToDevice, s));
+    OCPX_CUDA(cudaMemcpyAsync(ctx->nr_lT, ctx->ts_lT, D, cudaMemcpyDeviceToDevice, s));
+    OCPX_CUDA(cudaMemcpyAsync(ctx->nr_lN, ctx->b.lNi, D * ctx->nc, cudaMemcpyDeviceToDevice, s));
+    OCPX_CUDA(cudaMemcpyAsync(ctx->nr_lS, ctx->ts_lS, D * ctx->np, cudaMemcpyDeviceToDevice, s));
+    OCPX_CUDA(cudaMemcpyAsync(ctx->nr_res0, &ctx->norm_out->maxV, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return OCPX_OK;
+}
+
+namespace {
+ocpx_status read_change(ocpx_ctx* ctx, const double* dev, ocpx_change_max* out)
+{
+    if (!out) return OCPX_OK;
+    double v[5];
+    OCPX_CUDA(cudaMemcpyAsync(v, dev, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream));
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    *out = ocpx_change_max{v[0], v[1], v[2], v[3], v[4]};
+    return OCPX_OK;
+}
+}  // namespace
+
+ocpx_status ocpx_nr_max_change(ocpx_ctx* ctx, ocpx_change_max* out)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    OCPX_CUDA(launch_max_change(0, ctx->b, ctx->nr_lP, ctx->nr_lT, ctx->nr_lN, ctx->nr_lS, ctx->maxch_partial,
+                                ctx->nr_stats, ctx->stream));
+    ctx->launches += 2;
+    return read_change(ctx, ctx->nr_stats, out);
+}
+
+ocpx_status ocpx_step_max_change(ocpx_ctx* ctx, ocpx_change_max* out)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    OCPX_CUDA(launch_max_change(1, ctx->b, ctx->ts_lP, ctx->ts_lT, nullptr, ctx->ts_lS, ctx->maxch_partial,
+                                ctx->ts_stats, ctx->stream));
+    ctx->launches += 2;
+    return read_change(ctx, ctx->ts_stats, out);
+}
+
+ocpx_status ocpx_nr_check_converge(ocpx_ctx* ctx, const ocpx_nr_control* c, int* state)
+{
+    if (!ctx || !c) return fail(OCPX_INVALID_ARG, "null argument");
+    OCPX_CUDA(launch_nr_converge(*c, ctx->nr_stats, ctx->norm_out, ctx->nr_res0, ctx->nr_state, ctx->stream));
+    ctx->launches++;
+    if (state) {
+        OCPX_CUDA(cudaMemcpyAsync(state, ctx->nr_state, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_next_time_step(ocpx_ctx* ctx, const ocpx_nr_control* c, double* next_dt, double* predict_dt)
+{
+    if (!ctx || !c) return fail(OCPX_INVALID_ARG, "null argument");
+    OCPX_CUDA(launch_next_dt(*c, ctx->ts_stats, ctx->nr_dt, ctx->stream));
+    ctx->launches++;
+    if (next_dt || predict_dt) {
+        double v[2];
+        OCPX_CUDA(cudaMemcpyAsync(v, ctx->nr_dt, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream));
+        OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (next_dt) *next_dt = v[0];
+        if (predict_dt) *predict_dt = v[1];
+    }
     return OCPX_OK;
 }
 

@@ -5,6 +5,7 @@
 #include "bulk_view.cuh"
 #include "conn_ops.cuh"
 #include "flash_comp.cuh"
+#include "ocpx.h"
 
 namespace ocpx {
 
@@ -56,6 +57,20 @@ cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, uns
 // visiting cells in `order`
 cudaError_t launch_predefer(const Model* dm, const BulkView& b, const int* order, long long threshold,
                             const int* level, const DeferSink& sink, uint8_t* pre, cudaStream_t s);
+
+// Newton and time-step control (k_nrctl.cu).  mode 0: CalMaxChangeNR against
+// the last Newton iterate (lP, lT, lN, lS; replaced by the current state),
+// mode 1: CalMaxChangeTime against the last time step (lP, lT, lS, b.lNi).
+// out5 receives dP, dT, dN, dS, eV; partial holds MAX_CHANGE_BLOCKS x 5
+// candidates of 16 bytes.
+using NRControl = ocpx_nr_control;
+constexpr int MAX_CHANGE_BLOCKS = 1216;
+int max_change_blocks(int nb);
+cudaError_t launch_max_change(int mode, const BulkView& b, double* lP, double* lT, double* lN, double* lS,
+                              void* partial, double* out5, cudaStream_t s);
+cudaError_t launch_nr_converge(const NRControl& c, const double* nr5, const RowNorm* norm, const double* res0,
+                               int* state, cudaStream_t s);
+cudaError_t launch_next_dt(const NRControl& c, const double* ts5, double* out2, cudaStream_t s);
 
 cudaError_t launch_flash_bo(const Model* dm, const BulkView& b, int block, cudaStream_t s);
 cudaError_t launch_krpc_rock(const Model* dm, const BulkView& b, int block, cudaStream_t s);

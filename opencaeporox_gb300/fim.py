@@ -89,12 +89,41 @@ class Norms(C.Structure):
                 ("maxId_N", C.c_int)]
 
 
+class ChangeMax(C.Structure):
+    """ocpx_change_max: signed maxima of one Newton iteration or time step."""
+    _fields_ = [("dP", C.c_double), ("dT", C.c_double), ("dN", C.c_double), ("dS", C.c_double),
+                ("eV", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class NRControl(C.Structure):
+    """ocpx_nr_control: ControlNRParam / ControlTimeParam values, the time step
+    that ends, its Newton iterations, and the host-owned (well) terms."""
+    _fields_ = [("maxIter", C.c_int), ("tol", C.c_double), ("dPmin", C.c_double), ("dSmin", C.c_double),
+                ("maxIncreFac", C.c_double), ("minChopFac", C.c_double), ("dPlim", C.c_double),
+                ("dSlim", C.c_double), ("timeMax", C.c_double), ("timeMin", C.c_double), ("end_time", C.c_double),
+                ("current_dt", C.c_double), ("current_time", C.c_double), ("iterNR", C.c_int),
+                ("maxWellRelRes_mol", C.c_double), ("dPWmaxT", C.c_double), ("res_from_host", C.c_int),
+                ("maxRelRes_V", C.c_double), ("maxRelRes0_V", C.c_double), ("maxRelRes_N", C.c_double)]
+
+    @classmethod
+    def make(cls, **kw):
+        c = cls()
+        for k, v in kw.items():
+            setattr(c, k, v)
+        return c
+
+
 EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy", "ocpx_set_field",
            "ocpx_get_field", "ocpx_update_properties", "ocpx_calres", "ocpx_assemble", "ocpx_newton_update",
            "ocpx_update_last_step", "ocpx_synchronize", "ocpx_jacobian_dims", "ocpx_get_jacobian",
            "ocpx_jacobian_device", "ocpx_set_variant", "ocpx_step", "ocpx_enqueue_step", "ocpx_step_report",
            "ocpx_profile_enable", "ocpx_profile_read", "ocpx_checkpoint", "ocpx_measure_fp64_tflops",
-           "ocpx_stream", "ocpx_launch_count", "ocpx_set_param", "ocpx_get_param", "ocpx_adjoint"]
+           "ocpx_stream", "ocpx_launch_count", "ocpx_set_param", "ocpx_get_param", "ocpx_adjoint",
+           "ocpx_nr_init_step", "ocpx_nr_max_change", "ocpx_step_max_change", "ocpx_nr_check_converge",
+           "ocpx_next_time_step"]
 
 PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3, "predefer": 4, "coop_cells": 5,
           "predeferred": 6, "level": 7, "pre_blocks": 8,
@@ -137,6 +166,11 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.ocpx_adjoint.argtypes = [P, P, P, P, P]
     lib.ocpx_adjoint.restype = C.c_int
     lib.ocpx_set_param.argtypes = [P, C.c_int, C.c_longlong]
+    lib.ocpx_nr_init_step.argtypes = [P]
+    lib.ocpx_nr_max_change.argtypes = [P, C.POINTER(ChangeMax)]
+    lib.ocpx_step_max_change.argtypes = [P, C.POINTER(ChangeMax)]
+    lib.ocpx_nr_check_converge.argtypes = [P, C.POINTER(NRControl), C.POINTER(C.c_int)]
+    lib.ocpx_next_time_step.argtypes = [P, C.POINTER(NRControl), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.ocpx_get_param.argtypes = [P, C.c_int, C.POINTER(C.c_longlong)]
     for fn in ("ocpx_enqueue_step", "ocpx_step_report", "ocpx_profile_enable", "ocpx_profile_read",
                "ocpx_measure_fp64_tflops", "ocpx_checkpoint", "ocpx_set_param", "ocpx_get_param"):
@@ -431,6 +465,37 @@ class FimContext:
         ptr = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
         _check(self.lib.ocpx_adjoint(self.h, ptr(lam), ptr(out_jt), ptr(out_t), ptr(out_p)))
         return out_jt, out_t, out_p
+
+    # --- Newton-iteration and time-step control (bulk part, on the device)
+    def nr_init_step(self):
+        """OCPNRsuite::InitStep: the last Newton iterate := the last time step's
+        state; the initial residual norm := that of the last cal_res."""
+        _check(self.lib.ocpx_nr_init_step(self.h))
+
+    def nr_max_change(self) -> dict:
+        """OCPNRsuite::CalMaxChangeNR (bulk): signed maxima since the last call."""
+        out = ChangeMax()
+        _check(self.lib.ocpx_nr_max_change(self.h, C.byref(out)))
+        return out.as_dict()
+
+    def step_max_change(self) -> dict:
+        """OCPNRsuite::CalMaxChangeTime (bulk): signed maxima over the time step."""
+        out = ChangeMax()
+        _check(self.lib.ocpx_step_max_change(self.h, C.byref(out)))
+        return out.as_dict()
+
+    def nr_check_converge(self, ctrl: NRControl) -> int:
+        """ControlNR::CheckConverge({"res", "d"}): 0 converged, 1 continue,
+        2 not converged within maxIter."""
+        st = C.c_int()
+        _check(self.lib.ocpx_nr_check_converge(self.h, C.byref(ctrl), C.byref(st)))
+        return st.value
+
+    def next_time_step(self, ctrl: NRControl):
+        """ControlTime::CalNextTimeStep({"dP", "dS", "iter"}): (next dt, predicted dt)."""
+        dt, pdt = C.c_double(), C.c_double()
+        _check(self.lib.ocpx_next_time_step(self.h, C.byref(ctrl), C.byref(dt), C.byref(pdt)))
+        return dt.value, pdt.value
 
     def jacobian(self):
         nrow, nnz, bd = C.c_size_t(), C.c_size_t(), C.c_int()

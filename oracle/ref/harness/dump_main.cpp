@@ -312,6 +312,80 @@ void inject_ptn_moles(Reservoir& rs, const string& deck)
         for (USI i = 0; i < nc; i++) Ni[i][n] = buf[static_cast<size_t>(n) * nc + i];
 }
 
+// IsothermalSolver::FinishNR for a FIM-only run (src/IsoThermalSolver.cpp:220-250
+// with IsoT_FIM::FinishNR, src/IsoThermalMethod.cpp:838-864), unrolled so the
+// Newton statistics can be recorded before a reset clears them: the maximum
+// changes of CalMaxChangeNR, the residual norms and control parameters that
+// CheckConverge reads, and the state it returns as the integer value of
+// OCPNRStateC (0 converge, 1 continue iterating, 2 not converged).
+OCP_BOOL finish_nr(IsothermalSolver& S, IsoT_FIM& fim, Reservoir& rs, OCPControl& ctrl, const string& dir)
+{
+    if (S.curMethod != OCPNLMethod::FIM || S.mainMethod != OCPNLMethod::FIM) return S.FinishNR(rs, ctrl);
+    OCPNRsuite& NR = fim.NR;
+    NR.CalMaxChangeNR(rs);
+    put1(dir, "nr_dPBmax", NR.dPBmaxNR.back());
+    put1(dir, "nr_dPWmax", NR.dPWmaxNR.back());
+    put1(dir, "nr_dTmax", NR.dTmaxNR.back());
+    put1(dir, "nr_dNmax", NR.dNmaxNR.back());
+    put1(dir, "nr_dSmax", NR.dSmaxNR.back());
+    put1(dir, "nr_eVmax", NR.eVmaxNR.back());
+    put1(dir, "nr_maxRelRes_V", NR.res.maxRelRes_V);
+    put1(dir, "nr_maxRelRes0_V", NR.res.maxRelRes0_V);
+    put1(dir, "nr_maxRelRes_N", NR.res.maxRelRes_N);
+    put1(dir, "nr_maxWellRelRes_mol", NR.res.maxWellRelRes_mol);
+    puti(dir, "nr_iter", static_cast<int>(NR.GetIterNR()));
+    put1(dir, "nr_tol", ctrl.NR.wp->tol);
+    put1(dir, "nr_dPmin", ctrl.NR.wp->dPmin);
+    put1(dir, "nr_dSmin", ctrl.NR.wp->dSmin);
+    puti(dir, "nr_maxIter", static_cast<int>(ctrl.NR.wp->maxIter));
+    const OCPNRStateC st = ctrl.CheckConverge(NR, {"res", "d"});
+    puti(dir, "nr_state", static_cast<int>(st));
+    OCP_BOOL conv = OCP_FALSE;
+    if (st == OCPNRStateC::converge) {
+        if (!NR.CheckPhysical(rs, {"WellP"}, ctrl.time.GetCurrentDt())) {
+            ctrl.time.CutDt(NR);
+            fim.ResetToLastTimeStep(rs, ctrl);
+        }
+        else {
+            conv = OCP_TRUE;
+        }
+    }
+    else if (st == OCPNRStateC::not_converge) {
+        ctrl.time.CutDt();
+        fim.ResetToLastTimeStep(rs, ctrl);
+    }
+    puti(dir, "nr_finish", conv ? 1 : 0);
+    return conv;
+}
+
+// After IsothermalSolver::FinishStep: CalMaxChangeTime's maxima and the next
+// time step of CalNextTimeStep, with the control parameters it read.
+void dump_finish_step(IsoT_FIM& fim, OCPControl& ctrl, const string& dir, double time_before)
+{
+    put1(dir, "ts_time_before", time_before);
+    const OCPNRsuite& NR = fim.NR;
+    put1(dir, "ts_dPmax", NR.dPmaxT);
+    put1(dir, "ts_dPBmax", NR.dPBmaxT);
+    put1(dir, "ts_dPWmax", NR.dPWmaxT);
+    put1(dir, "ts_dTmax", NR.dTmaxT);
+    put1(dir, "ts_dNmax", NR.dNmaxT);
+    put1(dir, "ts_dSmax", NR.dSmaxT);
+    put1(dir, "ts_eVmax", NR.eVmaxT);
+    puti(dir, "ts_iter", static_cast<int>(NR.GetIterNR()));
+    const ControlTime& t = ctrl.time;
+    put1(dir, "ts_last_dt", t.last_dt);
+    put1(dir, "ts_current_time", t.current_time);
+    put1(dir, "ts_next_dt", t.current_dt);
+    put1(dir, "ts_predict_dt", t.predict_dt);
+    put1(dir, "ts_maxIncreFac", t.wp->maxIncreFac);
+    put1(dir, "ts_minChopFac", t.wp->minChopFac);
+    put1(dir, "ts_dPlim", t.wp->dPlim);
+    put1(dir, "ts_dSlim", t.wp->dSlim);
+    put1(dir, "ts_timeMax", t.wp->timeMax);
+    put1(dir, "ts_timeMin", t.wp->timeMin);
+    put1(dir, "ts_end_time", t.wp->end_time);
+}
+
 int run_fim(const string& deck, int max_iters)
 {
     const char* argv_[] = {"ocp_ref_dump", deck.c_str()};
@@ -338,6 +412,7 @@ int run_fim(const string& deck, int max_iters)
     vector<double> log_rows; // step, iter, dt, event, t_update, t_assemble
     int  it = 0, step = 0;
     bool stop = false;
+    string last_post;
     ctrl.simTime.Initialize();
     while (!stop) {
         INT d = ctrl.ApplyControl();
@@ -386,12 +461,15 @@ int run_fim(const string& deck, int max_iters)
                 dump_conn_res(dir + "/post", rs, fim, dt);
                 log_rows.insert(log_rows.end(), {double(step), double(nr), dt, 0.0, t_upd, t_asm});
                 it++; nr++;
-                const bool conv = S.FinishNR(rs, ctrl);
+                const bool conv = finish_nr(S, fim, rs, ctrl, dir + "/post");
+                last_post = dir + "/post";
                 if (it >= max_iters) { stop = true; break; }
                 if (conv) break;
             }
             if (stop) break;
+            const double time_before = ctrl.time.GetCurrentTime();
             S.FinishStep(rs, ctrl);
+            if (!last_post.empty()) dump_finish_step(fim, ctrl, last_post, time_before);
             step++;
         }
     }

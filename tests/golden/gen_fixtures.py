@@ -59,6 +59,15 @@ def load_dir(path, keys=None):
     return out
 
 
+# Newton control after each iteration (the harness's finish_nr) and, on the
+# last iteration of a time step, the time-step control (dump_finish_step)
+NR_KEYS = ["nr_dPBmax", "nr_dPWmax", "nr_dTmax", "nr_dNmax", "nr_dSmax", "nr_eVmax", "nr_maxRelRes_V",
+           "nr_maxRelRes0_V", "nr_maxRelRes_N", "nr_maxWellRelRes_mol", "nr_iter", "nr_tol", "nr_dPmin",
+           "nr_dSmin", "nr_maxIter", "nr_state", "nr_finish",
+           "ts_dPmax", "ts_dPBmax", "ts_dPWmax", "ts_dTmax", "ts_dNmax", "ts_dSmax", "ts_eVmax", "ts_iter",
+           "ts_last_dt", "ts_current_time", "ts_next_dt", "ts_predict_dt", "ts_maxIncreFac", "ts_minChopFac",
+           "ts_dPlim", "ts_dSlim", "ts_timeMax", "ts_timeMin", "ts_end_time", "ts_time_before"]
+
 PRE_KEYS = ["P", "T", "Pb", "Ni", "Nt", "Pj", "S", "phaseExist", "xij", "lNi",
             "skip_flag", "skip_minEigen", "skip_P", "skip_T", "skip_zi", "u", "dt", "dSmax"]
 
@@ -95,7 +104,7 @@ def pack_fim(outdir):
         post = os.path.join(base, "post")
         prev_post = None
         if os.path.isdir(post) and os.path.exists(os.path.join(post, "P.npy")):
-            pd = load_dir(post, set(STATE_KEYS + RES_KEYS + ["flash_ftype", "flash_iters"]))
+            pd = load_dir(post, set(STATE_KEYS + RES_KEYS + NR_KEYS + ["flash_ftype", "flash_iters"]))
             for k, v in pd.items():
                 data[f"it{it:03d}/post/{k}"] = v
             prev_post = (it, pd)

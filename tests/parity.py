@@ -233,3 +233,37 @@ def flash_sensitivity(model, grid, state, ref) -> dict:
         for k, v in state_errors(dict(ob.a), ref, model.nc, grid.nb).items():
             out[k] = max(out.get(k, 0.0), v)
     return out
+
+
+def nr_cases(fx: dict):
+    """Newton iterations whose control the reference recorded: (it, the last
+    Newton iterate = the state the iteration started from, the state after
+    its property update, the recorded values)."""
+    out = []
+    for it in iterations(fx):
+        post = group(fx, it + "/post")
+        if "nr_state" in post:
+            out.append((it, jac_state(fx, it), post, post))
+    return out
+
+
+def ts_cases(fx: dict):
+    """Time steps whose control the reference recorded, on their last Newton
+    iteration: (it, the state at the start of the step, the state at its end,
+    the recorded values).  The log's first column numbers the time steps."""
+    log = np.asarray(fx["log"])
+    its = iterations(fx)
+    out = []
+    for it in its:
+        post = group(fx, it + "/post")
+        if "ts_next_dt" not in post:
+            continue
+        step = log[int(it[2:]), 0]
+        first = int(np.nonzero(log[:, 0] == step)[0][0])
+        out.append((it, jac_state(fx, "it%03d" % first), post, post))
+    return out
+
+
+def state_dims(state: dict):
+    nb = len(state["P"])
+    return nb, len(state["Ni"]) // nb, len(state["S"]) // nb

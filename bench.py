@@ -418,7 +418,10 @@ def large_step(args, rt, local):
         out[variant] = dict(ms=statistics.median(times), stages={st: round(v[0], 3) for st, v in prof.items()},
                             deferred=ctx.get_param("deferred") if variant == 1 else 0,
                             predeferred=ctx.get_param("predeferred") if variant == 1 else 0,
-                            level=ctx.get_param("level") if variant == 1 else 0)
+                            level=ctx.get_param("level") if variant == 1 else 0,
+                            params={k: ctx.get_param(k) for k in ("flash_budget", "predefer", "coop_cells",
+                                                                 "coop_blocks", "pre_blocks", "cell_blocks",
+                                                                 "block_cell")} if variant == 1 else None)
         print(f"large: variant {variant} step {out[variant]['ms']:.1f} ms", file=sys.stderr, flush=True)
         ctx.close()
     if 0 not in out or 1 not in out:  # one form only (profiling runs): its times
@@ -433,7 +436,7 @@ def large_step(args, rt, local):
             "plain_value": n / (out[0]["ms"] * 1e-3), "plain_ms": out[0]["ms"],
             "batched_over_plain": out[0]["ms"] / out[1]["ms"], "stages_ms": out[1]["stages"],
             "plain_stages_ms": out[0]["stages"], "deferred_cells": out[1]["deferred"],
-            "predeferred_cells": out[1]["predeferred"], "level": out[1]["level"],
+            "predeferred_cells": out[1]["predeferred"], "level": out[1]["level"], "params": out[1]["params"],
             "timing": "CUDA events on the library stream around the step (the batched form's graph), "
                       "L2 flushed between steps; stage times from one eager profiled step (library defaults)"}
 
@@ -577,6 +580,7 @@ def main():
                         "predeferred_cells": ctx1.get_param("predeferred"), "level": ctx1.get_param("level"),
                         "block_cell": ctx1.get_param("block_cell"), "predefer": ctx1.get_param("predefer"),
                         "coop_cells": ctx1.get_param("coop_cells"), "pre_blocks": ctx1.get_param("pre_blocks"),
+                        "cell_blocks": ctx1.get_param("cell_blocks"),
                         "autotune": None if tuned is None else {k: v for k, v in tuned.items() if k != "trials"}},
             "clocks": ck, "gpu_launches": launches,
             "e2e": {"value": nb / (e2e_ms * 1e-3) * world, "unit": "cells/s", "h2d_bytes_per_step": h2d,

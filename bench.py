@@ -341,8 +341,8 @@ def flash_stress(args, rt, local):
             # tune on the flash stage (the step has no connections)
             from opencaeporox_gb300 import autotune
             # each flash of this workload takes seconds: a small candidate set, one round
-            space = {"flash_budget": (48, 192), "predefer": (0, 192), "coop_cells": (608, 1216, 4864),
-                     "coop_blocks": (608,), "block_cell": (128,), "pre_blocks": (0,)}
+            space = {"fused_blocks": ("sms", 0, 1, 2), "flash_budget": (48, 192), "predefer": (0, 192),
+                     "coop_cells": (608, 1216, 4864), "coop_blocks": (608,), "block_cell": (128,), "pre_blocks": (0,)}
             out["autotune"] = {k: v for k, v in autotune.tune(ctx, DT, slot=0, space=space, rounds=1,
                                                               reps=1).items() if k != "trials"}
         times = []
@@ -419,9 +419,9 @@ def large_step(args, rt, local):
                             deferred=ctx.get_param("deferred") if variant == 1 else 0,
                             predeferred=ctx.get_param("predeferred") if variant == 1 else 0,
                             level=ctx.get_param("level") if variant == 1 else 0,
-                            params={k: ctx.get_param(k) for k in ("flash_budget", "predefer", "coop_cells",
-                                                                 "coop_blocks", "pre_blocks", "cell_blocks",
-                                                                 "block_cell")} if variant == 1 else None)
+                            params={k: ctx.get_param(k) for k in ("fused_blocks", "flash_budget", "predefer",
+                                                                 "coop_cells", "coop_blocks", "pre_blocks",
+                                                                 "cell_blocks", "block_cell")} if variant == 1 else None)
         print(f"large: variant {variant} step {out[variant]['ms']:.1f} ms", file=sys.stderr, flush=True)
         ctx.close()
     if 0 not in out or 1 not in out:  # one form only (profiling runs): its times
@@ -551,7 +551,9 @@ def main():
     pk = peaks()
     hbm = pk.get("hbm_gbs")
     flash_ms = prof["flash"][0]
-    roof = {"kernel": "k_flash_comp (flash stage of the batched step)", "bound": "fp64", "unit": "TFLOP/s",
+    fused = results[1]["ctx"].get_param("fused_blocks") > 0
+    roof = {"kernel": ("k_flash_fused + k_flash_post" if fused else "k_flash_budget + k_flash_pe_coop + k_flash_post")
+                      + " (flash stage of the batched step)", "bound": "fp64", "unit": "TFLOP/s",
             "peak": fp64, "peak_source": "measured (DFMA-chain probe of this library, best of 3)",
             "achieved": None, "frac": None, "traffic": FLASH_DRAM_BYTES}
     if FLASH_FP64_FLOP_PER_CELL:
@@ -580,7 +582,7 @@ def main():
                         "predeferred_cells": ctx1.get_param("predeferred"), "level": ctx1.get_param("level"),
                         "block_cell": ctx1.get_param("block_cell"), "predefer": ctx1.get_param("predefer"),
                         "coop_cells": ctx1.get_param("coop_cells"), "pre_blocks": ctx1.get_param("pre_blocks"),
-                        "cell_blocks": ctx1.get_param("cell_blocks"),
+                        "cell_blocks": ctx1.get_param("cell_blocks"), "fused_blocks": ctx1.get_param("fused_blocks"),
                         "autotune": None if tuned is None else {k: v for k, v in tuned.items() if k != "trials"}},
             "clocks": ck, "gpu_launches": launches,
             "e2e": {"value": nb / (e2e_ms * 1e-3) * world, "unit": "cells/s", "h2d_bytes_per_step": h2d,

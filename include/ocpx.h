@@ -224,7 +224,7 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *                 reading it synchronizes the context stream;
  *   PREDEFER      cells whose last flash used more than this many work
  *                 units go to the cooperative kernel at once, on a second
- *                 stream, while the per-cell kernel runs (default 96);
+ *                 stream, while the per-cell kernel runs (default 192);
  *                 0: only cells that exceed the budget now are deferred;
  *   COOP_CELLS    adaptive floor of both thresholds, active only when
  *                 more than this many cells are predicted above the
@@ -252,7 +252,17 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *                 cells left over go to the cooperative kernel; with rounds
  *                 the adaptive floor no longer raises the budget (it still
  *                 limits pre-deferral);
- *   ROUND_GROWTH  budget factor per round (2..64, default 4). */
+ *   ROUND_GROWTH  budget factor per round (2..64, default 4);
+ *   FUSED_BLOCKS  > 0: the batched flash as one persistent kernel of this
+ *                 many blocks of four warps (one block per SM holds the SM
+ *                 alone when the count is at most the SM count).  Its warps
+ *                 run the pre-deferred cells cooperatively, then the
+ *                 cost-ordered cells one per lane with the budget, then the
+ *                 over-budget cells cooperatively as they are published;
+ *                 no second stream (default: the SM count).  0: the
+ *                 two-stream form (PRE_BLOCKS, CELL_BLOCKS, ROUNDS and
+ *                 COOP_BLOCKS apply to it only);
+ *   SMS           (read only) SMs of the context's device. */
 typedef enum ocpx_param {
     OCPX_PARAM_FLASH_BUDGET = 0,
     OCPX_PARAM_COOP_BLOCKS = 1,
@@ -265,7 +275,9 @@ typedef enum ocpx_param {
     OCPX_PARAM_PRE_BLOCKS = 8,
     OCPX_PARAM_CELL_BLOCKS = 9,
     OCPX_PARAM_ROUNDS = 10,
-    OCPX_PARAM_ROUND_GROWTH = 11
+    OCPX_PARAM_ROUND_GROWTH = 11,
+    OCPX_PARAM_FUSED_BLOCKS = 12,
+    OCPX_PARAM_SMS = 13
 } ocpx_param;
 ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value);
 ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value);

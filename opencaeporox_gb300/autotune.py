@@ -3,6 +3,8 @@
 The batched flash has knobs that change only how the work is laid out on
 the GPU, never the results:
 
+- the fused single-kernel form against the two-stream one, and the fused
+  kernel's grid;
 - the per-cell work budget after which a cell's phase equilibrium moves to
   the warp-cooperative kernel;
 - the pre-deferral threshold (cells that were expensive in their last flash
@@ -26,6 +28,7 @@ from __future__ import annotations
 import time
 
 DEFAULT_SPACE = {
+    "fused_blocks": ("sms", 0, 1, 2, 4),   # multiples of the SM count; "sms": the library default
     "flash_budget": (24, 32, 48, 64, 96, 128, 192),
     "predefer": (0, 48, 96, 192, 384),
     "coop_cells": (0, 1216, 4864),
@@ -58,6 +61,9 @@ def tune(ctx, dt: float, slot: int = 0, space: dict | None = None, rounds: int =
     must use the batched variant."""
     sp = dict(DEFAULT_SPACE)
     sp.update(space or {})
+    if "fused_blocks" in sp and sp["fused_blocks"] and sp["fused_blocks"][0] == "sms":
+        n = ctx.get_param("sms")
+        sp["fused_blocks"] = tuple(sorted({v * n for v in sp["fused_blocks"][1:]}, key=lambda v: (v != n, v)))
     point = {k: ctx.get_param(k) for k in sp}
     for k, cands in sp.items():
         if point[k] not in cands:

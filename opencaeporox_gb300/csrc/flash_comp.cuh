@@ -50,13 +50,18 @@ struct DeferRec {
     int cell;
     int ftype_in;
     unsigned lNP;
+    unsigned seq;  // nonzero once the record is complete (lists read while they fill)
 };
 
-// Append-only list of deferred cells (one atomic per deferred cell).
+// Append-only list of deferred cells (one atomic per deferred cell).  With
+// `seq` nonzero the record is published: its fields are written, then, after
+// a fence, its seq, so a reader in the same launch that sees the seq sees the
+// fields (the fused flash consumes the list while it fills).
 struct DeferSink {
     DeferRec* rec;
     unsigned* count;
     int cap;
+    unsigned seq = 0;
     OCPX_HD bool push(int cell, int ftype_in, unsigned lNP) const
     {
 #ifdef __CUDA_ARCH__
@@ -65,6 +70,10 @@ struct DeferSink {
         rec[slot].cell = cell;
         rec[slot].ftype_in = ftype_in;
         rec[slot].lNP = lNP;
+        if (seq) {
+            __threadfence();
+            atomicExch(&rec[slot].seq, seq);
+        }
         return true;
 #else
         (void)cell; (void)ftype_in; (void)lNP;

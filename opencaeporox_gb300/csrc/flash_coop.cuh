@@ -29,6 +29,7 @@ namespace ocpx {
 constexpr unsigned FULL_MASK = 0xffffffffu;
 constexpr int COOP_WARPS = 2;  // warps (cells in flight) per block
 constexpr int EXCL_WARPS = 4;  // warps per block of the SM-exclusive form: one per SM sub-partition
+constexpr int FUSED_WARPS = 4; // warps per block of the fused batched flash
 
 template <int NCM>
 struct CoopSh {

@@ -104,6 +104,88 @@ __global__ void __launch_bounds__(128) k_flash_round(const Model* __restrict__ M
     }
 }
 
+// Fused batched flash: one persistent kernel does what the per-cell kernel
+// and the two cooperative passes do on two streams, so the long cells never
+// compete with the per-cell work for an SM sub-partition's FP64 pipe, and no
+// block placement across streams decides when they start.  Each warp:
+//   1. takes pre-deferred cells, one at a time, and runs their equilibrium
+//      cooperatively (they are the longest chains, so they start first);
+//   2. then takes 32 cost-ordered cells at a time, one per lane, with the
+//      work budget; over-budget cells are published to the late list;
+//   3. then claims late cells in list order, one at a time, cooperatively.
+// A late cell is claimed only once its record is published; a warp that
+// meets an unpublished one stops claiming, and the cell's own publisher,
+// which enters step 3 after publishing, claims it.  So every late cell is
+// run exactly once and no warp ever waits on another.  The records are read
+// through L2 (another record in the same line may be cached in L1 from
+// before it was written).  Counters: ctr[0] pre slots, ctr[1] cell
+// positions, ctr[2] late slots, all zero before the launch; the late list's
+// seq fields are zero before the launch.
+template <int NCM>
+__global__ void __launch_bounds__(FUSED_WARPS * 32, 1) k_flash_fused(const Model* __restrict__ M, BulkView b,
+                                                                const int* __restrict__ order, int budget,
+                                                                const uint8_t* __restrict__ pre,
+                                                                const int* __restrict__ level,
+                                                                const DeferRec* __restrict__ pre_rec,
+                                                                const unsigned* __restrict__ pre_count,
+                                                                PERes* __restrict__ pre_pe, DeferSink late,
+                                                                PERes* __restrict__ late_pe,
+                                                                unsigned* __restrict__ ctr)
+{
+    __shared__ CoopSh<NCM> sh[FUSED_WARPS];
+    const int warp = threadIdx.x >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    // 1. pre-deferred cells
+    const unsigned npre = pre_count ? min(*pre_count, (unsigned)late.cap) : 0u;
+    for (;;) {
+        unsigned slot = 0;
+        if (lane == 0) slot = atomicAdd(&ctr[0], 1u);
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (slot >= npre) break;
+        CoopPE<NCM> pe(sh[warp], M->comp);
+        pe.run(*M, b, pre_rec[slot], pre_pe[slot]);
+        __syncwarp();
+    }
+    // 2. cost-ordered cells, one per lane
+    for (;;) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(&ctr[1], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= (unsigned)b.nb) break;
+        const unsigned p = base + lane;
+        if (p < (unsigned)b.nb) flash_budget_cell<NCM>(M, b, order[p], budget, late, pre, level);
+        __syncwarp();
+    }
+    // 3. late cells, in list order, once published
+    for (;;) {
+        unsigned got = 0xffffffffu;
+        if (lane == 0) {
+            volatile unsigned* vctr = &ctr[2];
+            volatile unsigned* vcount = late.count;
+            unsigned cur = *vctr;
+            for (;;) {
+                const unsigned n = min(*vcount, (unsigned)late.cap);
+                if (cur >= n) break;
+                if (*(volatile unsigned*)&late.rec[cur].seq != late.seq) break;
+                const unsigned prev = atomicCAS(&ctr[2], cur, cur + 1u);
+                if (prev == cur) { got = cur; break; }
+                cur = prev;
+            }
+        }
+        got = __shfl_sync(0xffffffffu, got, 0);
+        if (got == 0xffffffffu) break;
+        __threadfence();
+        DeferRec r;
+        r.cell = __ldcg(&late.rec[got].cell);
+        r.ftype_in = __ldcg(&late.rec[got].ftype_in);
+        r.lNP = __ldcg(&late.rec[got].lNP);
+        r.seq = late.seq;
+        CoopPE<NCM> pe(sh[warp], M->comp);
+        pe.run(*M, b, r, late_pe[got]);
+        __syncwarp();
+    }
+}
+
 // Step 2: the phase equilibrium of every deferred cell on a whole warp
 // (flash_coop.cuh).  Persistent: each warp takes the next list slot from the
 // counter `next` (zero before the launch) until the list is exhausted, so a
@@ -175,6 +257,18 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
                                                            fb.cell_blocks > 0 ? fb.cell_next : nullptr);
         break;
     }
+    case 4: {
+        // fused: pre list (rin, rin_count, pe_pre) and late list (rec, count, pe)
+        DeferSink late{fb.rec, fb.count, fb.cap};
+        late.seq = 1;
+        cudaLaunchConfig_t cfg = {};
+        cfg.stream = s;
+        cfg.gridDim = dim3(fb.cell_blocks);
+        cfg.blockDim = dim3(FUSED_WARPS * 32);
+        cfg.dynamicSmemBytes = fb.excl_blocks ? fb.excl_smem_fused : 0;
+        return cudaLaunchKernelEx(&cfg, k_flash_fused<OCPX_NCM>, dm, b, order, fb.budget, fb.pre, fb.level, fb.rin,
+                                  fb.rin_count, fb.pe_pre, late, fb.pe, fb.cell_next);
+    }
     case 3: {
         // re-budgeting round: from list (rin, rin_count) into (rec, count)
         const DeferSink sink{fb.rec, fb.count, fb.cap};
@@ -233,6 +327,17 @@ cudaError_t OCPX_CAT(setup_flash_batched_, OCPX_NCM)(int* excl_smem)
         e = cudaFuncSetAttribute(k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared);
     *excl_smem = dyn;
+    if (e != cudaSuccess) return e;
+    // the fused kernel, when it holds an SM alone (one block per SM)
+    cudaFuncAttributes ff{};
+    e = cudaFuncGetAttributes(&ff, k_flash_fused<OCPX_NCM>);
+    if (e != cudaSuccess) return e;
+    const int dynf = optin > (int)ff.sharedSizeBytes ? optin - (int)ff.sharedSizeBytes : 0;
+    e = cudaFuncSetAttribute(k_flash_fused<OCPX_NCM>, cudaFuncAttributeMaxDynamicSharedMemorySize, dynf);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_flash_fused<OCPX_NCM>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+    excl_smem[1] = dynf;
     return e;
 }
 

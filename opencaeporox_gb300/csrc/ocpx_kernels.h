@@ -34,14 +34,19 @@ struct FlashBatch {
     int cell_blocks;     // > 0: part 0 runs as this many persistent blocks taking 32 cells per warp
     unsigned* cell_next; // their position counter (zero before the launch); part 3's too
     unsigned* coop_next; // slot counter of part 1 (zero before the launch)
-    const DeferRec* rin;        // part 3: input list and its count
+    const DeferRec* rin;        // part 3: input list and its count; part 4: the pre-deferred list
     const unsigned* rin_count;
     long long mult;             // part 3: budget multiplier of the round
+    PERes* pe_pre;              // part 4: results of the pre-deferred list
+    int excl_smem_fused;        // part 4: dynamic shared memory that makes a fused block SM-exclusive
 };
-// once per device: configure the SM-exclusive cooperative kernel of capacity ncm
+// once per device: configure the SM-exclusive kernels of capacity ncm;
+// excl_smem[0]: the cooperative kernel's dynamic shared memory, [1]: the fused kernel's
 cudaError_t setup_flash_batched(int ncm, int* excl_smem);
 // part 0: budgeted thread-per-cell flash, 1: cooperative equilibrium, 2: finish deferred cells,
-// 3: re-budgeting round over a deferral list (thread per cell)
+// 3: re-budgeting round over a deferral list (thread per cell), 4: the fused kernel (pre list
+// rin / pe_pre, cost order, late list rec / pe; cell_blocks blocks; counters cell_next[0..2];
+// SM-exclusive blocks when excl_blocks is nonzero)
 cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, const int* order,
                                  const FlashBatch& fb, int part, cudaStream_t s);
 // Cells grouped by flash path (two-phase, one-phase, skip-flagged) and, within

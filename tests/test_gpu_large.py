@@ -59,14 +59,22 @@ def test_large_batched_matches_plain(case):
         assert np.array_equal(a[k], b[k], equal_nan=True), k
 
 
-def test_large_batched_launch_forms_match_plain(case):
-    """Re-budgeting rounds, the persistent per-cell kernel and SM-exclusive
-    pre-deferral blocks at 200,000 cells: the flash stays bit-identical."""
+@pytest.mark.parametrize("params", [dict(fused_blocks=0, flash_budget=8, rounds=3, round_growth=4, cell_blocks=152,
+                                         pre_blocks=38),
+                                    dict(fused_blocks=0),
+                                    dict(fused_blocks=152, flash_budget=8, coop_cells=0),
+                                    dict(fused_blocks=608, flash_budget=24)],
+                         ids=["rounds+persistent+exclusive", "two-stream", "fused-exclusive", "fused-shared"])
+def test_large_batched_launch_forms_match_plain(case, params):
+    """Re-budgeting rounds, the persistent per-cell kernel, SM-exclusive
+    pre-deferral blocks and the fused kernel at 200,000 cells: the flash
+    stays bit-identical."""
     _, _, out = case
     ctx = out[1]["ctx"]
-    keep = {k: ctx.get_param(k) for k in ("flash_budget", "rounds", "round_growth", "cell_blocks", "pre_blocks")}
+    keep = {k: ctx.get_param(k) for k in ("flash_budget", "rounds", "round_growth", "cell_blocks", "pre_blocks",
+                                          "fused_blocks", "coop_cells")}
     try:
-        for k, v in dict(flash_budget=8, rounds=3, round_growth=4, cell_blocks=152, pre_blocks=38).items():
+        for k, v in params.items():
             ctx.set_param(k, v)
         ctx.checkpoint(0, restore=True)
         ctx.update_property()

@@ -159,12 +159,21 @@ def test_batched_variant_against_reference(gpu_lib):
         check_update(ctx, fx, it, model, grid)
 
 
+TWO_STREAM = dict(fused_blocks=0)
 BATCH_CASES = [
-    dict(flash_budget=0), dict(flash_budget=3), dict(), dict(coop_cells=8), dict(coop_cells=0),
-    dict(coop_cells=0, predefer=1, pre_blocks=0), dict(coop_cells=0, predefer=1, pre_blocks=3),
-    dict(flash_budget=3, coop_cells=0, cell_blocks=2),
-    dict(flash_budget=3, coop_cells=0, rounds=2, round_growth=2),
-    dict(flash_budget=1, coop_cells=0, predefer=0, rounds=8, round_growth=2, cell_blocks=1),
+    # the default (fused) form
+    dict(flash_budget=0), dict(flash_budget=3), dict(), dict(coop_cells=8), dict(coop_cells=0, predefer=1),
+    dict(fused_blocks=2), dict(fused_blocks=2, flash_budget=0), dict(fused_blocks=2, flash_budget=3),
+    dict(fused_blocks=3, flash_budget=3, coop_cells=0, predefer=1),
+    dict(fused_blocks=1, flash_budget=1, coop_cells=0, predefer=0),
+    dict(fused_blocks=400, flash_budget=3, coop_cells=0, predefer=1),
+    # the two-stream form
+    dict(TWO_STREAM, flash_budget=0), dict(TWO_STREAM, flash_budget=3), dict(TWO_STREAM),
+    dict(TWO_STREAM, coop_cells=8), dict(TWO_STREAM, coop_cells=0),
+    dict(TWO_STREAM, coop_cells=0, predefer=1, pre_blocks=0), dict(TWO_STREAM, coop_cells=0, predefer=1, pre_blocks=3),
+    dict(TWO_STREAM, flash_budget=3, coop_cells=0, cell_blocks=2),
+    dict(TWO_STREAM, flash_budget=3, coop_cells=0, rounds=2, round_growth=2),
+    dict(TWO_STREAM, flash_budget=1, coop_cells=0, predefer=0, rounds=8, round_growth=2, cell_blocks=1),
 ]
 
 
@@ -178,7 +187,10 @@ def test_batched_variant_matches_plain(gpu_lib, name, params):
     sends the cells that needed an equilibrium last time to the second
     stream, on shared-SM or SM-exclusive blocks; persistent blocks run the
     per-cell kernel 32 cells per warp at a time; re-budgeting rounds rerun
-    the over-budget cells with growing budgets before the cooperative pass."""
+    the over-budget cells with growing budgets before the cooperative pass;
+    the fused kernel (SM-exclusive blocks, one to three of them, or 400
+    blocks that share SMs) consumes the over-budget cells while they are
+    being published."""
     budget = params.get("flash_budget")
     predefer = params.get("predefer")
     fx = P.load_fixture(name)

@@ -283,7 +283,8 @@ def fp64_peak(device=0):
 # algorithmic work in another order (profiles/k_flash_comp_comp6_36k.md).
 FLASH_FP64_FLOP_PER_CELL = (2 * 223408633 + 121682495 + 142721273) / 36000
 # DRAM bytes (read + write) of that launch, from the same capture.
-FLASH_DRAM_BYTES = 107259392 + 173581568
+FLASH_DRAM_BYTES = 107259392 + 173581568        # two-stream form: budgeted + cooperative kernels (ncu)
+FLASH_DRAM_BYTES_FUSED = 155323904 + 250230016  # k_flash_fused<6> on this step (ncu, one launch)
 
 
 def assembly_bytes(nb, nconn, nc, nnzb):
@@ -555,7 +556,7 @@ def main():
     roof = {"kernel": ("k_flash_fused + k_flash_post" if fused else "k_flash_budget + k_flash_pe_coop + k_flash_post")
                       + " (flash stage of the batched step)", "bound": "fp64", "unit": "TFLOP/s",
             "peak": fp64, "peak_source": "measured (DFMA-chain probe of this library, best of 3)",
-            "achieved": None, "frac": None, "traffic": FLASH_DRAM_BYTES}
+            "achieved": None, "frac": None, "traffic": FLASH_DRAM_BYTES_FUSED if fused else FLASH_DRAM_BYTES}
     if FLASH_FP64_FLOP_PER_CELL:
         roof["achieved"] = FLASH_FP64_FLOP_PER_CELL * nb / (flash_ms * 1e-3) / 1e12
         roof["frac"] = roof["achieved"] / fp64

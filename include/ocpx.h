@@ -259,7 +259,8 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *                 run the pre-deferred cells cooperatively, then the
  *                 cost-ordered cells one per lane with the budget, then the
  *                 over-budget cells cooperatively as they are published;
- *                 no second stream (default: the SM count).  0: the
+ *                 no second stream (default: the SM count below 131,072
+ *                 cells, four times it from there on).  0: the
  *                 two-stream form (PRE_BLOCKS, CELL_BLOCKS, ROUNDS and
  *                 COOP_BLOCKS apply to it only);
  *   SMS           (read only) SMs of the context's device. */

@@ -28,7 +28,7 @@ from __future__ import annotations
 import time
 
 DEFAULT_SPACE = {
-    "fused_blocks": ("sms", 0, 1, 2, 4),   # multiples of the SM count; "sms": the library default
+    "fused_blocks": ("sms", 0, 1, 2, 4),   # multiples of the SM count ("sms" marks the form)
     "flash_budget": (24, 32, 48, 64, 96, 128, 192),
     "predefer": (0, 48, 96, 192, 384),
     "coop_cells": (0, 1216, 4864),
@@ -62,8 +62,9 @@ def tune(ctx, dt: float, slot: int = 0, space: dict | None = None, rounds: int =
     sp = dict(DEFAULT_SPACE)
     sp.update(space or {})
     if "fused_blocks" in sp and sp["fused_blocks"] and sp["fused_blocks"][0] == "sms":
-        n = ctx.get_param("sms")
-        sp["fused_blocks"] = tuple(sorted({v * n for v in sp["fused_blocks"][1:]}, key=lambda v: (v != n, v)))
+        # the context's current grid first, so it stays unless another point is faster
+        n, cur = ctx.get_param("sms"), ctx.get_param("fused_blocks")
+        sp["fused_blocks"] = tuple(sorted({v * n for v in sp["fused_blocks"][1:]} | {cur}, key=lambda v: (v != cur, v)))
     point = {k: ctx.get_param(k) for k in sp}
     for k, cands in sp.items():
         if point[k] not in cands:

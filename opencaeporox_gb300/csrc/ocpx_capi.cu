@@ -468,10 +468,13 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     ctx->coop_blocks = sms * 4;
     ctx->sms = sms;
-    // the fused batched flash, one block of four warps per SM (measured: 36,000
-    // cells 15.0 ms per step against 16.8 ms for the tuned two-stream form;
-    // 250,000 cells 123 ms against 161 ms)
-    ctx->fused_blocks = sms;
+    // the fused batched flash: one block of four warps per SM on small grids,
+    // where the longest cells set the time (36,000 cells: 15.0 ms per step
+    // against 16.8 ms for the tuned two-stream form); four per SM on large
+    // ones, where the per-lane work dominates and more warps hide the
+    // per-thread frames' memory latency (4,000,000 cells: 1,289 ms against
+    // 1,484 ms with one block per SM and 1,439 ms two-stream)
+    ctx->fused_blocks = nb < 131072 ? sms : 4 * sms;
     *out = ctx;
     return OCPX_OK;
 }

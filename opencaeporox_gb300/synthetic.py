@@ -221,3 +221,31 @@ def flash_stress_cells(ctx_factory, n, ncomp, seed, near_frac=0.2, p_range=(50.0
         finally:
             ctx.close()
     return P, Ni
+
+
+def dipping_corner_point(nx, ny, nz, dxy, dz, top, dip_x_deg, dip_y_deg, pillar_tilt=0.0, seed=0):
+    """A corner-point grid (Eclipse COORD and ZCORN arrays) of nz layers of
+    thickness dz over an nx x ny plan with spacing dxy, its top dipping by
+    dip_x_deg / dip_y_deg.  Each pillar leans by a seeded slope within
+    +-pillar_tilt in x and y (non-vertical pillars).  Layer boundaries are
+    shared by neighbouring cells, so faces match (no faults)."""
+    rng = np.random.default_rng(seed)
+    X = np.arange(nx + 1) * float(dxy)
+    Y = np.arange(ny + 1) * float(dxy)
+    XX, YY = np.meshgrid(X, Y)                     # [J][I]
+    ztop = top + np.tan(np.deg2rad(dip_x_deg)) * XX + np.tan(np.deg2rad(dip_y_deg)) * YY
+    zbot = ztop + nz * dz + 10.0
+    sx = rng.uniform(-pillar_tilt, pillar_tilt, XX.shape)
+    sy = rng.uniform(-pillar_tilt, pillar_tilt, XX.shape)
+    coord = np.empty((ny + 1, nx + 1, 2, 3))
+    coord[:, :, 0, 0], coord[:, :, 0, 1], coord[:, :, 0, 2] = XX, YY, ztop
+    coord[:, :, 1, 0] = XX + sx * (zbot - ztop)
+    coord[:, :, 1, 1] = YY + sy * (zbot - ztop)
+    coord[:, :, 1, 2] = zbot
+    zb = ztop[None, :, :] + dz * np.arange(nz + 1)[:, None, None]   # [K][J][I] layer boundaries
+    zc = np.empty((nz, 2, ny, 2, nx, 2))
+    for tb in range(2):
+        for fb in range(2):
+            for lr in range(2):
+                zc[:, tb, :, fb, :, lr] = zb[tb:nz + tb, fb:ny + fb, lr:nx + lr]
+    return coord.ravel(), zc.ravel()

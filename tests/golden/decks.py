@@ -299,9 +299,35 @@ def comp_cells(nx, ny, nz, ncomp, seed, porosity=0.2, dxy=20.0, dz=5.0,
     return p, np.concatenate([ni, nw[:, None]], axis=1)
 
 
+def corner_grid_block(nx, ny, nz, coord, zcorn, poro, kx, ky, kz):
+    """DIMENS + COORD/ZCORN (Eclipse order) + rock arrays of a corner-point grid."""
+    return f"""DIMENS
+{nx} {ny} {nz} /
+
+COORD
+{_fmt(coord)}
+/
+ZCORN
+{_fmt(zcorn)}
+/
+PORO
+{_fmt(poro)}
+/
+PERMX
+{_fmt(kx)}
+/
+PERMY
+{_fmt(ky)}
+/
+PERMZ
+{_fmt(kz)}
+/
+"""
+
+
 def comp_deck(nx, ny, nz, ncomp, seed, perm=50.0, porosity=0.2, dxy=20.0, dz=5.0,
               temp_k=345.0, p_range=(100.0, 300.0), alpha=2.0, tsteps=(0.01, 0.01),
-              wells=True, smooth=False):
+              wells=True, smooth=False, grid_text=None):
     """Compositional PR-EoS FIM deck with a PTN (pressure + moles) start.
 
     Returns ``(deck_text, ni)``: the per-cell moles ``ni`` (cells x (ncomp+1),
@@ -313,8 +339,8 @@ def comp_deck(nx, ny, nz, ncomp, seed, perm=50.0, porosity=0.2, dxy=20.0, dz=5.0
     n = nx * ny * nz
     p, ni = comp_cells(nx, ny, nz, ncomp, seed, porosity, dxy, dz, p_range, alpha, temp_k, smooth)
     swof, sgof = corey_tables()
-    grid = _grid_block(nx, ny, nz, dxy, dxy, [dz] * nz, 2000.0, np.full(n, porosity),
-                       np.full(n, perm), np.full(n, perm))
+    grid = grid_text or _grid_block(nx, ny, nz, dxy, dxy, [dz] * nz, 2000.0, np.full(n, porosity),
+                                    np.full(n, perm), np.full(n, perm))
     init = ["INITPTN0", "PRESSURE", _fmt(p), "/"]
     for j in range(3):
         init += [f"PHASEP-{j}", _fmt(p), "/"]

@@ -168,11 +168,40 @@ def _comp_fim(nx, ny, nz, ncomp, seed, name, max_iters):
     return run_fim(text, name, max_iters, ni=ni, calibrate=True)
 
 
+def corner_fixture(nx=6, ny=5, nz=4, seed=7):
+    """The reference's corner-point ingest (COORD / ZCORN) on a dipping grid
+    with leaning pillars: the model dump (cells, connections, half areas,
+    transmissibilities) and the inputs that produced it."""
+    sys.path.insert(0, REPO)
+    from opencaeporox_gb300 import synthetic
+    coord, zcorn = synthetic.dipping_corner_point(nx, ny, nz, 20.0, 3.0, 2000.0, 4.0, -3.0, 0.05, seed=seed)
+    n = nx * ny * nz
+    rng = np.random.default_rng(seed)
+    kx = np.exp(rng.normal(np.log(100.0), 1.0, n))
+    ky = kx * rng.uniform(0.5, 1.5, n)
+    kz = 0.1 * kx
+    poro = rng.uniform(0.15, 0.3, n)
+    text = decks.corner_grid_block(nx, ny, nz, coord, zcorn, poro, kx, ky, kz)
+    ni, deck_text = decks.comp_deck(nx, ny, nz, 3, seed, grid_text=text)
+    with tempfile.TemporaryDirectory() as tmp:
+        deck = os.path.join(tmp, "cpg.data")
+        with open(deck, "w") as f:
+            f.write(deck_text)
+        ni.astype("<f8").tofile(deck + ".ptn_ni")
+        out = os.path.join(tmp, "out")
+        subprocess.run([DUMP, "fim", deck, out, "0"], check=True, stdout=subprocess.DEVNULL)
+        data = {f"model/{k}": v for k, v in load_dir(os.path.join(out, "model")).items()}
+    data.update({"input/dims": np.array([nx, ny, nz]), "input/coord": coord, "input/zcorn": zcorn,
+                 "input/kx": kx, "input/ky": ky, "input/kz": kz, "input/poro": poro})
+    return data
+
+
 FIXTURES = {
     "bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12),
     "comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4),
     "comp8_6x6x4": lambda: _comp_fim(6, 6, 4, 8, 4, "c8", 4),
     "flash10": lambda: run_flash(10, 1024, 3),
+    "cpg_6x5x4": corner_fixture,
 }
 
 

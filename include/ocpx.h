@@ -22,6 +22,7 @@
  *   ocpx_newton_update      IsoT_FIM::GetSolution, bulk part
  *                           (src/IsoThermalMethod.cpp:1282-1418)
  *   ocpx_update_last_step   IsoT_FIM::UpdateLastTimeStep, bulk part (:1473-1517)
+ *   ocpx_linsolve           the linear solve of the Newton system (bulk rows)
  *   ocpx_nr_*, ocpx_step_max_change, ocpx_next_time_step
  *                           Newton and time-step control (OCPNRsuite,
  *                           ControlNR, ControlTime), bulk part; see below
@@ -413,6 +414,29 @@ ocpx_status ocpx_nr_check_converge(ocpx_ctx* ctx, const ocpx_nr_control* c, int*
 /* next_dt: the length of the next time step (clamped to the end of the
  * current report interval, end_time); predict_dt: the same before that clamp */
 ocpx_status ocpx_next_time_step(ocpx_ctx* ctx, const ocpx_nr_control* c, double* next_dt, double* predict_dt);
+
+/* Linear solve of the Newton system on the device: J u = rhs, J the bulk
+ * Jacobian of the last ocpx_assemble and rhs the residual of the last
+ * ocpx_calres as the reference passes it to its solver (LinearSystem::CopyRhs
+ * of the negated residual, src/IsoThermalMethod.cpp:742-752).  The reference
+ * hands this system to an external package (FASP, PETSc or PARDISO,
+ * src/LinearSystem.cpp:35-89); here BiCGStab with right block-Jacobi
+ * preconditioning, from u = 0, until |rhs - J u| <= tol |rhs| or maxit
+ * iterations (the norm is checked every 10).  Bulk rows only: a host that
+ * couples wells solves the full system itself.  The solution stays on the
+ * device for ocpx_newton_update_device and is copied to u_host (nb*(nc+1))
+ * when that is not NULL.  The first call allocates the solver's work space
+ * (about 8 vectors and the inverted diagonal blocks).  Synchronizes. */
+typedef struct ocpx_solve_report {
+    int iterations;
+    double relres;   /* of the recursively updated residual */
+    int converged;
+    int breakdown;   /* 1: BiCGStab breakdown, 2: a singular diagonal block */
+} ocpx_solve_report;
+ocpx_status ocpx_linsolve(ocpx_ctx* ctx, double tol, int maxit, double* u_host, ocpx_solve_report* rep);
+/* IsoT_FIM::GetSolution, bulk part, with the update the last ocpx_linsolve
+ * left on the device. */
+ocpx_status ocpx_newton_update_device(ocpx_ctx* ctx, double dSmax);
 
 /* Stream the context launches on (a cudaStream_t), for callers that time or
  * order work around the library. */

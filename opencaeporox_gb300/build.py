@@ -37,7 +37,8 @@ def common_flags():
 
 def units():
     out = [("k_fim.cu", [], "k_fim.o"), ("ocpx_capi.cu", [], "ocpx_capi.o"), ("k_probe.cu", [], "k_probe.o"),
-           ("k_noalloc.cu", [], "k_noalloc.o"), ("k_nrctl.cu", [], "k_nrctl.o")]
+           ("k_noalloc.cu", [], "k_noalloc.o"), ("k_nrctl.cu", [], "k_nrctl.o"),
+           ("k_linsolve.cu", [], "k_linsolve.o")]
     for c in NCM_CAPS:
         out.append(("k_flash_comp.cu", [f"-DOCPX_NCM={c}"], f"k_flash_comp_{c}.o"))
     return out

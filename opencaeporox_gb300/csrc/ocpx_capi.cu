@@ -160,6 +160,7 @@ struct ocpx_ctx {
     double* nr_res0 = nullptr;      // initial relative residual of the time step
     int* nr_state = nullptr;        // last CheckConverge state
     double* nr_dt = nullptr;        // [2] next dt, predicted dt
+    double* ls_scratch = nullptr;   // linear solver work space (allocated by the first ocpx_linsolve)
     double* bmat = nullptr;         // per-connection Jacobian blocks (2 per connection)
     uint32_t* jac_rowptr = nullptr;
     uint32_t* jac_slot = nullptr;   // [2][nconn]: block index of connection c in row bId / row eId
@@ -489,6 +490,7 @@ void ocpx_destroy(ocpx_ctx* ctx)
     for (auto& m : ctx->marks) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
     for (auto e : ctx->free_events) cudaEventDestroy(e);
     if (ctx->arena) cudaFree(ctx->arena);
+    if (ctx->ls_scratch) cudaFree(ctx->ls_scratch);
     if (ctx->d_model) cudaFree(ctx->d_model);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     if (ctx->h_norm) cudaFreeHost(ctx->h_norm);
@@ -762,6 +764,35 @@ ocpx_status ocpx_assemble(ocpx_ctx* ctx, double dt)
 {
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
     return enqueue_assemble(ctx, dt);
+}
+
+ocpx_status ocpx_linsolve(ocpx_ctx* ctx, double tol, int maxit, double* u_host, ocpx_solve_report* rep)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    if (!(tol > 0) || maxit < 1) return fail(OCPX_INVALID_ARG, "tol must be > 0 and maxit >= 1");
+    const int dim = ctx->nc + 1;
+    if (!ctx->ls_scratch)
+        OCPX_CUDA(cudaMalloc(&ctx->ls_scratch, sizeof(double) * linsolve_scratch_doubles(ctx->nb, dim)));
+    LinsolveResult r{};
+    OCPX_CUDA(linsolve(ctx->jac_rowptr, ctx->jac_col, ctx->jac_val, ctx->nb, dim, ctx->res, ctx->u, ctx->ls_scratch,
+                       tol, maxit, 10, &r, &ctx->launches, ctx->stream));
+    if (u_host) {
+        OCPX_CUDA(cudaMemcpyAsync(u_host, ctx->u, sizeof(double) * (size_t)ctx->nb * dim, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+        OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    if (rep) *rep = ocpx_solve_report{r.iterations, r.relres, r.converged, r.breakdown};
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_newton_update_device(ocpx_ctx* ctx, double dSmax)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    const int mk = ctx->stage_begin(8);
+    OCPX_CUDA(launch_newton_update(ctx->b, ctx->u, dSmax, ctx->block_cell, ctx->stream));
+    ctx->stage_end(mk);
+    ctx->launches++;
+    return OCPX_OK;
 }
 
 ocpx_status ocpx_newton_update(ocpx_ctx* ctx, const double* u_host, double dSmax)

@@ -77,6 +77,21 @@ cudaError_t launch_nr_converge(const NRControl& c, const double* nr5, const RowN
                                int* state, cudaStream_t s);
 cudaError_t launch_next_dt(const NRControl& c, const double* ts5, double* out2, cudaStream_t s);
 
+// Linear solve of J u = rhs on the device (k_linsolve.cu): BiCGStab with right
+// block-Jacobi preconditioning, x from zero; scratch holds
+// linsolve_scratch_doubles(nb, dim) doubles.  The residual norm is read every
+// check_every iterations.
+struct LinsolveResult {
+    int iterations;
+    double relres;   // |rhs - J x| / |rhs| of the recursively updated residual
+    int converged;
+    int breakdown;   // 1: BiCGStab breakdown, 2: singular diagonal block
+};
+size_t linsolve_scratch_doubles(int nb, int dim);
+cudaError_t linsolve(const uint32_t* rowptr, const uint32_t* col, const double* val, int nb, int dim,
+                     const double* rhs, double* x, double* scratch, double tol, int maxit, int check_every,
+                     LinsolveResult* res, uint64_t* launches, cudaStream_t s);
+
 cudaError_t launch_flash_bo(const Model* dm, const BulkView& b, int block, cudaStream_t s);
 cudaError_t launch_krpc_rock(const Model* dm, const BulkView& b, int block, cudaStream_t s);
 cudaError_t launch_check(const BulkView& b, uint32_t* flags, int block, cudaStream_t s);

@@ -98,6 +98,11 @@ class ChangeMax(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class SolveReport(C.Structure):
+    """ocpx_solve_report."""
+    _fields_ = [("iterations", C.c_int), ("relres", C.c_double), ("converged", C.c_int), ("breakdown", C.c_int)]
+
+
 class NRControl(C.Structure):
     """ocpx_nr_control: ControlNRParam / ControlTimeParam values, the time step
     that ends, its Newton iterations, and the host-owned (well) terms."""
@@ -123,7 +128,7 @@ EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy",
            "ocpx_profile_enable", "ocpx_profile_read", "ocpx_checkpoint", "ocpx_measure_fp64_tflops",
            "ocpx_stream", "ocpx_launch_count", "ocpx_set_param", "ocpx_get_param", "ocpx_adjoint",
            "ocpx_nr_init_step", "ocpx_nr_max_change", "ocpx_step_max_change", "ocpx_nr_check_converge",
-           "ocpx_next_time_step"]
+           "ocpx_next_time_step", "ocpx_linsolve", "ocpx_newton_update_device"]
 
 PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3, "predefer": 4, "coop_cells": 5,
           "predeferred": 6, "level": 7, "pre_blocks": 8,
@@ -168,6 +173,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.ocpx_adjoint.restype = C.c_int
     lib.ocpx_set_param.argtypes = [P, C.c_int, C.c_longlong]
     lib.ocpx_nr_init_step.argtypes = [P]
+    lib.ocpx_linsolve.argtypes = [P, C.c_double, C.c_int, P, C.POINTER(SolveReport)]
+    lib.ocpx_newton_update_device.argtypes = [P, C.c_double]
     lib.ocpx_nr_max_change.argtypes = [P, C.POINTER(ChangeMax)]
     lib.ocpx_step_max_change.argtypes = [P, C.POINTER(ChangeMax)]
     lib.ocpx_nr_check_converge.argtypes = [P, C.POINTER(NRControl), C.POINTER(C.c_int)]
@@ -466,6 +473,20 @@ class FimContext:
         ptr = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
         _check(self.lib.ocpx_adjoint(self.h, ptr(lam), ptr(out_jt), ptr(out_t), ptr(out_p)))
         return out_jt, out_t, out_p
+
+    # --- linear solve of the Newton system (bulk rows, on the device)
+    def linsolve(self, tol: float = 1e-10, maxit: int = 2000, copy_out: bool = True):
+        """BiCGStab with block-Jacobi preconditioning of J u = rhs (the last
+        assembled Jacobian and residual); returns (u or None, report dict)."""
+        rep = SolveReport()
+        u = np.empty(self.nb * (self.nc + 1)) if copy_out else None
+        _check(self.lib.ocpx_linsolve(self.h, float(tol), int(maxit),
+                                      None if u is None else u.ctypes.data_as(C.c_void_p), C.byref(rep)))
+        return u, {k: getattr(rep, k) for k, _ in rep._fields_}
+
+    def newton_update_device(self, dSmax: float):
+        """GetSolution with the update the last linsolve left on the device."""
+        _check(self.lib.ocpx_newton_update_device(self.h, float(dSmax)))
 
     # --- Newton-iteration and time-step control (bulk part, on the device)
     def nr_init_step(self):

@@ -515,7 +515,7 @@ def main():
     rt.rt.cudaSetDevice(local)
     if args.workload != "fim":
         if rank == 0:
-            fn = flash_stress if args.workload == "flash-stress" else large_step
+            fn = {"flash-stress": flash_stress, "large": large_step}[args.workload]
             print(json.dumps(fn(args, rt, local)))
         return
     ranks = Ranks(world)

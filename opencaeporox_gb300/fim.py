@@ -494,8 +494,12 @@ class FimContext:
         state; the initial residual norm := that of the last cal_res."""
         _check(self.lib.ocpx_nr_init_step(self.h))
 
-    def nr_max_change(self) -> dict:
-        """OCPNRsuite::CalMaxChangeNR (bulk): signed maxima since the last call."""
+    def nr_max_change(self, read: bool = True):
+        """OCPNRsuite::CalMaxChangeNR (bulk): signed maxima since the last call
+        (left on the device, without a synchronisation, when read is False)."""
+        if not read:
+            _check(self.lib.ocpx_nr_max_change(self.h, None))
+            return None
         out = ChangeMax()
         _check(self.lib.ocpx_nr_max_change(self.h, C.byref(out)))
         return out.as_dict()

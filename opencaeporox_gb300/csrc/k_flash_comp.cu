@@ -110,13 +110,15 @@ __global__ void __launch_bounds__(128) k_flash_round(const Model* __restrict__ M
 // block placement across streams decides when they start.  Each warp:
 //   1. takes pre-deferred cells, one at a time, and runs their equilibrium
 //      cooperatively (they are the longest chains, so they start first);
-//   2. then takes 32 cost-ordered cells at a time, one per lane, with the
-//      work budget; over-budget cells are published to the late list;
-//   3. then claims late cells in list order, one at a time, cooperatively.
-// A late cell is claimed only once its record is published; a warp that
-// meets an unpublished one stops claiming, and the cell's own publisher,
-// which enters step 3 after publishing, claims it.  So every late cell is
-// run exactly once and no warp ever waits on another.  The records are read
+//   2. then, each time it is free: claims the next over-budget cell if one
+//      is published and runs it cooperatively, else takes 32 cost-ordered
+//      cells, one per lane, with the work budget (over-budget cells are
+//      published to the late list); when both are exhausted it leaves.
+// A late cell is claimed in list order and only once its record is
+// published; a warp that meets an unpublished one takes cells instead or
+// leaves, and the cell's own publisher, which looks for late cells right
+// after publishing, claims it.  So every late cell is run exactly once and
+// no warp ever waits on another.  The records are read
 // through L2 (another record in the same line may be cached in L1 from
 // before it was written).  Counters: ctr[0] pre slots, ctr[1] cell
 // positions, ctr[2] late slots, all zero before the launch; the late list's
@@ -146,17 +148,10 @@ __global__ void __launch_bounds__(FUSED_WARPS * 32, 1) k_flash_fused(const Model
         pe.run(*M, b, pre_rec[slot], pre_pe[slot]);
         __syncwarp();
     }
-    // 2. cost-ordered cells, one per lane
-    for (;;) {
-        unsigned base = 0;
-        if (lane == 0) base = atomicAdd(&ctr[1], 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= (unsigned)b.nb) break;
-        const unsigned p = base + lane;
-        if (p < (unsigned)b.nb) flash_budget_cell<NCM>(M, b, order[p], budget, late, pre, level);
-        __syncwarp();
-    }
-    // 3. late cells, in list order, once published
+    // 2. over-budget cells as soon as they are published, else the next 32
+    // cost-ordered cells (one per lane): a long cell that the budget caught
+    // starts its cooperative run at once instead of after the whole order
+    bool cells_left = true;
     for (;;) {
         unsigned got = 0xffffffffu;
         if (lane == 0) {
@@ -173,15 +168,28 @@ __global__ void __launch_bounds__(FUSED_WARPS * 32, 1) k_flash_fused(const Model
             }
         }
         got = __shfl_sync(0xffffffffu, got, 0);
-        if (got == 0xffffffffu) break;
-        __threadfence();
-        DeferRec r;
-        r.cell = __ldcg(&late.rec[got].cell);
-        r.ftype_in = __ldcg(&late.rec[got].ftype_in);
-        r.lNP = __ldcg(&late.rec[got].lNP);
-        r.seq = late.seq;
-        CoopPE<NCM> pe(sh[warp], M->comp);
-        pe.run(*M, b, r, late_pe[got]);
+        if (got != 0xffffffffu) {
+            __threadfence();
+            DeferRec r;
+            r.cell = __ldcg(&late.rec[got].cell);
+            r.ftype_in = __ldcg(&late.rec[got].ftype_in);
+            r.lNP = __ldcg(&late.rec[got].lNP);
+            r.seq = late.seq;
+            CoopPE<NCM> pe(sh[warp], M->comp);
+            pe.run(*M, b, r, late_pe[got]);
+            __syncwarp();
+            continue;
+        }
+        if (!cells_left) break;
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(&ctr[1], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= (unsigned)b.nb) {
+            cells_left = false;  // one more look for over-budget cells, then leave
+            continue;
+        }
+        const unsigned p = base + lane;
+        if (p < (unsigned)b.nb) flash_budget_cell<NCM>(M, b, order[p], budget, late, pre, level);
         __syncwarp();
     }
 }

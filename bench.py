@@ -342,7 +342,8 @@ def flash_stress(args, rt, local):
             # tune on the flash stage (the step has no connections)
             from opencaeporox_gb300 import autotune
             # each flash of this workload takes seconds: a small candidate set, one round
-            space = {"fused_blocks": ("sms", 0, 1, 2), "flash_budget": (48, 192), "predefer": (0, 192),
+            space = {"fused_blocks": ("sms", 0, 1, 2), "fused_coop_blocks": (0,), "flash_budget": (48, 192),
+                     "predefer": (0, 192),
                      "coop_cells": (608, 1216, 4864), "coop_blocks": (608,), "block_cell": (128,), "pre_blocks": (0,)}
             out["autotune"] = {k: v for k, v in autotune.tune(ctx, DT, slot=0, space=space, rounds=1,
                                                               reps=1).items() if k != "trials"}
@@ -420,7 +421,7 @@ def large_step(args, rt, local):
                             deferred=ctx.get_param("deferred") if variant == 1 else 0,
                             predeferred=ctx.get_param("predeferred") if variant == 1 else 0,
                             level=ctx.get_param("level") if variant == 1 else 0,
-                            params={k: ctx.get_param(k) for k in ("fused_blocks", "flash_budget", "predefer",
+                            params={k: ctx.get_param(k) for k in ("fused_blocks", "fused_coop_blocks", "flash_budget", "predefer",
                                                                  "coop_cells", "coop_blocks", "pre_blocks",
                                                                  "cell_blocks", "block_cell")} if variant == 1 else None)
         print(f"large: variant {variant} step {out[variant]['ms']:.1f} ms", file=sys.stderr, flush=True)
@@ -585,6 +586,7 @@ def main():
                         "block_cell": ctx1.get_param("block_cell"), "predefer": ctx1.get_param("predefer"),
                         "coop_cells": ctx1.get_param("coop_cells"), "pre_blocks": ctx1.get_param("pre_blocks"),
                         "cell_blocks": ctx1.get_param("cell_blocks"), "fused_blocks": ctx1.get_param("fused_blocks"),
+                        "fused_coop_blocks": ctx1.get_param("fused_coop_blocks"),
                         "autotune": None if tuned is None else {k: v for k, v in tuned.items() if k != "trials"}},
             "clocks": ck, "gpu_launches": launches,
             "e2e": {"value": nb / (e2e_ms * 1e-3) * world, "unit": "cells/s", "h2d_bytes_per_step": h2d,

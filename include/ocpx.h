@@ -264,7 +264,17 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *                 cells, four times it from there on).  0: the
  *                 two-stream form (PRE_BLOCKS, CELL_BLOCKS, ROUNDS and
  *                 COOP_BLOCKS apply to it only);
- *   SMS           (read only) SMs of the context's device. */
+ *   SMS           (read only) SMs of the context's device;
+ *   FUSED_COOP_BLOCKS  > 0: the first this many fused blocks run only the
+ *                 cooperative work (pre-deferred cells, then over-budget
+ *                 cells as they are published, waiting for them within a
+ *                 bound), the others the per-lane cells, so the long chains
+ *                 never share an SM with per-lane work.  The launch is then
+ *                 cooperative: FUSED_BLOCKS must fit on the device at once
+ *                 (one block per SM when at most the SM count), and be larger
+ *                 than this value.  -1 (default): 3/8 of FUSED_BLOCKS below
+ *                 131,072 cells when FUSED_BLOCKS is at most the SM count,
+ *                 else 0; reading the parameter gives the value in effect. */
 typedef enum ocpx_param {
     OCPX_PARAM_FLASH_BUDGET = 0,
     OCPX_PARAM_COOP_BLOCKS = 1,
@@ -279,7 +289,8 @@ typedef enum ocpx_param {
     OCPX_PARAM_ROUNDS = 10,
     OCPX_PARAM_ROUND_GROWTH = 11,
     OCPX_PARAM_FUSED_BLOCKS = 12,
-    OCPX_PARAM_SMS = 13
+    OCPX_PARAM_SMS = 13,
+    OCPX_PARAM_FUSED_COOP_BLOCKS = 14
 } ocpx_param;
 ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value);
 ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value);

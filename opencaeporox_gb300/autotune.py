@@ -3,8 +3,8 @@
 The batched flash has knobs that change only how the work is laid out on
 the GPU, never the results:
 
-- the fused single-kernel form against the two-stream one, and the fused
-  kernel's grid;
+- the fused single-kernel form against the two-stream one, the fused
+  kernel's grid, and how many of its blocks run only cooperative work;
 - the per-cell work budget after which a cell's phase equilibrium moves to
   the warp-cooperative kernel;
 - the pre-deferral threshold (cells that were expensive in their last flash
@@ -29,6 +29,7 @@ import time
 
 DEFAULT_SPACE = {
     "fused_blocks": ("sms", 0, 1, 2, 4),   # multiples of the SM count ("sms" marks the form)
+    "fused_coop_blocks": ("sms/8", 0, 2, 3, 4),   # eighths of the SM count
     "flash_budget": (24, 32, 48, 64, 96, 128, 192),
     "predefer": (0, 48, 96, 192, 384),
     "coop_cells": (0, 1216, 4864),
@@ -39,9 +40,15 @@ DEFAULT_SPACE = {
 
 
 def _step_ms(ctx, dt: float, slot: int, reps: int) -> float:
+    from .fim import OcpxError
     ctx.checkpoint(slot, restore=True)
-    ctx.enqueue_step(dt)          # captures the graph of this point
-    ctx.synchronize()
+    try:
+        ctx.enqueue_step(dt)      # captures the graph of this point
+        ctx.synchronize()
+    except OcpxError:
+        # a point the device cannot run (for instance a cooperative grid that
+        # does not fit on it at once): not a candidate
+        return float("inf")
     best = float("inf")
     for _ in range(reps):
         ctx.checkpoint(slot, restore=True)
@@ -61,10 +68,13 @@ def tune(ctx, dt: float, slot: int = 0, space: dict | None = None, rounds: int =
     must use the batched variant."""
     sp = dict(DEFAULT_SPACE)
     sp.update(space or {})
-    if "fused_blocks" in sp and sp["fused_blocks"] and sp["fused_blocks"][0] == "sms":
-        # the context's current grid first, so it stays unless another point is faster
-        n, cur = ctx.get_param("sms"), ctx.get_param("fused_blocks")
-        sp["fused_blocks"] = tuple(sorted({v * n for v in sp["fused_blocks"][1:]} | {cur}, key=lambda v: (v != cur, v)))
+    n = ctx.get_param("sms")
+    for key, unit in (("fused_blocks", "sms"), ("fused_coop_blocks", "sms/8")):
+        if key in sp and sp[key] and sp[key][0] == unit:
+            # the context's current value first, so it stays unless another point is faster
+            cur = ctx.get_param(key)
+            scale = n if unit == "sms" else n / 8
+            sp[key] = tuple(sorted({int(v * scale) for v in sp[key][1:]} | {cur}, key=lambda v: (v != cur, v)))
     point = {k: ctx.get_param(k) for k in sp}
     for k, cands in sp.items():
         if point[k] not in cands:

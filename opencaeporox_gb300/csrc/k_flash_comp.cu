@@ -132,27 +132,16 @@ __global__ void __launch_bounds__(FUSED_WARPS * 32, 1) k_flash_fused(const Model
                                                                 const unsigned* __restrict__ pre_count,
                                                                 PERes* __restrict__ pre_pe, DeferSink late,
                                                                 PERes* __restrict__ late_pe,
-                                                                unsigned* __restrict__ ctr)
+                                                                unsigned* __restrict__ ctr, int coop_n,
+                                                                uint32_t* __restrict__ watchdog)
 {
     __shared__ CoopSh<NCM> sh[FUSED_WARPS];
     const int warp = threadIdx.x >> 5;
     const unsigned lane = threadIdx.x & 31;
-    // 1. pre-deferred cells
-    const unsigned npre = pre_count ? min(*pre_count, (unsigned)late.cap) : 0u;
-    for (;;) {
-        unsigned slot = 0;
-        if (lane == 0) slot = atomicAdd(&ctr[0], 1u);
-        slot = __shfl_sync(0xffffffffu, slot, 0);
-        if (slot >= npre) break;
-        CoopPE<NCM> pe(sh[warp], M->comp);
-        pe.run(*M, b, pre_rec[slot], pre_pe[slot]);
-        __syncwarp();
-    }
-    // 2. over-budget cells as soon as they are published, else the next 32
-    // cost-ordered cells (one per lane): a long cell that the budget caught
-    // starts its cooperative run at once instead of after the whole order
-    bool cells_left = true;
-    for (;;) {
+    const bool roles = coop_n > 0;
+    const bool coop_only = roles && (int)blockIdx.x < coop_n;
+    // claims the next published over-budget cell (lane 0), or returns none
+    auto claim_late = [&]() -> unsigned {
         unsigned got = 0xffffffffu;
         if (lane == 0) {
             volatile unsigned* vctr = &ctr[2];
@@ -167,18 +156,68 @@ __global__ void __launch_bounds__(FUSED_WARPS * 32, 1) k_flash_fused(const Model
                 cur = prev;
             }
         }
-        got = __shfl_sync(0xffffffffu, got, 0);
-        if (got != 0xffffffffu) {
-            __threadfence();
-            DeferRec r;
-            r.cell = __ldcg(&late.rec[got].cell);
-            r.ftype_in = __ldcg(&late.rec[got].ftype_in);
-            r.lNP = __ldcg(&late.rec[got].lNP);
-            r.seq = late.seq;
+        return __shfl_sync(0xffffffffu, got, 0);
+    };
+    auto run_late = [&](unsigned got) {
+        __threadfence();
+        DeferRec r;
+        r.cell = __ldcg(&late.rec[got].cell);
+        r.ftype_in = __ldcg(&late.rec[got].ftype_in);
+        r.lNP = __ldcg(&late.rec[got].lNP);
+        r.seq = late.seq;
+        CoopPE<NCM> pe(sh[warp], M->comp);
+        pe.run(*M, b, r, late_pe[got]);
+        __syncwarp();
+    };
+    // 1. pre-deferred cells (with roles, on the cooperative blocks only: the
+    // other warps must not take slots from the shared counter at all)
+    const unsigned npre = pre_count ? min(*pre_count, (unsigned)late.cap) : 0u;
+    if (!roles || coop_only) {
+        for (;;) {
+            unsigned slot = 0;
+            if (lane == 0) slot = atomicAdd(&ctr[0], 1u);
+            slot = __shfl_sync(0xffffffffu, slot, 0);
+            if (slot >= npre) break;
             CoopPE<NCM> pe(sh[warp], M->comp);
-            pe.run(*M, b, r, late_pe[got]);
+            pe.run(*M, b, pre_rec[slot], pre_pe[slot]);
             __syncwarp();
-            continue;
+        }
+    }
+    if (coop_only) {
+        // 3'. the cooperative blocks: over-budget cells until every per-lane warp
+        // has finished and none is left.  The wait is bounded; past the bound
+        // the kernel reports a watchdog status instead of waiting on.
+        const unsigned expected = (gridDim.x - (unsigned)coop_n) * FUSED_WARPS;
+        unsigned spins = 0;
+        for (;;) {
+            const unsigned got = claim_late();
+            if (got != 0xffffffffu) { run_late(got); spins = 0; continue; }
+            unsigned done = 0;
+            if (lane == 0) done = *(volatile unsigned*)&ctr[3] >= expected ? 1u : 0u;
+            done = __shfl_sync(0xffffffffu, done, 0);
+            if (done) {
+                const unsigned last = claim_late();
+                if (last != 0xffffffffu) { run_late(last); continue; }
+                break;
+            }
+            if (++spins > (1u << 24)) {
+                if (lane == 0) atomicOr(watchdog, (uint32_t)ST_ITER_CAP);
+                break;
+            }
+            __nanosleep(256);
+        }
+        return;
+    }
+    // 2. over-budget cells as soon as they are published, else the next 32
+    // cost-ordered cells (one per lane): a long cell that the budget caught
+    // starts its cooperative run at once instead of after the whole order.
+    // With roles the per-lane blocks leave the over-budget cells to the
+    // cooperative blocks until the order is exhausted, then help.
+    bool cells_left = true;
+    for (;;) {
+        if (!roles || !cells_left) {
+            const unsigned got = claim_late();
+            if (got != 0xffffffffu) { run_late(got); continue; }
         }
         if (!cells_left) break;
         unsigned base = 0;
@@ -191,6 +230,10 @@ __global__ void __launch_bounds__(FUSED_WARPS * 32, 1) k_flash_fused(const Model
         const unsigned p = base + lane;
         if (p < (unsigned)b.nb) flash_budget_cell<NCM>(M, b, order[p], budget, late, pre, level);
         __syncwarp();
+    }
+    if (roles && lane == 0) {
+        __threadfence();
+        atomicAdd(&ctr[3], 1u);  // this warp's over-budget cells are all published
     }
 }
 
@@ -274,8 +317,16 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
         cfg.gridDim = dim3(fb.cell_blocks);
         cfg.blockDim = dim3(FUSED_WARPS * 32);
         cfg.dynamicSmemBytes = fb.excl_blocks ? fb.excl_smem_fused : 0;
+        // with cooperative-only blocks, those blocks wait for the others: a
+        // cooperative launch guarantees that all blocks are resident together
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = fb.coop_only_blocks > 0 ? 1 : 0;
         return cudaLaunchKernelEx(&cfg, k_flash_fused<OCPX_NCM>, dm, b, order, fb.budget, fb.pre, fb.level, fb.rin,
-                                  fb.rin_count, fb.pe_pre, late, fb.pe, fb.cell_next);
+                                  fb.rin_count, fb.pe_pre, late, fb.pe, fb.cell_next, fb.coop_only_blocks,
+                                  fb.watchdog);
     }
     case 3: {
         // re-budgeting round: from list (rin, rin_count) into (rec, count)
@@ -346,6 +397,12 @@ cudaError_t OCPX_CAT(setup_flash_batched_, OCPX_NCM)(int* excl_smem)
         e = cudaFuncSetAttribute(k_flash_fused<OCPX_NCM>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared);
     excl_smem[1] = dynf;
+    if (e != cudaSuccess) return e;
+    // fused blocks resident per SM without the shared-memory reservation (for
+    // the co-residency a cooperative launch needs)
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_flash_fused<OCPX_NCM>, FUSED_WARPS * 32, 0);
+    excl_smem[2] = per_sm;
     return e;
 }
 

@@ -146,8 +146,10 @@ struct ocpx_ctx {
     cudaStream_t stream2 = nullptr;    // high-priority stream of the pre-deferred cooperative kernel
     int prio_hi = 0;                   // greatest stream priority of the device
     int pre_blocks = 0;                // SM-exclusive blocks of the pre-deferred pass (0: shared-SM blocks)
-    int excl_smem[2] = {0, 0};         // dynamic shared memory of SM-exclusive blocks: cooperative, fused
+    int excl_smem[3] = {0, 0, 0};      // SM-exclusive blocks' dynamic shared memory (cooperative, fused),
+                                       // fused blocks resident per SM without it
     int fused_blocks = 0;              // > 0: the fused batched flash with this many blocks
+    int fused_coop_blocks = -1;        // leading fused blocks that run only cooperative work (-1: automatic)
     int sms = 0;                       // SMs of the device
     int cell_blocks = 0;               // persistent blocks of the per-cell kernel (0: one thread per cell)
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -283,6 +285,17 @@ FieldInfo ocpx_ctx::field(ocpx_field f) const
 namespace {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// FUSED_COOP_BLOCKS in effect.  Automatic: on small grids 3/8 of the fused
+// blocks run only the cooperative work when the fused blocks hold one SM each,
+// so the longest chains never share an SM with per-lane work (36,000 cells:
+// 12.7 ms per step against 14.6 ms with budget 24); none on large grids,
+// where four blocks per SM cannot all be resident.
+int fused_coop_blocks(const ocpx_ctx* ctx)
+{
+    if (ctx->fused_coop_blocks >= 0) return ctx->fused_coop_blocks;
+    return ctx->nb < 131072 && ctx->fused_blocks <= ctx->sms ? 3 * ctx->fused_blocks / 8 : 0;
+}
 
 }  // namespace
 
@@ -476,6 +489,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     // per-thread frames' memory latency (4,000,000 cells: 1,289 ms against
     // 1,484 ms with one block per SM and 1,439 ms two-stream)
     ctx->fused_blocks = nb < 131072 ? sms : 4 * sms;
+    ctx->fused_coop_blocks = -1;
     *out = ctx;
     return OCPX_OK;
 }
@@ -606,6 +620,18 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
                 ff.cell_next = cnt + 32;
                 ff.excl_blocks = ctx->fused_blocks <= ctx->sms ? 1 : 0;
                 ff.excl_smem_fused = ctx->excl_smem[1];
+                const int coop_only = fused_coop_blocks(ctx);
+                if (coop_only >= ctx->fused_blocks)
+                    return fail(OCPX_INVALID_ARG, "FUSED_COOP_BLOCKS must be smaller than FUSED_BLOCKS");
+                if (coop_only > 0) {
+                    const long long resident = ctx->fused_blocks <= ctx->sms ? ctx->sms
+                                                                             : (long long)ctx->excl_smem[2] * ctx->sms;
+                    if (ctx->fused_blocks > resident)
+                        return fail(OCPX_INVALID_ARG, "FUSED_COOP_BLOCKS needs all FUSED_BLOCKS resident at once (at most "
+                                                      + std::to_string(resident) + " here)");
+                }
+                ff.coop_only_blocks = coop_only;
+                ff.watchdog = ctx->flags + 1;
                 mk = ctx->stage_begin(10);
                 OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, ff, 4, s));
                 ctx->stage_end(mk);
@@ -1084,6 +1110,10 @@ ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value)
         if (value < 0 || value > 65535) return fail(OCPX_INVALID_ARG, "fused blocks out of range");
         ctx->fused_blocks = (int)value;
         return OCPX_OK;
+    case OCPX_PARAM_FUSED_COOP_BLOCKS:
+        if (value < -1 || value > 65535) return fail(OCPX_INVALID_ARG, "fused coop blocks out of range");
+        ctx->fused_coop_blocks = (int)value;
+        return OCPX_OK;
     case OCPX_PARAM_ROUNDS:
         if (value < 0 || value > 8) return fail(OCPX_INVALID_ARG, "rounds must be 0..8");
         ctx->rounds = (int)value;
@@ -1110,6 +1140,7 @@ ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value)
     case OCPX_PARAM_CELL_BLOCKS: *value = ctx->cell_blocks; return OCPX_OK;
     case OCPX_PARAM_ROUNDS: *value = ctx->rounds; return OCPX_OK;
     case OCPX_PARAM_FUSED_BLOCKS: *value = ctx->fused_blocks; return OCPX_OK;
+    case OCPX_PARAM_FUSED_COOP_BLOCKS: *value = fused_coop_blocks(ctx); return OCPX_OK;
     case OCPX_PARAM_SMS: *value = ctx->sms; return OCPX_OK;
     case OCPX_PARAM_ROUND_GROWTH: *value = ctx->round_growth; return OCPX_OK;
     case OCPX_PARAM_DEFERRED: {

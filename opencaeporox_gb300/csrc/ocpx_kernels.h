@@ -39,9 +39,12 @@ struct FlashBatch {
     long long mult;             // part 3: budget multiplier of the round
     PERes* pe_pre;              // part 4: results of the pre-deferred list
     int excl_smem_fused;        // part 4: dynamic shared memory that makes a fused block SM-exclusive
+    int coop_only_blocks;       // part 4: leading blocks that run only cooperative work (0: none)
+    uint32_t* watchdog;         // part 4: status word for a wait that ran out (ST_ITER_CAP)
 };
 // once per device: configure the SM-exclusive kernels of capacity ncm;
-// excl_smem[0]: the cooperative kernel's dynamic shared memory, [1]: the fused kernel's
+// excl_smem[0]: the cooperative kernel's dynamic shared memory, [1]: the fused kernel's,
+// [2]: fused blocks resident per SM without it
 cudaError_t setup_flash_batched(int ncm, int* excl_smem);
 // part 0: budgeted thread-per-cell flash, 1: cooperative equilibrium, 2: finish deferred cells,
 // 3: re-budgeting round over a deferral list (thread per cell), 4: the fused kernel (pre list

@@ -167,6 +167,8 @@ BATCH_CASES = [
     dict(fused_blocks=3, flash_budget=3, coop_cells=0, predefer=1),
     dict(fused_blocks=1, flash_budget=1, coop_cells=0, predefer=0),
     dict(fused_blocks=400, flash_budget=3, coop_cells=0, predefer=1),
+    dict(fused_blocks=3, fused_coop_blocks=1, flash_budget=3, coop_cells=0, predefer=1),
+    dict(fused_blocks=2, fused_coop_blocks=1, flash_budget=0, predefer=0),
     # the two-stream form
     dict(TWO_STREAM, flash_budget=0), dict(TWO_STREAM, flash_budget=3), dict(TWO_STREAM),
     dict(TWO_STREAM, coop_cells=8), dict(TWO_STREAM, coop_cells=0),
@@ -190,7 +192,8 @@ def test_batched_variant_matches_plain(gpu_lib, name, params):
     the over-budget cells with growing budgets before the cooperative pass;
     the fused kernel (SM-exclusive blocks, one to three of them, or 400
     blocks that share SMs) consumes the over-budget cells while they are
-    being published."""
+    being published, also with its first block reserved for the
+    cooperative work."""
     budget = params.get("flash_budget")
     predefer = params.get("predefer")
     fx = P.load_fixture(name)
@@ -219,3 +222,22 @@ def test_batched_variant_matches_plain(gpu_lib, name, params):
     for it, a, b in zip(its, outs[0], outs[1]):
         for k in FLASH_OUT:
             assert np.array_equal(a[k], b[k], equal_nan=True), f"{name} {it} {params}: {k} differs"
+
+
+def test_cooperative_fused_grid_that_does_not_fit_is_refused(gpu_lib):
+    """A fused grid with cooperative-only blocks must be resident at once; a
+    grid that cannot be is refused before anything is launched, and the
+    context stays usable."""
+    fx = P.load_fixture("comp6_8x8x3")
+    ctx, model, grid = make_ctx(fx, 1)
+    with ctx:
+        it = [it for it in P.iterations(fx) if "P" in P.group(fx, it + "/post")][0]
+        ctx.load_state(P.jac_state(fx, it))
+        ctx.load_state(P.group(fx, it + "/pre"))
+        ctx.set_param("fused_blocks", 64 * ctx.get_param("sms"))
+        ctx.set_param("fused_coop_blocks", 1)
+        with pytest.raises(fim.OcpxError, match="resident"):
+            ctx.update_property()
+        ctx.set_param("fused_blocks", ctx.get_param("sms"))
+        ctx.update_property()
+        assert np.all(np.isfinite(ctx.get("XI")))

@@ -317,13 +317,18 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
         cfg.gridDim = dim3(fb.cell_blocks);
         cfg.blockDim = dim3(FUSED_WARPS * 32);
         cfg.dynamicSmemBytes = fb.excl_blocks ? fb.excl_smem_fused : 0;
-        // with cooperative-only blocks, those blocks wait for the others: a
+        // without the SM-exclusive reservation the SM keeps as much L1 as the
+        // static shared memory allows: the per-lane cells' thread frames live there.
+        // With cooperative-only blocks, those blocks wait for the others: a
         // cooperative launch guarantees that all blocks are resident together
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeCooperative;
-        attr[0].val.cooperative = 1;
+        cudaLaunchAttribute attr[2];
+        attr[0].id = cudaLaunchAttributePreferredSharedMemoryCarveout;
+        attr[0].val.sharedMemCarveout = fb.excl_blocks ? (unsigned)cudaSharedmemCarveoutMaxShared
+                                                       : (unsigned)cudaSharedmemCarveoutMaxL1;
+        attr[1].id = cudaLaunchAttributeCooperative;
+        attr[1].val.cooperative = 1;
         cfg.attrs = attr;
-        cfg.numAttrs = fb.coop_only_blocks > 0 ? 1 : 0;
+        cfg.numAttrs = fb.coop_only_blocks > 0 ? 2 : 1;
         return cudaLaunchKernelEx(&cfg, k_flash_fused<OCPX_NCM>, dm, b, order, fb.budget, fb.pre, fb.level, fb.rin,
                                   fb.rin_count, fb.pe_pre, late, fb.pe, fb.cell_next, fb.coop_only_blocks,
                                   fb.watchdog);
@@ -340,7 +345,7 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
     default: {
         // parts 1 and 2 carry their own launch priority, which a stream
         // capture keeps in the graph's kernel node
-        cudaLaunchAttribute attr[1];
+        cudaLaunchAttribute attr[2];
         attr[0].id = cudaLaunchAttributePriority;
         attr[0].val.priority = fb.prio;
         cudaLaunchConfig_t cfg = {};
@@ -360,8 +365,14 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
             return cudaLaunchKernelEx(&cfg, k_flash_pe_coop<OCPX_NCM, COOP_WARPS>, dm, b, (const DeferRec*)fb.rec,
                                       (const unsigned*)fb.count, fb.cap, fb.coop_next, fb.pe);
         }
-        cfg.gridDim = dim3((fb.cap + 127) / 128);
-        cfg.blockDim = dim3(128);
+        // one thread per deferred cell; the SM's L1 as large as it goes, for
+        // the threads' frames
+        const int pb = fb.post_block > 0 ? fb.post_block : 128;
+        cfg.gridDim = dim3((fb.cap + pb - 1) / pb);
+        cfg.blockDim = dim3(pb);
+        attr[cfg.numAttrs].id = cudaLaunchAttributePreferredSharedMemoryCarveout;
+        attr[cfg.numAttrs].val.sharedMemCarveout = (unsigned)cudaSharedmemCarveoutMaxL1;
+        cfg.numAttrs++;
         return cudaLaunchKernelEx(&cfg, k_flash_post<OCPX_NCM>, dm, b, (const DeferRec*)fb.rec,
                                   (const unsigned*)fb.count, fb.cap, (const PERes*)fb.pe);
     }

@@ -150,6 +150,8 @@ struct ocpx_ctx {
                                        // fused blocks resident per SM without it
     int fused_blocks = 0;              // > 0: the fused batched flash with this many blocks
     int fused_coop_blocks = -1;        // leading fused blocks that run only cooperative work (-1: automatic)
+    int fused_excl = 0;                // fused blocks at most the SM count reserve an SM each
+    int post_block = 32;               // threads per block of the deferred cells' finishing kernel
     int sms = 0;                       // SMs of the device
     int cell_blocks = 0;               // persistent blocks of the per-cell kernel (0: one thread per cell)
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -598,7 +600,7 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             }
             ctx->stage_end(mk);
             unsigned* const cnt = ctx->defer_count;
-            const FlashBatch fbA{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
+            FlashBatch fbA{ctx->flash_budget, ctx->block_cell, ctx->coop_blocks, ctx->defer_cap,
                                  ctx->pre_rec, cnt + 1, ctx->pre_res, nullptr, nullptr, ctx->prio_hi,
                                  ctx->pre_blocks, ctx->excl_smem[0], 0, nullptr, cnt + 3, nullptr, nullptr, 0};
             // with re-budgeting rounds the rounds, not a budget raised to the
@@ -608,6 +610,8 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
                            ctx->defer_rec, cnt, ctx->pe_res, pre ? ctx->pre_flag : nullptr,
                            ctx->rounds > 0 ? nullptr : ctx->adapt_level, 0, 0, 0, ctx->cell_blocks, cnt + 4, cnt + 2,
                            nullptr, nullptr, 0};
+            fbA.post_block = ctx->post_block;
+            fbB.post_block = ctx->post_block;
             if (ctx->fused_blocks > 0) {
                 // one persistent kernel on this stream: pre-deferred cells first, then
                 // the cost-ordered cells, then the over-budget cells as they are published
@@ -618,18 +622,18 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
                 ff.pe_pre = ctx->pre_res;
                 ff.cell_blocks = ctx->fused_blocks;
                 ff.cell_next = cnt + 32;
-                ff.excl_blocks = ctx->fused_blocks <= ctx->sms ? 1 : 0;
+                ff.excl_blocks = ctx->fused_excl && ctx->fused_blocks <= ctx->sms ? 1 : 0;
                 ff.excl_smem_fused = ctx->excl_smem[1];
                 const int coop_only = fused_coop_blocks(ctx);
                 if (coop_only >= ctx->fused_blocks)
                     return fail(OCPX_INVALID_ARG, "FUSED_COOP_BLOCKS must be smaller than FUSED_BLOCKS");
-                if (coop_only > 0) {
-                    const long long resident = ctx->fused_blocks <= ctx->sms ? ctx->sms
-                                                                             : (long long)ctx->excl_smem[2] * ctx->sms;
-                    if (ctx->fused_blocks > resident)
-                        return fail(OCPX_INVALID_ARG, "FUSED_COOP_BLOCKS needs all FUSED_BLOCKS resident at once (at most "
-                                                      + std::to_string(resident) + " here)");
-                }
+                // the cooperative-only blocks wait for the others, so all must be
+                // resident at once; the form is kept to one block per SM (a
+                // cooperative launch of two blocks per SM without the SM-exclusive
+                // reservation once faulted, for a cause not found)
+                if (coop_only > 0 && (ctx->fused_blocks > ctx->sms || ctx->excl_smem[2] < 1))
+                    return fail(OCPX_INVALID_ARG, "FUSED_COOP_BLOCKS needs all FUSED_BLOCKS resident at once, one "
+                                                  "block per SM (at most " + std::to_string(ctx->sms) + " here)");
                 ff.coop_only_blocks = coop_only;
                 ff.watchdog = ctx->flags + 1;
                 mk = ctx->stage_begin(10);
@@ -1114,6 +1118,14 @@ ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value)
         if (value < -1 || value > 65535) return fail(OCPX_INVALID_ARG, "fused coop blocks out of range");
         ctx->fused_coop_blocks = (int)value;
         return OCPX_OK;
+    case OCPX_PARAM_FUSED_EXCL:
+        if (value < 0 || value > 1) return fail(OCPX_INVALID_ARG, "fused excl must be 0 or 1");
+        ctx->fused_excl = (int)value;
+        return OCPX_OK;
+    case OCPX_PARAM_POST_BLOCK:
+        if (value < 32 || value > 128 || value % 32) return fail(OCPX_INVALID_ARG, "post block must be 32, 64, 96 or 128");
+        ctx->post_block = (int)value;
+        return OCPX_OK;
     case OCPX_PARAM_ROUNDS:
         if (value < 0 || value > 8) return fail(OCPX_INVALID_ARG, "rounds must be 0..8");
         ctx->rounds = (int)value;
@@ -1142,6 +1154,8 @@ ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value)
     case OCPX_PARAM_FUSED_BLOCKS: *value = ctx->fused_blocks; return OCPX_OK;
     case OCPX_PARAM_FUSED_COOP_BLOCKS: *value = fused_coop_blocks(ctx); return OCPX_OK;
     case OCPX_PARAM_SMS: *value = ctx->sms; return OCPX_OK;
+    case OCPX_PARAM_FUSED_EXCL: *value = ctx->fused_excl; return OCPX_OK;
+    case OCPX_PARAM_POST_BLOCK: *value = ctx->post_block; return OCPX_OK;
     case OCPX_PARAM_ROUND_GROWTH: *value = ctx->round_growth; return OCPX_OK;
     case OCPX_PARAM_DEFERRED: {
         unsigned n[2] = {0, 0};

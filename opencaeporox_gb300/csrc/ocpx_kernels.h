@@ -41,6 +41,7 @@ struct FlashBatch {
     int excl_smem_fused;        // part 4: dynamic shared memory that makes a fused block SM-exclusive
     int coop_only_blocks;       // part 4: leading blocks that run only cooperative work (0: none)
     uint32_t* watchdog;         // part 4: status word for a wait that ran out (ST_ITER_CAP)
+    int post_block;             // part 2: threads per block (0: 128)
 };
 // once per device: configure the SM-exclusive kernels of capacity ncm;
 // excl_smem[0]: the cooperative kernel's dynamic shared memory, [1]: the fused kernel's,

@@ -133,7 +133,8 @@ EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy",
 PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3, "predefer": 4, "coop_cells": 5,
           "predeferred": 6, "level": 7, "pre_blocks": 8,
           "cell_blocks": 9, "rounds": 10, "round_growth": 11,
-          "fused_blocks": 12, "sms": 13, "fused_coop_blocks": 14}
+          "fused_blocks": 12, "sms": 13, "fused_coop_blocks": 14,
+          "fused_excl": 15, "post_block": 16}
 
 _lib = None
 

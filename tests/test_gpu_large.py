@@ -64,9 +64,10 @@ def test_large_batched_matches_plain(case):
                                     dict(fused_blocks=0),
                                     dict(fused_blocks=152, flash_budget=8, coop_cells=0),
                                     dict(fused_blocks=608, flash_budget=24),
-                                    dict(fused_blocks=152, fused_coop_blocks=38, flash_budget=24)],
+                                    dict(fused_blocks=152, fused_coop_blocks=38, flash_budget=24),
+                                    dict(fused_blocks=152, fused_coop_blocks=57, fused_excl=0, post_block=32)],
                          ids=["rounds+persistent+exclusive", "two-stream", "fused-exclusive", "fused-shared",
-                              "fused-roles"])
+                              "fused-roles", "fused-roles-l1"])
 def test_large_batched_launch_forms_match_plain(case, params):
     """Re-budgeting rounds, the persistent per-cell kernel, SM-exclusive
     pre-deferral blocks and the fused kernel at 200,000 cells: the flash
@@ -74,7 +75,7 @@ def test_large_batched_launch_forms_match_plain(case, params):
     _, _, out = case
     ctx = out[1]["ctx"]
     keep = {k: ctx.get_param(k) for k in ("flash_budget", "rounds", "round_growth", "cell_blocks", "pre_blocks",
-                                          "fused_blocks", "coop_cells", "fused_coop_blocks")}
+                                          "fused_blocks", "coop_cells", "fused_coop_blocks", "fused_excl", "post_block")}
     try:
         for k, v in params.items():
             ctx.set_param(k, v)

@@ -169,6 +169,8 @@ BATCH_CASES = [
     dict(fused_blocks=400, flash_budget=3, coop_cells=0, predefer=1),
     dict(fused_blocks=3, fused_coop_blocks=1, flash_budget=3, coop_cells=0, predefer=1),
     dict(fused_blocks=2, fused_coop_blocks=1, flash_budget=0, predefer=0),
+    dict(fused_excl=0, post_block=32, flash_budget=3, coop_cells=0, predefer=1),
+    dict(fused_blocks=3, fused_coop_blocks=1, fused_excl=0, post_block=64, flash_budget=3, predefer=1),
     # the two-stream form
     dict(TWO_STREAM, flash_budget=0), dict(TWO_STREAM, flash_budget=3), dict(TWO_STREAM),
     dict(TWO_STREAM, coop_cells=8), dict(TWO_STREAM, coop_cells=0),
@@ -176,6 +178,7 @@ BATCH_CASES = [
     dict(TWO_STREAM, flash_budget=3, coop_cells=0, cell_blocks=2),
     dict(TWO_STREAM, flash_budget=3, coop_cells=0, rounds=2, round_growth=2),
     dict(TWO_STREAM, flash_budget=1, coop_cells=0, predefer=0, rounds=8, round_growth=2, cell_blocks=1),
+    dict(TWO_STREAM, flash_budget=0, post_block=32),
 ]
 
 
@@ -193,7 +196,8 @@ def test_batched_variant_matches_plain(gpu_lib, name, params):
     the fused kernel (SM-exclusive blocks, one to three of them, or 400
     blocks that share SMs) consumes the over-budget cells while they are
     being published, also with its first block reserved for the
-    cooperative work."""
+    cooperative work, and without the SM-exclusive reservation; the kernel
+    that finishes the deferred cells with 32 to 128 threads per block."""
     budget = params.get("flash_budget")
     predefer = params.get("predefer")
     fx = P.load_fixture(name)

@@ -299,15 +299,47 @@ cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, uns
 // work level is at or above the adaptive level, are handed to the cooperative
 // kernel before the per-cell kernel runs, so that both run at the same time
 // (pre[cell] = 1).  Cells that the skip test will let through
-// (flash type 1) stay with the per-cell kernel.  Cells are visited in the cost
-// order, so the list comes out roughly heaviest first and the cooperative
-// kernel's warps, which take list slots in order, start with the longest cells.
+// (flash type 1) stay with the per-cell kernel.  Thread q visits the q-th cell
+// of the cost order taken level by level (all classes of the highest level
+// first), so the list comes out roughly heaviest first whatever the class, and
+// the cooperative warps, which take list slots in order, start with the
+// longest cells.  bucket_end: the end of each cost bucket in the order.
 __global__ void k_predefer(const Model* __restrict__ M, BulkView b, const int* __restrict__ order,
-                           long long threshold, const int* __restrict__ level, DeferSink sink,
-                           uint8_t* __restrict__ pre)
+                           const unsigned* __restrict__ bucket_end, long long threshold,
+                           const int* __restrict__ level, DeferSink sink, uint8_t* __restrict__ pre)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= b.nb) return;
+    constexpr int NCLS = COST_BUCKETS / 64;
+    __shared__ unsigned cnt[COST_BUCKETS];
+    __shared__ unsigned lstart[64];  // level-major position of level l's first cell
+    for (int k = threadIdx.x; k < COST_BUCKETS; k += blockDim.x)
+        cnt[k] = bucket_end[k] - (k ? bucket_end[k - 1] : 0u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned acc = 0;
+        for (int l = 63; l >= 0; l--) {
+            lstart[l] = acc;
+            for (int c = 0; c < NCLS; c++) acc += cnt[c * 64 + (63 - l)];
+        }
+    }
+    __syncthreads();
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= b.nb) return;
+    // the level holding position q: the lowest l with lstart[l] <= q
+    // (lstart falls as l rises)
+    int lo = 0, hi = 63;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (lstart[mid] <= (unsigned)q) hi = mid;
+        else lo = mid + 1;
+    }
+    unsigned r = (unsigned)q - lstart[lo];
+    int p = -1;
+    for (int c = 0; c < NCLS; c++) {
+        const int k = c * 64 + (63 - lo);
+        if (r < cnt[k]) { p = (int)(bucket_end[k] - cnt[k] + r); break; }
+        r -= cnt[k];
+    }
+    if (p < 0) return;  // not reached: the buckets hold every cell once
     const int cell = order[p];
     pre[cell] = 0;
     const long long w = predicted_work(b, cell);
@@ -330,10 +362,12 @@ __global__ void k_predefer(const Model* __restrict__ M, BulkView b, const int* _
     if (sink.push(cell, ftype_in, npPE)) pre[cell] = 1;
 }
 
-cudaError_t launch_predefer(const Model* dm, const BulkView& b, const int* order, long long threshold,
-                            const int* level, const DeferSink& sink, uint8_t* pre, cudaStream_t s)
+cudaError_t launch_predefer(const Model* dm, const BulkView& b, const int* order, const unsigned* bucket_end,
+                            long long threshold, const int* level, const DeferSink& sink, uint8_t* pre,
+                            cudaStream_t s)
 {
-    if (b.nb) k_predefer<<<grid_for(b.nb, 128), 128, 0, s>>>(dm, b, order, threshold, level, sink, pre);
+    if (b.nb)
+        k_predefer<<<grid_for(b.nb, 128), 128, 0, s>>>(dm, b, order, bucket_end, threshold, level, sink, pre);
     return cudaGetLastError();
 }
 

@@ -271,16 +271,27 @@ __global__ void __launch_bounds__(WARPS * 32) k_flash_pe_coop(const Model* __res
 }
 
 // Step 3: properties, derivatives and skip state of the deferred cells from
-// their equilibrium, one thread per deferred cell.
+// their equilibrium, one thread per deferred cell: the cells of the first list,
+// then those of the second (rec2 NULL: none), so that the busy threads are the
+// leading ones.  Each list holds at most cap cells.
 template <int NCM>
 __global__ void __launch_bounds__(128) k_flash_post(const Model* __restrict__ M, BulkView b,
                                                     const DeferRec* __restrict__ rec,
                                                     const unsigned* __restrict__ count, int cap,
-                                                    const PERes* __restrict__ pe)
+                                                    const PERes* __restrict__ pe,
+                                                    const DeferRec* __restrict__ rec2,
+                                                    const unsigned* __restrict__ count2,
+                                                    const PERes* __restrict__ pe2)
 {
-    const unsigned slot = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned slot = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned n = min(*count, (unsigned)cap);
-    if (slot >= n) return;
+    if (slot >= n) {
+        if (!rec2) return;
+        slot -= n;
+        if (slot >= min(*count2, (unsigned)cap)) return;
+        rec = rec2;
+        pe = pe2;
+    }
     CompCellUpdate<NCM> u;
     u.run(*M, b, rec[slot].cell, 0x7fffffff, nullptr, &pe[slot]);
 }
@@ -368,13 +379,15 @@ cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const Bul
         // one thread per deferred cell; the SM's L1 as large as it goes, for
         // the threads' frames
         const int pb = fb.post_block > 0 ? fb.post_block : 128;
-        cfg.gridDim = dim3((fb.cap + pb - 1) / pb);
+        const long long threads = (long long)fb.cap * (fb.rec2 ? 2 : 1);
+        cfg.gridDim = dim3((unsigned)((threads + pb - 1) / pb));
         cfg.blockDim = dim3(pb);
         attr[cfg.numAttrs].id = cudaLaunchAttributePreferredSharedMemoryCarveout;
         attr[cfg.numAttrs].val.sharedMemCarveout = (unsigned)cudaSharedmemCarveoutMaxL1;
         cfg.numAttrs++;
         return cudaLaunchKernelEx(&cfg, k_flash_post<OCPX_NCM>, dm, b, (const DeferRec*)fb.rec,
-                                  (const unsigned*)fb.count, fb.cap, (const PERes*)fb.pe);
+                                  (const unsigned*)fb.count, fb.cap, (const PERes*)fb.pe, fb.rec2, fb.count2,
+                                  fb.pe2);
     }
     }
     return cudaGetLastError();

@@ -594,8 +594,8 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             ctx->launches += 3;
             if (pre) {
                 const DeferSink sinkA{ctx->pre_rec, ctx->defer_count + 1, ctx->defer_cap};
-                OCPX_CUDA(launch_predefer(ctx->d_model, ctx->b, ctx->order, ctx->predefer, ctx->adapt_level, sinkA,
-                                          ctx->pre_flag, s));
+                OCPX_CUDA(launch_predefer(ctx->d_model, ctx->b, ctx->order, ctx->cost_hist, ctx->predefer,
+                                          ctx->adapt_level, sinkA, ctx->pre_flag, s));
                 ctx->launches++;
             }
             ctx->stage_end(mk);
@@ -640,12 +640,16 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
                 OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, ff, 4, s));
                 ctx->stage_end(mk);
                 ctx->late_count = 0;
+                // both lists' cells finished by one launch: each thread's chain
+                // is long, so two launches in a row would take twice as long
                 mk = ctx->stage_begin(12);
+                FlashBatch fp = fbB;
                 if (pre) {
-                    OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbA, 2, s));
-                    ctx->launches++;
+                    fp.rec2 = ctx->pre_rec;
+                    fp.count2 = cnt + 1;
+                    fp.pe2 = ctx->pre_res;
                 }
-                OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fbB, 2, s));
+                OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, fp, 2, s));
                 ctx->stage_end(mk);
                 ctx->launches += 2;
             }

@@ -42,6 +42,9 @@ struct FlashBatch {
     int coop_only_blocks;       // part 4: leading blocks that run only cooperative work (0: none)
     uint32_t* watchdog;         // part 4: status word for a wait that ran out (ST_ITER_CAP)
     int post_block;             // part 2: threads per block (0: 128)
+    const DeferRec* rec2;       // part 2: a second list finished in the same launch
+    const unsigned* count2;     //   (its count, capacity cap, and equilibria), NULL: none
+    const PERes* pe2;
 };
 // once per device: configure the SM-exclusive kernels of capacity ncm;
 // excl_smem[0]: the cooperative kernel's dynamic shared memory, [1]: the fused kernel's,
@@ -64,8 +67,11 @@ cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, uns
 // hand the cells whose last flash used more than `threshold` work units, at or
 // above the adaptive level, to the cooperative kernel up front (pre[cell] = 1),
 // visiting cells in `order`
-cudaError_t launch_predefer(const Model* dm, const BulkView& b, const int* order, long long threshold,
-                            const int* level, const DeferSink& sink, uint8_t* pre, cudaStream_t s);
+// bucket_end: launch_cost_order's bucket counts after it ran (the end of each
+// bucket in the order)
+cudaError_t launch_predefer(const Model* dm, const BulkView& b, const int* order, const unsigned* bucket_end,
+                            long long threshold, const int* level, const DeferSink& sink, uint8_t* pre,
+                            cudaStream_t s);
 
 // Newton and time-step control (k_nrctl.cu).  mode 0: CalMaxChangeNR against
 // the last Newton iterate (lP, lT, lN, lS; replaced by the current state),

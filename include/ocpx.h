@@ -272,7 +272,7 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *                 never share an SM with per-lane work.  The launch is then
  *                 cooperative: FUSED_BLOCKS must be at most the SM count (one
  *                 block per SM, all resident at once) and larger than this
- *                 value.  -1 (default): 3/8 of FUSED_BLOCKS below
+ *                 value.  -1 (default): half of FUSED_BLOCKS below
  *                 131,072 cells when FUSED_BLOCKS is at most the SM count,
  *                 else 0; reading the parameter gives the value in effect;
  *   FUSED_EXCL    1: fused blocks that number at most the SM count reserve

@@ -417,9 +417,12 @@ cudaError_t OCPX_CAT(setup_flash_batched_, OCPX_NCM)(int* excl_smem)
     if (e != cudaSuccess) return e;
     const int dynf = optin > (int)ff.sharedSizeBytes ? optin - (int)ff.sharedSizeBytes : 0;
     e = cudaFuncSetAttribute(k_flash_fused<OCPX_NCM>, cudaFuncAttributeMaxDynamicSharedMemorySize, dynf);
+    // maximum L1 unless a launch asks for the SM-exclusive shared memory (whose
+    // dynamic size forces the largest shared-memory configuration anyway): a
+    // cooperative launch kept the function's preference over the launch's
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_flash_fused<OCPX_NCM>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared);
+                                 (int)cudaSharedmemCarveoutMaxL1);
     excl_smem[1] = dynf;
     if (e != cudaSuccess) return e;
     // fused blocks resident per SM without the shared-memory reservation (for

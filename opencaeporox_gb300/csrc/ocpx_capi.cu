@@ -288,15 +288,16 @@ namespace {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// FUSED_COOP_BLOCKS in effect.  Automatic: on small grids 3/8 of the fused
+// FUSED_COOP_BLOCKS in effect.  Automatic: on small grids half of the fused
 // blocks run only the cooperative work when the fused blocks hold one SM each,
 // so the longest chains never share an SM with per-lane work (36,000 cells:
-// 12.7 ms per step against 14.6 ms with budget 24); none on large grids,
-// where four blocks per SM cannot all be resident.
+// 12.3 ms per step with 76 of 152 blocks and budget 32, 12.9 ms with 57 and
+// budget 48, 13.3 ms with none); none on large grids, where four blocks per
+// SM cannot all be resident.
 int fused_coop_blocks(const ocpx_ctx* ctx)
 {
     if (ctx->fused_coop_blocks >= 0) return ctx->fused_coop_blocks;
-    return ctx->nb < 131072 && ctx->fused_blocks <= ctx->sms ? 3 * ctx->fused_blocks / 8 : 0;
+    return ctx->nb < 131072 && ctx->fused_blocks <= ctx->sms ? ctx->fused_blocks / 2 : 0;
 }
 
 }  // namespace
@@ -492,6 +493,9 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     // 1,484 ms with one block per SM and 1,439 ms two-stream)
     ctx->fused_blocks = nb < 131072 ? sms : 4 * sms;
     ctx->fused_coop_blocks = -1;
+    // a tighter budget on small grids, where the cooperative-only blocks take
+    // the over-budget cells
+    ctx->flash_budget = nb < 131072 ? 32 : 48;
     *out = ctx;
     return OCPX_OK;
 }

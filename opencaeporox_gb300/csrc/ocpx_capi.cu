@@ -487,10 +487,13 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     ctx->sms = sms;
     // the fused batched flash: one block of four warps per SM on small grids,
     // where the longest cells set the time (36,000 cells: 15.0 ms per step
-    // against 16.8 ms for the tuned two-stream form); four per SM on large
-    // ones, where the per-lane work dominates and more warps hide the
-    // per-thread frames' memory latency (4,000,000 cells: 1,289 ms against
-    // 1,484 ms with one block per SM and 1,439 ms two-stream)
+    // against 16.8 ms for the tuned two-stream form); more on large ones,
+    // where the per-lane work dominates and more warps hide the per-thread
+    // frames' memory latency.  At 182 registers a thread two blocks fit on an
+    // SM, so the four per SM launched run two at a time, the later blocks
+    // finding the work taken (4,000,000 cells: 1,289 ms against 1,484 ms with
+    // one block per SM and 1,439 ms two-stream; 304 to 912 blocks all within
+    // 0.2 % of each other)
     ctx->fused_blocks = nb < 131072 ? sms : 4 * sms;
     ctx->fused_coop_blocks = -1;
     // a tighter budget on small grids, where the cooperative-only blocks take

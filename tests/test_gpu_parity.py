@@ -245,3 +245,36 @@ def test_cooperative_fused_grid_that_does_not_fit_is_refused(gpu_lib):
         ctx.set_param("fused_blocks", ctx.get_param("sms"))
         ctx.update_property()
         assert np.all(np.isfinite(ctx.get("XI")))
+
+
+def test_fused_launch_parameters(gpu_lib):
+    """Automatic cooperative-only blocks (half of the fused blocks while they
+    hold one SM each, none beyond), the small-grid defaults, the refusal of
+    cooperative-only blocks with two fused blocks per SM before anything is
+    launched, and the ranges of the launch parameters."""
+    fx = P.load_fixture("comp6_8x8x3")
+    ctx, model, grid = make_ctx(fx, 1)
+    with ctx:
+        sms = ctx.get_param("sms")
+        assert ctx.get_param("fused_blocks") == sms
+        assert ctx.get_param("fused_coop_blocks") == sms // 2
+        assert ctx.get_param("fused_excl") == 0
+        assert ctx.get_param("post_block") == 32
+        assert ctx.get_param("flash_budget") == 32
+        ctx.set_param("fused_blocks", 2 * sms)
+        assert ctx.get_param("fused_coop_blocks") == 0
+        it = [it for it in P.iterations(fx) if "P" in P.group(fx, it + "/post")][0]
+        ctx.load_state(P.jac_state(fx, it))
+        ctx.load_state(P.group(fx, it + "/pre"))
+        ctx.set_param("fused_coop_blocks", 1)
+        with pytest.raises(fim.OcpxError, match="one block per SM"):
+            ctx.update_property()
+        ctx.set_param("fused_coop_blocks", -1)
+        assert ctx.get_param("fused_coop_blocks") == 0
+        ctx.set_param("fused_blocks", sms)
+        assert ctx.get_param("fused_coop_blocks") == sms // 2
+        for k, v in (("post_block", 48), ("post_block", 256), ("fused_excl", 2), ("fused_coop_blocks", -2)):
+            with pytest.raises(fim.OcpxError, match="INVALID_ARG"):
+                ctx.set_param(k, v)
+        ctx.update_property()
+        assert np.all(np.isfinite(ctx.get("XI")))

@@ -51,3 +51,11 @@ def test_no_device_is_an_error_not_a_fallback(lib):
     model, grid = fim.model_and_grid_from_dump(fx)
     with pytest.raises(fim.OcpxError, match="NO_DEVICE"):
         fim.FimContext(model, grid)
+
+
+def test_python_parameter_names_match_the_header():
+    """fim.PARAMS names and numbers every ocpx_param of the header, and no other."""
+    text = open(HEADER).read()
+    enum = re.search(r"typedef enum ocpx_param \{(.*?)\}", text, flags=re.S).group(1)
+    declared = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"OCPX_PARAM_([A-Z0-9_]+)\s*=\s*(\d+)", enum)}
+    assert declared == fim.PARAMS

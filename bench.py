@@ -87,41 +87,63 @@ class Cudart:
 
 # ----------------------------------------------------------------- clocks ---
 class ClockSampler:
-    """nvidia-smi samples during the timed region."""
-    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    """nvidia-smi samples every 50 ms, of which those stamped inside the
+    window [start(), end()] (the timed loop) are kept; all samples when none
+    falls inside it."""
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
 
-    def __init__(self, gpu=0):
+    def __init__(self, gpu=0, interval_ms=50):
         self.p = None
+        self.t0 = self.t1 = None
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu), "--query-gpu=" + self.Q,
-                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
-                                      stderr=subprocess.DEVNULL, text=True)
+                                       "--format=csv,noheader,nounits", "-lms", str(interval_ms)],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.p = None
+
+    def start(self, t=None):
+        self.t0 = time.time() if t is None else t
+
+    def end(self, t=None):
+        self.t1 = time.time() if t is None else t
+
+    @staticmethod
+    def _stamp(s):
+        from datetime import datetime
+        for fmt in ("%Y/%m/%d %H:%M:%S.%f", "%Y/%m/%d %H:%M:%S"):
+            try:
+                return datetime.strptime(s, fmt).timestamp()
+            except ValueError:
+                pass
+        return None
 
     def stop(self):
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.p.terminate()
         out, _ = self.p.communicate(timeout=10)
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for line in out.strip().splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 8:
+            if len(f) < 9:
                 continue
             try:
-                sm.append(float(f[0]))
-                mx.append(float(f[1]))
+                sm, mx = float(f[1]), float(f[2])
             except ValueError:
                 continue
-            for nm, v in zip(names, f[4:8]):
-                if v.lower().startswith("active"):
-                    reasons.add(nm)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+            rows.append((self._stamp(f[0]), sm, mx, [nm for nm, v in zip(self.NAMES, f[5:9])
+                                                     if v.lower().startswith("active")]))
+        inside = [r for r in rows if r[0] is not None and self.t0 is not None and self.t1 is not None
+                  and self.t0 <= r[0] <= self.t1]
+        use = inside or rows
+        sm = [r[1] for r in use]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(r[2] for r in use) if use else None,
+                "reasons": sorted({nm for r in use for nm in r[3]}), "samples": len(use),
+                "window": "timed loop" if inside else "whole sampler run (no sample inside the timed loop)"}
 
 
 # ---------------------------------------------------------------- workload --
@@ -536,8 +558,11 @@ def main():
         results[variant] = dict(ms=ranks.max(statistics.median(t)), mean=statistics.fmean(t),
                                 launches=launches / args.steps, prof=prof, ctx=ctx, u=u)
     clocks = ClockSampler(local)
+    time.sleep(0.5)  # the sampler's first samples come after its start-up
     ranks.barrier(rt)
+    clocks.start()
     tb, launches = time_device(results[1]["ctx"], rt, args.steps, args.warmup, flush)
+    clocks.end()
     ranks.barrier(rt)
     ck = clocks.stop()
     ranks.barrier(rt)

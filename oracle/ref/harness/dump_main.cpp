@@ -200,6 +200,60 @@ void dump_state(const string& dir, Reservoir& rs)
     }
 }
 
+// Open wells in AllWells order and their perforations, as the residual just
+// computed used them (WellPeaceman.cpp: CalTrans, CalFlux, CalFactor,
+// CalResFIM): well arrays per well, perforation arrays concatenated.
+void dump_wells(const string& dir, Reservoir& rs)
+{
+    vector<int32_t> type, mode, nperf, loc;
+    vector<double>  bhp, tar_bhp, tar_rate, factor, inj_zi, qi, WI, mult, dG, P, transj, trans_inj, xi, pqi;
+    for (Well* w0 : rs.allWells.wells) {
+        PeacemanWell* w = dynamic_cast<PeacemanWell*>(w0);
+        if (!w || w->opt.state != WellState::open) continue;
+        type.push_back(w->opt.type == WellType::injector ? 0 : 1);
+        mode.push_back(w->opt.mode == WellOptMode::bhp ? 0 : 1);
+        nperf.push_back((int32_t)w->numPerf);
+        bhp.push_back(w->bhp);
+        tar_bhp.push_back(w->opt.tarBHP);
+        tar_rate.push_back(w->opt.tarRate);
+        for (USI i = 0; i < w->nc; i++) {
+            factor.push_back(w->factor.size() > i ? w->factor[i] : 0.0);
+            inj_zi.push_back(w->opt.injZi.size() > i ? w->opt.injZi[i] : 0.0);
+            qi.push_back(w->qi_lbmol[i]);
+        }
+        for (USI p = 0; p < w->numPerf; p++) {
+            const Perforation& f = w->perf[p];
+            loc.push_back((int32_t)f.location);
+            WI.push_back(f.WI);
+            mult.push_back(f.multiplier);
+            dG.push_back(w->dG[p]);
+            P.push_back(f.P);
+            for (USI j = 0; j < w->np; j++) transj.push_back(f.transj[j]);
+            trans_inj.push_back(f.transINJ);
+            xi.push_back(f.xi);
+            for (USI i = 0; i < w->nc; i++) pqi.push_back(f.qi_lbmol[i]);
+        }
+    }
+    put(dir, "well_type", type);
+    put(dir, "well_mode", mode);
+    put(dir, "well_nperf", nperf);
+    put(dir, "well_bhp", bhp);
+    put(dir, "well_tar_bhp", tar_bhp);
+    put(dir, "well_tar_rate", tar_rate);
+    put(dir, "well_factor", factor);
+    put(dir, "well_inj_zi", inj_zi);
+    put(dir, "well_qi", qi);
+    put(dir, "perf_loc", loc);
+    put(dir, "perf_WI", WI);
+    put(dir, "perf_mult", mult);
+    put(dir, "perf_dG", dG);
+    put(dir, "perf_P", P);
+    put(dir, "perf_transj", transj);
+    put(dir, "perf_trans_inj", trans_inj);
+    put(dir, "perf_xi", xi);
+    put(dir, "perf_qi", pqi);
+}
+
 void dump_conn_res(const string& dir, Reservoir& rs, IsoT_FIM& fim, OCP_DBL dt)
 {
     // bulk-only residual: the same CalRes with the well list detached, then the
@@ -223,6 +277,8 @@ void dump_conn_res(const string& dir, Reservoir& rs, IsoT_FIM& fim, OCP_DBL dt)
     wells.swap(rs.allWells.wells);
     fim.CalRes(rs, dt, OCP_FALSE);
     put(dir, "res_full", fim.NR.res.resAbs);
+    put1(dir, "maxWellRelRes_mol", fim.NR.res.maxWellRelRes_mol);
+    dump_wells(dir, rs);
 }
 
 void dump_jac(const string& dir, LinearSystem& ls, OCP_USI nbI)

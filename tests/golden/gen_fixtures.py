@@ -16,6 +16,9 @@ Fixtures (compressed .npz, one key per dumped array, "<group>/<name>"):
 * ``comp8_6x6x4``  eight-component PR-EoS FIM, 144 cells.
 * ``flash10``      ten-component flash-only cells: FlashDer from flash type 0
   without phase history, random and near-saturation feeds.
+* ``wells_bo_10x10x3``, ``wells_comp6_8x8x3``  the same runs as the FIM
+  fixtures above, with the wells' part of each iteration's residual: the
+  perforations' data and fluxes and the residual with and without the wells.
 """
 from __future__ import annotations
 
@@ -111,7 +114,33 @@ def pack_fim(outdir):
     return data
 
 
-def run_fim(deck_text, name, max_iters, ni=None, calibrate=False):
+# the wells' part of the residual (harness dump_wells) and the bulk state it reads
+WELL_KEYS = ["well_type", "well_mode", "well_nperf", "well_bhp", "well_tar_bhp", "well_tar_rate", "well_factor",
+             "well_inj_zi", "well_qi", "perf_loc", "perf_WI", "perf_mult", "perf_dG", "perf_P", "perf_transj",
+             "perf_trans_inj", "perf_xi", "perf_qi", "res_bulk", "res_full", "maxWellRelRes_mol",
+             "P", "Pj", "phaseExist", "kr", "mu", "xi", "xij"]
+
+
+def pack_wells(outdir, max_its=4):
+    """The wells' part of each Newton iteration's post state: perforation data,
+    fluxes and the residual with and without the wells."""
+    data = {}
+    for k, v in load_dir(os.path.join(outdir, "model")).items():
+        if k in ("nb", "np", "nc", "numWell"):
+            data[f"model/{k}"] = v
+    n = 0
+    for it in range(len(np.load(os.path.join(outdir, "log.npy")))):
+        post = os.path.join(outdir, f"it{it:03d}", "post")
+        if not os.path.exists(os.path.join(post, "well_type.npy")) or n >= max_its:
+            continue
+        for k, v in load_dir(post, set(WELL_KEYS)).items():
+            data[f"it{it:03d}/{k}"] = v
+        data[f"it{it:03d}/dt"] = np.load(os.path.join(outdir, f"it{it:03d}", "pre", "dt.npy"))
+        n += 1
+    return data
+
+
+def run_fim(deck_text, name, max_iters, ni=None, calibrate=False, packer=pack_fim):
     with tempfile.TemporaryDirectory() as tmp:
         deck = os.path.join(tmp, name + ".data")
         with open(deck, "w") as f:
@@ -128,7 +157,7 @@ def run_fim(deck_text, name, max_iters, ni=None, calibrate=False):
                 ni.astype("<f8").tofile(deck + ".ptn_ni")
         out = os.path.join(tmp, "out")
         subprocess.run([DUMP, "fim", deck, out, str(max_iters)], check=True, stdout=subprocess.DEVNULL)
-        data = pack_fim(out)
+        data = packer(out)
         if ni is not None:
             data["ptn_ni"] = ni
     return data
@@ -163,9 +192,12 @@ def run_flash(ncomp, ncell, seed):
     return data
 
 
-def _comp_fim(nx, ny, nz, ncomp, seed, name, max_iters):
+def _comp_fim(nx, ny, nz, ncomp, seed, name, max_iters, packer=pack_fim):
     ni, text = decks.comp_deck(nx, ny, nz, ncomp, seed=seed, tsteps=(0.02, 0.05, 0.1), smooth=True)
-    return run_fim(text, name, max_iters, ni=ni, calibrate=True)
+    data = run_fim(text, name, max_iters, ni=ni, calibrate=True, packer=packer)
+    if packer is not pack_fim:
+        data.pop("ptn_ni", None)
+    return data
 
 
 def corner_fixture(nx=6, ny=5, nz=4, seed=7):
@@ -202,6 +234,8 @@ FIXTURES = {
     "comp8_6x6x4": lambda: _comp_fim(6, 6, 4, 8, 4, "c8", 4),
     "flash10": lambda: run_flash(10, 1024, 3),
     "cpg_6x5x4": corner_fixture,
+    "wells_bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12, packer=pack_wells),
+    "wells_comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4, packer=pack_wells),
 }
 
 

@@ -295,6 +295,22 @@ void dump_jac(const string& dir, LinearSystem& ls, OCP_USI nbI)
     put(dir, "jac_val", val);
 }
 
+// every row of the assembled system after the wells' assembly: bulk rows
+// (with their well columns) and well rows
+void dump_jac_all(const string& dir, LinearSystem& ls)
+{
+    vector<uint32_t> rowptr(1, 0), col;
+    vector<double>   val;
+    for (OCP_USI r = 0; r < ls.mat.colId.size() && r < ls.mat.dim; r++) {
+        rowptr.push_back(rowptr.back() + ls.mat.colId[r].size());
+        col.insert(col.end(), ls.mat.colId[r].begin(), ls.mat.colId[r].end());
+        val.insert(val.end(), ls.mat.val[r].begin(), ls.mat.val[r].end());
+    }
+    put(dir, "jacw_rowptr", rowptr);
+    put(dir, "jacw_col", col);
+    put(dir, "jacw_val", val);
+}
+
 double now()
 {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -495,6 +511,8 @@ int run_fim(const string& deck, int max_iters)
                 double t_asm = now() - t0;
                 dump_jac(dir + "/jac_state", ls, nbI);
                 fim.AssembleMatWells(ls, rs, dt);
+                dump_jac_all(dir + "/jac_state", ls);
+                dump_wells(dir + "/jac_state", rs);
                 ls.CopyRhs(fim.NR.res.resAbs);
                 rs.domain.SetNumActWellLocal(rs.GetNumOpenWell());
 

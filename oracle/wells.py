@@ -136,3 +136,92 @@ def residual_with_wells(res_bulk, wells: list[dict], state: dict, dt: float, nc:
             max_rel = max(max_rel, abs(r / w["tar_rate"]))
         wid += length
     return -np.array(res), max_rel
+
+
+def _matmul_add(alpha, A, B, beta, C):
+    """alpha*A*B + beta*C of row-major dense blocks (DaABpbC,
+    src/DenseMat.cpp:61-85, which the reference hands to BLAS dgemm; the
+    summation order of a BLAS is not the reference's to fix, so this product is
+    compared within a tolerance)."""
+    return alpha * (np.asarray(A) @ np.asarray(B)) + beta * np.asarray(C)
+
+
+def well_jacobian(wells: list[dict], state: dict, dt: float, nb: int, nc: int, np_: int):
+    """PeacemanWellIsoT::AssembleMatInjFIM / AssembleMatProdFIM
+    (src/WellPeaceman.cpp:1268-1361, 1488-1613) for every open well in order.
+
+    Returns the blocks the wells add to the system, as (ncol x ncol) arrays:
+    ``bulk_add[n]`` summed into cell n's diagonal block, ``bulk_well[(n, w)]``
+    inserted in cell n's row at well w's column, ``well_diag[w]`` (the well's
+    diagonal block), and ``well_bulk[(w, n)]`` in the well's row at cell n's
+    column, w counted from nb.  state holds the bulk arrays the assembly reads
+    (BulkVarSet layout, dSec_dPri as [nb][ncol2][ncol])."""
+    ncol = nc + 1
+    ncol2 = np_ * nc + np_
+    dsec = np.asarray(state["dSec_dPri"]).reshape(-1, ncol2, ncol)
+    bulk_add, bulk_well, well_diag, well_bulk = {}, {}, {}, {}
+    for wi, w in enumerate(wells):
+        wid = nb + wi
+        transj, _ = perf_trans(w, state["phaseExist"], state["kr"], state["mu"], np_)
+        diag = np.zeros((ncol, ncol))
+        for p, n in enumerate(w["loc"]):
+            dQdXpB = np.zeros((ncol, ncol))
+            dQdXpW = np.zeros((ncol, ncol))
+            dQdXsB = np.zeros((ncol, ncol2))
+            wi_m = float(w["WI"][p]) * float(w["mult"][p])
+            for j in range(np_):
+                idx = n * np_ + j
+                if not state["phaseExist"][idx]:
+                    continue
+                mu, muP = float(state["mu"][idx]), float(state["muP"][idx])
+                tj = transj[p][j]
+                if w["type"] == 0:
+                    dP = float(state["P"][n]) - w["bhp"] - float(w["dG"][p])
+                    xi_inj = float(w["xi_inj"][p])
+                    for i in range(nc):
+                        zi = float(w["inj_zi"][i])
+                        transIJ = tj * xi_inj * zi
+                        dQdXpB[i + 1, 0] += transIJ * (1 - dP * muP / mu)
+                        dQdXpW[i + 1, 0] += -transIJ
+                        for k in range(np_):
+                            dQdXsB[i + 1, k] += (wi_m * xi_inj * zi * float(state["dKrdS"][idx * np_ + k])
+                                                 * dP / mu)
+                        for k in range(nc):
+                            dQdXsB[i + 1, np_ + j * nc + k] += -transIJ * dP / mu * float(
+                                state["mux"][idx * nc + k])
+                else:
+                    dP = float(state["Pj"][idx]) - w["bhp"] - float(w["dG"][p])
+                    xi, xiP = float(state["xi"][idx]), float(state["xiP"][idx])
+                    for i in range(nc):
+                        xij = float(state["xij"][idx * nc + i])
+                        transIJ = tj * xi * xij
+                        dQdXpB[i + 1, 0] += transIJ * (1 - dP * muP / mu) + dP * tj * xij * xiP
+                        dQdXpW[i + 1, 0] += -transIJ
+                        for k in range(np_):
+                            tmp = wi_m * dP / mu * xi * xij * float(state["dKrdS"][idx * np_ + k])
+                            tmp += transIJ * float(state["dPcdS"][idx * np_ + k])
+                            dQdXsB[i + 1, k] += tmp
+                        for k in range(nc):
+                            tmp = dP * tj * xij * (float(state["xix"][idx * nc + k])
+                                                   - xi / mu * float(state["mux"][idx * nc + k]))
+                            dQdXsB[i + 1, np_ + j * nc + k] += tmp
+                        dQdXsB[i + 1, np_ + j * nc + i] += tj * xi * dP
+            bb = _matmul_add(dt, dQdXsB, dsec[n], dt, dQdXpB)
+            bulk_add[n] = bulk_add.get(n, np.zeros((ncol, ncol))) + bb
+            bulk_well[(n, wid)] = dQdXpW * dt
+            if w["mode"] == 1:
+                ww = np.zeros((ncol, ncol))
+                for i in range(nc):
+                    ww[0, 0] += dQdXpW[i + 1, 0] * float(w["factor"][i])
+                    ww[i + 1, i + 1] = 1.0
+                diag = diag + ww
+                m = _matmul_add(1.0, dQdXsB, dsec[n], 1.0, dQdXpB)
+                wb = np.zeros((ncol, ncol))
+                for i in range(nc):
+                    wb[0, :] += float(w["factor"][i]) * m[i + 1, :]
+                well_bulk[(wid, n)] = wb
+            else:
+                diag = diag + np.eye(ncol)
+                well_bulk[(wid, n)] = np.zeros((ncol, ncol))
+        well_diag[wid] = diag
+    return dict(bulk_add=bulk_add, bulk_well=bulk_well, well_diag=well_diag, well_bulk=well_bulk)

@@ -121,9 +121,18 @@ WELL_KEYS = ["well_type", "well_mode", "well_nperf", "well_bhp", "well_tar_bhp",
              "P", "Pj", "phaseExist", "kr", "mu", "xi", "xij"]
 
 
+# the wells' part of the Jacobian: the system after the bulk assembly and after
+# the wells' (all rows), the wells as assembled, and the bulk state it reads
+WELL_JAC_KEYS = [k for k in WELL_KEYS if k.startswith(("well_", "perf_"))] + [
+    "jac_rowptr", "jac_col", "jac_val", "jacw_rowptr", "jacw_col", "jacw_val", "dt",
+    "P", "Pj", "phaseExist", "kr", "mu", "muP", "xi", "xiP", "xij", "xix", "mux", "dKrdS", "dPcdS", "dSec_dPri"]
+
+
 def pack_wells(outdir, max_its=4):
-    """The wells' part of each Newton iteration's post state: perforation data,
-    fluxes and the residual with and without the wells."""
+    """The wells' part of each Newton iteration: at its post state the
+    perforation data, fluxes and the residual with and without the wells; at
+    its Jacobian state ("jac/") the system before and after the wells'
+    assembly and what that assembly read."""
     data = {}
     for k, v in load_dir(os.path.join(outdir, "model")).items():
         if k in ("nb", "np", "nc", "numWell"):
@@ -136,6 +145,10 @@ def pack_wells(outdir, max_its=4):
         for k, v in load_dir(post, set(WELL_KEYS)).items():
             data[f"it{it:03d}/{k}"] = v
         data[f"it{it:03d}/dt"] = np.load(os.path.join(outdir, f"it{it:03d}", "pre", "dt.npy"))
+        js = os.path.join(outdir, f"it{it:03d}", "jac_state")
+        if os.path.exists(os.path.join(js, "jacw_rowptr.npy")):
+            for k, v in load_dir(js, set(WELL_JAC_KEYS)).items():
+                data[f"it{it:03d}/jac/{k}"] = v
         n += 1
     return data
 

@@ -61,3 +61,52 @@ def test_a_planted_error_is_caught():
     bad = dict(fx, Pj=2 * np.asarray(fx["perf_P"]).max() - np.asarray(fx["Pj"]))
     res, _ = W.residual_with_wells(fx["res_bulk"], wells, bad, float(fx["dt"][0]), nc, np_)
     assert not np.array_equal(res, fx["res_full"])
+
+
+def _blocks(rowptr, col, val, ncol):
+    bs = ncol * ncol
+    out = {}
+    for r in range(len(rowptr) - 1):
+        for e in range(int(rowptr[r]), int(rowptr[r + 1])):
+            out[(r, int(col[e]))] = np.asarray(val[e * bs:(e + 1) * bs]).reshape(ncol, ncol)
+    return out
+
+
+def _close(a, b, tol=1e-13):
+    return np.linalg.norm(a - b) <= tol * max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_well_jacobian_blocks(name):
+    """The blocks the wells' assembly adds to the system: bulk-to-well and the
+    wells' diagonal blocks exact; the blocks that carry dQ/dXs times
+    dSec_dPri (a BLAS product in the reference) within 1e-13 normwise; every
+    other block of the system untouched."""
+    checked = 0
+    for it, fx in iterations(name):
+        jac = {k.split("/", 1)[1]: v for k, v in fx.items() if k.startswith("jac/")}
+        if not jac:
+            continue
+        wells, nc, np_ = W.split_wells(jac)
+        ncol = nc + 1
+        nb = len(jac["jac_rowptr"]) - 1
+        before = _blocks(jac["jac_rowptr"], jac["jac_col"], jac["jac_val"], ncol)
+        after = _blocks(jac["jacw_rowptr"], jac["jacw_col"], jac["jacw_val"], ncol)
+        got = W.well_jacobian(wells, jac, float(jac["dt"][0]), nb, nc, np_)
+        expect_new = set(got["bulk_well"]) | {(w, w) for w in got["well_diag"]} | set(got["well_bulk"])
+        assert set(after) == set(before) | expect_new, it
+        for key, blk in after.items():
+            r, c = key
+            if key in got["bulk_well"]:
+                assert np.array_equal(blk, got["bulk_well"][key]), (it, key)
+            elif r >= nb and r == c:
+                assert np.array_equal(blk, got["well_diag"][r]), (it, key)
+            elif key in got["well_bulk"]:
+                assert _close(blk, got["well_bulk"][key]) or (
+                    not np.any(blk) and not np.any(got["well_bulk"][key])), (it, key)
+            elif r == c and r in got["bulk_add"]:
+                assert _close(blk, before[key] + got["bulk_add"][r]), (it, key)
+            else:
+                assert np.array_equal(blk, before[key]), (it, key)
+        checked += 1
+    assert checked > 0

@@ -396,6 +396,8 @@ ocpx_status ocpx_adjoint(ocpx_ctx* ctx, const double* lambda, double* jt_lambda,
  *                           (src/OCPControlNR.cpp:27-77), as IsoT_FIM::FinishNR
  *                           calls it (src/IsoThermalMethod.cpp:838-864)
  *   ocpx_next_time_step     ControlTime::CalNextTimeStep with {"dP", "dS", "iter"}
+ *   ocpx_wells_eval         PeacemanWell(IsoT) CalTrans, CalFlux, CalResFIM,
+ *                           AssembleMatInjFIM / AssembleMatProdFIM
  *                           (src/OCPControlTime.cpp:128-178), as IsoT_FIM::FinishStep
  *                           calls it (src/IsoThermalMethod.cpp:865-870)
  * The maxima are signed, with the reference's rule: the first entry in cell
@@ -436,6 +438,38 @@ ocpx_status ocpx_nr_check_converge(ocpx_ctx* ctx, const ocpx_nr_control* c, int*
 /* next_dt: the length of the next time step (clamped to the end of the
  * current report interval, end_time); predict_dt: the same before that clamp */
 ocpx_status ocpx_next_time_step(ocpx_ctx* ctx, const ocpx_nr_control* c, double* next_dt, double* predict_dt);
+
+/* Peaceman wells: the wells' part of the residual and of the Jacobian,
+ * computed on the device from the context's current bulk state (kr, mu, xi,
+ * xij and their derivatives, dSec_dPri) and, for the residual, its last
+ * ocpx_calres.  Replaces PeacemanWell::CalTrans / CalFlux and
+ * PeacemanWellIsoT::CalResFIM / AssembleMatInjFIM / AssembleMatProdFIM
+ * (src/WellPeaceman.cpp:365-466, 1226-1361, 1488-1613) for open wells; the
+ * unweighted-permeability option is not supported.  Inputs the reference
+ * computes at well setup or from the mixture are passed in: WI*multiplier and
+ * dG per perforation, the injected fluid's molar density per perforation, the
+ * rate-control factors (CalFactor). */
+typedef struct ocpx_well {
+    int type;               /* 0 injector, 1 producer */
+    int mode;               /* 0 BHP control, 1 rate control */
+    double bhp, tar_bhp, tar_rate;
+    int nperf;
+    const int* cell;        /* [nperf] perforated cells */
+    const double* WI;       /* [nperf] WI * multiplier */
+    const double* dG;       /* [nperf] perforation pressure minus bhp */
+    const double* xi_inj;   /* [nperf] injected fluid molar density (injectors) */
+    const double* inj_zi;   /* [nc] injected composition (injectors) */
+    const double* factor;   /* [nc] rate factors (rate control) */
+} ocpx_well;
+/* res_out [(nb + nwell) * (nc + 1)], may be NULL: the residual with the
+ * wells, in the reference's sign (IsoT_FIM::CalRes negates it), well w's row
+ * at nb + w.  blocks_out, may be NULL: (nc + 1)^2 values, row-major, per
+ * block: for each perforation in order the block added to its cell's
+ * diagonal, the cell-to-well block (row cell, column nb + w) and the
+ * well-to-cell block (row nb + w, column cell); then each well's diagonal
+ * block.  max_rel, may be NULL: maxWellRelRes_mol. */
+ocpx_status ocpx_wells_eval(ocpx_ctx* ctx, int nwell, const ocpx_well* wells, double dt, double* res_out,
+                            double* blocks_out, double* max_rel);
 
 /* Linear solve of the Newton system on the device: J u = rhs, J the bulk
  * Jacobian of the last ocpx_assemble and rhs the residual of the last

@@ -5,6 +5,10 @@ compiled once per component capacity (4, 6, 8, 10, 12 EoS components).
 Objects go to opencaeporox_gb300/_build/, the library next to this file.
 Parity builds use --fmad=false: the reference is compiled without FMA
 contraction, and the black-oil and assembly arithmetic is then bit-identical.
+The host code is compiled with -ffp-contract=off for the same reason: GCC
+contracts a*b + c into one fused operation by default where the target has
+one (aarch64 does, baseline x86-64 does not), and the host sums of the C ABI
+(the wells' rows, for one) must round the same on both.
 """
 from __future__ import annotations
 
@@ -32,13 +36,14 @@ def nvcc_path() -> str:
 
 def common_flags():
     return ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+                   "-Xcompiler", "-ffp-contract=off",
                    "-I" + os.path.join(REPO, "include"), "-I" + CSRC, "-diag-suppress", "177"]
 
 
 def units():
     out = [("k_fim.cu", [], "k_fim.o"), ("ocpx_capi.cu", [], "ocpx_capi.o"), ("k_probe.cu", [], "k_probe.o"),
            ("k_noalloc.cu", [], "k_noalloc.o"), ("k_nrctl.cu", [], "k_nrctl.o"),
-           ("k_linsolve.cu", [], "k_linsolve.o")]
+           ("k_linsolve.cu", [], "k_linsolve.o"), ("k_wells.cu", [], "k_wells.o")]
     for c in NCM_CAPS:
         out.append(("k_flash_comp.cu", [f"-DOCPX_NCM={c}"], f"k_flash_comp_{c}.o"))
     return out

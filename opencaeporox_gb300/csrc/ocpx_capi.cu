@@ -1024,6 +1024,130 @@ ocpx_status ocpx_next_time_step(ocpx_ctx* ctx, const ocpx_nr_control* c, double*
     return OCPX_OK;
 }
 
+ocpx_status ocpx_wells_eval(ocpx_ctx* ctx, int nwell, const ocpx_well* wells, double dt, double* res_out,
+                            double* blocks_out, double* max_rel)
+{
+    if (!ctx || nwell < 0 || (nwell > 0 && !wells)) return fail(OCPX_INVALID_ARG, "null argument");
+    const int nb = ctx->nb, nc = ctx->nc, ncol = nc + 1;
+    const size_t bs = (size_t)ncol * ncol;
+    if (ctx->np != 3 || nc + 1 > NCT_MAX + 1) return fail(OCPX_INVALID_ARG, "wells need three phases");
+    std::vector<WellPerf> perf;
+    std::vector<double> zi((size_t)nwell * nc, 0.0), fac((size_t)nwell * nc, 0.0);
+    for (int w = 0; w < nwell; w++) {
+        const ocpx_well& W = wells[w];
+        if ((W.type != 0 && W.type != 1) || (W.mode != 0 && W.mode != 1) || W.nperf < 0)
+            return fail(OCPX_INVALID_ARG, "well " + std::to_string(w) + ": type, mode or perforation count");
+        if (W.nperf > 0 && (!W.cell || !W.WI || !W.dG || (W.type == 0 && !W.xi_inj)))
+            return fail(OCPX_INVALID_ARG, "well " + std::to_string(w) + ": missing perforation data");
+        if ((W.type == 0 && !W.inj_zi) || (W.mode == 1 && (!W.factor || W.tar_rate == 0.0)))
+            return fail(OCPX_INVALID_ARG, "well " + std::to_string(w) + ": missing injection or rate data");
+        for (int i = 0; i < nc; i++) {
+            if (W.inj_zi) zi[(size_t)w * nc + i] = W.inj_zi[i];
+            if (W.factor) fac[(size_t)w * nc + i] = W.factor[i];
+        }
+        for (int q = 0; q < W.nperf; q++) {
+            if (W.cell[q] < 0 || W.cell[q] >= nb)
+                return fail(OCPX_INVALID_ARG, "well " + std::to_string(w) + ": perforated cell out of range");
+            perf.push_back(WellPerf{W.cell[q], w, W.type, W.mode, W.bhp, W.WI[q], W.dG[q],
+                                    W.type == 0 ? W.xi_inj[q] : 0.0});
+        }
+    }
+    const int np_ = (int)perf.size();
+    std::vector<double> qi((size_t)np_ * nc), dqw((size_t)np_ * nc), bb((size_t)np_ * bs), wb((size_t)np_ * bs);
+    if (np_ > 0) {
+        // one allocation for the call's inputs and outputs
+        const size_t n_in = sizeof(WellPerf) * np_, n_z = sizeof(double) * zi.size();
+        const size_t n_q = sizeof(double) * qi.size(), n_b = sizeof(double) * bb.size();
+        char* buf = nullptr;
+        const size_t off_z = align256(n_in), off_f = off_z + align256(n_z), off_q = off_f + align256(n_z);
+        const size_t off_w = off_q + align256(n_q), off_bb = off_w + align256(n_q), off_wb = off_bb + align256(n_b);
+        OCPX_CUDA(cudaMalloc(&buf, off_wb + align256(n_b)));
+        cudaStream_t s = ctx->stream;
+        cudaError_t e = cudaMemcpyAsync(buf, perf.data(), n_in, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && n_z) e = cudaMemcpyAsync(buf + off_z, zi.data(), n_z, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && n_z) e = cudaMemcpyAsync(buf + off_f, fac.data(), n_z, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = launch_well_perf(ctx->b, (const WellPerf*)buf, np_, (const double*)(buf + off_z),
+                                 (const double*)(buf + off_f), dt, (double*)(buf + off_q), (double*)(buf + off_w),
+                                 (double*)(buf + off_bb), (double*)(buf + off_wb), s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(qi.data(), buf + off_q, n_q, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dqw.data(), buf + off_w, n_q, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(bb.data(), buf + off_bb, n_b, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(wb.data(), buf + off_wb, n_b, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        cudaFree(buf);
+        ctx->launches++;
+        if (e != cudaSuccess) return fail(OCPX_CUDA_ERROR, std::string("wells: ") + cudaGetErrorString(e));
+    }
+    // the wells' rows and the perforated cells' rows, summed per well in
+    // perforation order as CalResFIM does, on the residual before CalRes's
+    // negation (negation is exact)
+    double mrel = 0.0;
+    std::vector<double> R;
+    if (res_out) {
+        R.assign((size_t)(nb + nwell) * ncol, 0.0);
+        OCPX_CUDA(cudaMemcpyAsync(R.data(), ctx->res, sizeof(double) * (size_t)nb * ncol, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+        OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (size_t k = 0; k < (size_t)nb * ncol; k++) R[k] = -R[k];
+    }
+    size_t q0 = 0;
+    for (int w = 0; w < nwell; w++) {
+        const ocpx_well& W = wells[w];
+        std::vector<double> qw(nc, 0.0);
+        for (int q = 0; q < W.nperf; q++) {
+            const size_t pq = q0 + q;
+            for (int i = 0; i < nc; i++) qw[i] += qi[pq * nc + i];
+            if (res_out)
+                for (int i = 0; i < nc; i++) R[(size_t)W.cell[q] * ncol + 1 + i] += qi[pq * nc + i] * dt;
+        }
+        double r;
+        if (W.mode == 0) r = W.bhp - W.tar_bhp;
+        else {
+            r = W.type == 0 ? W.tar_rate : -W.tar_rate;
+            for (int i = 0; i < nc; i++) r += qw[i] * W.factor[i];
+            mrel = std::max(mrel, std::fabs(r / W.tar_rate));
+        }
+        if (res_out) R[(size_t)(nb + w) * ncol] = r;
+        q0 += W.nperf;
+    }
+    if (res_out)
+        for (size_t k = 0; k < R.size(); k++) res_out[k] = -R[k];
+    if (blocks_out) {
+        double* out = blocks_out;
+        for (int pq = 0; pq < np_; pq++) {
+            std::copy(bb.begin() + pq * bs, bb.begin() + (pq + 1) * bs, out);
+            out += bs;
+            std::fill(out, out + bs, 0.0);
+            for (int i = 0; i < nc; i++) out[(size_t)(i + 1) * ncol] = dqw[(size_t)pq * nc + i] * dt;
+            out += bs;
+            if (perf[pq].mode == 1) std::copy(wb.begin() + pq * bs, wb.begin() + (pq + 1) * bs, out);
+            else std::fill(out, out + bs, 0.0);
+            out += bs;
+        }
+        q0 = 0;
+        for (int w = 0; w < nwell; w++) {
+            const ocpx_well& W = wells[w];
+            std::fill(out, out + bs, 0.0);
+            for (int q = 0; q < W.nperf; q++) {
+                if (W.mode == 0) {
+                    for (int i = 0; i < ncol; i++) out[(size_t)i * ncol + i] += 1.0;
+                }
+                else {
+                    double d0 = 0.0;
+                    for (int i = 0; i < nc; i++) d0 += dqw[(q0 + q) * nc + i] * W.factor[i];
+                    out[0] += d0;
+                    for (int i = 0; i < nc; i++) out[(size_t)(i + 1) * ncol + i + 1] += 1.0;
+                }
+            }
+            out += bs;
+            q0 += W.nperf;
+        }
+    }
+    if (max_rel) *max_rel = mrel;
+    return OCPX_OK;
+}
+
 ocpx_status ocpx_checkpoint(ocpx_ctx* ctx, int slot, int restore)
 {
     if (!ctx || slot < 0 || slot > 1) return fail(OCPX_INVALID_ARG, "checkpoint slot must be 0 or 1");

@@ -87,6 +87,17 @@ cudaError_t launch_nr_converge(const NRControl& c, const double* nr5, const RowN
                                int* state, cudaStream_t s);
 cudaError_t launch_next_dt(const NRControl& c, const double* ts5, double* out2, cudaStream_t s);
 
+// one perforation of a Peaceman well (k_wells.cu)
+struct WellPerf {
+    int cell, well, type, mode;
+    double bhp, WIm, dG, xi_inj;
+};
+// per perforation: qi [nc], dQ/dP_well [nc], the cell's diagonal addition and
+// the well-to-cell block (rate control) [(nc+1)^2 each]
+cudaError_t launch_well_perf(const BulkView& b, const WellPerf* perf, int nperf, const double* inj_zi,
+                             const double* factor, double dt, double* qi, double* dqw, double* bb, double* wb,
+                             cudaStream_t s);
+
 // Linear solve of J u = rhs on the device (k_linsolve.cu): BiCGStab with right
 // block-Jacobi preconditioning, x from zero; scratch holds
 // linsolve_scratch_doubles(nb, dim) doubles.  The residual norm is read every

@@ -53,6 +53,14 @@ REF_NAMES = {"P": "P", "T": "T", "Pb": "PB", "Ni": "NI", "lNi": "LNI", "Nt": "NT
              "skip_zi": "SKIP_ZI"}
 
 
+class Well(C.Structure):
+    """ocpx_well (include/ocpx.h)."""
+    _fields_ = [("type", C.c_int), ("mode", C.c_int), ("bhp", C.c_double), ("tar_bhp", C.c_double),
+                ("tar_rate", C.c_double), ("nperf", C.c_int), ("cell", C.POINTER(C.c_int)),
+                ("WI", C.POINTER(C.c_double)), ("dG", C.POINTER(C.c_double)), ("xi_inj", C.POINTER(C.c_double)),
+                ("inj_zi", C.POINTER(C.c_double)), ("factor", C.POINTER(C.c_double))]
+
+
 class Table(C.Structure):
     _fields_ = [("nrow", C.c_int), ("ncol", C.c_int), ("data", C.POINTER(C.c_double))]
 
@@ -128,7 +136,7 @@ EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy",
            "ocpx_profile_enable", "ocpx_profile_read", "ocpx_checkpoint", "ocpx_measure_fp64_tflops",
            "ocpx_stream", "ocpx_launch_count", "ocpx_set_param", "ocpx_get_param", "ocpx_adjoint",
            "ocpx_nr_init_step", "ocpx_nr_max_change", "ocpx_step_max_change", "ocpx_nr_check_converge",
-           "ocpx_next_time_step", "ocpx_linsolve", "ocpx_newton_update_device"]
+           "ocpx_next_time_step", "ocpx_linsolve", "ocpx_newton_update_device", "ocpx_wells_eval"]
 
 PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3, "predefer": 4, "coop_cells": 5,
           "predeferred": 6, "level": 7, "pre_blocks": 8,
@@ -180,6 +188,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.ocpx_step_max_change.argtypes = [P, C.POINTER(ChangeMax)]
     lib.ocpx_nr_check_converge.argtypes = [P, C.POINTER(NRControl), C.POINTER(C.c_int)]
     lib.ocpx_next_time_step.argtypes = [P, C.POINTER(NRControl), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.ocpx_wells_eval.argtypes = [P, C.c_int, C.POINTER(Well), C.c_double, P, P, C.POINTER(C.c_double)]
     lib.ocpx_get_param.argtypes = [P, C.c_int, C.POINTER(C.c_longlong)]
     for fn in ("ocpx_enqueue_step", "ocpx_step_report", "ocpx_profile_enable", "ocpx_profile_read",
                "ocpx_measure_fp64_tflops", "ocpx_checkpoint", "ocpx_set_param", "ocpx_get_param"):
@@ -523,6 +532,42 @@ class FimContext:
         dt, pdt = C.c_double(), C.c_double()
         _check(self.lib.ocpx_next_time_step(self.h, C.byref(ctrl), C.byref(dt), C.byref(pdt)))
         return dt.value, pdt.value
+
+    def wells_eval(self, wells: list, dt: float):
+        """The wells' part of the residual and Jacobian (ocpx_wells_eval).
+        wells: dicts with type, mode, bhp, tar_bhp, tar_rate, cell, WI (times
+        the multiplier), dG, xi_inj, inj_zi, factor.  Returns the residual
+        with the wells ((nb + nwell) * (nc + 1)), the blocks as
+        [nperf][3][nc+1][nc+1] (cell diagonal addition, cell-to-well,
+        well-to-cell) and [nwell][nc+1][nc+1] (well diagonals), and
+        maxWellRelRes_mol."""
+        keep, arr = [], (Well * max(len(wells), 1))()
+        for k, w in enumerate(wells):
+            def dptr(key, n):
+                v = w.get(key)
+                if v is None:
+                    return None
+                a = np.ascontiguousarray(np.asarray(v, dtype=np.float64).ravel())
+                assert a.size >= n, key
+                keep.append(a)
+                return a.ctypes.data_as(C.POINTER(C.c_double))
+            cell = np.ascontiguousarray(np.asarray(w["cell"], dtype=np.int32).ravel())
+            keep.append(cell)
+            n = cell.size
+            arr[k] = Well(int(w["type"]), int(w["mode"]), float(w["bhp"]), float(w.get("tar_bhp", 0.0)),
+                          float(w.get("tar_rate", 0.0)), n, cell.ctypes.data_as(C.POINTER(C.c_int)),
+                          dptr("WI", n), dptr("dG", n), dptr("xi_inj", n), dptr("inj_zi", self.nc),
+                          dptr("factor", self.nc))
+        ncol = self.nc + 1
+        nperf = sum(len(np.ravel(w["cell"])) for w in wells)
+        res = np.empty((self.nb + len(wells)) * ncol)
+        blocks = np.empty((3 * nperf + len(wells)) * ncol * ncol)
+        mrel = C.c_double()
+        _check(self.lib.ocpx_wells_eval(self.h, len(wells), arr, dt, res.ctypes.data_as(C.c_void_p),
+                                        blocks.ctypes.data_as(C.c_void_p), C.byref(mrel)))
+        pb = blocks[:3 * nperf * ncol * ncol].reshape(nperf, 3, ncol, ncol)
+        wd = blocks[3 * nperf * ncol * ncol:].reshape(len(wells), ncol, ncol)
+        return res, pb, wd, mrel.value
 
     def jacobian(self):
         nrow, nnz, bd = C.c_size_t(), C.c_size_t(), C.c_int()

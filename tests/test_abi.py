@@ -59,3 +59,44 @@ def test_python_parameter_names_match_the_header():
     enum = re.search(r"typedef enum ocpx_param \{(.*?)\}", text, flags=re.S).group(1)
     declared = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"OCPX_PARAM_([A-Z0-9_]+)\s*=\s*(\d+)", enum)}
     assert declared == fim.PARAMS
+
+
+STRUCTS = {"ocpx_well": "Well", "ocpx_table": "Table", "ocpx_model_desc": "ModelDesc", "ocpx_grid_desc": "GridDesc",
+           "ocpx_report": "Report", "ocpx_norms": "Norms", "ocpx_change_max": "ChangeMax",
+           "ocpx_solve_report": "SolveReport", "ocpx_nr_control": "NRControl"}
+
+
+def test_python_structs_match_the_header(tmp_path):
+    """Every struct the Python mirror passes through the ABI has the size and
+    alignment the C compiler gives the header's struct, and each field sits
+    at the C offset of the field of the same name."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void) {"]
+    for cname, pname in STRUCTS.items():
+        lines.append(f'printf("{cname} size %zu align %zu\\n", sizeof({cname}), _Alignof({cname}));')
+        for fname, _ in getattr(fim, pname)._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines()
+    got = {}
+    for line in out:
+        parts = line.split()
+        if parts[1] == "size":
+            got[(parts[0], "size")] = int(parts[2])
+            got[(parts[0], "align")] = int(parts[4])
+        else:
+            got[(parts[0], parts[1])] = int(parts[2])
+    for cname, pname in STRUCTS.items():
+        st = getattr(fim, pname)
+        assert C.sizeof(st) == got[(cname, "size")], cname
+        assert C.alignment(st) == got[(cname, "align")], cname
+        for fname, _ in st._fields_:
+            assert getattr(st, fname).offset == got[(cname, fname)], (cname, fname)

@@ -205,8 +205,10 @@ void dump_state(const string& dir, Reservoir& rs)
 // CalResFIM): well arrays per well, perforation arrays concatenated.
 void dump_wells(const string& dir, Reservoir& rs)
 {
-    vector<int32_t> type, mode, nperf, loc;
+    vector<int32_t> type, mode, nperf, loc, pdir;
     vector<double>  bhp, tar_bhp, tar_rate, factor, inj_zi, qi, WI, mult, dG, P, transj, trans_inj, xi, pqi;
+    vector<double>  kh, radius, skin, cdx, cdy, cdz, cntg, ckx, cky, ckz;
+    const BulkVarSet& bvs = rs.bulk.vs;
     for (Well* w0 : rs.allWells.wells) {
         PeacemanWell* w = dynamic_cast<PeacemanWell*>(w0);
         if (!w || w->opt.state != WellState::open) continue;
@@ -232,8 +234,31 @@ void dump_wells(const string& dir, Reservoir& rs)
             trans_inj.push_back(f.transINJ);
             xi.push_back(f.xi);
             for (USI i = 0; i < w->nc; i++) pqi.push_back(f.qi_lbmol[i]);
+            pdir.push_back((int32_t)f.direction);
+            kh.push_back(f.kh);
+            radius.push_back(f.radius);
+            skin.push_back(f.skinFactor);
+            cdx.push_back(bvs.dx[f.location]);
+            cdy.push_back(bvs.dy[f.location]);
+            cdz.push_back(bvs.dz[f.location]);
+            cntg.push_back(bvs.ntg[f.location]);
+            ckx.push_back(bvs.rockKx[f.location]);
+            cky.push_back(bvs.rockKy[f.location]);
+            ckz.push_back(bvs.rockKz[f.location]);
         }
     }
+    put(dir, "perf_dir", pdir);
+    put(dir, "perf_kh", kh);
+    put(dir, "perf_radius", radius);
+    put(dir, "perf_skin", skin);
+    put(dir, "perf_cell_dx", cdx);
+    put(dir, "perf_cell_dy", cdy);
+    put(dir, "perf_cell_dz", cdz);
+    put(dir, "perf_cell_ntg", cntg);
+    put(dir, "perf_cell_kx", ckx);
+    put(dir, "perf_cell_ky", cky);
+    put(dir, "perf_cell_kz", ckz);
+    put1(dir, "conv_darcy", CONV_DARCY);
     put(dir, "well_type", type);
     put(dir, "well_mode", mode);
     put(dir, "well_nperf", nperf);

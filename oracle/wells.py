@@ -20,8 +20,11 @@ iteration:
   under rate control, which also updates maxWellRelRes_mol; the caller then
   negates the whole residual (src/IsoThermalMethod.cpp:1170).
 
+The perforations' WI is restated too (PeacemanWell::CalWI, Peaceman's
+equivalent radius for x, y or z perforations, from the cell's size, net to
+gross and permeabilities, the well radius and skin; well_index below).
 Inputs not restated here and taken from the reference's dump: the
-perforations' WI, multiplier and dG (well setup), the injected fluid's molar
+perforations' multiplier and dG (well setup), the injected fluid's molar
 density xi_inj (the reference's PVT at the perforation pressure, computed at
 the first flux of a time step) and the rate-control factors (CalFactor,
 src/WellPeaceman.cpp:654-712: the mixture at surface conditions).
@@ -225,3 +228,32 @@ def well_jacobian(wells: list[dict], state: dict, dt: float, nb: int, nc: int, n
                 well_bulk[(wid, n)] = np.zeros((ncol, ncol))
         well_diag[wid] = diag
     return dict(bulk_add=bulk_add, bulk_well=bulk_well, well_diag=well_diag, well_bulk=well_bulk)
+
+
+PI = 3.141592653  # include/OCPConst.hpp:32, the reference's value
+
+
+def well_index(direction: int, dx: float, dy: float, dz: float, ntg: float, kx: float, ky: float, kz: float,
+               radius: float, skin: float, conv_darcy: float, kh: float = -1.0):
+    """PeacemanWell::CalWI (src/WellPeaceman.cpp:277-361) for a perforation
+    whose WI is not given: Peaceman's equivalent radius for a perforation
+    along x (0), y (1) or z (2); kh < 0 means derived from the cell.  Returns
+    (WI, kh).  math.pow and math.log are the C library's, as the reference's."""
+    import math
+    dz = dz * ntg
+    if direction == 0:
+        a, b, l1, l2, length = ky, kz, dy, dz, dx
+    elif direction == 1:
+        a, b, l1, l2, length = kz, kx, dz, dx, dy
+    elif direction == 2:
+        a, b, l1, l2, length = kx, ky, dx, dy, dz
+    else:
+        raise ValueError("unstructured perforations are not restated")
+    ab = a * b
+    a_b = a / b
+    ro = 0.28 * math.pow((l1 * l1 * math.pow(1 / a_b, 0.5) + l2 * l2 * math.pow(a_b, 0.5)), 0.5)
+    ro /= (math.pow(a_b, 0.25) + math.pow(1 / a_b, 0.25))
+    if kh < 0:
+        kh = length * math.pow(ab, 0.5)
+    wi = (2 * PI) * kh / (math.log(ro / radius) + skin)
+    return wi * conv_darcy, kh

@@ -118,6 +118,8 @@ def pack_fim(outdir):
 WELL_KEYS = ["well_type", "well_mode", "well_nperf", "well_bhp", "well_tar_bhp", "well_tar_rate", "well_factor",
              "well_inj_zi", "well_qi", "perf_loc", "perf_WI", "perf_mult", "perf_dG", "perf_P", "perf_transj",
              "perf_trans_inj", "perf_xi", "perf_qi", "res_bulk", "res_full", "maxWellRelRes_mol",
+             "perf_dir", "perf_kh", "perf_radius", "perf_skin", "perf_cell_dx", "perf_cell_dy", "perf_cell_dz",
+             "perf_cell_ntg", "perf_cell_kx", "perf_cell_ky", "perf_cell_kz", "conv_darcy",
              "P", "Pj", "phaseExist", "kr", "mu", "xi", "xij"]
 
 

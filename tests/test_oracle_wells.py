@@ -110,3 +110,17 @@ def test_well_jacobian_blocks(name):
                 assert np.array_equal(blk, before[key]), (it, key)
         checked += 1
     assert checked > 0
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_well_index(name):
+    """Peaceman's WI and the derived kh of every perforation, from the cell
+    and the well radius and skin, bit-identical (the decks give no WI or kh)."""
+    for it, fx in iterations(name):
+        conv = float(fx["conv_darcy"][0])
+        for p in range(len(fx["perf_loc"])):
+            wi, kh = W.well_index(int(fx["perf_dir"][p]), *(float(fx["perf_cell_" + k][p]) for k in
+                                                            ("dx", "dy", "dz", "ntg", "kx", "ky", "kz")),
+                                  float(fx["perf_radius"][p]), float(fx["perf_skin"][p]), conv)
+            assert kh == float(fx["perf_kh"][p]), (it, p)
+            assert wi == float(fx["perf_WI"][p]), (it, p)

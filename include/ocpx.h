@@ -361,8 +361,10 @@ ocpx_status ocpx_measure_fp64_tflops(int device, int iters, double* tflops);
  * OCPX_RELRES_NOALLOC_MAX_CELLS returns OCPX_INVALID_ARG.  The scratch's
  * block counter starts at zero and every call leaves it at zero.  Calls
  * whose kernels overlap in time race on the scratch: serialise them (one
- * stream).  The first call on each device looks up the scratch address
- * (cudaGetSymbolAddress): make it outside any stream capture.  Errors are
+ * stream).  Every call looks up the scratch's address in the current
+ * device's context (cudaGetSymbolAddress, which allocates nothing); the first
+ * call on a device may load the library's module there, so make it outside
+ * any stream capture.  Errors are
  * returned as status only; ocpx_last_error is not updated. */
 #define OCPX_RELRES_NOALLOC_MAX_BLOCKS 1024
 #define OCPX_RELRES_NOALLOC_MAX_CELLS 2097152

@@ -6,6 +6,9 @@
 #ifndef OCPX_NCM
 #error "compile with -DOCPX_NCM=<capacity>"
 #endif
+#ifndef OCPX_FLASH_PART
+#error "compile with -DOCPX_FLASH_PART=<0..6>"
+#endif
 
 namespace ocpx {
 
@@ -298,8 +301,35 @@ __global__ void __launch_bounds__(128) k_flash_post(const Model* __restrict__ M,
 
 #define OCPX_CAT2(a, b) a##b
 #define OCPX_CAT(a, b) OCPX_CAT2(a, b)
+#define OCPX_NAME(base) OCPX_CAT(base, OCPX_NCM)
 
-cudaError_t OCPX_CAT(launch_flash_comp_, OCPX_NCM)(const Model* dm, const BulkView& b, int block, cudaStream_t s)
+// Each kernel of a capacity is compiled in its own translation unit
+// (OCPX_FLASH_PART, build.py), so the large kernels compile in parallel.  Part
+// 0 holds the plain kernel and the dispatch of the batched parts; the others
+// hold one kernel each and the launch that uses it.
+cudaError_t OCPX_NAME(flash_part_budget_)(const Model*, const BulkView&, const int*, const FlashBatch&, cudaStream_t);
+cudaError_t OCPX_NAME(flash_part_fused_)(const Model*, const BulkView&, const int*, const FlashBatch&, cudaStream_t);
+cudaError_t OCPX_NAME(flash_part_round_)(const Model*, const BulkView&, const FlashBatch&, cudaStream_t);
+cudaError_t OCPX_NAME(flash_part_coop_)(const Model*, const BulkView&, const FlashBatch&, cudaStream_t);
+cudaError_t OCPX_NAME(flash_part_post_)(const Model*, const BulkView&, const FlashBatch&, cudaStream_t);
+cudaError_t OCPX_NAME(setup_flash_coop_)(int, int, int*);
+cudaError_t OCPX_NAME(setup_flash_fused_)(int, int*);
+
+// parts 1 and 2 carry their own launch priority, which a stream capture keeps
+// in the graph's kernel node
+static inline void priority_attr(cudaLaunchConfig_t& cfg, cudaLaunchAttribute* attr, const FlashBatch& fb,
+                                 cudaStream_t s)
+{
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = fb.prio;
+    cfg = {};
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = fb.prio ? 1 : 0;
+}
+
+#if OCPX_FLASH_PART == 0
+cudaError_t OCPX_NAME(launch_flash_comp_)(const Model* dm, const BulkView& b, int block, cudaStream_t s)
 {
     if (b.nb == 0) return cudaSuccess;
     const int grid = (b.nb + block - 1) / block;
@@ -307,113 +337,80 @@ cudaError_t OCPX_CAT(launch_flash_comp_, OCPX_NCM)(const Model* dm, const BulkVi
     return cudaGetLastError();
 }
 
-cudaError_t OCPX_CAT(launch_flash_batched_, OCPX_NCM)(const Model* dm, const BulkView& b, const int* order,
-                                                      const FlashBatch& fb, int part, cudaStream_t s)
+cudaError_t OCPX_NAME(launch_flash_batched_)(const Model* dm, const BulkView& b, const int* order,
+                                             const FlashBatch& fb, int part, cudaStream_t s)
 {
     if (b.nb == 0) return cudaSuccess;
     switch (part) {
-    case 0: {
-        const DeferSink sink{fb.rec, fb.count, fb.cap};
-        const int grid = fb.cell_blocks > 0 ? fb.cell_blocks : (b.nb + fb.block - 1) / fb.block;
-        k_flash_budget<OCPX_NCM><<<grid, fb.block, 0, s>>>(dm, b, order, fb.budget, sink, fb.pre, fb.level,
-                                                           fb.cell_blocks > 0 ? fb.cell_next : nullptr);
-        break;
+    case 0: return OCPX_NAME(flash_part_budget_)(dm, b, order, fb, s);
+    case 4: return OCPX_NAME(flash_part_fused_)(dm, b, order, fb, s);
+    case 3: return OCPX_NAME(flash_part_round_)(dm, b, fb, s);
+    case 1: return OCPX_NAME(flash_part_coop_)(dm, b, fb, s);
+    case 2:
+    default: return OCPX_NAME(flash_part_post_)(dm, b, fb, s);
     }
-    case 4: {
-        // fused: pre list (rin, rin_count, pe_pre) and late list (rec, count, pe)
-        DeferSink late{fb.rec, fb.count, fb.cap};
-        late.seq = 1;
-        cudaLaunchConfig_t cfg = {};
-        cfg.stream = s;
-        cfg.gridDim = dim3(fb.cell_blocks);
-        cfg.blockDim = dim3(FUSED_WARPS * 32);
-        cfg.dynamicSmemBytes = fb.excl_blocks ? fb.excl_smem_fused : 0;
-        // without the SM-exclusive reservation the SM keeps as much L1 as the
-        // static shared memory allows: the per-lane cells' thread frames live there.
-        // With cooperative-only blocks, those blocks wait for the others: a
-        // cooperative launch guarantees that all blocks are resident together
-        cudaLaunchAttribute attr[2];
-        attr[0].id = cudaLaunchAttributePreferredSharedMemoryCarveout;
-        attr[0].val.sharedMemCarveout = fb.excl_blocks ? (unsigned)cudaSharedmemCarveoutMaxShared
-                                                       : (unsigned)cudaSharedmemCarveoutMaxL1;
-        attr[1].id = cudaLaunchAttributeCooperative;
-        attr[1].val.cooperative = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = fb.coop_only_blocks > 0 ? 2 : 1;
-        return cudaLaunchKernelEx(&cfg, k_flash_fused<OCPX_NCM>, dm, b, order, fb.budget, fb.pre, fb.level, fb.rin,
-                                  fb.rin_count, fb.pe_pre, late, fb.pe, fb.cell_next, fb.coop_only_blocks,
-                                  fb.watchdog);
-    }
-    case 3: {
-        // re-budgeting round: from list (rin, rin_count) into (rec, count)
-        const DeferSink sink{fb.rec, fb.count, fb.cap};
-        const int grid = fb.cell_blocks > 0 ? fb.cell_blocks : 304;
-        k_flash_round<OCPX_NCM><<<grid, fb.block, 0, s>>>(dm, b, fb.rin, fb.rin_count, fb.cap, fb.budget, fb.mult,
-                                                          sink, fb.level, fb.cell_next);
-        break;
-    }
-    case 1:
-    default: {
-        // parts 1 and 2 carry their own launch priority, which a stream
-        // capture keeps in the graph's kernel node
-        cudaLaunchAttribute attr[2];
-        attr[0].id = cudaLaunchAttributePriority;
-        attr[0].val.priority = fb.prio;
-        cudaLaunchConfig_t cfg = {};
-        cfg.stream = s;
-        cfg.attrs = attr;
-        cfg.numAttrs = fb.prio ? 1 : 0;
-        if (part == 1 && fb.excl_blocks > 0) {
-            cfg.gridDim = dim3(fb.excl_blocks);
-            cfg.blockDim = dim3(EXCL_WARPS * 32);
-            cfg.dynamicSmemBytes = fb.excl_smem;
-            return cudaLaunchKernelEx(&cfg, k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>, dm, b, (const DeferRec*)fb.rec,
-                                      (const unsigned*)fb.count, fb.cap, fb.coop_next, fb.pe);
-        }
-        if (part == 1) {
-            cfg.gridDim = dim3(fb.coop_blocks);
-            cfg.blockDim = dim3(COOP_WARPS * 32);
-            return cudaLaunchKernelEx(&cfg, k_flash_pe_coop<OCPX_NCM, COOP_WARPS>, dm, b, (const DeferRec*)fb.rec,
-                                      (const unsigned*)fb.count, fb.cap, fb.coop_next, fb.pe);
-        }
-        // one thread per deferred cell; the SM's L1 as large as it goes, for
-        // the threads' frames
-        const int pb = fb.post_block > 0 ? fb.post_block : 128;
-        const long long threads = (long long)fb.cap * (fb.rec2 ? 2 : 1);
-        cfg.gridDim = dim3((unsigned)((threads + pb - 1) / pb));
-        cfg.blockDim = dim3(pb);
-        attr[cfg.numAttrs].id = cudaLaunchAttributePreferredSharedMemoryCarveout;
-        attr[cfg.numAttrs].val.sharedMemCarveout = (unsigned)cudaSharedmemCarveoutMaxL1;
-        cfg.numAttrs++;
-        return cudaLaunchKernelEx(&cfg, k_flash_post<OCPX_NCM>, dm, b, (const DeferRec*)fb.rec,
-                                  (const unsigned*)fb.count, fb.cap, (const PERes*)fb.pe, fb.rec2, fb.count2,
-                                  fb.pe2);
-    }
-    }
-    return cudaGetLastError();
 }
 
 // Once per device (that device current): the SM-exclusive cooperative kernel
-// may use all the shared memory a block can opt into; *excl_smem receives the
-// dynamic part that fills it.
-cudaError_t OCPX_CAT(setup_flash_batched_, OCPX_NCM)(int* excl_smem)
+// may use all the shared memory a block can opt into; excl_smem[0] receives
+// the dynamic part that fills it, excl_smem[1] the fused kernel's, and
+// excl_smem[2] the fused blocks resident per SM without it.
+cudaError_t OCPX_NAME(setup_flash_batched_)(int* excl_smem)
 {
     int dev = 0, optin = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaFuncAttributes fa{};
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>);
-    if (e != cudaSuccess) return e;
-    const int dyn = optin > (int)fa.sharedSizeBytes ? optin - (int)fa.sharedSizeBytes : 0;
-    e = cudaFuncSetAttribute(k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared);
-    *excl_smem = dyn;
-    if (e != cudaSuccess) return e;
-    // the fused kernel, when it holds an SM alone (one block per SM)
+    if (e == cudaSuccess) e = OCPX_NAME(setup_flash_coop_)(dev, optin, excl_smem);
+    if (e == cudaSuccess) e = OCPX_NAME(setup_flash_fused_)(optin, excl_smem);
+    return e;
+}
+#endif
+
+#if OCPX_FLASH_PART == 1
+cudaError_t OCPX_NAME(flash_part_budget_)(const Model* dm, const BulkView& b, const int* order, const FlashBatch& fb,
+                                          cudaStream_t s)
+{
+    const DeferSink sink{fb.rec, fb.count, fb.cap};
+    const int grid = fb.cell_blocks > 0 ? fb.cell_blocks : (b.nb + fb.block - 1) / fb.block;
+    k_flash_budget<OCPX_NCM><<<grid, fb.block, 0, s>>>(dm, b, order, fb.budget, sink, fb.pre, fb.level,
+                                                       fb.cell_blocks > 0 ? fb.cell_next : nullptr);
+    return cudaGetLastError();
+}
+#endif
+
+#if OCPX_FLASH_PART == 2
+cudaError_t OCPX_NAME(flash_part_fused_)(const Model* dm, const BulkView& b, const int* order, const FlashBatch& fb,
+                                         cudaStream_t s)
+{
+    // fused: pre list (rin, rin_count, pe_pre) and late list (rec, count, pe)
+    DeferSink late{fb.rec, fb.count, fb.cap};
+    late.seq = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.stream = s;
+    cfg.gridDim = dim3(fb.cell_blocks);
+    cfg.blockDim = dim3(FUSED_WARPS * 32);
+    cfg.dynamicSmemBytes = fb.excl_blocks ? fb.excl_smem_fused : 0;
+    // without the SM-exclusive reservation the SM keeps as much L1 as the
+    // static shared memory allows: the per-lane cells' thread frames live there.
+    // With cooperative-only blocks, those blocks wait for the others: a
+    // cooperative launch guarantees that all blocks are resident together
+    cudaLaunchAttribute attr[2];
+    attr[0].id = cudaLaunchAttributePreferredSharedMemoryCarveout;
+    attr[0].val.sharedMemCarveout = fb.excl_blocks ? (unsigned)cudaSharedmemCarveoutMaxShared
+                                                   : (unsigned)cudaSharedmemCarveoutMaxL1;
+    attr[1].id = cudaLaunchAttributeCooperative;
+    attr[1].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = fb.coop_only_blocks > 0 ? 2 : 1;
+    return cudaLaunchKernelEx(&cfg, k_flash_fused<OCPX_NCM>, dm, b, order, fb.budget, fb.pre, fb.level, fb.rin,
+                              fb.rin_count, fb.pe_pre, late, fb.pe, fb.cell_next, fb.coop_only_blocks, fb.watchdog);
+}
+
+// the fused kernel, when it holds an SM alone (one block per SM)
+cudaError_t OCPX_NAME(setup_flash_fused_)(int optin, int* excl_smem)
+{
     cudaFuncAttributes ff{};
-    e = cudaFuncGetAttributes(&ff, k_flash_fused<OCPX_NCM>);
+    cudaError_t e = cudaFuncGetAttributes(&ff, k_flash_fused<OCPX_NCM>);
     if (e != cudaSuccess) return e;
     const int dynf = optin > (int)ff.sharedSizeBytes ? optin - (int)ff.sharedSizeBytes : 0;
     e = cudaFuncSetAttribute(k_flash_fused<OCPX_NCM>, cudaFuncAttributeMaxDynamicSharedMemorySize, dynf);
@@ -432,5 +429,83 @@ cudaError_t OCPX_CAT(setup_flash_batched_, OCPX_NCM)(int* excl_smem)
     excl_smem[2] = per_sm;
     return e;
 }
+#endif
+
+#if OCPX_FLASH_PART == 3
+cudaError_t OCPX_NAME(flash_part_round_)(const Model* dm, const BulkView& b, const FlashBatch& fb, cudaStream_t s)
+{
+    // re-budgeting round: from list (rin, rin_count) into (rec, count)
+    const DeferSink sink{fb.rec, fb.count, fb.cap};
+    const int grid = fb.cell_blocks > 0 ? fb.cell_blocks : 304;
+    k_flash_round<OCPX_NCM><<<grid, fb.block, 0, s>>>(dm, b, fb.rin, fb.rin_count, fb.cap, fb.budget, fb.mult, sink,
+                                                      fb.level, fb.cell_next);
+    return cudaGetLastError();
+}
+#endif
+
+#if OCPX_FLASH_PART == 4
+cudaError_t OCPX_NAME(flash_part_coop_excl_)(const Model*, const BulkView&, const FlashBatch&, cudaStream_t);
+
+cudaError_t OCPX_NAME(flash_part_coop_)(const Model* dm, const BulkView& b, const FlashBatch& fb, cudaStream_t s)
+{
+    if (fb.excl_blocks > 0) return OCPX_NAME(flash_part_coop_excl_)(dm, b, fb, s);
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg;
+    priority_attr(cfg, attr, fb, s);
+    cfg.gridDim = dim3(fb.coop_blocks);
+    cfg.blockDim = dim3(COOP_WARPS * 32);
+    return cudaLaunchKernelEx(&cfg, k_flash_pe_coop<OCPX_NCM, COOP_WARPS>, dm, b, (const DeferRec*)fb.rec,
+                              (const unsigned*)fb.count, fb.cap, fb.coop_next, fb.pe);
+}
+#endif
+
+#if OCPX_FLASH_PART == 5
+cudaError_t OCPX_NAME(flash_part_coop_excl_)(const Model* dm, const BulkView& b, const FlashBatch& fb, cudaStream_t s)
+{
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg;
+    priority_attr(cfg, attr, fb, s);
+    cfg.gridDim = dim3(fb.excl_blocks);
+    cfg.blockDim = dim3(EXCL_WARPS * 32);
+    cfg.dynamicSmemBytes = fb.excl_smem;
+    return cudaLaunchKernelEx(&cfg, k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>, dm, b, (const DeferRec*)fb.rec,
+                              (const unsigned*)fb.count, fb.cap, fb.coop_next, fb.pe);
+}
+
+cudaError_t OCPX_NAME(setup_flash_coop_)(int dev, int optin, int* excl_smem)
+{
+    (void)dev;
+    cudaFuncAttributes fa{};
+    cudaError_t e = cudaFuncGetAttributes(&fa, k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>);
+    if (e != cudaSuccess) return e;
+    const int dyn = optin > (int)fa.sharedSizeBytes ? optin - (int)fa.sharedSizeBytes : 0;
+    e = cudaFuncSetAttribute(k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_flash_pe_coop<OCPX_NCM, EXCL_WARPS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+    excl_smem[0] = dyn;
+    return e;
+}
+#endif
+
+#if OCPX_FLASH_PART == 6
+cudaError_t OCPX_NAME(flash_part_post_)(const Model* dm, const BulkView& b, const FlashBatch& fb, cudaStream_t s)
+{
+    // one thread per deferred cell; the SM's L1 as large as it goes, for the
+    // threads' frames
+    cudaLaunchAttribute attr[2];
+    cudaLaunchConfig_t cfg;
+    priority_attr(cfg, attr, fb, s);
+    const int pb = fb.post_block > 0 ? fb.post_block : 128;
+    const long long threads = (long long)fb.cap * (fb.rec2 ? 2 : 1);
+    cfg.gridDim = dim3((unsigned)((threads + pb - 1) / pb));
+    cfg.blockDim = dim3(pb);
+    attr[cfg.numAttrs].id = cudaLaunchAttributePreferredSharedMemoryCarveout;
+    attr[cfg.numAttrs].val.sharedMemCarveout = (unsigned)cudaSharedmemCarveoutMaxL1;
+    cfg.numAttrs++;
+    return cudaLaunchKernelEx(&cfg, k_flash_post<OCPX_NCM>, dm, b, (const DeferRec*)fb.rec,
+                              (const unsigned*)fb.count, fb.cap, (const PERes*)fb.pe, fb.rec2, fb.count2, fb.pe2);
+}
+#endif
 
 }  // namespace ocpx

@@ -22,8 +22,6 @@
 // Callers serialise the calls, e.g. by issuing them on one stream.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "ocpx.h"
 
 namespace {
@@ -134,21 +132,16 @@ k_relres_noalloc(const double* __restrict__ res, const double* __restrict__ rock
     }
 }
 
-constexpr int MAX_DEVICES = 64;
-std::mutex g_addr_mutex;
-RelresScratch* g_addr[MAX_DEVICES];
-
-// Device address of the scratch, looked up once per device.
-cudaError_t scratch_address(int dev, RelresScratch** out)
+// Device address of the scratch in the current device's context, looked up on
+// every call: the lookup allocates nothing and is cheap, and an address kept
+// from an earlier call could be stale after the context was torn down and the
+// module loaded again (cudaDeviceReset).
+cudaError_t scratch_address(RelresScratch** out)
 {
-    std::lock_guard<std::mutex> lock(g_addr_mutex);
-    if (!g_addr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_relres_scratch);
-        if (e != cudaSuccess) return e;
-        g_addr[dev] = static_cast<RelresScratch*>(p);
-    }
-    *out = g_addr[dev];
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_relres_scratch);
+    if (e != cudaSuccess) return e;
+    *out = static_cast<RelresScratch*>(p);
     return cudaSuccess;
 }
 
@@ -162,9 +155,8 @@ extern "C" ocpx_status ocpx_relres_noalloc(const double* d_res, const double* d_
     if (nb <= 0 || nb > OCPX_RELRES_NOALLOC_MAX_CELLS || len < 2) return OCPX_INVALID_ARG;
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return OCPX_NO_DEVICE;
-    if (dev < 0 || dev >= MAX_DEVICES) return OCPX_INVALID_ARG;
     RelresScratch* scratch = nullptr;
-    if (scratch_address(dev, &scratch) != cudaSuccess) return OCPX_CUDA_ERROR;
+    if (scratch_address(&scratch) != cudaSuccess) return OCPX_CUDA_ERROR;
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int blocks = (nb + RELRES_CELLS_PER_BLOCK - 1) / RELRES_CELLS_PER_BLOCK;
     k_relres_noalloc<<<blocks, RELRES_THREADS, 0, s>>>(d_res, d_rockVp, d_Nt, nb, len, d_resRelV, d_resRelN);

@@ -3,9 +3,11 @@
 * ``build()``: the C restatement ocpx_oracle.c -> oracle/_build/liboracle.so
   (cc -O2 -ffp-contract=off -fopenmp; no FMA contraction, like a baseline
   x86-64 build of the reference).
-* ``build_reference_if_present()``: where the reference sources exist at
-  REF (this container), the reference itself via oracle/ref/Makefile into
-  oracle/_ref/ (used to regenerate the golden fixtures).
+* ``build_reference_if_present()``: where the reference sources exist (the
+  directory in OCPX_REFERENCE_DIR, else the checkout this recipe reads by
+  default), the reference itself via oracle/ref/Makefile into oracle/_ref/
+  (used to regenerate the golden fixtures).  This recipe is the one place
+  that names the checkout's default location.
 """
 from __future__ import annotations
 

@@ -190,6 +190,12 @@ int ocpx_abi_version(void);
 /* Host <-> device state in the reference layout; count is the element count. */
 ocpx_status ocpx_set_field(ocpx_ctx* ctx, ocpx_field f, const void* host, size_t count);
 ocpx_status ocpx_get_field(ocpx_ctx* ctx, ocpx_field f, void* host, size_t count);
+/* The same for the entities [first, first + n) of a field (cells, or
+ * connections for the connection fields): host holds n entities in the
+ * reference layout, e.g. n*np*nc values of OCPX_F_XIJ.  For reading windows of
+ * a large grid and for writing a subdomain's ghost cells. */
+ocpx_status ocpx_set_field_range(ocpx_ctx* ctx, ocpx_field f, size_t first, size_t n, const void* host);
+ocpx_status ocpx_get_field_range(ocpx_ctx* ctx, ocpx_field f, size_t first, size_t n, void* host);
 
 /* Newton-step pieces (asynchronous on the context stream unless noted). */
 ocpx_status ocpx_update_properties(ocpx_ctx* ctx, ocpx_report* rep); /* synchronizes to fill rep */
@@ -328,10 +334,11 @@ ocpx_status ocpx_step_report(ocpx_ctx* ctx, ocpx_report* rep);
  * 9 pre-deferral and cost order, 10 budgeted per-cell flash, 11 cooperative
  * equilibrium and properties of the pre-deferred cells (second stream,
  * concurrent with 10), 12 properties of the cells deferred by 10,
- * 13 cooperative equilibrium of the cells deferred by 10.  ocpx_profile_read synchronizes and returns, per
+ * 13 cooperative equilibrium of the cells deferred by 10; 14 the adjoint
+ * products of the step (ocpx_set_adjoint_seed).  ocpx_profile_read synchronizes and returns, per
  * stage, the summed milliseconds and the number of timed launches since
  * profiling was enabled. */
-#define OCPX_STAGE_COUNT 14
+#define OCPX_STAGE_COUNT 15
 ocpx_status ocpx_profile_enable(ocpx_ctx* ctx, int enable);
 ocpx_status ocpx_profile_read(ocpx_ctx* ctx, double* ms, uint64_t* launches);
 
@@ -384,6 +391,16 @@ ocpx_status ocpx_relres_noalloc(const double* d_res, const double* d_rockVp, con
  * Outputs may be NULL.  Synchronizes. */
 ocpx_status ocpx_adjoint(ocpx_ctx* ctx, const double* lambda, double* jt_lambda, double* dr_dtrans,
                          double* dr_dporo);
+/* The same products as part of every Newton step: with a seed set, each
+ * ocpx_enqueue_step / ocpx_step computes J^T lambda, (dR/dT)^T lambda and
+ * (dR/dporoInit)^T lambda on the device right after its Jacobian (inside the
+ * step's graph in the batched variant), and ocpx_get_adjoint copies the last
+ * step's products to the host (any pointer may be NULL; synchronizes).  The
+ * seed [nb*(nc+1)] is copied to the device once; NULL turns the products off.
+ * The first seed allocates their device buffers (2*nb*(nc+1) + nb + nconn
+ * doubles).  ocpx_adjoint keeps its own buffers and leaves the seed alone. */
+ocpx_status ocpx_set_adjoint_seed(ocpx_ctx* ctx, const double* lambda);
+ocpx_status ocpx_get_adjoint(ocpx_ctx* ctx, double* jt_lambda, double* dr_dtrans, double* dr_dporo);
 
 /* Newton-iteration and time-step control of the FIM run, bulk part, on the
  * device.  Replaces, for the bulk cells:

@@ -124,18 +124,21 @@ __global__ void k_report(BulkView b, uint32_t* __restrict__ out)
 }
 
 template <typename T>
-__global__ void k_transpose(T* __restrict__ dst, const T* __restrict__ src, int n, int width, bool to_soa)
+__global__ void k_transpose(T* __restrict__ dst, const T* __restrict__ src, int n, int width, size_t N, size_t first,
+                            bool to_soa)
 {
+    // entities [first, first + n) of an SoA array a[k * N + i] <-> an AoS
+    // array of n entities; t runs over the strided side so that its accesses
+    // are coalesced
     const size_t total = (size_t)n * width;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
-        // t indexes the destination linearly so stores are coalesced
         if (to_soa) {
             const size_t k = t / n, i = t % n;
-            dst[t] = src[i * width + k];
+            dst[k * N + first + i] = src[i * width + k];
         }
         else {
             const size_t i = t / width, k = t % width;
-            dst[t] = src[k * (size_t)n + i];
+            dst[t] = src[k * N + first + i];
         }
     }
 }
@@ -420,16 +423,17 @@ cudaError_t launch_report(const BulkView& b, uint32_t* out3, int block, cudaStre
     return cudaGetLastError();
 }
 cudaError_t launch_transpose(void* dst, const void* src, int n, int width, int elem_bytes, bool to_soa,
-                             cudaStream_t s)
+                             cudaStream_t s, size_t N, size_t first)
 {
     const size_t total = (size_t)n * width;
     if (!total) return cudaSuccess;
+    if (N == 0) N = (size_t)n;
     const int block = 256;
     const int grid = (int)((total + block - 1) / block < 4096 ? (total + block - 1) / block : 4096);
     switch (elem_bytes) {
-    case 1: k_transpose<uint8_t><<<grid, block, 0, s>>>((uint8_t*)dst, (const uint8_t*)src, n, width, to_soa); break;
-    case 4: k_transpose<uint32_t><<<grid, block, 0, s>>>((uint32_t*)dst, (const uint32_t*)src, n, width, to_soa); break;
-    case 8: k_transpose<double><<<grid, block, 0, s>>>((double*)dst, (const double*)src, n, width, to_soa); break;
+    case 1: k_transpose<uint8_t><<<grid, block, 0, s>>>((uint8_t*)dst, (const uint8_t*)src, n, width, N, first, to_soa); break;
+    case 4: k_transpose<uint32_t><<<grid, block, 0, s>>>((uint32_t*)dst, (const uint32_t*)src, n, width, N, first, to_soa); break;
+    case 8: k_transpose<double><<<grid, block, 0, s>>>((double*)dst, (const double*)src, n, width, N, first, to_soa); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

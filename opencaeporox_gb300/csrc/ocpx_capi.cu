@@ -170,6 +170,11 @@ struct ocpx_ctx {
     uint32_t* jac_slot = nullptr;   // [2][nconn]: block index of connection c in row bId / row eId
     double* adj = nullptr;          // adjoint workspace: lambda, J^T lambda [nb*(nc+1)] each
     double* adj_conn = nullptr;     // [nconn]
+    // adjoint products inside the step (ocpx_set_adjoint_seed): one allocation
+    // holding the seed lambda and J^T lambda [nb*(nc+1)] each, (dR/dporoInit)^T
+    // lambda [nb] and (dR/dT)^T lambda [nconn]
+    double* step_adj = nullptr;
+    bool adj_in_step = false;
     double last_dt = 0;             // dt of the last residual / Jacobian
     uint32_t* jac_col = nullptr;
     double* jac_val = nullptr;
@@ -514,6 +519,7 @@ void ocpx_destroy(ocpx_ctx* ctx)
     for (auto e : ctx->free_events) cudaEventDestroy(e);
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->ls_scratch) cudaFree(ctx->ls_scratch);
+    if (ctx->step_adj) cudaFree(ctx->step_adj);
     if (ctx->d_model) cudaFree(ctx->d_model);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     if (ctx->h_norm) cudaFreeHost(ctx->h_norm);
@@ -536,17 +542,7 @@ ocpx_status ocpx_set_field(ocpx_ctx* ctx, ocpx_field f, const void* host, size_t
     if (count != expect)
         return fail(OCPX_INVALID_ARG, "field " + std::to_string((int)f) + ": expected " + std::to_string(expect) +
                                           " elements, got " + std::to_string(count));
-    const size_t bytes = expect * fi.elem;
-    if (fi.width == 1 || !fi.soa) {
-        OCPX_CUDA(cudaMemcpyAsync(fi.dev, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    }
-    else {
-        OCPX_CUDA(cudaMemcpyAsync(ctx->staging, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
-        OCPX_CUDA(launch_transpose(fi.dev, ctx->staging, fi.n, fi.width, fi.elem, true, ctx->stream));
-        ctx->launches++;
-    }
-    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
-    return OCPX_OK;
+    return ocpx_set_field_range(ctx, f, 0, (size_t)fi.n, host);
 }
 
 ocpx_status ocpx_get_field(ocpx_ctx* ctx, ocpx_field f, void* host, size_t count)
@@ -558,17 +554,56 @@ ocpx_status ocpx_get_field(ocpx_ctx* ctx, ocpx_field f, void* host, size_t count
     if (count != expect)
         return fail(OCPX_INVALID_ARG, "field " + std::to_string((int)f) + ": expected " + std::to_string(expect) +
                                           " elements, got " + std::to_string(count));
-    const size_t bytes = expect * fi.elem;
+    return ocpx_get_field_range(ctx, f, 0, (size_t)fi.n, host);
+}
+
+}  // extern "C"
+
+namespace {
+// entities [first, first + n) of a field between the host (reference layout)
+// and the device
+ocpx_status field_transfer(ocpx_ctx* ctx, ocpx_field f, size_t first, size_t n, void* host, bool to_device)
+{
+    if (!ctx || (!host && n)) return fail(OCPX_INVALID_ARG, "null argument");
+    const FieldInfo fi = ctx->field(f);
+    if (!fi.dev) return fail(OCPX_INVALID_ARG, "unknown field " + std::to_string((int)f));
+    if (to_device && !fi.writable) return fail(OCPX_INVALID_ARG, "field not writable: " + std::to_string((int)f));
+    if (first > (size_t)fi.n || n > (size_t)fi.n - first)
+        return fail(OCPX_INVALID_ARG, "field " + std::to_string((int)f) + ": range [" + std::to_string(first) + ", " +
+                                          std::to_string(first + n) + ") outside " + std::to_string(fi.n) + " entities");
+    if (!n) return OCPX_OK;
+    const size_t bytes = n * fi.width * fi.elem;
+    const cudaMemcpyKind kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
     if (fi.width == 1 || !fi.soa) {
-        OCPX_CUDA(cudaMemcpyAsync(host, fi.dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        char* dev = (char*)fi.dev + first * fi.width * fi.elem;
+        OCPX_CUDA(cudaMemcpyAsync(to_device ? (void*)dev : host, to_device ? (const void*)host : (const void*)dev, bytes,
+                                  kind, ctx->stream));
+    }
+    else if (to_device) {
+        OCPX_CUDA(cudaMemcpyAsync(ctx->staging, host, bytes, kind, ctx->stream));
+        OCPX_CUDA(launch_transpose(fi.dev, ctx->staging, (int)n, fi.width, fi.elem, true, ctx->stream, fi.n, first));
+        ctx->launches++;
     }
     else {
-        OCPX_CUDA(launch_transpose(ctx->staging, fi.dev, fi.n, fi.width, fi.elem, false, ctx->stream));
+        OCPX_CUDA(launch_transpose(ctx->staging, fi.dev, (int)n, fi.width, fi.elem, false, ctx->stream, fi.n, first));
         ctx->launches++;
-        OCPX_CUDA(cudaMemcpyAsync(host, ctx->staging, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        OCPX_CUDA(cudaMemcpyAsync(host, ctx->staging, bytes, kind, ctx->stream));
     }
     OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
     return OCPX_OK;
+}
+}  // namespace
+
+extern "C" {
+
+ocpx_status ocpx_set_field_range(ocpx_ctx* ctx, ocpx_field f, size_t first, size_t n, const void* host)
+{
+    return field_transfer(ctx, f, first, n, const_cast<void*>(host), true);
+}
+
+ocpx_status ocpx_get_field_range(ocpx_ctx* ctx, ocpx_field f, size_t first, size_t n, void* host)
+{
+    return field_transfer(ctx, f, first, n, host, false);
 }
 
 }  // extern "C"
@@ -852,12 +887,33 @@ ocpx_status ocpx_newton_update(ocpx_ctx* ctx, const double* u_host, double dSmax
 
 namespace {
 
+// the adjoint products of the step (ocpx_set_adjoint_seed), after its Jacobian
+ocpx_status enqueue_step_adjoint(ocpx_ctx* ctx)
+{
+    cudaStream_t s = ctx->stream;
+    const size_t nv = (size_t)ctx->nb * (ctx->nc + 1);
+    const double* lam = ctx->step_adj;
+    const int mk = ctx->stage_begin(14);
+    OCPX_CUDA(launch_jt_lambda(ctx->b, ctx->cv, ctx->jac_rowptr, ctx->jac_val, ctx->jac_slot, lam,
+                               ctx->step_adj + nv, ctx->block_cell, s));
+    OCPX_CUDA(launch_vjp_poro(ctx->d_model, ctx->b, lam, ctx->step_adj + 2 * nv, ctx->block_cell, s));
+    ctx->launches += 2;
+    if (ctx->nconn) {
+        OCPX_CUDA(launch_vjp_trans(ctx->b, ctx->cv, ctx->last_dt, lam, ctx->step_adj + 2 * nv + ctx->nb,
+                                   ctx->block_conn, s));
+        ctx->launches++;
+    }
+    ctx->stage_end(mk);
+    return OCPX_OK;
+}
+
 ocpx_status enqueue_step_kernels(ocpx_ctx* ctx, double dt)
 {
     ocpx_status st;
     if ((st = enqueue_properties(ctx)) != OCPX_OK) return st;
     if ((st = enqueue_calres(ctx, dt)) != OCPX_OK) return st;
-    return enqueue_assemble(ctx, dt);
+    if ((st = enqueue_assemble(ctx, dt)) != OCPX_OK) return st;
+    return ctx->adj_in_step ? enqueue_step_adjoint(ctx) : OCPX_OK;
 }
 
 // Capture the step into a CUDA graph (batched variant).  The graph holds no
@@ -1346,6 +1402,41 @@ ocpx_status ocpx_adjoint(ocpx_ctx* ctx, const double* lambda, double* jt_lambda,
         ctx->launches++;
         OCPX_CUDA(cudaMemcpyAsync(dr_dporo, d_out, sizeof(double) * ctx->nb, cudaMemcpyDeviceToHost, s));
     }
+    OCPX_CUDA(cudaStreamSynchronize(s));
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_set_adjoint_seed(ocpx_ctx* ctx, const double* lambda)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    ctx->drop_graph();
+    if (!lambda) {
+        ctx->adj_in_step = false;
+        return OCPX_OK;
+    }
+    const size_t nv = (size_t)ctx->nb * (ctx->nc + 1);
+    if (!ctx->step_adj)
+        OCPX_CUDA(cudaMalloc(&ctx->step_adj, sizeof(double) * (2 * nv + ctx->nb + (size_t)ctx->nconn)));
+    OCPX_CUDA(cudaMemcpyAsync(ctx->step_adj, lambda, sizeof(double) * nv, cudaMemcpyHostToDevice, ctx->stream));
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->adj_in_step = true;
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_get_adjoint(ocpx_ctx* ctx, double* jt_lambda, double* dr_dtrans, double* dr_dporo)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    if (!ctx->adj_in_step) return fail(OCPX_INVALID_ARG, "no adjoint seed is set (ocpx_set_adjoint_seed)");
+    const size_t nv = (size_t)ctx->nb * (ctx->nc + 1);
+    cudaStream_t s = ctx->stream;
+    if (jt_lambda)
+        OCPX_CUDA(cudaMemcpyAsync(jt_lambda, ctx->step_adj + nv, sizeof(double) * nv, cudaMemcpyDeviceToHost, s));
+    if (dr_dporo)
+        OCPX_CUDA(cudaMemcpyAsync(dr_dporo, ctx->step_adj + 2 * nv, sizeof(double) * ctx->nb, cudaMemcpyDeviceToHost,
+                                  s));
+    if (dr_dtrans && ctx->nconn)
+        OCPX_CUDA(cudaMemcpyAsync(dr_dtrans, ctx->step_adj + 2 * nv + ctx->nb, sizeof(double) * ctx->nconn,
+                                  cudaMemcpyDeviceToHost, s));
     OCPX_CUDA(cudaStreamSynchronize(s));
     return OCPX_OK;
 }

@@ -134,8 +134,10 @@ cudaError_t launch_vjp_poro(const Model* dm, const BulkView& b, const double* la
                             cudaStream_t s);
 
 // layout conversion between the reference's cell-major arrays and the
-// device structure-of-arrays: dst[k*n + i] = src[i*width + k] (to_soa) and back
+// device structure-of-arrays, for the n entities starting at `first` of an
+// SoA array of N entities (N = 0: N = n, first = 0):
+// dst[k*N + first + i] = src[i*width + k] (to_soa) and back
 cudaError_t launch_transpose(void* dst, const void* src, int n, int width, int elem_bytes, bool to_soa,
-                             cudaStream_t s);
+                             cudaStream_t s, size_t N = 0, size_t first = 0);
 
 }  // namespace ocpx

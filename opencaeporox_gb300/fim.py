@@ -136,7 +136,8 @@ EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy",
            "ocpx_profile_enable", "ocpx_profile_read", "ocpx_checkpoint", "ocpx_measure_fp64_tflops",
            "ocpx_stream", "ocpx_launch_count", "ocpx_set_param", "ocpx_get_param", "ocpx_adjoint",
            "ocpx_nr_init_step", "ocpx_nr_max_change", "ocpx_step_max_change", "ocpx_nr_check_converge",
-           "ocpx_next_time_step", "ocpx_linsolve", "ocpx_newton_update_device", "ocpx_wells_eval"]
+           "ocpx_next_time_step", "ocpx_linsolve", "ocpx_newton_update_device", "ocpx_wells_eval",
+           "ocpx_set_field_range", "ocpx_get_field_range", "ocpx_set_adjoint_seed", "ocpx_get_adjoint"]
 
 PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3, "predefer": 4, "coop_cells": 5,
           "predeferred": 6, "level": 7, "pre_blocks": 8,
@@ -190,6 +191,10 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.ocpx_next_time_step.argtypes = [P, C.POINTER(NRControl), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.ocpx_wells_eval.argtypes = [P, C.c_int, C.POINTER(Well), C.c_double, P, P, C.POINTER(C.c_double)]
     lib.ocpx_get_param.argtypes = [P, C.c_int, C.POINTER(C.c_longlong)]
+    lib.ocpx_set_field_range.argtypes = [P, C.c_int, C.c_size_t, C.c_size_t, P]
+    lib.ocpx_get_field_range.argtypes = [P, C.c_int, C.c_size_t, C.c_size_t, P]
+    lib.ocpx_set_adjoint_seed.argtypes = [P, P]
+    lib.ocpx_get_adjoint.argtypes = [P, P, P, P]
     for fn in ("ocpx_enqueue_step", "ocpx_step_report", "ocpx_profile_enable", "ocpx_profile_read",
                "ocpx_measure_fp64_tflops", "ocpx_checkpoint", "ocpx_set_param", "ocpx_get_param"):
         getattr(lib, fn).restype = C.c_int
@@ -392,6 +397,43 @@ class FimContext:
         _check(self.lib.ocpx_get_field(self.h, FIELD_ID[name], out.ctypes.data_as(C.c_void_p), out.size))
         return out
 
+    def field_width(self, name: str) -> int:
+        n = self.nconn if name in ("UPBLOCK", "CONN_DP", "FLUX_VJ", "FLUX_NI", "TRANS") else self.nb
+        return self.field_size(name) // max(n, 1)
+
+    def get_range(self, name: str, first: int, n: int) -> np.ndarray:
+        """Entities [first, first + n) of a field, in the reference layout."""
+        dt = FIELD_DTYPE.get(name, np.float64)
+        out = np.empty(n * self.field_width(name), dtype=dt)
+        _check(self.lib.ocpx_get_field_range(self.h, FIELD_ID[name], first, n, out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def set_range(self, name: str, first: int, values):
+        """Write entities [first, first + n) of a field (n from the values)."""
+        dt = FIELD_DTYPE.get(name, np.float64)
+        a = np.ascontiguousarray(np.asarray(values).astype(dt, copy=False).ravel())
+        w = self.field_width(name)
+        if a.size % w:
+            raise ValueError(f"{name}: {a.size} values are not whole entities of {w}")
+        _check(self.lib.ocpx_set_field_range(self.h, FIELD_ID[name], first, a.size // w, a.ctypes.data_as(C.c_void_p)))
+
+    def set_adjoint_seed(self, lam):
+        """Adjoint products inside every step from now on (None: off)."""
+        if lam is None:
+            _check(self.lib.ocpx_set_adjoint_seed(self.h, None))
+            return
+        self._adj_seed = np.ascontiguousarray(np.asarray(lam, np.float64).ravel())
+        if self._adj_seed.size != self.nb * (self.nc + 1):
+            raise ValueError("lambda must have nb*(nc+1) entries")
+        _check(self.lib.ocpx_set_adjoint_seed(self.h, self._adj_seed.ctypes.data_as(C.c_void_p)))
+
+    def get_adjoint(self):
+        """(J^T lam, (dR/dT)^T lam, (dR/dporoInit)^T lam) of the last step."""
+        jt, tr, po = np.empty(self.nb * (self.nc + 1)), np.empty(self.nconn), np.empty(self.nb)
+        _check(self.lib.ocpx_get_adjoint(self.h, jt.ctypes.data_as(C.c_void_p), tr.ctypes.data_as(C.c_void_p),
+                                         po.ctypes.data_as(C.c_void_p)))
+        return jt, tr, po
+
     def load_state(self, state: dict, skip_missing: bool = True):
         """Upload arrays named as in BulkVarSet (P, Ni, S, xij, phaseExist, ...)."""
         for ref_name, fid in REF_NAMES.items():
@@ -459,7 +501,7 @@ class FimContext:
         return rep
 
     STAGES = ["check", "flash", "krpc_rock", "report", "flux", "residual", "jac_conn", "jac_rows", "newton_update",
-              "flash_order", "flash_budget", "flash_coop", "flash_post", "flash_coop_late"]
+              "flash_order", "flash_budget", "flash_coop", "flash_post", "flash_coop_late", "adjoint"]
 
     def profile(self, enable: bool = True):
         _check(self.lib.ocpx_profile_enable(self.h, 1 if enable else 0))

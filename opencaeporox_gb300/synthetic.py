@@ -82,18 +82,23 @@ def comp_model(ncomp, seed, pvtw=(200.0, 1.01, 4.5e-5, 0.5, 0.0), rock=(200.0, 4
     return Model(a)
 
 
-def comp_initial_state(grid, ncomp, seed, p_range=(100.0, 300.0), alpha=2.0, temp_c=71.85, smooth=False, nx=None):
+def comp_initial_state(grid, ncomp, seed, p_range=(100.0, 300.0), alpha=2.0, temp_c=71.85, smooth=False, nx=None,
+                       n_total=None, first=0):
     """PTN start: per-cell pressure and moles (hydrocarbons then water) with
     z ~ Dirichlet(alpha), P ~ U(p_range); hydrocarbons fill 80 % of the pore
     volume at an assumed Z = 0.6 and water 20 % (Bw ~ 1.01).  Phase state is
-    empty, as BulkInitializer::InitPTNi leaves it (src/BulkInitializer.cpp:104-143)."""
+    empty, as BulkInitializer::InitPTNi leaves it (src/BulkInitializer.cpp:104-143).
+    With n_total, grid holds the cells [first, first + grid.nb) of a grid of
+    n_total cells, and gets the values those cells have there."""
     rng = np.random.default_rng(seed + 1000)
     n = grid.nb
-    p = rng.uniform(*p_range, n)
+    nd = n if n_total is None else n_total
+    p = rng.uniform(*p_range, nd)
     if smooth:
-        ix = np.arange(n) % nx
-        p = p_range[0] + (p_range[1] - p_range[0]) * ix / max(nx - 1, 1) + rng.uniform(-1, 1, n)
-    z = rng.dirichlet(np.full(ncomp, alpha), n)
+        ix = np.arange(nd) % nx
+        p = p_range[0] + (p_range[1] - p_range[0]) * ix / max(nx - 1, 1) + rng.uniform(-1, 1, nd)
+    z = rng.dirichlet(np.full(ncomp, alpha), nd)
+    p, z = p[first:first + n], z[first:first + n]
     vp = grid.v * grid.poro_init
     vm = 0.6 * METRIC["GAS_CONSTANT"] * (temp_c + 273.15) / p
     ni = z * (0.8 * vp / vm)[:, None]
@@ -133,11 +138,13 @@ def comp_grid_lognormal(nx, ny, nz, median=200.0, sigma_ln=1.5, corr_cells=10, s
                            conv_darcy=METRIC["CONV_DARCY"])
 
 
-def ptn_workload(ctx, grid, ncomp, seed, dt=0.1, dsmax=0.2, p_range=(100.0, 300.0)):
+def ptn_workload(ctx, grid, ncomp, seed, dt=0.1, dsmax=0.2, p_range=(100.0, 300.0), slot_before_last=None):
     """Drive a context to the input of the second Newton iteration of a time
     step from a seeded PTN start (pores filled by scaling the moles), as the
     bench does; returns the two seeded Newton updates (u1 applied, u2 the one
-    that produced the returned state)."""
+    that produced the returned state).  slot_before_last: a checkpoint slot
+    that receives the state just before u2 is applied (the input of a whole
+    Newton iteration, update included), or None."""
     st = comp_initial_state(grid, ncomp, seed, p_range=p_range)
     ctx.load_state(st)
     ctx.update_property()
@@ -149,17 +156,31 @@ def ptn_workload(ctx, grid, ncomp, seed, dt=0.1, dsmax=0.2, p_range=(100.0, 300.
     ctx.update_property()
     ctx.cal_res(dt)
     ctx.update_last_time_step()
-    us = []
-    for k in range(2):
-        rng = np.random.default_rng(seed + 77 + k)
-        u = np.zeros((grid.nb, ncomp + 2))
-        u[:, 0] = rng.normal(0.0, 2.0, grid.nb)
-        u[:, 1:] = Ni.reshape(grid.nb, -1) * rng.normal(0.0, 2e-3, (grid.nb, ncomp + 1))
-        us.append(u.ravel())
+    us = ptn_updates(Ni, grid.nb, ncomp, seed)
     ctx.get_solution(us[0], dsmax)
     ctx.update_property()
     ctx.cal_res(dt)
+    if slot_before_last is not None:
+        ctx.checkpoint(slot_before_last)
     ctx.get_solution(us[1], dsmax)
+    return us
+
+
+def ptn_updates(Ni, nb, ncomp, seed, n_total=None, first=0):
+    """The two seeded Newton updates of ptn_workload (dP ~ N(0, 2) bar, dNi =
+    Ni N(0, 2e-3)) for cells with moles Ni; with n_total, the cells are
+    [first, first + nb) of a grid of n_total cells and get the draws those
+    cells have there."""
+    nd = nb if n_total is None else n_total
+    us = []
+    for k in range(2):
+        rng = np.random.default_rng(seed + 77 + k)
+        dp = rng.normal(0.0, 2.0, nd)[first:first + nb]
+        dn = rng.normal(0.0, 2e-3, (nd, ncomp + 1))[first:first + nb]
+        u = np.zeros((nb, ncomp + 2))
+        u[:, 0] = dp
+        u[:, 1:] = np.asarray(Ni).reshape(nb, -1) * dn
+        us.append(u.ravel())
     return us
 
 
@@ -223,12 +244,16 @@ def flash_stress_cells(ctx_factory, n, ncomp, seed, near_frac=0.2, p_range=(50.0
     return P, Ni
 
 
-def dipping_corner_point(nx, ny, nz, dxy, dz, top, dip_x_deg, dip_y_deg, pillar_tilt=0.0, seed=0):
+def dipping_corner_point(nx, ny, nz, dxy, dz, top, dip_x_deg, dip_y_deg, pillar_tilt=0.0, seed=0,
+                         pillar_jitter=0.0):
     """A corner-point grid (Eclipse COORD and ZCORN arrays) of nz layers of
     thickness dz over an nx x ny plan with spacing dxy, its top dipping by
     dip_x_deg / dip_y_deg.  Each pillar leans by a seeded slope within
-    +-pillar_tilt in x and y (non-vertical pillars).  Layer boundaries are
-    shared by neighbouring cells, so faces match (no faults)."""
+    +-pillar_tilt in x and y (non-vertical pillars), and its top and bottom
+    points are moved, independently, by seeded offsets within
+    +-pillar_jitter * dxy in x and y, so every point of a pillar lies within
+    that distance of its unperturbed place when pillar_tilt is 0.  Layer
+    boundaries are shared by neighbouring cells, so faces match (no faults)."""
     rng = np.random.default_rng(seed)
     X = np.arange(nx + 1) * float(dxy)
     Y = np.arange(ny + 1) * float(dxy)
@@ -242,6 +267,12 @@ def dipping_corner_point(nx, ny, nz, dxy, dz, top, dip_x_deg, dip_y_deg, pillar_
     coord[:, :, 1, 0] = XX + sx * (zbot - ztop)
     coord[:, :, 1, 1] = YY + sy * (zbot - ztop)
     coord[:, :, 1, 2] = zbot
+    if pillar_jitter:
+        j = rng.uniform(-pillar_jitter, pillar_jitter, (2, 2) + XX.shape) * float(dxy)
+        coord[:, :, 0, 0] += j[0, 0]
+        coord[:, :, 0, 1] += j[0, 1]
+        coord[:, :, 1, 0] += j[1, 0]
+        coord[:, :, 1, 1] += j[1, 1]
     zb = ztop[None, :, :] + dz * np.arange(nz + 1)[:, None, None]   # [K][J][I] layer boundaries
     zc = np.empty((nz, 2, ny, 2, nx, 2))
     for tb in range(2):

@@ -49,7 +49,7 @@
 extern "C" {
 #endif
 
-#define OCPX_ABI_VERSION 1
+#define OCPX_ABI_VERSION 2
 
 typedef enum ocpx_status {
     OCPX_OK = 0,
@@ -104,16 +104,29 @@ typedef struct ocpx_model_desc {
     int skip_psa;             /* SkipPSA enabled (reference default 1) */
 } ocpx_model_desc;
 
-/* Cells and connections (Bulk + BulkConn after Reservoir::Setup and CalTrans). */
+/* Cells and connections (Bulk + BulkConn after Reservoir::Setup and CalTrans).
+ * A subdomain of a grid split over several GPUs (BulkVarSet::nbI < nb in the
+ * reference) lists its own cells first, [0, nb_interior), then its ghost
+ * cells, [nb_interior, nb): copies of neighbouring subdomains' cells whose
+ * properties it computes itself (the flash runs on all nb cells, as
+ * IsoT_FIM::CalFlash does) but whose rows it does not own.  Residual rows,
+ * residual norms, Jacobian rows and the Newton-control maxima then cover the
+ * interior cells only (CalRes and AssembleMatBulks loop to nbI,
+ * src/IsoThermalMethod.cpp:1095, 1197-1210; OCPNRsuite, src/OCPNRsuite.cpp:26);
+ * Jacobian columns >= nb_interior are ghost columns.  Every connection needs
+ * an interior end; its two ends keep their roles (bId, eId) whatever their
+ * local numbers, so a subdomain's rows are bit-identical to the same rows of
+ * the whole grid when its connections keep the whole grid's order. */
 typedef struct ocpx_grid_desc {
-    int nb;                  /* cells (single domain: all interior) */
-    int nconn;               /* connections, in the reference's order (eId > bId) */
+    int nb;                  /* cells: interior, then ghost */
+    int nconn;               /* connections, in the reference's order */
     const double* v;         /* bulk volume */
     const double* depth;
     const double* poro_init;
     const uint32_t* conn_b;
     const uint32_t* conn_e;
     const double* conn_trans; /* BulkConnPair::trans, CONV_DARCY included */
+    int nb_interior;         /* cells [0, nb_interior) are interior; 0: all nb (a single domain) */
 } ocpx_grid_desc;
 
 /* State fields, reference layout.  Type: d = double, u8 = uint8 flag, u32. */
@@ -160,7 +173,7 @@ typedef enum ocpx_field {
     OCPX_F_CONN_DP,      /* d  [nconn*np] (read only) */
     OCPX_F_FLUX_VJ,      /* d  [nconn*np] (read only) */
     OCPX_F_FLUX_NI,      /* d  [nconn*nc] (read only) */
-    OCPX_F_RES,          /* d  [nb*(nc+1)] bulk residual, negated as LinearSystem expects (read only) */
+    OCPX_F_RES,          /* d  [nb*(nc+1)] bulk residual, negated as LinearSystem expects; ghost rows 0 (read only) */
     OCPX_F_RES_REL_V,    /* d  [nb] (read only) */
     OCPX_F_RES_REL_N,    /* d  [nb] (read only) */
     OCPX_F_TRANS,        /* d  [nconn] connection transmissibility (BulkConnPair::trans) */

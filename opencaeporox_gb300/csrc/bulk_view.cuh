@@ -12,7 +12,8 @@
 namespace ocpx {
 
 struct BulkView {
-    int nb;    // cells
+    int nb;    // cells: interior, then ghost
+    int nbI;   // interior cells (rows of the residual and the Jacobian)
     int np;    // phases
     int nc;    // components (incl. water)
     // static

@@ -45,7 +45,7 @@ __global__ void k_residual(BulkView b, ConnView cv, double dt, double* __restric
                            double* __restrict__ resRelN, RowNorm* __restrict__ rn)
 {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n < b.nb) cell_residual(b, cv, n, dt, res, resRelV, resRelN, rn + n);
+    if (n < b.nbI) cell_residual(b, cv, n, dt, res, resRelV, resRelN, rn + n);
 }
 
 // Global maxima with the reference's tie rule (first cell in index order wins),
@@ -100,7 +100,7 @@ __global__ void k_jac_rows(BulkView b, ConnView cv, const double* __restrict__ b
                            double* __restrict__ val)
 {
     const long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (r < b.nb) row_assemble_warp(b, cv, (int)r, bmat, rowptr, val, threadIdx.x & 31);
+    if (r < b.nbI) row_assemble_warp(b, cv, (int)r, bmat, rowptr, val, threadIdx.x & 31);
 }
 
 // out[0]: OR of status bits, out[1]: two-phase cells, out[2]: flagged cells
@@ -173,9 +173,9 @@ cudaError_t launch_conn_flux(const Model* dm, const BulkView& b, const ConnView&
 cudaError_t launch_residual(const BulkView& b, const ConnView& cv, double dt, double* res, double* resRelV,
                             double* resRelN, RowNorm* rn, RowNorm* rn_out, int block, cudaStream_t s)
 {
-    if (!b.nb) return cudaSuccess;
-    k_residual<<<grid_for(b.nb, block), block, 0, s>>>(b, cv, dt, res, resRelV, resRelN, rn);
-    k_norm_reduce<<<1, 256, 0, s>>>(rn, b.nb, rn_out);
+    if (!b.nbI) return cudaSuccess;
+    k_residual<<<grid_for(b.nbI, block), block, 0, s>>>(b, cv, dt, res, resRelV, resRelN, rn);
+    k_norm_reduce<<<1, 256, 0, s>>>(rn, b.nbI, rn_out);
     return cudaGetLastError();
 }
 cudaError_t launch_jac_conn(int nct, const Model* dm, const BulkView& b, const ConnView& cv, double dt, double* bmat,
@@ -198,7 +198,7 @@ cudaError_t launch_jac_rows(const BulkView& b, const ConnView& cv, const double*
                             double* val, int block, cudaStream_t s)
 {
     const int wpb = block / 32;  // rows per block
-    if (b.nb) k_jac_rows<<<(b.nb + wpb - 1) / wpb, block, 0, s>>>(b, cv, bmat, rowptr, val);
+    if (b.nbI) k_jac_rows<<<(b.nbI + wpb - 1) / wpb, block, 0, s>>>(b, cv, bmat, rowptr, val);
     return cudaGetLastError();
 }
 // Work level of a predicted work w >= 1: floor(4 log2 w), at most 63 (levels

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_max_change(BulkView b, double* 
     Cand c[NQ];
     for (int q = 0; q < NQ; q++) c[q] = none();
     const int nc = b.nc, np = b.np;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < b.nb; n += gridDim.x * blockDim.x) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < b.nbI; n += gridDim.x * blockDim.x) {
         const double P = b.P[n], T = b.T[n];
         c[0] = pick(c[0], Cand{P - lP[n], n});
         c[1] = pick(c[1], Cand{T - lT[n], n});
@@ -180,7 +180,7 @@ int max_change_blocks(int nb)
 cudaError_t launch_max_change(int mode, const BulkView& b, double* lP, double* lT, double* lN, double* lS,
                               void* partial, double* out5, cudaStream_t s)
 {
-    const int g = max_change_blocks(b.nb);
+    const int g = max_change_blocks(b.nbI);
     Cand* part = static_cast<Cand*>(partial);
     if (mode == 0)
         k_max_change<0><<<g, RED_THREADS, 0, s>>>(b, lP, lT, lN, lS, part);

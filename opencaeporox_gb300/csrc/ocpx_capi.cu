@@ -111,7 +111,7 @@ struct ocpx_ctx {
     cudaStream_t stream = nullptr;
     Model host_model{};
     Model* d_model = nullptr;
-    int nb = 0, np = 3, nc = 0, nconn = 0, NC = 0, ncm = 0, nct_cap = 0;
+    int nb = 0, nbI = 0, np = 3, nc = 0, nconn = 0, NC = 0, ncm = 0, nct_cap = 0;
     int variant = 0;
     // one arena for everything
     char* arena = nullptr;
@@ -319,11 +319,17 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     if (gd->nb <= 0 || gd->nconn < 0 || !gd->v || !gd->depth || !gd->poro_init ||
         (gd->nconn > 0 && (!gd->conn_b || !gd->conn_e || !gd->conn_trans)))
         return fail(OCPX_INVALID_ARG, "grid description incomplete");
+    if (gd->nb_interior < 0 || gd->nb_interior > gd->nb)
+        return fail(OCPX_INVALID_ARG, "nb_interior must lie in [0, nb]");
+    const uint32_t nbI_ = gd->nb_interior > 0 ? (uint32_t)gd->nb_interior : (uint32_t)gd->nb;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(OCPX_NO_DEVICE, "no CUDA device");
-    for (int c = 0; c < gd->nconn; c++)
+    for (int c = 0; c < gd->nconn; c++) {
         if (gd->conn_b[c] >= (uint32_t)gd->nb || gd->conn_e[c] >= (uint32_t)gd->nb || gd->conn_b[c] == gd->conn_e[c])
             return fail(OCPX_INVALID_ARG, "connection endpoint out of range at " + std::to_string(c));
+        if (gd->conn_b[c] >= nbI_ && gd->conn_e[c] >= nbI_)
+            return fail(OCPX_INVALID_ARG, "connection " + std::to_string(c) + " joins two ghost cells");
+    }
 
     ocpx_ctx* ctx = new ocpx_ctx();
     std::string merr;
@@ -337,6 +343,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
         cudaGetDevice(&ctx->device);
     }
     ctx->nb = gd->nb;
+    ctx->nbI = (int)nbI_;
     ctx->nc = md->nc;
     ctx->np = 3;
     ctx->nconn = gd->nconn;
@@ -345,24 +352,25 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     ctx->nct_cap = cap_nct(md->nc);
     if (ctx->nct_cap < 0 || (md->mixture == 1 && ctx->ncm < 0)) { delete ctx; return fail(OCPX_INVALID_ARG, "too many components"); }
 
-    const int nb = ctx->nb, np = ctx->np, nc = ctx->nc, nconn = ctx->nconn;
+    const int nb = ctx->nb, nbI = ctx->nbI, np = ctx->np, nc = ctx->nc, nconn = ctx->nconn;
     const int lend = np * (nc + 1) * (nc + 1), bsize = (nc + 1) * (nc + 1);
 
     // row -> incident connections (increasing connection index) and the
-    // block-CSR pattern: diagonal first, then one block per incident connection
+    // block-CSR pattern of the interior rows: diagonal first, then one block
+    // per incident connection
     std::vector<uint32_t> deg(nb + 1, 0);
     for (int c = 0; c < nconn; c++) { deg[gd->conn_b[c]]++; deg[gd->conn_e[c]]++; }
     std::vector<uint32_t> row_ptr(nb + 1, 0);
     for (int n = 0; n < nb; n++) row_ptr[n + 1] = row_ptr[n] + deg[n];
     std::vector<uint32_t> row_conn(row_ptr[nb]);
     std::vector<uint32_t> fill(row_ptr.begin(), row_ptr.end() - 1);
-    std::vector<uint32_t> jrow(nb + 1, 0), jcol;
-    jcol.reserve(nb + 2 * (size_t)nconn);
+    std::vector<uint32_t> jrow(nbI + 1, 0), jcol;
+    jcol.reserve(nbI + 2 * (size_t)nconn);
     for (int c = 0; c < nconn; c++) {
         row_conn[fill[gd->conn_b[c]]++] = ((uint32_t)c << 1) | 0u;
         row_conn[fill[gd->conn_e[c]]++] = ((uint32_t)c << 1) | 1u;
     }
-    for (int n = 0; n < nb; n++) {
+    for (int n = 0; n < nbI; n++) {
         jrow[n + 1] = jrow[n] + 1 + (row_ptr[n + 1] - row_ptr[n]);
         jcol.push_back(n);
         for (uint32_t k = row_ptr[n]; k < row_ptr[n + 1]; k++) {
@@ -371,9 +379,10 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
         }
     }
     ctx->jac_nnz = jcol.size();
-    // block index of each connection in the rows of its two cells (adjoint transpose)
-    std::vector<uint32_t> jslot(2 * (size_t)(nconn > 0 ? nconn : 1), 0);
-    for (int n = 0; n < nb; n++)
+    // block index of each connection in the rows of its two cells (adjoint
+    // transpose; a ghost cell's side has none)
+    std::vector<uint32_t> jslot(2 * (size_t)(nconn > 0 ? nconn : 1), 0xffffffffu);
+    for (int n = 0; n < nbI; n++)
         for (uint32_t k = row_ptr[n]; k < row_ptr[n + 1]; k++) {
             const uint32_t c = row_conn[k] >> 1, side = row_conn[k] & 1u;
             jslot[(size_t)side * nconn + c] = jrow[n] + 1 + (k - row_ptr[n]);
@@ -384,7 +393,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     std::vector<Slot> slots;
     auto add = [&](void* pp, size_t bytes) { slots.push_back({(void**)pp, bytes}); };
     BulkView& b = ctx->b;
-    b.nb = nb; b.np = np; b.nc = nc;
+    b.nb = nb; b.nbI = nbI; b.np = np; b.nc = nc;
     const size_t D = sizeof(double) * (size_t)nb;
     add(&b.v, D); add(&b.depth, D); add(&b.poroInit, D);
     add(&b.P, D); add(&b.T, D); add(&b.Pb, D);
@@ -429,7 +438,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     add(&ctx->nr_stats, sizeof(double) * 5); add(&ctx->ts_stats, sizeof(double) * 5);
     add(&ctx->nr_res0, sizeof(double)); add(&ctx->nr_state, sizeof(int)); add(&ctx->nr_dt, sizeof(double) * 2);
     add(&ctx->bmat, sizeof(double) * C * 2 * bsize);
-    add(&ctx->jac_rowptr, sizeof(uint32_t) * (nb + 1)); add(&ctx->jac_col, sizeof(uint32_t) * jcol.size());
+    add(&ctx->jac_rowptr, sizeof(uint32_t) * (nbI + 1)); add(&ctx->jac_col, sizeof(uint32_t) * jcol.size());
     add(&ctx->jac_slot, sizeof(uint32_t) * jslot.size());
     add(&ctx->adj, D * (nc + 1) * 2); add(&ctx->adj_conn, sizeof(double) * C);
     add(&ctx->jac_val, sizeof(double) * jcol.size() * bsize);
@@ -481,7 +490,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     cudaMemcpy((void*)cv.row_ptr, row_ptr.data(), sizeof(uint32_t) * (nb + 1), cudaMemcpyHostToDevice);
     if (!row_conn.empty())
         cudaMemcpy((void*)cv.row_conn, row_conn.data(), sizeof(uint32_t) * row_conn.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(ctx->jac_rowptr, jrow.data(), sizeof(uint32_t) * (nb + 1), cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->jac_rowptr, jrow.data(), sizeof(uint32_t) * (nbI + 1), cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->jac_col, jcol.data(), sizeof(uint32_t) * jcol.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->jac_slot, jslot.data(), sizeof(uint32_t) * jslot.size(), cudaMemcpyHostToDevice);
     const cudaError_t e = cudaDeviceSynchronize();
@@ -846,6 +855,7 @@ ocpx_status ocpx_linsolve(ocpx_ctx* ctx, double tol, int maxit, double* u_host, 
 {
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
     if (!(tol > 0) || maxit < 1) return fail(OCPX_INVALID_ARG, "tol must be > 0 and maxit >= 1");
+    if (ctx->nbI < ctx->nb) return fail(OCPX_INVALID_ARG, "the device solve needs a single domain (no ghost cells)");
     const int dim = ctx->nc + 1;
     if (!ctx->ls_scratch)
         OCPX_CUDA(cudaMalloc(&ctx->ls_scratch, sizeof(double) * linsolve_scratch_doubles(ctx->nb, dim)));
@@ -1102,8 +1112,9 @@ ocpx_status ocpx_wells_eval(ocpx_ctx* ctx, int nwell, const ocpx_well* wells, do
             if (W.factor) fac[(size_t)w * nc + i] = W.factor[i];
         }
         for (int q = 0; q < W.nperf; q++) {
-            if (W.cell[q] < 0 || W.cell[q] >= nb)
-                return fail(OCPX_INVALID_ARG, "well " + std::to_string(w) + ": perforated cell out of range");
+            if (W.cell[q] < 0 || W.cell[q] >= ctx->nbI)
+                return fail(OCPX_INVALID_ARG, "well " + std::to_string(w) + ": perforated cell out of range "
+                                              "(or a ghost cell)");
             perf.push_back(WellPerf{W.cell[q], w, W.type, W.mode, W.bhp, W.WI[q], W.dG[q],
                                     W.type == 0 ? W.xi_inj[q] : 0.0});
         }
@@ -1229,7 +1240,7 @@ ocpx_status ocpx_synchronize(ocpx_ctx* ctx)
 ocpx_status ocpx_jacobian_dims(ocpx_ctx* ctx, size_t* nrow, size_t* nnz_blocks, int* block_dim)
 {
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
-    if (nrow) *nrow = ctx->nb;
+    if (nrow) *nrow = ctx->nbI;
     if (nnz_blocks) *nnz_blocks = ctx->jac_nnz;
     if (block_dim) *block_dim = ctx->nc + 1;
     return OCPX_OK;
@@ -1240,7 +1251,7 @@ ocpx_status ocpx_get_jacobian(ocpx_ctx* ctx, uint32_t* rowptr, uint32_t* col, do
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
     const size_t bsize = (size_t)(ctx->nc + 1) * (ctx->nc + 1);
     if (rowptr)
-        OCPX_CUDA(cudaMemcpyAsync(rowptr, ctx->jac_rowptr, sizeof(uint32_t) * (ctx->nb + 1), cudaMemcpyDeviceToHost,
+        OCPX_CUDA(cudaMemcpyAsync(rowptr, ctx->jac_rowptr, sizeof(uint32_t) * (ctx->nbI + 1), cudaMemcpyDeviceToHost,
                                   ctx->stream));
     if (col)
         OCPX_CUDA(cudaMemcpyAsync(col, ctx->jac_col, sizeof(uint32_t) * ctx->jac_nnz, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1381,6 +1392,7 @@ ocpx_status ocpx_adjoint(ocpx_ctx* ctx, const double* lambda, double* jt_lambda,
                          double* dr_dporo)
 {
     if (!ctx || !lambda) return fail(OCPX_INVALID_ARG, "null argument");
+    if (ctx->nbI < ctx->nb) return fail(OCPX_INVALID_ARG, "the adjoint needs a single domain (no ghost cells)");
     cudaStream_t s = ctx->stream;
     const size_t nv = (size_t)ctx->nb * (ctx->nc + 1);
     double* d_lam = ctx->adj;
@@ -1409,6 +1421,8 @@ ocpx_status ocpx_adjoint(ocpx_ctx* ctx, const double* lambda, double* jt_lambda,
 ocpx_status ocpx_set_adjoint_seed(ocpx_ctx* ctx, const double* lambda)
 {
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    if (lambda && ctx->nbI < ctx->nb)
+        return fail(OCPX_INVALID_ARG, "the adjoint needs a single domain (no ghost cells)");
     ctx->drop_graph();
     if (!lambda) {
         ctx->adj_in_step = false;

@@ -85,7 +85,7 @@ class GridDesc(C.Structure):
     _fields_ = [("nb", C.c_int), ("nconn", C.c_int), ("v", C.POINTER(C.c_double)),
                 ("depth", C.POINTER(C.c_double)), ("poro_init", C.POINTER(C.c_double)),
                 ("conn_b", C.POINTER(C.c_uint32)), ("conn_e", C.POINTER(C.c_uint32)),
-                ("conn_trans", C.POINTER(C.c_double))]
+                ("conn_trans", C.POINTER(C.c_double)), ("nb_interior", C.c_int)]
 
 
 class Report(C.Structure):
@@ -298,13 +298,16 @@ class Model:
 @dataclass
 class Grid:
     """Bulk geometry and the connection list (bId < eId pairs in the
-    reference's order) with transmissibilities."""
+    reference's order) with transmissibilities.  A subdomain (halo.py) lists
+    its interior cells first, nb_interior of them (0: all cells), then its
+    ghost cells."""
     v: np.ndarray
     depth: np.ndarray
     poro_init: np.ndarray
     conn_b: np.ndarray
     conn_e: np.ndarray
     conn_trans: np.ndarray
+    nb_interior: int = 0
 
     @property
     def nb(self):
@@ -320,7 +323,7 @@ class Grid:
                 np.ascontiguousarray(self.conn_e, np.uint32), np.ascontiguousarray(self.conn_trans, np.float64)]
         g = GridDesc(self.nb, self.nconn, _dptr(keep[0]), _dptr(keep[1]), _dptr(keep[2]),
                      keep[3].ctypes.data_as(C.POINTER(C.c_uint32)), keep[4].ctypes.data_as(C.POINTER(C.c_uint32)),
-                     _dptr(keep[5]))
+                     _dptr(keep[5]), int(self.nb_interior))
         return g, keep
 
 
@@ -342,6 +345,7 @@ class FimContext:
         self.model = model
         self.grid = grid
         self.nb = grid.nb
+        self.nbI = grid.nb_interior or grid.nb
         self.np = 3
         self.nc = model.nc
         self.nconn = grid.nconn
@@ -614,7 +618,7 @@ class FimContext:
     def jacobian(self):
         nrow, nnz, bd = C.c_size_t(), C.c_size_t(), C.c_int()
         _check(self.lib.ocpx_jacobian_dims(self.h, C.byref(nrow), C.byref(nnz), C.byref(bd)))
-        rp = np.empty(nrow.value + 1, np.uint32)
+        rp = np.empty(nrow.value + 1, np.uint32)   # interior rows
         col = np.empty(nnz.value, np.uint32)
         val = np.empty(nnz.value * bd.value * bd.value, np.float64)
         _check(self.lib.ocpx_get_jacobian(self.h, rp.ctypes.data_as(C.c_void_p), col.ctypes.data_as(C.c_void_p),

@@ -1,21 +1,35 @@
 #!/usr/bin/env python3
 """FIM Newton-step throughput on GB300: cells/s of one Newton iteration of
 the compositional PR-EoS path (property update with flash and FlashDer,
-kr/Pc, rock, flux, residual and block-CSR Jacobian), batched GPU form vs the
-plain per-kernel form, beside the reference algorithm on the host cores.
+kr/Pc, rock, flux, residual, block-CSR Jacobian and the adjoint products),
+batched GPU form vs the plain per-kernel form, beside the reference
+algorithm on the host cores.
 
-Workload (the compositional single-Newton-step case): 60 x 60 x 10 = 36,000
-cells, 6 seeded pseudo-components, per-cell feed z ~ Dirichlet(2), P ~
-U(10, 30) MPa, T = 345 K, 50 mD, porosity 0.2, PTN start; the timed step is
-the second Newton iteration of the time step (two seeded Newton updates).  Wells are
-host-side in the reference design and not part of the GPU step.
+Workloads (--workload):
+  large (default)  200 x 200 x 100 = 4,000,000 cells, 9 seeded components,
+                   corner-point grid (COORD / ZCORN) whose layers dip by
+                   seeded angles within +-5 degrees and whose pillars are
+                   moved by seeded offsets within 10 % of the cell size,
+                   lognormal permeability (median 100 mD, sigma_ln 2.0,
+                   correlation 10 cells); every step also computes J^T lambda,
+                   (dR/dT)^T lambda and (dR/dporo)^T lambda (lambda ~ N(0, 1)).
+  fim              60 x 60 x 10 = 36,000 cells, 6 seeded components, 50 mD.
+  flash-stress     1,048,576 independent 10-component flashes.
+Both FIM workloads start from a seeded PTN start (P ~ U(10, 30) MPa,
+z ~ Dirichlet(2), T = 345 K, pores filled) and time the second Newton
+iteration of the time step (two seeded Newton updates), so the flash starts
+from the phase state and iteration history of the first.  Wells are not part
+of the step.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload W]
 
 Prints one JSON line (rank 0).  value = device-resident cells/s of the
-batched form (CUDA events on the library's stream, L2 flushed between
-steps); e2e = the same metric through the C ABI with host buffers (pinned
-Newton update in, residual and Jacobian values out) inside the timed region.
+batched form (its CUDA graph replayed on the library's stream, timed with
+CUDA events, L2 flushed between steps); e2e = the same metric through the C
+ABI with host buffers (the pinned Newton update in, the residual, Jacobian
+values and adjoint products out) inside the timed region; parity = the timed
+step against the oracle run from the same inputs on a window of the grid
+(the large workload: two whole layers with their ghost layers).
 """
 from __future__ import annotations
 
@@ -33,10 +47,10 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-NX, NY, NZ, NCOMP, SEED = 60, 60, 10, 6, 2
 DT, DSMAX = 0.1, 0.2
 METRIC = "FIM Newton-step cells/s (flash+assembly), batched vs plain GPU, <=1e-10 rel err"
-WORKLOAD = "compositional PR-EoS FIM, 6 components, 60x60x10 = 36000 cells, single Newton step"
+REL_TOL = 1e-10
+LIBM_FACTOR = 4.0  # CUDA and glibc transcendentals differ by up to about 2 ulp per call; margin 2
 
 
 # ------------------------------------------------------------ CUDA runtime --
@@ -56,10 +70,13 @@ class Cudart:
         rt.cudaEventSynchronize.argtypes = [C.c_void_p]
         rt.cudaEventElapsedTime.argtypes = [C.POINTER(C.c_float), C.c_void_p, C.c_void_p]
         rt.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+        rt.cudaFree.argtypes = [C.c_void_p]
         rt.cudaMallocHost.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+        rt.cudaFreeHost.argtypes = [C.c_void_p]
         rt.cudaMemsetAsync.argtypes = [C.c_void_p, C.c_int, C.c_size_t, C.c_void_p]
         rt.cudaStreamSynchronize.argtypes = [C.c_void_p]
         rt.cudaSetDevice.argtypes = [C.c_int]
+        self.pinned_ptrs = []
 
     def event(self):
         e = C.c_void_p()
@@ -79,10 +96,16 @@ class Cudart:
 
     def pinned(self, n, dtype=np.float64):
         p = C.c_void_p()
-        nbytes = int(n * np.dtype(dtype).itemsize)
-        assert self.rt.cudaMallocHost(C.byref(p), nbytes) == 0
+        nbytes = int(max(n, 1) * np.dtype(dtype).itemsize)
+        assert self.rt.cudaMallocHost(C.byref(p), nbytes) == 0, f"cudaMallocHost({nbytes}) failed"
+        self.pinned_ptrs.append(p)
         buf = (C.c_char * nbytes).from_address(p.value)
         return np.frombuffer(buf, dtype=dtype, count=n)
+
+    def free_pinned(self):
+        for p in self.pinned_ptrs:
+            self.rt.cudaFreeHost(p)
+        self.pinned_ptrs = []
 
 
 # ----------------------------------------------------------------- clocks ---
@@ -146,48 +169,128 @@ class ClockSampler:
                 "window": "timed loop" if inside else "whole sampler run (no sample inside the timed loop)"}
 
 
-# ---------------------------------------------------------------- workload --
-def newton_updates(grid, Ni):
-    """Two seeded Newton updates (dP ~ N(0, 2) bar, dNi = Ni N(0, 2e-3))."""
-    out = []
-    for k in range(2):
-        rng = np.random.default_rng(SEED + 77 + k)
-        u = np.zeros((grid.nb, NCOMP + 2))
-        u[:, 0] = rng.normal(0.0, 2.0, grid.nb)
-        u[:, 1:] = Ni.reshape(grid.nb, -1) * rng.normal(0.0, 2e-3, (grid.nb, NCOMP + 1))
-        out.append(u.ravel())
-    return out
+# -------------------------------------------------------------- workloads ---
+class FimWorkload:
+    """The compositional Newton step on 60 x 60 x 10 = 36,000 cells."""
+    key = "fim"
+    ncomp, seed = 6, 2
+    dims = (60, 60, 10)
+    adjoint = False
+
+    def __init__(self, args):
+        self.args = args
+
+    @property
+    def description(self):
+        nx, ny, nz = self.dims
+        return (f"compositional PR-EoS FIM, {self.ncomp} components, {nx}x{ny}x{nz} = {nx * ny * nz} cells, "
+                "single Newton step")
+
+    def model(self):
+        from opencaeporox_gb300 import synthetic
+        return synthetic.comp_model(self.ncomp, self.seed)
+
+    def grid(self):
+        from opencaeporox_gb300 import synthetic
+        return synthetic.comp_grid(*self.dims)
+
+    def parity_cells(self):
+        """(owned cells, ghost cells) of the parity window: the whole grid."""
+        nb = int(np.prod(self.dims))
+        return np.arange(nb), np.zeros(0, np.int64)
+
+    def cpu_sample(self):
+        """(grid, cells of the whole grid it holds, description) of the CPU
+        baseline's sample: the whole grid."""
+        g = self.grid()
+        return g, np.arange(g.nb), f"the whole {g.nb}-cell grid"
 
 
-def build_workload(variant, device=0):
-    """PTN start, pores filled; first Newton iteration of the time step; the
-    timed step is the second Newton iteration (the flash then starts from the
-    phase state and iteration history of the first, as in a simulation)."""
+class LargeWorkload(FimWorkload):
+    """200 x 200 x 100 = 4,000,000 cells, 9 components, dipping corner-point
+    grid with moved pillars, lognormal permeability; the adjoint products in
+    every step."""
+    key = "large"
+    ncomp, seed = 9, 5
+    dxy, dz, top = 20.0, 2.0, 2000.0
+    adjoint = True
+    _grid = None
+
+    def __init__(self, args):
+        super().__init__(args)
+        self.dims = tuple(args.large_dims)
+
+    @property
+    def description(self):
+        nx, ny, nz = self.dims
+        return (f"{nx}x{ny}x{nz} = {nx * ny * nz:,} cells, {self.ncomp} components, lognormal k (median 100 mD, "
+                "sigma_ln 2.0, correlation 10 cells), corner-point grid (COORD/ZCORN: layers dipping within +-5 "
+                "degrees, pillars moved within 10% of the cell size), second Newton iteration with the adjoint "
+                "products J^T lambda, (dR/dT)^T lambda, (dR/dporo)^T lambda")
+
+    def geometry(self):
+        from opencaeporox_gb300 import synthetic
+        nx, ny, nz = self.dims
+        rng = np.random.default_rng(self.seed)
+        dip_x, dip_y = rng.uniform(-5, 5, 2)
+        coord, zcorn = synthetic.dipping_corner_point(nx, ny, nz, self.dxy, self.dz, self.top, dip_x, dip_y, 0.0,
+                                                      seed=self.seed, pillar_jitter=0.1)
+        k = synthetic.layered_lognormal_perm(nx, ny, nz, 100.0, 2.0, 10, self.seed)
+        return coord, zcorn, k
+
+    def _ingest(self, k0, k1):
+        """The layers [k0, k1) as a grid of their own (the same cells and, among
+        them, the same connections as in the whole grid)."""
+        from opencaeporox_gb300 import synthetic
+        from opencaeporox_gb300.grid import corner_point_grid
+        nx, ny, nz = self.dims
+        coord, zcorn, k = self.geometry()
+        zc = zcorn.reshape(nz, -1)[k0:k1].ravel()
+        ks = k.reshape(nz, -1)[k0:k1].ravel()
+        n = ks.size
+        return corner_point_grid(nx, ny, k1 - k0, coord, zc, ks, ks, 0.1 * ks, np.full(n, 0.2),
+                                 conv_darcy=synthetic.METRIC["CONV_DARCY"])
+
+    def grid(self):
+        if LargeWorkload._grid is None or LargeWorkload._grid[0] != self.dims:
+            t0 = time.perf_counter()
+            g = self._ingest(0, self.dims[2])
+            print(f"large: corner-point ingest {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
+            LargeWorkload._grid = (self.dims, g)
+        return LargeWorkload._grid[1]
+
+    def parity_cells(self):
+        nx, ny, nz = self.dims
+        layer = nx * ny
+        k0 = max(1, nz // 2 - 1)
+        k1 = min(nz - 1, k0 + 2)
+        owned = np.arange(k0 * layer, k1 * layer)
+        ghost = np.concatenate([np.arange((k0 - 1) * layer, k0 * layer), np.arange(k1 * layer, (k1 + 1) * layer)])
+        return owned, ghost
+
+    def cpu_sample(self):
+        nx, ny, nz = self.dims
+        layers = min(nz, max(1, int(self.args.cpu_layers)))
+        k0 = max(0, nz // 2 - layers // 2)
+        g = self._ingest(k0, k0 + layers)
+        first = k0 * nx * ny
+        return g, np.arange(first, first + g.nb), (f"layers {k0}..{k0 + layers - 1} of the grid ({g.nb:,} cells, "
+                                                   "their state from the same seeds) as a grid of their own")
+
+
+# -------------------------------------------------------------- GPU legs ---
+def prepare(wl, model, grid, variant, device):
+    """A context at the input of the timed Newton iteration: checkpoint 0 =
+    the state after the second Newton update, checkpoint 1 = the state just
+    before it.  Returns (ctx, u2)."""
     from opencaeporox_gb300 import synthetic
     from opencaeporox_gb300.fim import FimContext
-    model = synthetic.comp_model(NCOMP, SEED)
-    grid = synthetic.comp_grid(NX, NY, NZ)
-    st = synthetic.comp_initial_state(grid, NCOMP, SEED)
     ctx = FimContext(model, grid, device=device, variant=variant)
-    ctx.load_state(st)
-    ctx.update_property()  # PTN start: FlashDer with no phase history (MixtureUnit::InitFlashFIM)
-    # scale the moles so the fluid fills the pores, then flash again from scratch
-    scale = ctx.get("ROCKVP") / ctx.get("VF")
-    Ni = (st["Ni"].reshape(grid.nb, -1) * scale[:, None]).ravel()
-    st.update(Ni=Ni, lNi=Ni, Nt=Ni.reshape(grid.nb, -1).sum(axis=1))
-    ctx.load_state(st)
-    ctx.set("SKIP_FLAG", np.zeros(grid.nb, np.uint8))
-    ctx.update_property()
-    ctx.cal_res(DT)
-    ctx.update_last_time_step()
-    u1, u2 = newton_updates(grid, Ni)
-    ctx.get_solution(u1, DSMAX)  # Newton iteration 1
-    ctx.update_property()
-    ctx.cal_res(DT)
-    ctx.checkpoint(1)  # before the second Newton update
-    ctx.get_solution(u2, DSMAX)
-    ctx.checkpoint(0)  # input of the timed Newton iteration
-    return ctx, model, grid, u2
+    us = synthetic.ptn_workload(ctx, grid, wl.ncomp, wl.seed, dt=DT, dsmax=DSMAX, slot_before_last=1)
+    ctx.checkpoint(0)
+    if wl.adjoint:
+        ctx.set_adjoint_seed(np.random.default_rng(wl.seed + 500).normal(size=grid.nb * (wl.ncomp + 2)))
+    return ctx, us[1]
 
 
 def time_device(ctx, rt, steps, warmup, flush):
@@ -213,16 +316,17 @@ def time_device(ctx, rt, steps, warmup, flush):
     return times, ctx.launch_count - launches0
 
 
-def time_e2e(ctx, rt, steps, warmup, flush, u):
-    """End to end through the C ABI: pinned u in, residual + Jacobian values out."""
+def time_e2e(ctx, rt, steps, warmup, flush, u, adjoint):
+    """End to end through the C ABI: the pinned Newton update in, residual,
+    Jacobian values (and the adjoint products) out to pinned host buffers."""
     stream = C.c_void_p(ctx.stream)
     nb, nc = ctx.nb, ctx.nc
-    _, nnz_col, _ = None, None, None
-    rp, col, val = ctx.jacobian()
+    nnz = ctx_nnz(ctx)
     u_pin = rt.pinned(u.size)
     u_pin[:] = u
     res_pin = rt.pinned(nb * (nc + 1))
-    jac_pin = rt.pinned(val.size)
+    jac_pin = rt.pinned(nnz * (nc + 1) ** 2)
+    adj = (rt.pinned(nb * (nc + 1)), rt.pinned(ctx.nconn), rt.pinned(nb)) if adjoint else None
     times = []
     for k in range(warmup + steps):
         ctx.checkpoint(1, restore=True)
@@ -230,13 +334,22 @@ def time_e2e(ctx, rt, steps, warmup, flush, u):
         rt.rt.cudaStreamSynchronize(stream)
         t0 = time.perf_counter()
         ctx.step(u=u_pin, dSmax=DSMAX, dt=DT, res_out=res_pin, jac_out=jac_pin)
+        if adjoint:
+            ctx.get_adjoint(out=adj)
         t1 = time.perf_counter()
         if k >= warmup:
             times.append((t1 - t0) * 1e3)
-    return times, u.nbytes, res_pin.nbytes + jac_pin.nbytes
+    d2h = res_pin.nbytes + jac_pin.nbytes + (sum(a.nbytes for a in adj) if adjoint else 0)
+    return times, u.nbytes, d2h
 
 
-def stage_profile(ctx, rt, flush, reps=3):
+def ctx_nnz(ctx):
+    nrow, nnz, bd = C.c_size_t(), C.c_size_t(), C.c_int()
+    ctx.lib.ocpx_jacobian_dims(ctx.h, C.byref(nrow), C.byref(nnz), C.byref(bd))
+    return nnz.value
+
+
+def stage_profile(ctx, rt, flush, reps=1):
     stream = C.c_void_p(ctx.stream)
     ctx.profile(True)
     for k in range(reps):
@@ -249,45 +362,211 @@ def stage_profile(ctx, rt, flush, reps=3):
     return {k: (v[0] / max(v[1], 1), v[1] // reps) for k, v in prof.items() if v[1]}
 
 
-def cpu_baseline(threads=None):
-    """The reference algorithm (oracle port, C, OpenMP over cells) on the host
-    cores: the same workload and Newton iteration, timed on the host."""
+# --------------------------------------------------------------- parity ---
+ORACLE_FIELDS = ["P", "T", "PB", "NI", "LNI", "NT", "VF", "VFP", "VFI", "PJ", "PC", "S", "PHASE_EXIST", "XIJ", "RHO",
+                 "XI", "MU", "RHOP", "XIP", "MUP", "RHOX", "XIX", "MUX", "KR", "DKRDS", "DPCDS", "DSEC_DPRI", "PORO",
+                 "POROP", "ROCKVP", "SKIP_FLAG", "SKIP_MINEIG", "SKIP_P", "SKIP_T", "SKIP_ZI"]
+FLASH_KEYS = {"S": "S", "XIJ": "xij", "RHO": "rho", "XI": "xi", "MU": "mu", "RHOX": "rhox", "XIX": "xix",
+              "MUX": "mux", "RHOP": "rhoP", "XIP": "xiP", "MUP": "muP", "VF": "vf", "VFP": "vfP", "VFI": "vfi",
+              "NT": "Nt", "DSEC_DPRI": "dSec_dPri"}
+PHASE_KEYS = ("RHO", "XI", "MU", "RHOP", "XIP", "MUP")
+PHASE_COMP_KEYS = ("XIJ", "RHOX", "XIX", "MUX")
+CELLWISE_KEYS = ("VFI", "VFP", "DSEC_DPRI")   # outputs of the NC x NC derivative solve: normwise per cell
+
+
+def cells_ranges(cells):
+    """Runs of consecutive cell numbers: [(first, count)]."""
+    cells = np.asarray(cells, np.int64)
+    if cells.size == 0:
+        return []
+    cut = np.nonzero(np.diff(cells) != 1)[0] + 1
+    starts = np.concatenate([[0], cut])
+    ends = np.concatenate([cut, [cells.size]])
+    return [(int(cells[s]), int(e - s)) for s, e in zip(starts, ends)]
+
+
+def get_cells(ctx, name, cells):
+    return np.concatenate([ctx.get_range(name, f, n) for f, n in cells_ranges(cells)])
+
+
+def flash_errors(got, ref, pe, nc):
+    """Max relative error per flash output (floor 1e-12 x the array's
+    scale); phase quantities where the phase exists; derivative-solve outputs
+    normwise per cell."""
+    out = {}
+    n = pe.shape[0]
+    for k in FLASH_KEYS:
+        a = np.asarray(got[k], np.float64).reshape(n, -1)
+        b = np.asarray(ref[k], np.float64).reshape(n, -1)
+        if k in CELLWISE_KEYS:
+            out[k] = float(np.max(np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)))
+            continue
+        if k in PHASE_KEYS:
+            m = pe
+        elif k in PHASE_COMP_KEYS:
+            m = np.repeat(pe, nc, axis=1)
+        else:
+            m = np.ones_like(a, bool)
+        a, b = a[m], b[m]
+        if a.size == 0:
+            out[k] = 0.0
+            continue
+        floor = max(np.max(np.abs(b)) * 1e-12, 1e-300)
+        out[k] = float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor)))
+    return out
+
+
+def parity(ctx, wl, model, grid):
+    """The timed step (the replayed graph) against the oracle from the same
+    inputs on a window: owned cells with their ghost cells.  Upwind choices
+    exact; phase labels exact except in cells whose labels the oracle itself
+    changes under one-ulp perturbations of its transcendentals (counted);
+    flash outputs of the other cells within max(1e-10, 4 x the oracle's own
+    one-ulp libm sensitivity on them); residual rows on each equation's scale
+    and Jacobian rows normwise within 1e-10, from the GPU's post-flash state."""
+    from opencaeporox_gb300 import halo
+    from opencaeporox_gb300.fim import REF_NAMES
+    from oracle.pyoracle import OracleBulk
+    t0 = time.perf_counter()
+    owned, ghost = wl.parity_cells()
+    sub_grid, cells, conns = halo.subdomain(grid, owned, ghost)
+    no = owned.size
+    nc = model.nc
+    inv = {v: k for k, v in REF_NAMES.items()}
+    ctx.checkpoint(0, restore=True)
+    inputs = {f: get_cells(ctx, f, cells) for f in ORACLE_FIELDS}
+    ctx.enqueue_step(DT)
+    ctx.step_report()
+    got = {f: get_cells(ctx, f, owned) for f in list(FLASH_KEYS) + ["PHASE_EXIST"]}
+    res_g = get_cells(ctx, "RES", owned).reshape(no, -1)
+    c0, c1 = int(conns.min()), int(conns.max()) + 1
+    up_g = ctx.get_range("UPBLOCK", c0, c1 - c0).reshape(-1, 3)[conns - c0]
+    runs = cells_ranges(owned)
+    jac_g = [ctx.jacobian_rows(f, f + n) for f, n in runs]
+
+    def oracle(variant="exact", seed=None):
+        ob = OracleBulk(model, sub_grid, variant=variant)
+        if seed is not None:
+            ob.set_nudge_seed(seed)
+        ob.load({inv[f]: v for f, v in inputs.items()})
+        ob.update_property()
+        return ob
+
+    ob = oracle()
+    pe_o = ob.a["phaseExist"].reshape(-1, 3)[:no].astype(bool)
+    pe_g = got["PHASE_EXIST"].reshape(-1, 3).astype(bool)
+    # cells whose phase labels the reference algorithm itself changes when its
+    # transcendentals round one ulp differently (near a phase boundary): there
+    # the GPU's libm may decide either way
+    nudged = []
+    sensitive = np.zeros(no, bool)
+    for seed in (1, 2, 3):
+        nb_ = oracle("ulp", seed)
+        pe_n = nb_.a["phaseExist"].reshape(-1, 3)[:no].astype(bool)
+        sensitive |= np.any(pe_n != pe_o, axis=1)
+        nudged.append({k: nb_.a[v].reshape(cells.size, -1)[:no].copy() for k, v in FLASH_KEYS.items()})
+        del nb_
+    mismatch = np.any(pe_o != pe_g, axis=1)
+    label_mismatch = int(mismatch.sum())
+    unexplained = int(np.sum(mismatch & ~sensitive))
+    keep = ~(mismatch | sensitive)
+    ref = {k: ob.a[v].reshape(cells.size, -1)[:no][keep] for k, v in FLASH_KEYS.items()}
+    errs = flash_errors({k: np.asarray(got[k]).reshape(no, -1)[keep] for k in FLASH_KEYS}, ref, pe_o[keep], nc)
+    sens = {}
+    for nz in nudged:
+        for k, v in flash_errors({k: nz[k][keep] for k in FLASH_KEYS}, ref, pe_o[keep], nc).items():
+            sens[k] = max(sens.get(k, 0.0), v)
+    tol = {k: max(REL_TOL, LIBM_FACTOR * sens.get(k, 0.0)) for k in FLASH_KEYS}
+    # residual and Jacobian of the oracle from the GPU's post-flash state
+    post = {f: get_cells(ctx, f, cells) for f in ORACLE_FIELDS}
+    oc = OracleBulk(model, sub_grid)
+    oc.load({inv[f]: v for f, v in post.items()})
+    oc.cal_res(DT)
+    rp, col, val = oc.assemble(DT)
+    up_mismatch = int(np.sum(cells[oc.conn["upblock"].reshape(-1, 3)] != up_g))
+    r_o = oc.res.reshape(cells.size, -1)[:no]
+    scale = np.empty_like(r_o)
+    scale[:, 0] = post["ROCKVP"][:no]
+    scale[:, 1:] = post["NT"][:no, None]
+    res_err = float(np.max(np.abs(res_g - r_o) / scale))
+    bs = (nc + 1) ** 2
+    jac_err, pattern_mismatch, row = 0.0, 0, 0
+    for (f, n), (grp, gcol, gval) in zip(runs, jac_g):
+        for q in range(n):
+            a = gval[grp[q] * bs:grp[q + 1] * bs]
+            b = val[rp[row] * bs:rp[row + 1] * bs]
+            if not np.array_equal(gcol[grp[q]:grp[q + 1]], cells[col[rp[row]:rp[row + 1]]]):
+                pattern_mismatch += 1
+            jac_err = max(jac_err, float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)))
+            row += 1
+    flash_ok = all(errs[k] <= tol[k] for k in errs)
+    ok = (unexplained == 0 and up_mismatch == 0 and pattern_mismatch == 0 and flash_ok and res_err <= REL_TOL
+          and jac_err <= REL_TOL)
+    return {"window": f"{no:,} owned cells with {ghost.size:,} ghost cells, {conns.size:,} connections",
+            "against": "oracle (CPU restatement pinned to the reference) from the timed step's own inputs",
+            "label_mismatch_cells": label_mismatch,
+            "libm_sensitive_cells": int(sensitive.sum()),
+            "label_mismatch_outside_libm_sensitive_cells": unexplained,
+            "flash_values_compared_on": f"{int(keep.sum()):,} cells (the others' labels differ or are libm-sensitive)",
+            "upwind_mismatches": up_mismatch,
+            "jacobian_pattern_mismatch_rows": pattern_mismatch,
+            "flash_max_rel_err": {k: float(f"{v:.3g}") for k, v in errs.items()},
+            "flash_tolerance": {k: float(f"{v:.3g}") for k, v in tol.items()},
+            "residual_max_rel_err": res_err, "jacobian_max_rowwise_rel_err": jac_err, "tolerance": REL_TOL,
+            "pass": bool(ok), "seconds": round(time.perf_counter() - t0, 1)}
+
+
+# ------------------------------------------------------------ CPU legs ---
+def cpu_state(wl):
+    """The CPU sample at the input of the timed Newton iteration, built on the
+    host by the oracle from the same seeds: (OracleBulk, saved state, cells)."""
     from opencaeporox_gb300 import synthetic
     from oracle.pyoracle import OracleBulk
-    model = synthetic.comp_model(NCOMP, SEED)
-    grid = synthetic.comp_grid(NX, NY, NZ)
-    st = synthetic.comp_initial_state(grid, NCOMP, SEED)
-    ob = OracleBulk(model, grid)
+    g, cells, desc = wl.cpu_sample()
+    n_total = int(np.prod(wl.dims))
+    first = int(cells[0])
+    st = synthetic.comp_initial_state(g, wl.ncomp, wl.seed, n_total=n_total, first=first)
+    ob = OracleBulk(wl.model(), g)
     ob.load(st)
     ob.update_property()
     scale = ob.a["rockVp"] / ob.a["vf"]
-    Ni = (st["Ni"].reshape(grid.nb, -1) * scale[:, None]).ravel()
-    st.update(Ni=Ni, lNi=Ni, Nt=Ni.reshape(grid.nb, -1).sum(axis=1))
+    Ni = (st["Ni"].reshape(g.nb, -1) * scale[:, None]).ravel()
+    st.update(Ni=Ni, lNi=Ni, Nt=Ni.reshape(g.nb, -1).sum(axis=1))
     ob.load(st)
     ob.a["skip_flag"][:] = 0
     ob.update_property()
     ob.cal_res(DT)
     ob.a["lNi"][:] = ob.a["Ni"]
-    u1, u2 = newton_updates(grid, Ni)
+    u1, u2 = synthetic.ptn_updates(Ni, g.nb, wl.ncomp, wl.seed, n_total=n_total, first=first)
     ob.newton_update(u1, DSMAX)
     ob.update_property()
     ob.cal_res(DT)
     ob.newton_update(u2, DSMAX)
-    saved = {k: v.copy() for k, v in ob.a.items()}
+    return ob, {k: v.copy() for k, v in ob.a.items()}, g.nb, desc
+
+
+def cpu_step(ob, saved):
+    for k, v in saved.items():
+        ob.a[k][:] = v
+    t0 = time.perf_counter()
+    ob.update_property()
+    ob.cal_res(DT)
+    ob.assemble(DT)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(wl, seconds=12.0, max_reps=50):
+    """The reference algorithm (oracle port, C, OpenMP over cells) on the host
+    cores: the timed Newton iteration on the workload's CPU sample."""
+    ob, saved, n, desc = cpu_state(wl)
     times = []
-    t_end = time.perf_counter() + 12.0
+    t_end = time.perf_counter() + seconds
     while time.perf_counter() < t_end or len(times) < 2:
-        for k, v in saved.items():
-            ob.a[k][:] = v
-        t0 = time.perf_counter()
-        ob.update_property()
-        ob.cal_res(DT)
-        ob.assemble(DT)
-        times.append(time.perf_counter() - t0)
-        if len(times) >= 50:
+        times.append(cpu_step(ob, saved))
+        if len(times) >= max_reps:
             break
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return grid.nb / statistics.median(times), cores, len(times)
+    return n / statistics.median(times), cores, f"{desc}: the timed Newton iteration, {len(times)} repetitions, median"
 
 
 def fp64_peak(device=0):
@@ -297,16 +576,20 @@ def fp64_peak(device=0):
     return max(measure_fp64_tflops(device, 20000) for _ in range(3))
 
 
-# FP64 operations of the flash on this workload, per cell: 2 x DFMA + DADD + DMUL
-# thread-level instructions of the plain one-thread-per-cell kernel (k_flash_comp)
-# for the timed Newton iteration (ncu smsp__sass_thread_inst_executed_op_
-# {dfma,dadd,dmul}_pred_on.sum: 223.4 M, 121.7 M, 142.7 M = 711.2 MFLOP), divided by
-# the 36,000 cells; libm internals included.  The batched form does the same
-# algorithmic work in another order (profiles/k_flash_comp_comp6_36k.md).
-FLASH_FP64_FLOP_PER_CELL = (2 * 223408633 + 121682495 + 142721273) / 36000
-# DRAM bytes (read + write) of that launch, from the same capture.
-FLASH_DRAM_BYTES = 107259392 + 173581568        # two-stream form: budgeted + cooperative kernels (ncu)
-FLASH_DRAM_BYTES_FUSED = 155323904 + 250230016  # k_flash_fused<6> on this step (ncu, one launch)
+# FP64 operations of the flash per cell of each workload's timed Newton
+# iteration: 2 x DFMA + DADD + DMUL thread-level instructions of the plain
+# one-thread-per-cell kernel (ncu smsp__sass_thread_inst_executed_op_{dfma,
+# dadd,dmul}_pred_on.sum over one launch, libm internals included) divided by
+# the cells of that launch; the batched form does the same algorithmic work in
+# another order.  fim: 223.4 M DFMA, 121.7 M DADD, 142.7 M DMUL over 36,000
+# cells (profiles/k_flash_comp_comp6_36k.md).  large: the same counts on the
+# workload's generator at 200 x 200 x 25 = 1,000,000 cells
+# (profiles/k_flash_comp_large_1m.md).
+FLASH_FP64_FLOP_PER_CELL = {"fim": (2 * 223408633 + 121682495 + 142721273) / 36000,
+                            "large": (2 * 12605259882 + 6716773959 + 8614568226) / 1000000}
+# DRAM bytes (read + write) per cell of one fused-flash launch on the workload
+# (ncu dram__bytes_read.sum + dram__bytes_write.sum of k_flash_fused)
+FLASH_DRAM_BYTES_PER_CELL = {"fim": (155323904 + 250230016) / 36000, "large": None}
 
 
 def assembly_bytes(nb, nconn, nc, nnzb):
@@ -402,74 +685,10 @@ def flash_stress(args, rt, local):
     return line
 
 
-# ------------------------------------------------------ large Newton step ---
-LG_NX, LG_NY, LG_NZ, LG_NCOMP, LG_SEED = 200, 200, 100, 9, 5
-LG_METRIC = "FIM Newton-step cells/s, 4,000,000-cell compositional grid, 9 components"
-
-
-def large_step(args, rt, local):
-    """200 x 200 x 100 = 4,000,000 cells, 9 seeded components, lognormal
-    permeability (median 100 mD, sigma_ln 2.0, correlation 10 cells), on a
-    corner-point grid (COORD / ZCORN) whose layers dip by seeded angles within
-    +-5 degrees and whose pillars lean by seeded slopes within +-0.02, read by
-    the corner-point ingest.  PTN start, the second Newton iteration timed as
-    in the default workload; plain vs batched form, library defaults."""
-    from opencaeporox_gb300 import synthetic
-    from opencaeporox_gb300.fim import FimContext
-    from opencaeporox_gb300.grid import corner_point_grid
-    nx, ny, nz = args.large_dims
-    rng = np.random.default_rng(LG_SEED)
-    dxy, dz = 20.0, 2.0
-    dip_x, dip_y = rng.uniform(-5, 5, 2)
-    n = nx * ny * nz
-    t0 = time.perf_counter()
-    coord, zcorn = synthetic.dipping_corner_point(nx, ny, nz, dxy, dz, 2000.0, dip_x, dip_y, 0.02, seed=LG_SEED)
-    k = synthetic.layered_lognormal_perm(nx, ny, nz, 100.0, 2.0, 10, LG_SEED)
-    grid = corner_point_grid(nx, ny, nz, coord, zcorn, k, k, 0.1 * k, np.full(n, 0.2),
-                             conv_darcy=synthetic.METRIC["CONV_DARCY"])
-    print(f"large: corner-point ingest {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
-    model = synthetic.comp_model(LG_NCOMP, LG_SEED)
-    out = {}
-    flush = (rt.malloc(512 << 20), 512 << 20)
-    for variant in args.large_variants:
-        t0 = time.perf_counter()
-        ctx = FimContext(model, grid, device=local, variant=variant)
-        synthetic.ptn_workload(ctx, grid, LG_NCOMP, LG_SEED, dt=DT, dsmax=DSMAX)
-        ctx.checkpoint(0)
-        print(f"large: variant {variant} set up in {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
-        times, _ = time_device(ctx, rt, args.steps, args.warmup, flush)
-        prof = stage_profile(ctx, rt, flush, reps=1)
-        out[variant] = dict(ms=statistics.median(times), stages={st: round(v[0], 3) for st, v in prof.items()},
-                            deferred=ctx.get_param("deferred") if variant == 1 else 0,
-                            predeferred=ctx.get_param("predeferred") if variant == 1 else 0,
-                            level=ctx.get_param("level") if variant == 1 else 0,
-                            params={k: ctx.get_param(k) for k in ("fused_blocks", "fused_coop_blocks", "flash_budget", "predefer",
-                                                                 "coop_cells", "coop_blocks", "pre_blocks",
-                                                                 "cell_blocks", "block_cell")} if variant == 1 else None)
-        print(f"large: variant {variant} step {out[variant]['ms']:.1f} ms", file=sys.stderr, flush=True)
-        ctx.close()
-    if 0 not in out or 1 not in out:  # one form only (profiling runs): its times
-        return {"large_dims": [nx, ny, nz], **{f"variant{v}": o for v, o in out.items()}}
-    metric = LG_METRIC if n == LG_NX * LG_NY * LG_NZ else LG_METRIC.replace("4,000,000", f"{n:,}")
-    return {"metric": metric, "value": n / (out[1]["ms"] * 1e-3), "unit": "cells/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out[1]["ms"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": f"{nx}x{ny}x{nz} = {n:,} cells, 9 components, lognormal k (median 100 mD, "
-                                   "sigma_ln 2.0), corner-point grid (COORD/ZCORN: layers dipping within "
-                                   "+-5 degrees, leaning pillars), second Newton iteration",
-                       "connections": int(grid.nconn)},
-            "plain_value": n / (out[0]["ms"] * 1e-3), "plain_ms": out[0]["ms"],
-            "batched_over_plain": out[0]["ms"] / out[1]["ms"], "stages_ms": out[1]["stages"],
-            "plain_stages_ms": out[0]["stages"], "deferred_cells": out[1]["deferred"],
-            "predeferred_cells": out[1]["predeferred"], "level": out[1]["level"], "params": out[1]["params"],
-            "timing": "CUDA events on the library stream around the step (the batched form's graph), "
-                      "L2 flushed between steps; stage times from one eager profiled step (library defaults)"}
-
-
 class Ranks:
-    """torchrun ranks: one replica of the workload per GPU (the path has no
-    cross-rank exchange inside a Newton step here); host barrier and max over
-    ranks through torch.distributed (gloo)."""
+    """torchrun ranks: one replica of the workload per GPU (each rank runs the
+    whole Newton step of its own grid); host barrier and max over ranks
+    through torch.distributed (gloo)."""
 
     def __init__(self, world):
         self.dist = None
@@ -497,132 +716,188 @@ class Ranks:
             self.dist.destroy_process_group()
 
 
+TUNE_SPACE_LARGE = {"fused_blocks": ("sms", 2, 4), "fused_coop_blocks": (0,), "flash_budget": (32, 48, 64),
+                    "predefer": (96, 192), "coop_cells": (1216, 4864), "coop_blocks": (608,), "block_cell": (128,),
+                    "pre_blocks": (0,)}
+
+
+def log(msg):
+    print(msg, file=sys.stderr, flush=True)
+
+
+def run_fim(args, wl, rt, local, rank, world):
+    """The FIM Newton-step bench of one workload: plain form, then the
+    batched form (autotuned, graph-replayed), e2e, parity, rooflines, CPU
+    baseline."""
+    ranks = Ranks(world)
+    model = wl.model()
+    grid = wl.grid()
+    nb = grid.nb
+    large = wl.key == "large"
+    flush_bytes = 512 << 20
+    flush = (rt.malloc(flush_bytes), flush_bytes)
+    # plain form: fewer steps on the large grid, where one takes seconds
+    t0 = time.perf_counter()
+    ctx0, _ = prepare(wl, model, grid, 0, local)
+    log(f"{wl.key}: plain form set up in {time.perf_counter() - t0:.1f} s")
+    p_steps, p_warm = (min(args.steps, 3), 1) if large else (args.steps, args.warmup)
+    ranks.barrier(rt)
+    t_plain, _ = time_device(ctx0, rt, p_steps, p_warm, flush)
+    ranks.barrier(rt)
+    plain_ms = ranks.max(statistics.median(t_plain))
+    plain_prof = stage_profile(ctx0, rt, flush)
+    log(f"{wl.key}: plain step {plain_ms:.1f} ms")
+    ctx0.close()
+    del ctx0
+    # batched form
+    t0 = time.perf_counter()
+    ctx, u2 = prepare(wl, model, grid, 1, local)
+    log(f"{wl.key}: batched form set up in {time.perf_counter() - t0:.1f} s")
+    tuned = None
+    if not args.no_tune:
+        from opencaeporox_gb300 import autotune
+        tuned = autotune.tune(ctx, DT, slot=0, space=TUNE_SPACE_LARGE if large else None, rounds=1 if large else 2,
+                              reps=1 if large else 2)
+        log(f"{wl.key}: tuned {({k: v for k, v in tuned.items() if k != 'trials'})}")
+    clocks = ClockSampler(local)
+    time.sleep(0.5)  # the sampler's first samples come after its start-up
+    ranks.barrier(rt)
+    clocks.start()
+    tb, launches = time_device(ctx, rt, args.steps, args.warmup, flush)
+    clocks.end()
+    ranks.barrier(rt)
+    ck = clocks.stop()
+    ms = ranks.max(statistics.median(tb))
+    log(f"{wl.key}: batched step {ms:.1f} ms")
+    prof = stage_profile(ctx, rt, flush)
+    ranks.barrier(rt)
+    e2e_t, h2d, d2h = time_e2e(ctx, rt, args.steps, args.warmup, flush, u2, wl.adjoint)
+    ranks.barrier(rt)
+    e2e_ms = ranks.max(statistics.median(e2e_t))
+    rt.free_pinned()
+    log(f"{wl.key}: e2e step {e2e_ms:.1f} ms")
+    par = None
+    if rank == 0 and not args.no_parity:
+        par = parity(ctx, wl, model, grid)
+        log(f"{wl.key}: parity {par}")
+    value = nb / (ms * 1e-3) * world
+    plain = nb / (plain_ms * 1e-3) * world
+    fp64 = fp64_peak(local)
+    pk = peaks()
+    hbm = pk.get("hbm_gbs")
+    flash_ms = prof["flash"][0]
+    fused = ctx.get_param("fused_blocks") > 0
+    flop_cell = FLASH_FP64_FLOP_PER_CELL.get(wl.key)
+    dram_cell = FLASH_DRAM_BYTES_PER_CELL.get(wl.key)
+    roof = {"kernel": ("k_flash_fused + k_flash_post" if fused else "k_flash_budget + k_flash_pe_coop + k_flash_post")
+                      + " (flash stage of the batched step)", "bound": "fp64", "unit": "TFLOP/s",
+            "peak": fp64, "peak_source": "measured (DFMA-chain probe of this library, best of 3)",
+            "flop_per_cell": flop_cell, "achieved": None, "frac": None,
+            "traffic": dram_cell * nb if dram_cell else None}
+    if flop_cell:
+        roof["achieved"] = flop_cell * nb / (flash_ms * 1e-3) / 1e12
+        roof["frac"] = roof["achieved"] / fp64
+    asm_ms = prof["jac_conn"][0] + prof["jac_rows"][0]
+    abytes = assembly_bytes(nb, ctx.nconn, ctx.nc, ctx_nnz(ctx))
+    roof_asm = {"kernel": "k_jac_conn + k_jac_rows (Jacobian assembly)", "bound": "hbm", "unit": "GB/s",
+                "algorithmic_bytes": abytes, "achieved": abytes / (asm_ms * 1e-3) / 1e9, "peak": hbm,
+                "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "of fallback 6800",
+                "traffic": None}
+    roof_asm["frac"] = roof_asm["achieved"] / (hbm or 6800.0)
+    dom = max(prof, key=lambda k: prof[k][0] if k not in ("flash_budget", "flash_post", "flash_order") else -1)
+    line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": wl.description, "cells": nb, "connections": int(grid.nconn),
+                       "l2": "flushed between steps (512 MiB memset); inputs larger than L2" if large
+                       else "flushed between steps (512 MiB memset)", "variant": "batched",
+                       "parallelism": f"replicas x{world} (one grid per GPU)"},
+            "plain_value": plain, "plain_ms_per_step": plain_ms, "plain_steps": p_steps,
+            "batched_over_plain": value / plain,
+            "plain_stages_ms": {k: round(v[0], 4) for k, v in plain_prof.items()},
+            "stages_ms": {k: round(v[0], 4) for k, v in prof.items()}, "dominant_stage": dom,
+            "roofline": roof, "roofline_assembly": roof_asm, "fp64_peak_tflops": fp64,
+            "batched": {k: ctx.get_param(k) for k in ("flash_budget", "coop_blocks", "block_cell", "predefer",
+                                                      "coop_cells", "pre_blocks", "cell_blocks", "fused_blocks",
+                                                      "fused_coop_blocks")},
+            "autotune": None if tuned is None else {k: v for k, v in tuned.items() if k != "trials"},
+            "clocks": ck, "gpu_launches": launches,
+            "e2e": {"value": nb / (e2e_ms * 1e-3) * world, "unit": "cells/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+            "parity": par}
+    line["batched"].update(deferred_cells=ctx.get_param("deferred"), predeferred_cells=ctx.get_param("predeferred"),
+                           level=ctx.get_param("level"))
+    ctx.close()
+    if rank == 0 and world == 1 and os.environ.get("OCPX_BENCH_NO_CPU") != "1":
+        v, cores, sample = cpu_baseline(wl)
+        line["cpu_baseline"] = {"value": v, "unit": "cells/s", "cores": cores, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line))
+    ranks.close()
+
+
+def reference_arm(args, wl):
+    """The reference algorithm on the host cores (the oracle port, OpenMP over
+    cells; the reference's own sources are not on the GPU machine): each step
+    the timed Newton iteration on the workload's CPU sample."""
+    from oracle import build as ob_build
+    ob_build.build()
+    ob, saved, n, desc = cpu_state(wl)
+    times = []
+    for k in range(args.warmup + args.steps):
+        t = cpu_step(ob, saved)
+        if k >= args.warmup:
+            times.append(t)
+    v = n / statistics.median(times)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    sample = f"{desc}: the timed Newton iteration per step, median of {len(times)}"
+    return {"metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": statistics.median(times) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": wl.description, "cells": int(np.prod(wl.dims))}, "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "cells/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner (library defaults)")
-    ap.add_argument("--workload", default="fim", choices=["fim", "flash-stress", "large"],
-                    help="fim: the compositional Newton step (default); flash-stress: 1M independent flashes; "
-                         "large: the 4M-cell Newton step")
-    ap.add_argument("--large-dims", type=lambda v: tuple(int(x) for x in v.split(",")), default=(LG_NX, LG_NY, LG_NZ),
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the timed step")
+    ap.add_argument("--workload", default="large", choices=["large", "fim", "flash-stress"],
+                    help="large: the 4,000,000-cell Newton step with the adjoint (default); fim: the 36,000-cell "
+                         "Newton step; flash-stress: 1M independent flashes")
+    ap.add_argument("--large-dims", type=lambda v: tuple(int(x) for x in v.split(",")), default=(200, 200, 100),
                     help="grid of the large workload, NX,NY,NZ (default 200,200,100)")
-    ap.add_argument("--large-variants", type=lambda v: tuple(int(x) for x in v.split(",")), default=(0, 1),
-                    help="forms the large workload runs: 0 plain, 1 batched (default 0,1)")
+    ap.add_argument("--cpu-layers", type=int, default=5,
+                    help="layers of the large workload's grid in the CPU baseline's sample (default 5)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    wl = {"large": LargeWorkload, "fim": FimWorkload}.get(args.workload, FimWorkload)(args)
 
     if args.impl == "reference":
         if rank != 0:
             return
-        from oracle import build as ob
-        ob.build()
-        v, cores, n = cpu_baseline()
-        line = {"metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": args.gpus, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": NX * NY * NZ / v * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-                "config": {"workload": WORKLOAD}, "impl": "reference",
-                "cpu_baseline": {"value": v, "unit": "cells/s", "cores": cores, "kind": "port",
-                                 "sample": f"full 36000-cell second Newton iteration, {n} repetitions, median"},
-                "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        if args.workload == "flash-stress":
+            print(json.dumps({"impl": "reference", "unavailable": "the flash-stress workload has no CPU arm"}))
+            return
+        print(json.dumps(reference_arm(args, wl)))
         return
 
     from opencaeporox_gb300 import build as gb
     gb.build()
     rt = Cudart()
     rt.rt.cudaSetDevice(local)
-    if args.workload != "fim":
+    if args.workload == "flash-stress":
         if rank == 0:
-            fn = {"flash-stress": flash_stress, "large": large_step}[args.workload]
-            print(json.dumps(fn(args, rt, local)))
+            print(json.dumps(flash_stress(args, rt, local)))
         return
-    ranks = Ranks(world)
-    flush_bytes = 512 << 20
-    flush = (rt.malloc(flush_bytes), flush_bytes)
-    results = {}
-    tuned = None
-    for variant in (0, 1):
-        ctx, model, grid, u = build_workload(variant, device=local)
-        if variant == 1 and not args.no_tune:
-            from opencaeporox_gb300 import autotune
-            tuned = autotune.tune(ctx, DT, slot=0)
-        ranks.barrier(rt)
-        t, launches = time_device(ctx, rt, args.steps, args.warmup, flush)
-        ranks.barrier(rt)
-        prof = stage_profile(ctx, rt, flush)
-        results[variant] = dict(ms=ranks.max(statistics.median(t)), mean=statistics.fmean(t),
-                                launches=launches / args.steps, prof=prof, ctx=ctx, u=u)
-    clocks = ClockSampler(local)
-    time.sleep(0.5)  # the sampler's first samples come after its start-up
-    ranks.barrier(rt)
-    clocks.start()
-    tb, launches = time_device(results[1]["ctx"], rt, args.steps, args.warmup, flush)
-    clocks.end()
-    ranks.barrier(rt)
-    ck = clocks.stop()
-    ranks.barrier(rt)
-    e2e_t, h2d, d2h = time_e2e(results[1]["ctx"], rt, args.steps, args.warmup, flush, results[1]["u"])
-    ranks.barrier(rt)
-    nb = NX * NY * NZ
-    ms = ranks.max(statistics.median(tb))
-    value = nb / (ms * 1e-3) * world
-    plain = nb / (results[0]["ms"] * 1e-3) * world
-    e2e_ms = ranks.max(statistics.median(e2e_t))
-    prof = results[1]["prof"]
-    dom = max(prof, key=lambda k: prof[k][0])
-    fp64 = fp64_peak(local)
-    pk = peaks()
-    hbm = pk.get("hbm_gbs")
-    flash_ms = prof["flash"][0]
-    fused = results[1]["ctx"].get_param("fused_blocks") > 0
-    roof = {"kernel": ("k_flash_fused + k_flash_post" if fused else "k_flash_budget + k_flash_pe_coop + k_flash_post")
-                      + " (flash stage of the batched step)", "bound": "fp64", "unit": "TFLOP/s",
-            "peak": fp64, "peak_source": "measured (DFMA-chain probe of this library, best of 3)",
-            "achieved": None, "frac": None, "traffic": FLASH_DRAM_BYTES_FUSED if fused else FLASH_DRAM_BYTES}
-    if FLASH_FP64_FLOP_PER_CELL:
-        roof["achieved"] = FLASH_FP64_FLOP_PER_CELL * nb / (flash_ms * 1e-3) / 1e12
-        roof["frac"] = roof["achieved"] / fp64
-    ctx1 = results[1]["ctx"]
-    rp, _, _ = ctx1.jacobian()
-    asm_ms = prof["jac_conn"][0] + prof["jac_rows"][0]
-    abytes = assembly_bytes(nb, ctx1.nconn, ctx1.nc, int(rp[-1]))
-    roof_asm = {"kernel": "k_jac_conn + k_jac_rows (Jacobian assembly)", "bound": "hbm", "unit": "GB/s",
-                "algorithmic_bytes": abytes, "achieved": abytes / (asm_ms * 1e-3) / 1e9, "peak": hbm,
-                "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "of fallback 6800",
-                "traffic": None}
-    roof_asm["frac"] = roof_asm["achieved"] / (hbm or 6800.0)
-    line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "l2": "flushed between steps (512 MiB memset)", "variant": "batched",
-                       "parallelism": f"replicas x{world} (one 36000-cell grid per GPU)"},
-            "plain_value": plain, "plain_ms_per_step": results[0]["ms"], "batched_over_plain": value / plain,
-            "plain_stages_ms": {k: round(v[0], 4) for k, v in results[0]["prof"].items()},
-            "stages_ms": {k: round(v[0], 4) for k, v in prof.items()}, "dominant_stage": dom,
-            "roofline": roof, "roofline_assembly": roof_asm, "fp64_peak_tflops": fp64,
-            "batched": {"flash_budget": ctx1.get_param("flash_budget"), "coop_blocks": ctx1.get_param("coop_blocks"),
-                        "deferred_cells": ctx1.get_param("deferred"),
-                        "predeferred_cells": ctx1.get_param("predeferred"), "level": ctx1.get_param("level"),
-                        "block_cell": ctx1.get_param("block_cell"), "predefer": ctx1.get_param("predefer"),
-                        "coop_cells": ctx1.get_param("coop_cells"), "pre_blocks": ctx1.get_param("pre_blocks"),
-                        "cell_blocks": ctx1.get_param("cell_blocks"), "fused_blocks": ctx1.get_param("fused_blocks"),
-                        "fused_coop_blocks": ctx1.get_param("fused_coop_blocks"),
-                        "autotune": None if tuned is None else {k: v for k, v in tuned.items() if k != "trials"}},
-            "clocks": ck, "gpu_launches": launches,
-            "e2e": {"value": nb / (e2e_ms * 1e-3) * world, "unit": "cells/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h}}
-    if rank == 0 and world == 1 and os.environ.get("OCPX_BENCH_NO_CPU") != "1":
-        v, cores, n = cpu_baseline()
-        line["cpu_baseline"] = {"value": v, "unit": "cells/s", "cores": cores, "kind": "port",
-                                "sample": f"full 36000-cell second Newton iteration, {n} repetitions, median"}
-    if rank == 0:
-        print(json.dumps(line))
-    ranks.close()
+    run_fim(args, wl, rt, local, rank, world)
 
 
 if __name__ == "__main__":

@@ -223,6 +223,10 @@ ocpx_status ocpx_synchronize(ocpx_ctx* ctx);
  * blocks (nc+1)x(nc+1) row-major. */
 ocpx_status ocpx_jacobian_dims(ocpx_ctx* ctx, size_t* nrow, size_t* nnz_blocks, int* block_dim);
 ocpx_status ocpx_get_jacobian(ocpx_ctx* ctx, uint32_t* rowptr, uint32_t* col, double* val);
+/* Rows [r0, r1) only: rowptr receives r1 - r0 + 1 offsets into the whole
+ * matrix's block arrays (rowptr[0] is the first row's), col and val the
+ * blocks from rowptr[0] to rowptr[r1 - r0]; for windows of large grids. */
+ocpx_status ocpx_get_jacobian_rows(ocpx_ctx* ctx, size_t r0, size_t r1, uint32_t* rowptr, uint32_t* col, double* val);
 /* Device pointers of the same arrays (valid until ocpx_destroy). */
 ocpx_status ocpx_jacobian_device(ocpx_ctx* ctx, const uint32_t** rowptr, const uint32_t** col, const double** val);
 

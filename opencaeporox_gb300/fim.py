@@ -137,7 +137,8 @@ EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy",
            "ocpx_stream", "ocpx_launch_count", "ocpx_set_param", "ocpx_get_param", "ocpx_adjoint",
            "ocpx_nr_init_step", "ocpx_nr_max_change", "ocpx_step_max_change", "ocpx_nr_check_converge",
            "ocpx_next_time_step", "ocpx_linsolve", "ocpx_newton_update_device", "ocpx_wells_eval",
-           "ocpx_set_field_range", "ocpx_get_field_range", "ocpx_set_adjoint_seed", "ocpx_get_adjoint"]
+           "ocpx_set_field_range", "ocpx_get_field_range", "ocpx_set_adjoint_seed", "ocpx_get_adjoint",
+           "ocpx_get_jacobian_rows"]
 
 PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3, "predefer": 4, "coop_cells": 5,
           "predeferred": 6, "level": 7, "pre_blocks": 8,
@@ -195,6 +196,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.ocpx_get_field_range.argtypes = [P, C.c_int, C.c_size_t, C.c_size_t, P]
     lib.ocpx_set_adjoint_seed.argtypes = [P, P]
     lib.ocpx_get_adjoint.argtypes = [P, P, P, P]
+    lib.ocpx_get_jacobian_rows.argtypes = [P, C.c_size_t, C.c_size_t, P, P, P]
     for fn in ("ocpx_enqueue_step", "ocpx_step_report", "ocpx_profile_enable", "ocpx_profile_read",
                "ocpx_measure_fp64_tflops", "ocpx_checkpoint", "ocpx_set_param", "ocpx_get_param"):
         getattr(lib, fn).restype = C.c_int
@@ -431,9 +433,11 @@ class FimContext:
             raise ValueError("lambda must have nb*(nc+1) entries")
         _check(self.lib.ocpx_set_adjoint_seed(self.h, self._adj_seed.ctypes.data_as(C.c_void_p)))
 
-    def get_adjoint(self):
-        """(J^T lam, (dR/dT)^T lam, (dR/dporoInit)^T lam) of the last step."""
-        jt, tr, po = np.empty(self.nb * (self.nc + 1)), np.empty(self.nconn), np.empty(self.nb)
+    def get_adjoint(self, out=None):
+        """(J^T lam, (dR/dT)^T lam, (dR/dporoInit)^T lam) of the last step,
+        into the arrays `out` when given."""
+        jt, tr, po = out if out is not None else (np.empty(self.nb * (self.nc + 1)), np.empty(self.nconn),
+                                                  np.empty(self.nb))
         _check(self.lib.ocpx_get_adjoint(self.h, jt.ctypes.data_as(C.c_void_p), tr.ctypes.data_as(C.c_void_p),
                                          po.ctypes.data_as(C.c_void_p)))
         return jt, tr, po
@@ -624,6 +628,18 @@ class FimContext:
         _check(self.lib.ocpx_get_jacobian(self.h, rp.ctypes.data_as(C.c_void_p), col.ctypes.data_as(C.c_void_p),
                                           val.ctypes.data_as(C.c_void_p)))
         return rp, col, val
+
+    def jacobian_rows(self, r0: int, r1: int):
+        """Rows [r0, r1) of the Jacobian: (rowptr relative to the first row,
+        columns, block values)."""
+        rp = np.empty(r1 - r0 + 1, np.uint32)
+        _check(self.lib.ocpx_get_jacobian_rows(self.h, r0, r1, rp.ctypes.data_as(C.c_void_p), None, None))
+        n = int(rp[-1] - rp[0])
+        col = np.empty(n, np.uint32)
+        val = np.empty(n * (self.nc + 1) ** 2)
+        _check(self.lib.ocpx_get_jacobian_rows(self.h, r0, r1, rp.ctypes.data_as(C.c_void_p),
+                                               col.ctypes.data_as(C.c_void_p), val.ctypes.data_as(C.c_void_p)))
+        return rp - rp[0], col, val
 
     def step(self, u=None, dSmax=0.2, dt=1.0, res_out=None, jac_out=None):
         rep = Report()

@@ -1262,6 +1262,24 @@ ocpx_status ocpx_get_jacobian(ocpx_ctx* ctx, uint32_t* rowptr, uint32_t* col, do
     return OCPX_OK;
 }
 
+ocpx_status ocpx_get_jacobian_rows(ocpx_ctx* ctx, size_t r0, size_t r1, uint32_t* rowptr, uint32_t* col, double* val)
+{
+    if (!ctx || !rowptr) return fail(OCPX_INVALID_ARG, "null argument");
+    if (r0 > r1 || r1 > (size_t)ctx->nbI) return fail(OCPX_INVALID_ARG, "row range outside the interior rows");
+    const size_t bsize = (size_t)(ctx->nc + 1) * (ctx->nc + 1);
+    OCPX_CUDA(cudaMemcpyAsync(rowptr, ctx->jac_rowptr + r0, sizeof(uint32_t) * (r1 - r0 + 1), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    const size_t b0 = rowptr[0], nblk = rowptr[r1 - r0] - b0;
+    if (col && nblk)
+        OCPX_CUDA(cudaMemcpyAsync(col, ctx->jac_col + b0, sizeof(uint32_t) * nblk, cudaMemcpyDeviceToHost, ctx->stream));
+    if (val && nblk)
+        OCPX_CUDA(cudaMemcpyAsync(val, ctx->jac_val + b0 * bsize, sizeof(double) * nblk * bsize, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return OCPX_OK;
+}
+
 ocpx_status ocpx_jacobian_device(ocpx_ctx* ctx, const uint32_t** rowptr, const uint32_t** col, const double** val)
 {
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");

@@ -38,6 +38,11 @@
  * last failure in this thread is available from ocpx_last_error(), and the
  * per-cell status bits of the last property update are readable as the
  * OCPX_F_STATUS field.  One context is used by one host thread at a time.
+ *
+ * Wells (ocpx_set_wells) add one row and column per open well after the
+ * cells, as the reference's LinearSystem orders them: the residual, the
+ * Newton update and the adjoint vectors then hold nb + nwell rows of nc + 1
+ * values, and the Jacobian nb + nwell block rows.
  */
 #ifndef OCPX_H
 #define OCPX_H
@@ -173,7 +178,7 @@ typedef enum ocpx_field {
     OCPX_F_CONN_DP,      /* d  [nconn*np] (read only) */
     OCPX_F_FLUX_VJ,      /* d  [nconn*np] (read only) */
     OCPX_F_FLUX_NI,      /* d  [nconn*nc] (read only) */
-    OCPX_F_RES,          /* d  [nb*(nc+1)] bulk residual, negated as LinearSystem expects; ghost rows 0 (read only) */
+    OCPX_F_RES,          /* d  [(nb+nwell)*(nc+1)] residual, negated as LinearSystem expects; ghost rows 0 (read only) */
     OCPX_F_RES_REL_V,    /* d  [nb] (read only) */
     OCPX_F_RES_REL_N,    /* d  [nb] (read only) */
     OCPX_F_TRANS,        /* d  [nconn] connection transmissibility (BulkConnPair::trans) */
@@ -329,9 +334,9 @@ typedef enum ocpx_param {
 ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value);
 ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value);
 
-/* One Newton iteration: optional host Newton update u (nb*(nc+1), may be
+/* One Newton iteration: optional host Newton update u ((nb+nwell)*(nc+1), may be
  * NULL), then properties, residual and Jacobian; optional host copies of the
- * residual (nb*(nc+1)) and Jacobian block values.  Synchronizes. */
+ * residual ((nb+nwell)*(nc+1)) and Jacobian block values.  Synchronizes. */
 ocpx_status ocpx_step(ocpx_ctx* ctx, const double* u_host, double dSmax, double dt, double* res_host,
                       double* jac_val_host, ocpx_report* rep);
 
@@ -397,9 +402,9 @@ ocpx_status ocpx_relres_noalloc(const double* d_res, const double* d_rockVp, con
 
 /* Adjoint of the bulk residual R (the negated residual of ocpx_calres) at the
  * state of the last ocpx_assemble, as vector-Jacobian products with a host
- * vector lambda [nb*(nc+1)] (cell-major, like the residual).  No counterpart
+ * vector lambda [(nb+nwell)*(nc+1)] (cell-major, like the residual).  No counterpart
  * in the reference, which has no adjoint:
- *   jt_lambda  [nb*(nc+1)]  J^T lambda, J the assembled Jacobian dR/d(P, Ni);
+ *   jt_lambda  [(nb+nwell)*(nc+1)]  J^T lambda, J the assembled Jacobian dR/d(P, Ni);
  *   dr_dtrans  [nconn]      (dR/dT_c)^T lambda for every connection's
  *                           transmissibility (R is linear in T_c: the flux of
  *                           OCPConvection01::CalFlux scales with it);
@@ -413,8 +418,8 @@ ocpx_status ocpx_adjoint(ocpx_ctx* ctx, const double* lambda, double* jt_lambda,
  * (dR/dporoInit)^T lambda on the device right after its Jacobian (inside the
  * step's graph in the batched variant), and ocpx_get_adjoint copies the last
  * step's products to the host (any pointer may be NULL; synchronizes).  The
- * seed [nb*(nc+1)] is copied to the device once; NULL turns the products off.
- * The first seed allocates their device buffers (2*nb*(nc+1) + nb + nconn
+ * seed [(nb+nwell)*(nc+1)] is copied to the device once; NULL turns the products off.
+ * The first seed allocates their device buffers (2*(nb+nwell)*(nc+1) + nb + nconn
  * doubles).  ocpx_adjoint keeps its own buffers and leaves the seed alone. */
 ocpx_status ocpx_set_adjoint_seed(ocpx_ctx* ctx, const double* lambda);
 ocpx_status ocpx_get_adjoint(ocpx_ctx* ctx, double* jt_lambda, double* dr_dtrans, double* dr_dporo);
@@ -438,9 +443,10 @@ ocpx_status ocpx_get_adjoint(ocpx_ctx* ctx, double* jt_lambda, double* dr_dtrans
  *                           calls it (src/IsoThermalMethod.cpp:865-870)
  * The maxima are signed, with the reference's rule: the first entry in cell
  * order whose magnitude is the largest, 0 when every change is 0; results
- * are bit-identical to the reference's.  Wells stay with the host (their
- * equations are not on the device), so their terms enter through
- * ocpx_nr_control.  Every output pointer may be NULL: the values then stay
+ * are bit-identical to the reference's.  Without ocpx_set_wells the wells
+ * stay with the host, and their terms enter through ocpx_nr_control; with
+ * it, ocpx_nr_check_converge uses the device's maxWellRelRes_mol (unless
+ * res_from_host).  Every output pointer may be NULL: the values then stay
  * on the device for the next call, and nothing synchronizes. */
 typedef struct ocpx_change_max {
     double dP, dT, dN, dS, eV;  /* pressure, temperature, relative moles, saturation, volume error */
@@ -503,9 +509,39 @@ typedef struct ocpx_well {
  * block: for each perforation in order the block added to its cell's
  * diagonal, the cell-to-well block (row cell, column nb + w) and the
  * well-to-cell block (row nb + w, column cell); then each well's diagonal
- * block.  max_rel, may be NULL: maxWellRelRes_mol. */
+ * block.  max_rel, may be NULL: maxWellRelRes_mol.  res_out needs an
+ * ocpx_calres at the current state (after the last property update, field
+ * write, Newton update or checkpoint restore): otherwise OCPX_INVALID_ARG.
+ * For a host that keeps its own well code; see ocpx_set_wells for the wells
+ * inside the step. */
 ocpx_status ocpx_wells_eval(ocpx_ctx* ctx, int nwell, const ocpx_well* wells, double dt, double* res_out,
                             double* blocks_out, double* max_rel);
+
+/* Peaceman wells inside the Newton step.  The well set (types, controls,
+ * targets, perforations with WI*multiplier and dG, injected fluid, rate
+ * factors, and each well's current bhp) is copied to the device; from then on
+ * ocpx_calres, ocpx_assemble, ocpx_step and the step's graph add the wells'
+ * terms on the device after the bulk rows, in the reference's order
+ * (IsoT_FIM::CalRes with PeacemanWellIsoT::CalResFIM, src/WellPeaceman.cpp:
+ * 1226-1265; IsoT_FIM::AssembleMatWells, src/IsoThermalMethod.cpp:1272-1280,
+ * with AssembleMatInjFIM / AssembleMatProdFIM, src/WellPeaceman.cpp:1268-1361,
+ * 1488-1613): each perforated cell's residual rows and diagonal block, one
+ * bulk-to-well block per perforation after the cell's connection blocks, and
+ * per open well w a row nb + w (its control equation; diagonal block, then one
+ * well-to-bulk block per perforation).  ocpx_assemble uses the perforation
+ * terms of the last ocpx_calres, as the reference assembles from the state
+ * its residual was computed at.  The Newton update adds u of row nb + w to
+ * well w's bhp (GetSolutionFIM, :1198-1204); the checkpoints carry the bhp;
+ * the device linear solve and the adjoint cover the wells' rows.  Call it
+ * again when a control switches or a new time step changes dG: with the same
+ * perforations nothing is reallocated, otherwise the system's storage is
+ * rebuilt (its contents and any adjoint seed are dropped).  nwell = 0 removes
+ * the wells.  Single domain only (no ghost cells); ocpx_wells_eval is refused
+ * while wells are set.  ocpx_get_wells reads each well's bhp and the
+ * maxWellRelRes_mol of the last ocpx_calres (synchronizes).  The
+ * unweighted-permeability option is not supported. */
+ocpx_status ocpx_set_wells(ocpx_ctx* ctx, int nwell, const ocpx_well* wells);
+ocpx_status ocpx_get_wells(ocpx_ctx* ctx, double* bhp, double* max_rel);
 
 /* Linear solve of the Newton system on the device: J u = rhs, J the bulk
  * Jacobian of the last ocpx_assemble and rhs the residual of the last
@@ -514,10 +550,11 @@ ocpx_status ocpx_wells_eval(ocpx_ctx* ctx, int nwell, const ocpx_well* wells, do
  * hands this system to an external package (FASP, PETSc or PARDISO,
  * src/LinearSystem.cpp:35-89); here BiCGStab with right block-Jacobi
  * preconditioning, from u = 0, until |rhs - J u| <= tol |rhs| or maxit
- * iterations (the norm is checked every 10).  Bulk rows only: a host that
- * couples wells solves the full system itself.  The solution stays on the
- * device for ocpx_newton_update_device and is copied to u_host (nb*(nc+1))
- * when that is not NULL.  The first call allocates the solver's work space
+ * iterations (the norm is checked every 10).  The system holds the wells'
+ * rows when ocpx_set_wells gave them; a host that keeps its own well code
+ * solves the full system itself.  Single domain only.  The solution stays on
+ * the device for ocpx_newton_update_device and is copied to u_host
+ * ((nb+nwell)*(nc+1)) when that is not NULL.  The first call allocates the solver's work space
  * (about 8 vectors and the inverted diagonal blocks).  Synchronizes. */
 typedef struct ocpx_solve_report {
     int iterations;

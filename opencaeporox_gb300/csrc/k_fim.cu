@@ -175,7 +175,12 @@ cudaError_t launch_residual(const BulkView& b, const ConnView& cv, double dt, do
 {
     if (!b.nbI) return cudaSuccess;
     k_residual<<<grid_for(b.nbI, block), block, 0, s>>>(b, cv, dt, res, resRelV, resRelN, rn);
-    k_norm_reduce<<<1, 256, 0, s>>>(rn, b.nbI, rn_out);
+    if (rn_out) k_norm_reduce<<<1, 256, 0, s>>>(rn, b.nbI, rn_out);
+    return cudaGetLastError();
+}
+cudaError_t launch_norm_reduce(const RowNorm* rn, int nbI, RowNorm* rn_out, cudaStream_t s)
+{
+    if (nbI) k_norm_reduce<<<1, 256, 0, s>>>(rn, nbI, rn_out);
     return cudaGetLastError();
 }
 cudaError_t launch_jac_conn(int nct, const Model* dm, const BulkView& b, const ConnView& cv, double dt, double* bmat,

@@ -126,16 +126,19 @@ __device__ __forceinline__ double smin(double a, double b) { return b < a ? b : 
 __device__ __forceinline__ double smax(double a, double b) { return a < b ? b : a; }
 
 __global__ void k_nr_converge(NRControl c, const double* __restrict__ nr, const RowNorm* __restrict__ norm,
-                              const double* __restrict__ res0, int* __restrict__ state)
+                              const double* __restrict__ res0, const double* __restrict__ wellrel,
+                              int* __restrict__ state)
 {
     const double V = c.res_from_host ? c.maxRelRes_V : norm->maxV;
     const double N = c.res_from_host ? c.maxRelRes_N : norm->maxN;
     const double V0 = c.res_from_host ? c.maxRelRes0_V : *res0;
+    // the wells' rate equations: the device's own residual when it holds the wells
+    const double W = (!c.res_from_host && wellrel) ? *wellrel : c.maxWellRelRes_mol;
     const double tmpfac = 1.0;
     bool conv = false;
     // "res"
     if ((V <= V0 * c.tol * tmpfac || V <= c.tol * tmpfac || N <= c.tol * tmpfac) &&
-        c.maxWellRelRes_mol <= c.tol * tmpfac)
+        W <= c.tol * tmpfac)
         conv = true;
     // "d": DPBmaxNRc, DSmaxNRc
     if (fabs(nr[0]) <= c.dPmin && fabs(nr[3]) <= c.dSmin) conv = true;
@@ -191,9 +194,9 @@ cudaError_t launch_max_change(int mode, const BulkView& b, double* lP, double* l
 }
 
 cudaError_t launch_nr_converge(const NRControl& c, const double* nr5, const RowNorm* norm, const double* res0,
-                               int* state, cudaStream_t s)
+                               const double* wellrel, int* state, cudaStream_t s)
 {
-    k_nr_converge<<<1, 1, 0, s>>>(c, nr5, norm, res0, state);
+    k_nr_converge<<<1, 1, 0, s>>>(c, nr5, norm, res0, wellrel, state);
     return cudaGetLastError();
 }
 

@@ -175,6 +175,24 @@ struct ocpx_ctx {
     // lambda [nb] and (dR/dT)^T lambda [nconn]
     double* step_adj = nullptr;
     bool adj_in_step = false;
+    // the linear system's storage (build_system): block-CSR pattern and values
+    // of the interior rows and the wells' rows, the residual and the Newton
+    // update of the cells and the wells, the adjoint's vectors
+    char* sys = nullptr;
+    int nrow = 0;                   // system rows: interior cells, then open wells
+    std::vector<uint32_t> h_row_ptr, h_row_conn, h_conn_b, h_conn_e;  // connectivity, kept for rebuilds
+    // wells inside the step (ocpx_set_wells)
+    char* wbuf = nullptr;
+    WellSys ws{};
+    std::vector<int> well_cells;    // perforated cells, well by well, in perforation order
+    std::vector<int> well_nperf;    // perforations per well
+    std::vector<uint32_t> h_slot_bw, h_slot_wb;  // their blocks in the system (build_system)
+    size_t nv() const { return (size_t)(nb + ws.nw) * (nc + 1); }
+    // ocpx_wells_eval's device buffer (grows as needed) and the state
+    // generation the last residual was computed at
+    char* weval = nullptr;
+    size_t weval_bytes = 0;
+    uint64_t state_gen = 1, res_gen = 0;
     double last_dt = 0;             // dt of the last residual / Jacobian
     uint32_t* jac_col = nullptr;
     double* jac_val = nullptr;
@@ -280,7 +298,7 @@ FieldInfo ocpx_ctx::field(ocpx_field f) const
     case OCPX_F_CONN_DP: return {cv.dP, nconn, np, 8, true, false};
     case OCPX_F_FLUX_VJ: return {cv.flux_vj, nconn, np, 8, true, false};
     case OCPX_F_FLUX_NI: return {cv.flux_ni, nconn, nc, 8, true, false};
-    case OCPX_F_RES: return {res, nb, nc + 1, 8, false, false};
+    case OCPX_F_RES: return {res, nb + ws.nw, nc + 1, 8, false, false};
     case OCPX_F_RES_REL_V: return {resRelV, nb, 1, 8, true, false};
     case OCPX_F_RES_REL_N: return {resRelN, nb, 1, 8, true, false};
     case OCPX_F_TRANS: return {(void*)cv.trans, nconn, 1, 8, true, true};
@@ -303,6 +321,98 @@ int fused_coop_blocks(const ocpx_ctx* ctx)
 {
     if (ctx->fused_coop_blocks >= 0) return ctx->fused_coop_blocks;
     return ctx->nb < 131072 && ctx->fused_blocks <= ctx->sms ? ctx->fused_blocks / 2 : 0;
+}
+
+// The system's storage and block-CSR pattern: per interior row the diagonal
+// block, one block per incident connection in connection order
+// (AssembleMatBulks), then one bulk-to-well block per perforation of the cell
+// in well then perforation order (AssembleMatWells); per open well its
+// diagonal block, then one well-to-bulk block per perforation.  Rebuilt when
+// the wells' structure changes; slot_bw / slot_wb receive each perforation's
+// block indices.  The contents (residual, update, values) start at zero.
+ocpx_status build_system(ocpx_ctx* ctx, std::vector<uint32_t>* slot_bw, std::vector<uint32_t>* slot_wb)
+{
+    const int nbI = ctx->nbI, nb = ctx->nb, nconn = ctx->nconn, dim = ctx->nc + 1;
+    const int nw = (int)ctx->well_nperf.size();
+    const size_t bsize = (size_t)dim * dim;
+    const std::vector<uint32_t>& rp = ctx->h_row_ptr;
+    const std::vector<uint32_t>& rc = ctx->h_row_conn;
+    std::vector<uint32_t> pcount(nbI, 0);
+    for (int c : ctx->well_cells) pcount[c]++;
+    std::vector<uint32_t> jrow((size_t)nbI + nw + 1, 0);
+    for (int n = 0; n < nbI; n++) jrow[n + 1] = jrow[n] + 1 + (rp[n + 1] - rp[n]) + pcount[n];
+    for (int w = 0; w < nw; w++) jrow[nbI + w + 1] = jrow[nbI + w] + 1 + ctx->well_nperf[w];
+    const size_t nnz = jrow.back();
+    std::vector<uint32_t> jcol(nnz);
+    for (int n = 0; n < nbI; n++) {
+        size_t pos = jrow[n];
+        jcol[pos++] = n;
+        for (uint32_t k = rp[n]; k < rp[n + 1]; k++) {
+            const uint32_t c = rc[k] >> 1;
+            jcol[pos++] = (rc[k] & 1u) ? ctx->h_conn_b[c] : ctx->h_conn_e[c];
+        }
+    }
+    std::vector<uint32_t> placed(nbI, 0);
+    if (slot_bw) slot_bw->assign(ctx->well_cells.size(), 0);
+    if (slot_wb) slot_wb->assign(ctx->well_cells.size(), 0);
+    size_t p = 0;
+    for (int w = 0; w < nw; w++) {
+        const uint32_t wrow = nbI + w;
+        jcol[jrow[wrow]] = wrow;
+        for (int q = 0; q < ctx->well_nperf[w]; q++, p++) {
+            const int c = ctx->well_cells[p];
+            const size_t bw = jrow[c] + 1 + (rp[c + 1] - rp[c]) + placed[c]++;
+            jcol[bw] = wrow;
+            const size_t wb = jrow[wrow] + 1 + q;
+            jcol[wb] = (uint32_t)c;
+            if (slot_bw) (*slot_bw)[p] = (uint32_t)bw;
+            if (slot_wb) (*slot_wb)[p] = (uint32_t)wb;
+        }
+    }
+    // block index of each connection in the rows of its two cells (adjoint
+    // transpose; a ghost cell's side has none)
+    std::vector<uint32_t> jslot(2 * (size_t)(nconn > 0 ? nconn : 1), 0xffffffffu);
+    for (int n = 0; n < nbI; n++)
+        for (uint32_t k = rp[n]; k < rp[n + 1]; k++) {
+            const uint32_t c = rc[k] >> 1, side = rc[k] & 1u;
+            jslot[(size_t)side * nconn + c] = jrow[n] + 1 + (k - rp[n]);
+        }
+    const size_t nv = (size_t)(nb + nw) * dim;
+    const size_t o_row = 0, o_col = o_row + align256(sizeof(uint32_t) * jrow.size());
+    const size_t o_slot = o_col + align256(sizeof(uint32_t) * nnz);
+    const size_t o_res = o_slot + align256(sizeof(uint32_t) * jslot.size());
+    const size_t o_u = o_res + align256(sizeof(double) * nv), o_adj = o_u + align256(sizeof(double) * nv);
+    const size_t o_val = o_adj + align256(sizeof(double) * 2 * nv);
+    const size_t total = o_val + align256(sizeof(double) * nnz * bsize);
+    ctx->drop_graph();
+    if (ctx->stream) OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (ctx->sys) cudaFree(ctx->sys);
+    ctx->sys = nullptr;
+    ctx->jac_rowptr = nullptr;
+    ctx->jac_col = nullptr;
+    ctx->jac_slot = nullptr;
+    ctx->jac_val = nullptr;
+    ctx->res = ctx->u = ctx->adj = nullptr;
+    if (cudaMalloc(&ctx->sys, total) != cudaSuccess)
+        return fail(OCPX_CUDA_ERROR, "cudaMalloc of " + std::to_string(total) + " bytes (the linear system) failed");
+    ctx->jac_rowptr = (uint32_t*)(ctx->sys + o_row);
+    ctx->jac_col = (uint32_t*)(ctx->sys + o_col);
+    ctx->jac_slot = (uint32_t*)(ctx->sys + o_slot);
+    ctx->res = (double*)(ctx->sys + o_res);
+    ctx->u = (double*)(ctx->sys + o_u);
+    ctx->adj = (double*)(ctx->sys + o_adj);
+    ctx->jac_val = (double*)(ctx->sys + o_val);
+    ctx->jac_nnz = nnz;
+    ctx->nrow = nbI + nw;
+    OCPX_CUDA(cudaMemset(ctx->sys, 0, o_val));
+    OCPX_CUDA(cudaMemcpy(ctx->jac_rowptr, jrow.data(), sizeof(uint32_t) * jrow.size(), cudaMemcpyHostToDevice));
+    OCPX_CUDA(cudaMemcpy(ctx->jac_col, jcol.data(), sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice));
+    OCPX_CUDA(cudaMemcpy(ctx->jac_slot, jslot.data(), sizeof(uint32_t) * jslot.size(), cudaMemcpyHostToDevice));
+    if (ctx->ls_scratch) {  // the solver's work space is sized by the rows
+        cudaFree(ctx->ls_scratch);
+        ctx->ls_scratch = nullptr;
+    }
+    return OCPX_OK;
 }
 
 }  // namespace
@@ -364,29 +474,10 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     for (int n = 0; n < nb; n++) row_ptr[n + 1] = row_ptr[n] + deg[n];
     std::vector<uint32_t> row_conn(row_ptr[nb]);
     std::vector<uint32_t> fill(row_ptr.begin(), row_ptr.end() - 1);
-    std::vector<uint32_t> jrow(nbI + 1, 0), jcol;
-    jcol.reserve(nbI + 2 * (size_t)nconn);
     for (int c = 0; c < nconn; c++) {
         row_conn[fill[gd->conn_b[c]]++] = ((uint32_t)c << 1) | 0u;
         row_conn[fill[gd->conn_e[c]]++] = ((uint32_t)c << 1) | 1u;
     }
-    for (int n = 0; n < nbI; n++) {
-        jrow[n + 1] = jrow[n] + 1 + (row_ptr[n + 1] - row_ptr[n]);
-        jcol.push_back(n);
-        for (uint32_t k = row_ptr[n]; k < row_ptr[n + 1]; k++) {
-            const uint32_t c = row_conn[k] >> 1;
-            jcol.push_back((row_conn[k] & 1u) ? gd->conn_b[c] : gd->conn_e[c]);
-        }
-    }
-    ctx->jac_nnz = jcol.size();
-    // block index of each connection in the rows of its two cells (adjoint
-    // transpose; a ghost cell's side has none)
-    std::vector<uint32_t> jslot(2 * (size_t)(nconn > 0 ? nconn : 1), 0xffffffffu);
-    for (int n = 0; n < nbI; n++)
-        for (uint32_t k = row_ptr[n]; k < row_ptr[n + 1]; k++) {
-            const uint32_t c = row_conn[k] >> 1, side = row_conn[k] & 1u;
-            jslot[(size_t)side * nconn + c] = jrow[n] + 1 + (k - row_ptr[n]);
-        }
 
     // arena layout
     struct Slot { void** p; size_t bytes; };
@@ -419,7 +510,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     add(&cv.upblock, sizeof(uint32_t) * C * np); add(&cv.dP, sizeof(double) * C * np);
     add(&cv.flux_vj, sizeof(double) * C * np); add(&cv.flux_ni, sizeof(double) * C * nc);
     add(&cv.row_ptr, sizeof(uint32_t) * (nb + 1)); add(&cv.row_conn, sizeof(uint32_t) * (row_conn.size() + 1));
-    add(&ctx->res, D * (nc + 1)); add(&ctx->resRelV, D); add(&ctx->resRelN, D);
+    add(&ctx->resRelV, D); add(&ctx->resRelN, D);
     add(&ctx->rownorm, sizeof(RowNorm) * (size_t)nb); add(&ctx->norm_out, sizeof(RowNorm));
     add(&ctx->flags, sizeof(uint32_t) * 4);
     ctx->defer_cap = std::max(1024, nb / 4);
@@ -429,7 +520,6 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     add(&ctx->pe_res, sizeof(PERes) * (size_t)ctx->defer_cap);
     add(&ctx->pre_rec, sizeof(DeferRec) * (size_t)ctx->defer_cap); add(&ctx->pre_res, sizeof(PERes) * (size_t)ctx->defer_cap);
     add(&ctx->pre_flag, (size_t)nb); add(&ctx->adapt_level, sizeof(int) * 4);
-    add(&ctx->u, D * (nc + 1));
     // Newton / time-step control: last Newton iterate, last time step (P, T, S;
     // Ni's is b.lNi), reduction candidates, results
     add(&ctx->nr_lP, D); add(&ctx->nr_lT, D); add(&ctx->nr_lN, D * nc); add(&ctx->nr_lS, D * np);
@@ -438,10 +528,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     add(&ctx->nr_stats, sizeof(double) * 5); add(&ctx->ts_stats, sizeof(double) * 5);
     add(&ctx->nr_res0, sizeof(double)); add(&ctx->nr_state, sizeof(int)); add(&ctx->nr_dt, sizeof(double) * 2);
     add(&ctx->bmat, sizeof(double) * C * 2 * bsize);
-    add(&ctx->jac_rowptr, sizeof(uint32_t) * (nbI + 1)); add(&ctx->jac_col, sizeof(uint32_t) * jcol.size());
-    add(&ctx->jac_slot, sizeof(uint32_t) * jslot.size());
-    add(&ctx->adj, D * (nc + 1) * 2); add(&ctx->adj_conn, sizeof(double) * C);
-    add(&ctx->jac_val, sizeof(double) * jcol.size() * bsize);
+    add(&ctx->adj_conn, sizeof(double) * C);
     size_t staging = D * lend;
     staging = std::max(staging, sizeof(double) * C * nc);
     add(&ctx->staging, staging);
@@ -490,11 +577,16 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     cudaMemcpy((void*)cv.row_ptr, row_ptr.data(), sizeof(uint32_t) * (nb + 1), cudaMemcpyHostToDevice);
     if (!row_conn.empty())
         cudaMemcpy((void*)cv.row_conn, row_conn.data(), sizeof(uint32_t) * row_conn.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(ctx->jac_rowptr, jrow.data(), sizeof(uint32_t) * (nbI + 1), cudaMemcpyHostToDevice);
-    cudaMemcpy(ctx->jac_col, jcol.data(), sizeof(uint32_t) * jcol.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(ctx->jac_slot, jslot.data(), sizeof(uint32_t) * jslot.size(), cudaMemcpyHostToDevice);
+    ctx->h_row_ptr = std::move(row_ptr);
+    ctx->h_row_conn = std::move(row_conn);
+    ctx->h_conn_b.assign(gd->conn_b, gd->conn_b + nconn);
+    ctx->h_conn_e.assign(gd->conn_e, gd->conn_e + nconn);
     const cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return fail_ctx(OCPX_CUDA_ERROR, std::string("context setup: ") + cudaGetErrorString(e));
+    {
+        const ocpx_status sst = build_system(ctx, nullptr, nullptr);
+        if (sst != OCPX_OK) { const std::string m = g_err; ocpx_destroy(ctx); return fail(sst, m); }
+    }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     ctx->coop_blocks = sms * 4;
@@ -529,6 +621,9 @@ void ocpx_destroy(ocpx_ctx* ctx)
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->ls_scratch) cudaFree(ctx->ls_scratch);
     if (ctx->step_adj) cudaFree(ctx->step_adj);
+    if (ctx->sys) cudaFree(ctx->sys);
+    if (ctx->wbuf) cudaFree(ctx->wbuf);
+    if (ctx->weval) cudaFree(ctx->weval);
     if (ctx->d_model) cudaFree(ctx->d_model);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     if (ctx->h_norm) cudaFreeHost(ctx->h_norm);
@@ -581,6 +676,7 @@ ocpx_status field_transfer(ocpx_ctx* ctx, ocpx_field f, size_t first, size_t n, 
         return fail(OCPX_INVALID_ARG, "field " + std::to_string((int)f) + ": range [" + std::to_string(first) + ", " +
                                           std::to_string(first + n) + ") outside " + std::to_string(fi.n) + " entities");
     if (!n) return OCPX_OK;
+    if (to_device) ctx->state_gen++;
     const size_t bytes = n * fi.width * fi.elem;
     const cudaMemcpyKind kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
     if (fi.width == 1 || !fi.soa) {
@@ -623,6 +719,7 @@ namespace {
 ocpx_status enqueue_properties(ocpx_ctx* ctx)
 {
     cudaStream_t s = ctx->stream;
+    ctx->state_gen++;
     OCPX_CUDA(cudaMemsetAsync(ctx->flags, 0, sizeof(uint32_t) * 4, s));
     int mk = ctx->stage_begin(0);
     OCPX_CUDA(launch_check(ctx->b, ctx->flags, ctx->block_cell, s));
@@ -779,10 +876,18 @@ ocpx_status enqueue_calres(ocpx_ctx* ctx, double dt)
     OCPX_CUDA(launch_conn_flux(ctx->d_model, ctx->b, ctx->cv, ctx->block_conn, s));
     ctx->stage_end(mk);
     mk = ctx->stage_begin(5);
-    OCPX_CUDA(launch_residual(ctx->b, ctx->cv, dt, ctx->res, ctx->resRelV, ctx->resRelN, ctx->rownorm, ctx->norm_out,
-                              ctx->block_cell, s));
+    const bool wells = ctx->ws.nw > 0;
+    OCPX_CUDA(launch_residual(ctx->b, ctx->cv, dt, ctx->res, ctx->resRelV, ctx->resRelN, ctx->rownorm,
+                              wells ? nullptr : ctx->norm_out, ctx->block_cell, s));
+    if (wells) {
+        // CalResFIM of every well after the bulk rows, then the norms
+        OCPX_CUDA(launch_wells_res(ctx->b, ctx->ws, dt, ctx->res, ctx->resRelV, ctx->resRelN, ctx->rownorm, s));
+        OCPX_CUDA(launch_norm_reduce(ctx->rownorm, ctx->nbI, ctx->norm_out, s));
+        ctx->launches += 3;
+    }
     ctx->stage_end(mk);
     ctx->launches += 3;
+    ctx->res_gen = ctx->state_gen;
     return OCPX_OK;
 }
 
@@ -794,6 +899,11 @@ ocpx_status enqueue_assemble(ocpx_ctx* ctx, double dt)
     ctx->stage_end(mk);
     mk = ctx->stage_begin(7);
     OCPX_CUDA(launch_jac_rows(ctx->b, ctx->cv, ctx->bmat, ctx->jac_rowptr, ctx->jac_val, ctx->block_cell, s));
+    if (ctx->ws.nw > 0) {
+        // AssembleMatWells after AssembleMatBulks, from the terms of the last ocpx_calres
+        OCPX_CUDA(launch_wells_jac(ctx->b, ctx->ws, dt, ctx->jac_rowptr, ctx->jac_val, s));
+        ctx->launches += 2;
+    }
     ctx->stage_end(mk);
     ctx->launches += 2;
     return OCPX_OK;
@@ -858,13 +968,12 @@ ocpx_status ocpx_linsolve(ocpx_ctx* ctx, double tol, int maxit, double* u_host, 
     if (ctx->nbI < ctx->nb) return fail(OCPX_INVALID_ARG, "the device solve needs a single domain (no ghost cells)");
     const int dim = ctx->nc + 1;
     if (!ctx->ls_scratch)
-        OCPX_CUDA(cudaMalloc(&ctx->ls_scratch, sizeof(double) * linsolve_scratch_doubles(ctx->nb, dim)));
+        OCPX_CUDA(cudaMalloc(&ctx->ls_scratch, sizeof(double) * linsolve_scratch_doubles(ctx->nrow, dim)));
     LinsolveResult r{};
-    OCPX_CUDA(linsolve(ctx->jac_rowptr, ctx->jac_col, ctx->jac_val, ctx->nb, dim, ctx->res, ctx->u, ctx->ls_scratch,
-                       tol, maxit, 10, &r, &ctx->launches, ctx->stream));
+    OCPX_CUDA(linsolve(ctx->jac_rowptr, ctx->jac_col, ctx->jac_val, ctx->nrow, dim, ctx->res, ctx->u,
+                       ctx->ls_scratch, tol, maxit, 10, &r, &ctx->launches, ctx->stream));
     if (u_host) {
-        OCPX_CUDA(cudaMemcpyAsync(u_host, ctx->u, sizeof(double) * (size_t)ctx->nb * dim, cudaMemcpyDeviceToHost,
-                                  ctx->stream));
+        OCPX_CUDA(cudaMemcpyAsync(u_host, ctx->u, sizeof(double) * ctx->nv(), cudaMemcpyDeviceToHost, ctx->stream));
         OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
     }
     if (rep) *rep = ocpx_solve_report{r.iterations, r.relres, r.converged, r.breakdown};
@@ -876,20 +985,24 @@ ocpx_status ocpx_newton_update_device(ocpx_ctx* ctx, double dSmax)
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
     const int mk = ctx->stage_begin(8);
     OCPX_CUDA(launch_newton_update(ctx->b, ctx->u, dSmax, ctx->block_cell, ctx->stream));
+    OCPX_CUDA(launch_wells_update(ctx->b, ctx->ws, ctx->u, ctx->stream));
     ctx->stage_end(mk);
-    ctx->launches++;
+    ctx->launches += ctx->ws.nw > 0 ? 2 : 1;
+    ctx->state_gen++;
     return OCPX_OK;
 }
 
 ocpx_status ocpx_newton_update(ocpx_ctx* ctx, const double* u_host, double dSmax)
 {
     if (!ctx || !u_host) return fail(OCPX_INVALID_ARG, "null argument");
-    const size_t bytes = sizeof(double) * (size_t)ctx->nb * (ctx->nc + 1);
+    const size_t bytes = sizeof(double) * ctx->nv();
     OCPX_CUDA(cudaMemcpyAsync(ctx->u, u_host, bytes, cudaMemcpyHostToDevice, ctx->stream));
     const int mk = ctx->stage_begin(8);
     OCPX_CUDA(launch_newton_update(ctx->b, ctx->u, dSmax, ctx->block_cell, ctx->stream));
+    OCPX_CUDA(launch_wells_update(ctx->b, ctx->ws, ctx->u, ctx->stream));
     ctx->stage_end(mk);
-    ctx->launches++;
+    ctx->launches += ctx->ws.nw > 0 ? 2 : 1;
+    ctx->state_gen++;
     return OCPX_OK;
 }
 
@@ -901,11 +1014,15 @@ namespace {
 ocpx_status enqueue_step_adjoint(ocpx_ctx* ctx)
 {
     cudaStream_t s = ctx->stream;
-    const size_t nv = (size_t)ctx->nb * (ctx->nc + 1);
+    const size_t nv = ctx->nv();
     const double* lam = ctx->step_adj;
     const int mk = ctx->stage_begin(14);
     OCPX_CUDA(launch_jt_lambda(ctx->b, ctx->cv, ctx->jac_rowptr, ctx->jac_val, ctx->jac_slot, lam,
                                ctx->step_adj + nv, ctx->block_cell, s));
+    if (ctx->ws.nw > 0) {
+        OCPX_CUDA(launch_wells_jt(ctx->b, ctx->ws, ctx->jac_rowptr, ctx->jac_val, lam, ctx->step_adj + nv, s));
+        ctx->launches += 2;
+    }
     OCPX_CUDA(launch_vjp_poro(ctx->d_model, ctx->b, lam, ctx->step_adj + 2 * nv, ctx->block_cell, s));
     ctx->launches += 2;
     if (ctx->nconn) {
@@ -1066,7 +1183,8 @@ ocpx_status ocpx_step_max_change(ocpx_ctx* ctx, ocpx_change_max* out)
 ocpx_status ocpx_nr_check_converge(ocpx_ctx* ctx, const ocpx_nr_control* c, int* state)
 {
     if (!ctx || !c) return fail(OCPX_INVALID_ARG, "null argument");
-    OCPX_CUDA(launch_nr_converge(*c, ctx->nr_stats, ctx->norm_out, ctx->nr_res0, ctx->nr_state, ctx->stream));
+    OCPX_CUDA(launch_nr_converge(*c, ctx->nr_stats, ctx->norm_out, ctx->nr_res0,
+                                 ctx->ws.nw > 0 ? ctx->ws.maxrel : nullptr, ctx->nr_state, ctx->stream));
     ctx->launches++;
     if (state) {
         OCPX_CUDA(cudaMemcpyAsync(state, ctx->nr_state, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1090,15 +1208,13 @@ ocpx_status ocpx_next_time_step(ocpx_ctx* ctx, const ocpx_nr_control* c, double*
     return OCPX_OK;
 }
 
-ocpx_status ocpx_wells_eval(ocpx_ctx* ctx, int nwell, const ocpx_well* wells, double dt, double* res_out,
-                            double* blocks_out, double* max_rel)
+}  // extern "C"
+
+namespace {
+ocpx_status check_wells(const ocpx_ctx* ctx, int nwell, const ocpx_well* wells)
 {
-    if (!ctx || nwell < 0 || (nwell > 0 && !wells)) return fail(OCPX_INVALID_ARG, "null argument");
-    const int nb = ctx->nb, nc = ctx->nc, ncol = nc + 1;
-    const size_t bs = (size_t)ncol * ncol;
-    if (ctx->np != 3 || nc + 1 > NCT_MAX + 1) return fail(OCPX_INVALID_ARG, "wells need three phases");
-    std::vector<WellPerf> perf;
-    std::vector<double> zi((size_t)nwell * nc, 0.0), fac((size_t)nwell * nc, 0.0);
+    if (nwell < 0 || (nwell > 0 && !wells)) return fail(OCPX_INVALID_ARG, "null argument");
+    if (ctx->np != 3 || ctx->nc + 1 > NCT_MAX + 1) return fail(OCPX_INVALID_ARG, "wells need three phases");
     for (int w = 0; w < nwell; w++) {
         const ocpx_well& W = wells[w];
         if ((W.type != 0 && W.type != 1) || (W.mode != 0 && W.mode != 1) || W.nperf < 0)
@@ -1107,28 +1223,187 @@ ocpx_status ocpx_wells_eval(ocpx_ctx* ctx, int nwell, const ocpx_well* wells, do
             return fail(OCPX_INVALID_ARG, "well " + std::to_string(w) + ": missing perforation data");
         if ((W.type == 0 && !W.inj_zi) || (W.mode == 1 && (!W.factor || W.tar_rate == 0.0)))
             return fail(OCPX_INVALID_ARG, "well " + std::to_string(w) + ": missing injection or rate data");
+        for (int q = 0; q < W.nperf; q++)
+            if (W.cell[q] < 0 || W.cell[q] >= ctx->nbI)
+                return fail(OCPX_INVALID_ARG, "well " + std::to_string(w) + ": perforated cell out of range "
+                                              "(or a ghost cell)");
+    }
+    return OCPX_OK;
+}
+}  // namespace
+
+extern "C" {
+
+ocpx_status ocpx_set_wells(ocpx_ctx* ctx, int nwell, const ocpx_well* wells)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    ocpx_status st = check_wells(ctx, nwell, wells);
+    if (st != OCPX_OK) return st;
+    if (nwell > 0 && ctx->nbI < ctx->nb) return fail(OCPX_INVALID_ARG, "wells in the step need a single domain");
+    const int nc = ctx->nc, ncol = nc + 1;
+    const size_t bs = (size_t)ncol * ncol;
+    std::vector<int> cells, nperf;
+    for (int w = 0; w < nwell; w++) {
+        nperf.push_back(wells[w].nperf);
+        for (int q = 0; q < wells[w].nperf; q++) cells.push_back(wells[w].cell[q]);
+    }
+    const bool same = cells == ctx->well_cells && nperf == ctx->well_nperf && (nwell == 0) == (ctx->wbuf == nullptr);
+    if (!same) {
+        OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (ctx->wbuf) cudaFree(ctx->wbuf);
+        ctx->wbuf = nullptr;
+        ctx->ws = WellSys{};
+        ctx->well_cells = cells;
+        ctx->well_nperf = nperf;
+        // the residual, update and adjoint vectors grow by the wells' rows
+        if (ctx->step_adj) cudaFree(ctx->step_adj);
+        ctx->step_adj = nullptr;
+        ctx->adj_in_step = false;
+        st = build_system(ctx, &ctx->h_slot_bw, &ctx->h_slot_wb);
+        if (st != OCPX_OK) return st;
+        ctx->res_gen = 0;
+    }
+    if (nwell == 0) return OCPX_OK;
+    const int np_ = (int)cells.size();
+    std::vector<WellDev> wd(nwell);
+    std::vector<double> bhp(nwell), zi((size_t)nwell * nc, 0.0), fac((size_t)nwell * nc, 0.0);
+    std::vector<WellPerf> perf;
+    int p0 = 0;
+    for (int w = 0; w < nwell; w++) {
+        const ocpx_well& W = wells[w];
+        wd[w] = WellDev{W.type, W.mode, p0, p0 + W.nperf, W.tar_bhp, W.tar_rate};
+        bhp[w] = W.bhp;
         for (int i = 0; i < nc; i++) {
             if (W.inj_zi) zi[(size_t)w * nc + i] = W.inj_zi[i];
             if (W.factor) fac[(size_t)w * nc + i] = W.factor[i];
         }
-        for (int q = 0; q < W.nperf; q++) {
-            if (W.cell[q] < 0 || W.cell[q] >= ctx->nbI)
-                return fail(OCPX_INVALID_ARG, "well " + std::to_string(w) + ": perforated cell out of range "
-                                              "(or a ghost cell)");
+        for (int q = 0; q < W.nperf; q++)
             perf.push_back(WellPerf{W.cell[q], w, W.type, W.mode, W.bhp, W.WI[q], W.dG[q],
                                     W.type == 0 ? W.xi_inj[q] : 0.0});
+        p0 += W.nperf;
+    }
+    // perforations grouped by cell, each group in well then perforation order
+    std::vector<int> order(np_);
+    for (int q = 0; q < np_; q++) order[q] = q;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cells[a] < cells[b]; });
+    std::vector<int> pc_cell, pc_start;
+    for (int k = 0; k < np_; k++)
+        if (k == 0 || cells[order[k]] != cells[order[k - 1]]) {
+            pc_cell.push_back(cells[order[k]]);
+            pc_start.push_back(k);
         }
+    pc_start.push_back(np_);
+    const int npc = (int)pc_cell.size();
+    // one buffer: inputs, the bhp with its two checkpoint slots, then the
+    // per-perforation terms
+    size_t off = 0;
+    auto at = [&](size_t bytes) { const size_t o = off; off += align256(bytes ? bytes : 1); return o; };
+    const size_t o_wd = at(sizeof(WellDev) * nwell), o_bhp = at(sizeof(double) * 3 * nwell);
+    const size_t o_zi = at(sizeof(double) * zi.size()), o_fac = at(sizeof(double) * fac.size());
+    const size_t o_perf = at(sizeof(WellPerf) * np_), o_sbw = at(sizeof(uint32_t) * np_);
+    const size_t o_swb = at(sizeof(uint32_t) * np_), o_pcc = at(sizeof(int) * npc);
+    const size_t o_pcs = at(sizeof(int) * (npc + 1)), o_pcp = at(sizeof(int) * np_);
+    const size_t o_qi = at(sizeof(double) * np_ * nc), o_dqb = at(sizeof(double) * np_ * ncol);
+    const size_t o_dqw = at(sizeof(double) * np_ * nc), o_S = at(sizeof(double) * np_ * bs);
+    const size_t o_wrel = at(sizeof(double) * nwell), o_max = at(sizeof(double));
+    if (!ctx->wbuf) {
+        OCPX_CUDA(cudaMalloc(&ctx->wbuf, off));
+        OCPX_CUDA(cudaMemset(ctx->wbuf, 0, off));
+    }
+    char* B = ctx->wbuf;
+    WellSys& ws = ctx->ws;
+    ws.nw = nwell;
+    ws.nperf = np_;
+    ws.npc = npc;
+    ws.well = (const WellDev*)(B + o_wd);
+    ws.bhp = (double*)(B + o_bhp);
+    ws.zi = (const double*)(B + o_zi);
+    ws.factor = (const double*)(B + o_fac);
+    ws.perf = (const WellPerf*)(B + o_perf);
+    ws.slot_bw = (const uint32_t*)(B + o_sbw);
+    ws.slot_wb = (const uint32_t*)(B + o_swb);
+    ws.pc_cell = (const int*)(B + o_pcc);
+    ws.pc_start = (const int*)(B + o_pcs);
+    ws.pc_perf = (const int*)(B + o_pcp);
+    ws.qi = (double*)(B + o_qi);
+    ws.dqb = (double*)(B + o_dqb);
+    ws.dqw = (double*)(B + o_dqw);
+    ws.S = (double*)(B + o_S);
+    ws.wrel = (double*)(B + o_wrel);
+    ws.maxrel = (double*)(B + o_max);
+    cudaStream_t s = ctx->stream;
+    OCPX_CUDA(cudaMemcpyAsync(B + o_wd, wd.data(), sizeof(WellDev) * nwell, cudaMemcpyHostToDevice, s));
+    OCPX_CUDA(cudaMemcpyAsync(B + o_bhp, bhp.data(), sizeof(double) * nwell, cudaMemcpyHostToDevice, s));
+    OCPX_CUDA(cudaMemcpyAsync(B + o_zi, zi.data(), sizeof(double) * zi.size(), cudaMemcpyHostToDevice, s));
+    OCPX_CUDA(cudaMemcpyAsync(B + o_fac, fac.data(), sizeof(double) * fac.size(), cudaMemcpyHostToDevice, s));
+    if (np_ > 0) {
+        OCPX_CUDA(cudaMemcpyAsync(B + o_perf, perf.data(), sizeof(WellPerf) * np_, cudaMemcpyHostToDevice, s));
+        OCPX_CUDA(cudaMemcpyAsync(B + o_sbw, ctx->h_slot_bw.data(), sizeof(uint32_t) * np_, cudaMemcpyHostToDevice, s));
+        OCPX_CUDA(cudaMemcpyAsync(B + o_swb, ctx->h_slot_wb.data(), sizeof(uint32_t) * np_, cudaMemcpyHostToDevice, s));
+        OCPX_CUDA(cudaMemcpyAsync(B + o_pcc, pc_cell.data(), sizeof(int) * npc, cudaMemcpyHostToDevice, s));
+        OCPX_CUDA(cudaMemcpyAsync(B + o_pcs, pc_start.data(), sizeof(int) * (npc + 1), cudaMemcpyHostToDevice, s));
+        OCPX_CUDA(cudaMemcpyAsync(B + o_pcp, order.data(), sizeof(int) * np_, cudaMemcpyHostToDevice, s));
+    }
+    OCPX_CUDA(cudaStreamSynchronize(s));
+    ctx->state_gen++;
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_get_wells(ocpx_ctx* ctx, double* bhp, double* max_rel)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
+    if (ctx->ws.nw == 0) return fail(OCPX_INVALID_ARG, "no wells are set (ocpx_set_wells)");
+    if (bhp)
+        OCPX_CUDA(cudaMemcpyAsync(bhp, ctx->ws.bhp, sizeof(double) * ctx->ws.nw, cudaMemcpyDeviceToHost, ctx->stream));
+    if (max_rel) OCPX_CUDA(cudaMemcpyAsync(max_rel, ctx->ws.maxrel, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_wells_eval(ocpx_ctx* ctx, int nwell, const ocpx_well* wells, double dt, double* res_out,
+                            double* blocks_out, double* max_rel)
+{
+    if (!ctx) return fail(OCPX_INVALID_ARG, "null argument");
+    ocpx_status cst = check_wells(ctx, nwell, wells);
+    if (cst != OCPX_OK) return cst;
+    if (ctx->ws.nw > 0)
+        return fail(OCPX_INVALID_ARG, "the context holds wells in its step (ocpx_set_wells): their terms are "
+                                      "already in its residual and Jacobian");
+    if (res_out && ctx->res_gen != ctx->state_gen)
+        return fail(OCPX_INVALID_ARG, "the bulk residual is older than the state: call ocpx_calres first");
+    const int nb = ctx->nb, nc = ctx->nc, ncol = nc + 1;
+    const size_t bs = (size_t)ncol * ncol;
+    std::vector<WellPerf> perf;
+    std::vector<double> zi((size_t)nwell * nc, 0.0), fac((size_t)nwell * nc, 0.0);
+    for (int w = 0; w < nwell; w++) {
+        const ocpx_well& W = wells[w];
+        for (int i = 0; i < nc; i++) {
+            if (W.inj_zi) zi[(size_t)w * nc + i] = W.inj_zi[i];
+            if (W.factor) fac[(size_t)w * nc + i] = W.factor[i];
+        }
+        for (int q = 0; q < W.nperf; q++)
+            perf.push_back(WellPerf{W.cell[q], w, W.type, W.mode, W.bhp, W.WI[q], W.dG[q],
+                                    W.type == 0 ? W.xi_inj[q] : 0.0});
     }
     const int np_ = (int)perf.size();
     std::vector<double> qi((size_t)np_ * nc), dqw((size_t)np_ * nc), bb((size_t)np_ * bs), wb((size_t)np_ * bs);
     if (np_ > 0) {
-        // one allocation for the call's inputs and outputs
+        // the call's inputs and outputs in one buffer
         const size_t n_in = sizeof(WellPerf) * np_, n_z = sizeof(double) * zi.size();
         const size_t n_q = sizeof(double) * qi.size(), n_b = sizeof(double) * bb.size();
         char* buf = nullptr;
         const size_t off_z = align256(n_in), off_f = off_z + align256(n_z), off_q = off_f + align256(n_z);
         const size_t off_w = off_q + align256(n_q), off_bb = off_w + align256(n_q), off_wb = off_bb + align256(n_b);
-        OCPX_CUDA(cudaMalloc(&buf, off_wb + align256(n_b)));
+        // the context's buffer for these calls, grown when a call needs more
+        const size_t need = off_wb + align256(n_b);
+        if (ctx->weval_bytes < need) {
+            if (ctx->weval) cudaFree(ctx->weval);
+            ctx->weval = nullptr;
+            ctx->weval_bytes = 0;
+            OCPX_CUDA(cudaMalloc(&ctx->weval, need));
+            ctx->weval_bytes = need;
+        }
+        buf = ctx->weval;
         cudaStream_t s = ctx->stream;
         cudaError_t e = cudaMemcpyAsync(buf, perf.data(), n_in, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess && n_z) e = cudaMemcpyAsync(buf + off_z, zi.data(), n_z, cudaMemcpyHostToDevice, s);
@@ -1142,7 +1417,6 @@ ocpx_status ocpx_wells_eval(ocpx_ctx* ctx, int nwell, const ocpx_well* wells, do
         if (e == cudaSuccess) e = cudaMemcpyAsync(bb.data(), buf + off_bb, n_b, cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(wb.data(), buf + off_wb, n_b, cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        cudaFree(buf);
         ctx->launches++;
         if (e != cudaSuccess) return fail(OCPX_CUDA_ERROR, std::string("wells: ") + cudaGetErrorString(e));
     }
@@ -1223,10 +1497,20 @@ ocpx_status ocpx_checkpoint(ocpx_ctx* ctx, int slot, int restore)
         OCPX_CUDA(cudaMalloc(&ctx->ckpt[slot], ctx->state_bytes));
     }
     char* state = ctx->arena + ctx->state_off;
-    if (restore)
+    // the wells' bottom-hole pressures travel with the bulk state
+    // (ResetToLastTimeStep resets them too); their slots follow bhp[] in the
+    // wells' buffer
+    const size_t wb = sizeof(double) * ctx->ws.nw;
+    double* wslot = ctx->ws.nw > 0 ? ctx->ws.bhp + (size_t)(1 + slot) * ctx->ws.nw : nullptr;
+    if (restore) {
         OCPX_CUDA(cudaMemcpyAsync(state, ctx->ckpt[slot], ctx->state_bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    else
+        if (wslot) OCPX_CUDA(cudaMemcpyAsync(ctx->ws.bhp, wslot, wb, cudaMemcpyDeviceToDevice, ctx->stream));
+        ctx->state_gen++;
+    }
+    else {
         OCPX_CUDA(cudaMemcpyAsync(ctx->ckpt[slot], state, ctx->state_bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+        if (wslot) OCPX_CUDA(cudaMemcpyAsync(wslot, ctx->ws.bhp, wb, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
     return OCPX_OK;
 }
 
@@ -1240,7 +1524,7 @@ ocpx_status ocpx_synchronize(ocpx_ctx* ctx)
 ocpx_status ocpx_jacobian_dims(ocpx_ctx* ctx, size_t* nrow, size_t* nnz_blocks, int* block_dim)
 {
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
-    if (nrow) *nrow = ctx->nbI;
+    if (nrow) *nrow = ctx->nrow;
     if (nnz_blocks) *nnz_blocks = ctx->jac_nnz;
     if (block_dim) *block_dim = ctx->nc + 1;
     return OCPX_OK;
@@ -1251,7 +1535,7 @@ ocpx_status ocpx_get_jacobian(ocpx_ctx* ctx, uint32_t* rowptr, uint32_t* col, do
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
     const size_t bsize = (size_t)(ctx->nc + 1) * (ctx->nc + 1);
     if (rowptr)
-        OCPX_CUDA(cudaMemcpyAsync(rowptr, ctx->jac_rowptr, sizeof(uint32_t) * (ctx->nbI + 1), cudaMemcpyDeviceToHost,
+        OCPX_CUDA(cudaMemcpyAsync(rowptr, ctx->jac_rowptr, sizeof(uint32_t) * (ctx->nrow + 1), cudaMemcpyDeviceToHost,
                                   ctx->stream));
     if (col)
         OCPX_CUDA(cudaMemcpyAsync(col, ctx->jac_col, sizeof(uint32_t) * ctx->jac_nnz, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1265,7 +1549,7 @@ ocpx_status ocpx_get_jacobian(ocpx_ctx* ctx, uint32_t* rowptr, uint32_t* col, do
 ocpx_status ocpx_get_jacobian_rows(ocpx_ctx* ctx, size_t r0, size_t r1, uint32_t* rowptr, uint32_t* col, double* val)
 {
     if (!ctx || !rowptr) return fail(OCPX_INVALID_ARG, "null argument");
-    if (r0 > r1 || r1 > (size_t)ctx->nbI) return fail(OCPX_INVALID_ARG, "row range outside the interior rows");
+    if (r0 > r1 || r1 > (size_t)ctx->nrow) return fail(OCPX_INVALID_ARG, "row range outside the system's rows");
     const size_t bsize = (size_t)(ctx->nc + 1) * (ctx->nc + 1);
     OCPX_CUDA(cudaMemcpyAsync(rowptr, ctx->jac_rowptr + r0, sizeof(uint32_t) * (r1 - r0 + 1), cudaMemcpyDeviceToHost,
                               ctx->stream));
@@ -1412,7 +1696,7 @@ ocpx_status ocpx_adjoint(ocpx_ctx* ctx, const double* lambda, double* jt_lambda,
     if (!ctx || !lambda) return fail(OCPX_INVALID_ARG, "null argument");
     if (ctx->nbI < ctx->nb) return fail(OCPX_INVALID_ARG, "the adjoint needs a single domain (no ghost cells)");
     cudaStream_t s = ctx->stream;
-    const size_t nv = (size_t)ctx->nb * (ctx->nc + 1);
+    const size_t nv = ctx->nv();
     double* d_lam = ctx->adj;
     double* d_out = ctx->adj + nv;
     OCPX_CUDA(cudaMemcpyAsync(d_lam, lambda, sizeof(double) * nv, cudaMemcpyHostToDevice, s));
@@ -1420,6 +1704,10 @@ ocpx_status ocpx_adjoint(ocpx_ctx* ctx, const double* lambda, double* jt_lambda,
         OCPX_CUDA(launch_jt_lambda(ctx->b, ctx->cv, ctx->jac_rowptr, ctx->jac_val, ctx->jac_slot, d_lam, d_out,
                                    ctx->block_cell, s));
         ctx->launches++;
+        if (ctx->ws.nw > 0) {
+            OCPX_CUDA(launch_wells_jt(ctx->b, ctx->ws, ctx->jac_rowptr, ctx->jac_val, d_lam, d_out, s));
+            ctx->launches += 2;
+        }
         OCPX_CUDA(cudaMemcpyAsync(jt_lambda, d_out, sizeof(double) * nv, cudaMemcpyDeviceToHost, s));
     }
     if (dr_dtrans && ctx->nconn) {
@@ -1446,7 +1734,7 @@ ocpx_status ocpx_set_adjoint_seed(ocpx_ctx* ctx, const double* lambda)
         ctx->adj_in_step = false;
         return OCPX_OK;
     }
-    const size_t nv = (size_t)ctx->nb * (ctx->nc + 1);
+    const size_t nv = ctx->nv();
     if (!ctx->step_adj)
         OCPX_CUDA(cudaMalloc(&ctx->step_adj, sizeof(double) * (2 * nv + ctx->nb + (size_t)ctx->nconn)));
     OCPX_CUDA(cudaMemcpyAsync(ctx->step_adj, lambda, sizeof(double) * nv, cudaMemcpyHostToDevice, ctx->stream));
@@ -1459,7 +1747,7 @@ ocpx_status ocpx_get_adjoint(ocpx_ctx* ctx, double* jt_lambda, double* dr_dtrans
 {
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
     if (!ctx->adj_in_step) return fail(OCPX_INVALID_ARG, "no adjoint seed is set (ocpx_set_adjoint_seed)");
-    const size_t nv = (size_t)ctx->nb * (ctx->nc + 1);
+    const size_t nv = ctx->nv();
     cudaStream_t s = ctx->stream;
     if (jt_lambda)
         OCPX_CUDA(cudaMemcpyAsync(jt_lambda, ctx->step_adj + nv, sizeof(double) * nv, cudaMemcpyDeviceToHost, s));
@@ -1485,8 +1773,8 @@ ocpx_status ocpx_step(ocpx_ctx* ctx, const double* u_host, double dSmax, double 
     if ((st = ocpx_enqueue_step(ctx, dt)) != OCPX_OK) return st;
     const size_t bsize = (size_t)(ctx->nc + 1) * (ctx->nc + 1);
     if (res_host)
-        OCPX_CUDA(cudaMemcpyAsync(res_host, ctx->res, sizeof(double) * (size_t)ctx->nb * (ctx->nc + 1),
-                                  cudaMemcpyDeviceToHost, ctx->stream));
+        OCPX_CUDA(cudaMemcpyAsync(res_host, ctx->res, sizeof(double) * ctx->nv(), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
     if (jac_val_host)
         OCPX_CUDA(cudaMemcpyAsync(jac_val_host, ctx->jac_val, sizeof(double) * ctx->jac_nnz * bsize,
                                   cudaMemcpyDeviceToHost, ctx->stream));

@@ -84,7 +84,7 @@ int max_change_blocks(int nb);
 cudaError_t launch_max_change(int mode, const BulkView& b, double* lP, double* lT, double* lN, double* lS,
                               void* partial, double* out5, cudaStream_t s);
 cudaError_t launch_nr_converge(const NRControl& c, const double* nr5, const RowNorm* norm, const double* res0,
-                               int* state, cudaStream_t s);
+                               const double* wellrel, int* state, cudaStream_t s);
 cudaError_t launch_next_dt(const NRControl& c, const double* ts5, double* out2, cudaStream_t s);
 
 // one perforation of a Peaceman well (k_wells.cu)
@@ -93,10 +93,49 @@ struct WellPerf {
     double bhp, WIm, dG, xi_inj;
 };
 // per perforation: qi [nc], dQ/dP_well [nc], the cell's diagonal addition and
-// the well-to-cell block (rate control) [(nc+1)^2 each]
+// the well-to-cell block (rate control) [(nc+1)^2 each] (ocpx_wells_eval)
 cudaError_t launch_well_perf(const BulkView& b, const WellPerf* perf, int nperf, const double* inj_zi,
                              const double* factor, double dt, double* qi, double* dqw, double* bb, double* wb,
                              cudaStream_t s);
+
+// The wells inside the Newton step (k_wells.cu).  Well w's row and column are
+// nb + w; perforations are listed well by well in perforation order.
+struct WellDev {
+    int type, mode;          // 0 injector / 1 producer; 0 BHP / 1 rate control
+    int p0, p1;              // its perforations [p0, p1)
+    double tar_bhp, tar_rate;
+};
+struct WellSys {
+    int nw = 0, nperf = 0, npc = 0;
+    const WellDev* well = nullptr;
+    double* bhp = nullptr;           // [nw] bottom-hole pressures (state), then two checkpoint slots of nw
+    const double* zi = nullptr;      // [nw*nc] injected composition
+    const double* factor = nullptr;  // [nw*nc] rate factors
+    const WellPerf* perf = nullptr;  // [nperf] (bhp unused: bhp[well])
+    const uint32_t* slot_bw = nullptr;  // [nperf] bulk-to-well block index (in the perforated cell's row)
+    const uint32_t* slot_wb = nullptr;  // [nperf] well-to-bulk block index (in the well's row)
+    const int* pc_cell = nullptr;    // [npc] perforated cells
+    const int* pc_start = nullptr;   // [npc+1] their perforations in pc_perf
+    const int* pc_perf = nullptr;    // [nperf] perforation indices grouped by cell, in well then perforation order
+    double* qi = nullptr;            // [nperf*nc] mole rates
+    double* dqb = nullptr;           // [nperf*(nc+1)] dQ/dP of the perforated cell (row 0 zero)
+    double* dqw = nullptr;           // [nperf*nc] dQ/dP_well
+    double* S = nullptr;             // [nperf*(nc+1)^2] dQ/dXs * dSec_dPri
+    double* wrel = nullptr;          // [nw] |R_w / target rate|
+    double* maxrel = nullptr;        // [1] maxWellRelRes_mol
+};
+// after the bulk residual (before its norms are reduced): the perforations'
+// terms, the perforated rows and their relative residuals, the wells' rows
+cudaError_t launch_wells_res(const BulkView& b, const WellSys& w, double dt, double* res, double* resRelV,
+                             double* resRelN, RowNorm* rn, cudaStream_t s);
+// after the bulk Jacobian rows: perforated rows' additions, the wells' rows
+cudaError_t launch_wells_jac(const BulkView& b, const WellSys& w, double dt, const uint32_t* rowptr, double* val,
+                             cudaStream_t s);
+// GetSolutionFIM of every well
+cudaError_t launch_wells_update(const BulkView& b, const WellSys& w, const double* u, cudaStream_t s);
+// J^T lambda: the wells' blocks added to the perforated cells' entries, and the wells' entries
+cudaError_t launch_wells_jt(const BulkView& b, const WellSys& w, const uint32_t* rowptr, const double* val,
+                            const double* lam, double* out, cudaStream_t s);
 
 // Linear solve of J u = rhs on the device (k_linsolve.cu): BiCGStab with right
 // block-Jacobi preconditioning, x from zero; scratch holds
@@ -120,6 +159,9 @@ cudaError_t launch_newton_update(const BulkView& b, const double* u, double dSma
 cudaError_t launch_conn_flux(const Model* dm, const BulkView& b, const ConnView& cv, int block, cudaStream_t s);
 cudaError_t launch_residual(const BulkView& b, const ConnView& cv, double dt, double* res, double* resRelV,
                             double* resRelN, RowNorm* rn, RowNorm* rn_out, int block, cudaStream_t s);
+// the norm reduction of launch_residual alone (launch_residual with rn_out NULL
+// leaves it out, so that the wells' rows can be added first)
+cudaError_t launch_norm_reduce(const RowNorm* rn, int nbI, RowNorm* rn_out, cudaStream_t s);
 cudaError_t launch_jac_conn(int nct, const Model* dm, const BulkView& b, const ConnView& cv, double dt,
                             double* bmat, int block, cudaStream_t s);
 cudaError_t launch_jac_rows(const BulkView& b, const ConnView& cv, const double* bmat, const uint32_t* rowptr,

@@ -138,7 +138,7 @@ EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy",
            "ocpx_nr_init_step", "ocpx_nr_max_change", "ocpx_step_max_change", "ocpx_nr_check_converge",
            "ocpx_next_time_step", "ocpx_linsolve", "ocpx_newton_update_device", "ocpx_wells_eval",
            "ocpx_set_field_range", "ocpx_get_field_range", "ocpx_set_adjoint_seed", "ocpx_get_adjoint",
-           "ocpx_get_jacobian_rows"]
+           "ocpx_get_jacobian_rows", "ocpx_set_wells", "ocpx_get_wells"]
 
 PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3, "predefer": 4, "coop_cells": 5,
           "predeferred": 6, "level": 7, "pre_blocks": 8,
@@ -197,6 +197,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.ocpx_set_adjoint_seed.argtypes = [P, P]
     lib.ocpx_get_adjoint.argtypes = [P, P, P, P]
     lib.ocpx_get_jacobian_rows.argtypes = [P, C.c_size_t, C.c_size_t, P, P, P]
+    lib.ocpx_set_wells.argtypes = [P, C.c_int, C.POINTER(Well)]
+    lib.ocpx_get_wells.argtypes = [P, P, P]
     for fn in ("ocpx_enqueue_step", "ocpx_step_report", "ocpx_profile_enable", "ocpx_profile_read",
                "ocpx_measure_fp64_tflops", "ocpx_checkpoint", "ocpx_set_param", "ocpx_get_param"):
         getattr(lib, fn).restype = C.c_int
@@ -348,6 +350,7 @@ class FimContext:
         self.grid = grid
         self.nb = grid.nb
         self.nbI = grid.nb_interior or grid.nb
+        self.nwell = 0
         self.np = 3
         self.nc = model.nc
         self.nconn = grid.nconn
@@ -390,6 +393,8 @@ class FimContext:
         cw = {"UPBLOCK": np_, "CONN_DP": np_, "FLUX_VJ": np_, "FLUX_NI": nc, "TRANS": 1}
         if name in cw:
             return nconn * cw[name]
+        if name == "RES":
+            return (nb + self.nwell) * (nc + 1)
         return nb * w[name]
 
     def set(self, name: str, values):
@@ -405,6 +410,8 @@ class FimContext:
 
     def field_width(self, name: str) -> int:
         n = self.nconn if name in ("UPBLOCK", "CONN_DP", "FLUX_VJ", "FLUX_NI", "TRANS") else self.nb
+        if name == "RES":
+            n += self.nwell
         return self.field_size(name) // max(n, 1)
 
     def get_range(self, name: str, first: int, n: int) -> np.ndarray:
@@ -429,15 +436,14 @@ class FimContext:
             _check(self.lib.ocpx_set_adjoint_seed(self.h, None))
             return
         self._adj_seed = np.ascontiguousarray(np.asarray(lam, np.float64).ravel())
-        if self._adj_seed.size != self.nb * (self.nc + 1):
-            raise ValueError("lambda must have nb*(nc+1) entries")
+        if self._adj_seed.size != self.nv:
+            raise ValueError(f"lambda must have {self.nv} entries")
         _check(self.lib.ocpx_set_adjoint_seed(self.h, self._adj_seed.ctypes.data_as(C.c_void_p)))
 
     def get_adjoint(self, out=None):
         """(J^T lam, (dR/dT)^T lam, (dR/dporoInit)^T lam) of the last step,
         into the arrays `out` when given."""
-        jt, tr, po = out if out is not None else (np.empty(self.nb * (self.nc + 1)), np.empty(self.nconn),
-                                                  np.empty(self.nb))
+        jt, tr, po = out if out is not None else (np.empty(self.nv), np.empty(self.nconn), np.empty(self.nb))
         _check(self.lib.ocpx_get_adjoint(self.h, jt.ctypes.data_as(C.c_void_p), tr.ctypes.data_as(C.c_void_p),
                                          po.ctypes.data_as(C.c_void_p)))
         return jt, tr, po
@@ -471,8 +477,20 @@ class FimContext:
         _check(self.lib.ocpx_assemble(self.h, float(dt)))
         _check(self.lib.ocpx_synchronize(self.h))
 
+    @property
+    def nv(self) -> int:
+        """Entries of the residual, Newton update and adjoint vectors: nc + 1
+        per cell and per well."""
+        return (self.nb + self.nwell) * (self.nc + 1)
+
     def get_solution(self, u, dSmax: float):
-        a = np.ascontiguousarray(np.asarray(u, dtype=np.float64)[: self.nb * (self.nc + 1)])
+        """GetSolution with a host Newton update u: nv entries, or nb*(nc+1)
+        (the wells' bhp then unchanged)."""
+        a = np.ascontiguousarray(np.asarray(u, dtype=np.float64).ravel())
+        if a.size == self.nb * (self.nc + 1) and self.nwell:
+            a = np.concatenate([a, np.zeros(self.nwell * (self.nc + 1))])
+        if a.size != self.nv:
+            raise ValueError(f"u must have {self.nv} entries")
         _check(self.lib.ocpx_newton_update(self.h, a.ctypes.data_as(C.c_void_p), float(dSmax)))
         _check(self.lib.ocpx_synchronize(self.h))
 
@@ -525,8 +543,8 @@ class FimContext:
         state: (J^T lam, (dR/dT)^T lam, (dR/dporoInit)^T lam); None for the ones
         not requested."""
         lam = np.ascontiguousarray(np.asarray(lam, np.float64).ravel())
-        if lam.size != self.nb * (self.nc + 1):
-            raise ValueError("lambda must have nb*(nc+1) entries")
+        if lam.size != self.nv:
+            raise ValueError(f"lambda must have {self.nv} entries")
         out_jt = np.empty(lam.size) if jt else None
         out_t = np.empty(self.nconn) if trans else None
         out_p = np.empty(self.nb) if poro else None
@@ -539,7 +557,7 @@ class FimContext:
         """BiCGStab with block-Jacobi preconditioning of J u = rhs (the last
         assembled Jacobian and residual); returns (u or None, report dict)."""
         rep = SolveReport()
-        u = np.empty(self.nb * (self.nc + 1)) if copy_out else None
+        u = np.empty(self.nv) if copy_out else None
         _check(self.lib.ocpx_linsolve(self.h, float(tol), int(maxit),
                                       None if u is None else u.ctypes.data_as(C.c_void_p), C.byref(rep)))
         return u, {k: getattr(rep, k) for k, _ in rep._fields_}
@@ -583,14 +601,8 @@ class FimContext:
         _check(self.lib.ocpx_next_time_step(self.h, C.byref(ctrl), C.byref(dt), C.byref(pdt)))
         return dt.value, pdt.value
 
-    def wells_eval(self, wells: list, dt: float):
-        """The wells' part of the residual and Jacobian (ocpx_wells_eval).
-        wells: dicts with type, mode, bhp, tar_bhp, tar_rate, cell, WI (times
-        the multiplier), dG, xi_inj, inj_zi, factor.  Returns the residual
-        with the wells ((nb + nwell) * (nc + 1)), the blocks as
-        [nperf][3][nc+1][nc+1] (cell diagonal addition, cell-to-well,
-        well-to-cell) and [nwell][nc+1][nc+1] (well diagonals), and
-        maxWellRelRes_mol."""
+    def _wells_array(self, wells: list):
+        """ocpx_well records of well dicts (and the arrays they point to)."""
         keep, arr = [], (Well * max(len(wells), 1))()
         for k, w in enumerate(wells):
             def dptr(key, n):
@@ -608,21 +620,46 @@ class FimContext:
                           float(w.get("tar_rate", 0.0)), n, cell.ctypes.data_as(C.POINTER(C.c_int)),
                           dptr("WI", n), dptr("dG", n), dptr("xi_inj", n), dptr("inj_zi", self.nc),
                           dptr("factor", self.nc))
+        return arr, keep
+
+    def set_wells(self, wells: list):
+        """Wells inside the Newton step (ocpx_set_wells): dicts with type,
+        mode, bhp, tar_bhp, tar_rate, cell, WI (times the multiplier), dG,
+        xi_inj, inj_zi, factor; [] removes them."""
+        arr, keep = self._wells_array(wells)
+        _check(self.lib.ocpx_set_wells(self.h, len(wells), arr))
+        self.nwell = len(wells)
+
+    def get_wells(self):
+        """(bhp of each well, maxWellRelRes_mol of the last cal_res)."""
+        bhp, mrel = np.empty(max(self.nwell, 1)), C.c_double()
+        _check(self.lib.ocpx_get_wells(self.h, bhp.ctypes.data_as(C.c_void_p), C.byref(mrel)))
+        return bhp[:self.nwell], mrel.value
+
+    def wells_eval(self, wells: list, dt: float, residual: bool = True):
+        """The wells' part of the residual and Jacobian (ocpx_wells_eval), for
+        a host that keeps its own well code.  wells: dicts as for set_wells.
+        Returns the residual with the wells ((nb + nwell) * (nc + 1); None
+        without `residual`), the blocks as [nperf][3][nc+1][nc+1] (cell
+        diagonal addition, cell-to-well, well-to-cell) and [nwell][nc+1][nc+1]
+        (well diagonals), and maxWellRelRes_mol."""
+        arr, keep = self._wells_array(wells)
         ncol = self.nc + 1
         nperf = sum(len(np.ravel(w["cell"])) for w in wells)
         res = np.empty((self.nb + len(wells)) * ncol)
         blocks = np.empty((3 * nperf + len(wells)) * ncol * ncol)
         mrel = C.c_double()
-        _check(self.lib.ocpx_wells_eval(self.h, len(wells), arr, dt, res.ctypes.data_as(C.c_void_p),
+        _check(self.lib.ocpx_wells_eval(self.h, len(wells), arr, dt,
+                                        res.ctypes.data_as(C.c_void_p) if residual else None,
                                         blocks.ctypes.data_as(C.c_void_p), C.byref(mrel)))
         pb = blocks[:3 * nperf * ncol * ncol].reshape(nperf, 3, ncol, ncol)
         wd = blocks[3 * nperf * ncol * ncol:].reshape(len(wells), ncol, ncol)
-        return res, pb, wd, mrel.value
+        return (res if residual else None), pb, wd, mrel.value
 
     def jacobian(self):
         nrow, nnz, bd = C.c_size_t(), C.c_size_t(), C.c_int()
         _check(self.lib.ocpx_jacobian_dims(self.h, C.byref(nrow), C.byref(nnz), C.byref(bd)))
-        rp = np.empty(nrow.value + 1, np.uint32)   # interior rows
+        rp = np.empty(nrow.value + 1, np.uint32)   # interior cells' rows, then the wells'
         col = np.empty(nnz.value, np.uint32)
         val = np.empty(nnz.value * bd.value * bd.value, np.float64)
         _check(self.lib.ocpx_get_jacobian(self.h, rp.ctypes.data_as(C.c_void_p), col.ctypes.data_as(C.c_void_p),

@@ -432,8 +432,8 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     if (gd->nb_interior < 0 || gd->nb_interior > gd->nb)
         return fail(OCPX_INVALID_ARG, "nb_interior must lie in [0, nb]");
     const uint32_t nbI_ = gd->nb_interior > 0 ? (uint32_t)gd->nb_interior : (uint32_t)gd->nb;
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(OCPX_NO_DEVICE, "no CUDA device");
+    // the descriptions are checked before the device, so a host without one
+    // can still validate them (OCPX_INVALID_ARG before OCPX_NO_DEVICE)
     for (int c = 0; c < gd->nconn; c++) {
         if (gd->conn_b[c] >= (uint32_t)gd->nb || gd->conn_e[c] >= (uint32_t)gd->nb || gd->conn_b[c] == gd->conn_e[c])
             return fail(OCPX_INVALID_ARG, "connection endpoint out of range at " + std::to_string(c));
@@ -445,6 +445,9 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     std::string merr;
     ocpx_status st = build_model(md, ctx->host_model, merr);
     if (st != OCPX_OK) { delete ctx; return fail(st, merr); }
+    if (md->mixture == 1 && cap_ncm(md->nc - 1) < 0) { delete ctx; return fail(OCPX_INVALID_ARG, "too many components"); }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { delete ctx; return fail(OCPX_NO_DEVICE, "no CUDA device"); }
     if (device >= 0) {
         if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return fail(OCPX_NO_DEVICE, "cudaSetDevice failed"); }
         ctx->device = device;

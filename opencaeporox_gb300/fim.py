@@ -484,12 +484,19 @@ class FimContext:
         return (self.nb + self.nwell) * (self.nc + 1)
 
     def get_solution(self, u, dSmax: float):
-        """GetSolution with a host Newton update u: nv entries, or nb*(nc+1)
-        (the wells' bhp then unchanged)."""
+        """GetSolution with a host Newton update u: its cells' entries, then
+        the wells' rows when the context holds wells (nb*(nc+1) entries alone
+        leave the wells' bhp unchanged).  Without wells on the context, rows
+        past the cells (a host's own wells) are ignored."""
         a = np.ascontiguousarray(np.asarray(u, dtype=np.float64).ravel())
-        if a.size == self.nb * (self.nc + 1) and self.nwell:
+        ncell = self.nb * (self.nc + 1)
+        if a.size < ncell:
+            raise ValueError(f"u must have at least {ncell} entries")
+        if self.nwell == 0:
+            a = a[:ncell]
+        elif a.size == ncell:
             a = np.concatenate([a, np.zeros(self.nwell * (self.nc + 1))])
-        if a.size != self.nv:
+        elif a.size != self.nv:
             raise ValueError(f"u must have {self.nv} entries")
         _check(self.lib.ocpx_newton_update(self.h, a.ctypes.data_as(C.c_void_p), float(dSmax)))
         _check(self.lib.ocpx_synchronize(self.h))

@@ -59,6 +59,17 @@ def build_reference_if_present() -> str | None:
     return os.path.join(HERE, "_ref", "ocp_ref_dump")
 
 
+def build_binding() -> str:
+    """The reference-side binding of the GPU library compiled against the
+    reference's headers (oracle/ref/Makefile, target gpu_binding); needs the
+    library built and the reference's sources."""
+    r = subprocess.run(["make", "-C", os.path.join(HERE, "ref"), "-j8", "gpu_binding", f"REF={REF}"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("binding build failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
+    return os.path.join(HERE, "_ref", "ocp_gpu_binding")
+
+
 if __name__ == "__main__":
     print(build(force=True))
     print(build_reference_if_present())

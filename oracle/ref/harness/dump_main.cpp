@@ -19,6 +19,7 @@
 #include "OCP.hpp"
 #include "PreProcess.hpp"
 #include "npy.hpp"
+#include "ptn_moles.hpp"
 
 #include <chrono>
 #include <sys/stat.h>
@@ -382,31 +383,6 @@ OCP_BOOL update_property(IsoT_FIM& fim, Reservoir& rs, OCPControl& ctrl, const s
     put(dir, "flash_ftype", ftype);
     put(dir, "flash_iters", iters);
     return OCP_TRUE;
-}
-
-// The reference's grid distributor refuses more than 30 per-cell input arrays
-// (src/Reservoir.cpp:38-66), so a PTN start with more than four hydrocarbon
-// components cannot carry its COMPM-* arrays through the deck.  Decks written
-// for this harness therefore leave COMPM-* out and place the per-cell moles
-// (cell-major, hydrocarbons then water) in "<deck>.ptn_ni"; they are copied
-// into the bulk initializer exactly where the deck reader would have put them.
-void inject_ptn_moles(Reservoir& rs, const string& deck)
-{
-    const string path = deck + ".ptn_ni";
-    FILE* f = std::fopen(path.c_str(), "rb");
-    if (!f) return;
-    const OCP_USI nb = rs.bulk.vs.nb;
-    const USI     nc = rs.bulk.vs.nc;
-    vector<double> buf(static_cast<size_t>(nb) * nc);
-    if (std::fread(buf.data(), sizeof(double), buf.size(), f) != buf.size()) {
-        std::cerr << "short ptn_ni file\n";
-        std::exit(6);
-    }
-    std::fclose(f);
-    auto& Ni = rs.bulk.INITm.GetNi();
-    Ni.assign(nc, vector<OCP_DBL>(nb));
-    for (OCP_USI n = 0; n < nb; n++)
-        for (USI i = 0; i < nc; i++) Ni[i][n] = buf[static_cast<size_t>(n) * nc + i];
 }
 
 // IsothermalSolver::FinishNR for a FIM-only run (src/IsoThermalSolver.cpp:220-250

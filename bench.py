@@ -437,6 +437,30 @@ def flash_errors(got, ref, pe, nc):
     return out
 
 
+def cell_errors(got, ref, pe, nc):
+    """Per cell, the largest relative error over its flash outputs (floor
+    1e-12 x each array's scale; phase quantities where the phase exists; the
+    derivative-solve outputs normwise)."""
+    n = pe.shape[0]
+    out = np.zeros(n)
+    for k in FLASH_KEYS:
+        a = np.asarray(got[k], np.float64).reshape(n, -1)
+        b = np.asarray(ref[k], np.float64).reshape(n, -1)
+        if k in CELLWISE_KEYS:
+            e = np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+        else:
+            if k in PHASE_KEYS:
+                m = pe
+            elif k in PHASE_COMP_KEYS:
+                m = np.repeat(pe, nc, axis=1)
+            else:
+                m = np.ones_like(a, bool)
+            floor = max(np.max(np.abs(b[m])) * 1e-12, 1e-300) if np.any(m) else 1e-300
+            e = np.max(np.where(m, np.abs(a - b) / np.maximum(np.abs(b), floor), 0.0), axis=1)
+        out = np.maximum(out, e)
+    return out
+
+
 def parity(ctx, wl, model, grid):
     """The timed step (the replayed graph) against the oracle from the same
     inputs on a window: owned cells with their ghost cells.  Upwind choices
@@ -498,6 +522,14 @@ def parity(ctx, wl, model, grid):
         for k, v in flash_errors({k: nz[k][keep] for k in FLASH_KEYS}, ref, pe_o[keep], nc).items():
             sens[k] = max(sens.get(k, 0.0), v)
     tol = {k: max(REL_TOL, LIBM_FACTOR * sens.get(k, 0.0)) for k in FLASH_KEYS}
+    # per cell: the GPU's error against the oracle's own one-ulp sensitivity
+    got_k = {k: np.asarray(got[k]).reshape(no, -1)[keep] for k in FLASH_KEYS}
+    e_cell = cell_errors(got_k, ref, pe_o[keep], nc)
+    s_cell = np.zeros_like(e_cell)
+    for nz in nudged:
+        s_cell = np.maximum(s_cell, cell_errors({k: nz[k][keep] for k in FLASH_KEYS}, ref, pe_o[keep], nc))
+    above = e_cell > REL_TOL
+    unexplained_cells = int(np.sum(e_cell > np.maximum(REL_TOL, LIBM_FACTOR * s_cell)))
     # residual and Jacobian of the oracle from the GPU's post-flash state
     post = {f: get_cells(ctx, f, cells) for f in ORACLE_FIELDS}
     oc = OracleBulk(model, sub_grid)
@@ -530,7 +562,7 @@ def parity(ctx, wl, model, grid):
             row += 1
     flash_ok = all(errs[k] <= tol[k] for k in errs)
     ok = (unexplained == 0 and up_mismatch == 0 and pattern_mismatch == 0 and flash_ok and res_err <= REL_TOL
-          and jac_err <= REL_TOL)
+          and jac_err <= REL_TOL and unexplained_cells == 0)
     return {"window": f"{no:,} owned cells with {ghost.size:,} ghost cells, {conns.size:,} connections",
             "against": "oracle (CPU restatement pinned to the reference) from the timed step's own inputs",
             "label_mismatch_cells": label_mismatch,
@@ -541,6 +573,9 @@ def parity(ctx, wl, model, grid):
             "residual_and_jacobian_rows_compared": int(plain_rows.sum()),
             "perforated_rows_left_out": int((~plain_rows).sum()),
             "jacobian_pattern_mismatch_rows": pattern_mismatch,
+            "flash_cells_above_1e-10": int(above.sum()),
+            "flash_cells_above_1e-10_within_4x_their_libm_sensitivity": int(np.sum(above & (e_cell <= LIBM_FACTOR * s_cell))),
+            "flash_cells_unexplained": unexplained_cells,
             "flash_max_rel_err": {k: float(f"{v:.3g}") for k, v in errs.items()},
             "flash_tolerance": {k: float(f"{v:.3g}") for k, v in tol.items()},
             "residual_max_rel_err": res_err, "jacobian_max_rowwise_rel_err": jac_err, "tolerance": REL_TOL,

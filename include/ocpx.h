@@ -201,6 +201,29 @@ typedef struct ocpx_norms {
 
 /* Context. device < 0 selects the current device. */
 ocpx_status ocpx_create(const ocpx_model_desc* model, const ocpx_grid_desc* grid, int device, ocpx_ctx** out);
+
+/* Options of ocpx_create_ex; struct_size = sizeof(ocpx_options), the other
+ * fields zero for the defaults (ocpx_create's).
+ *   recompute_flash_der  1: dSec_dPri (OCPMixtureMethodComp::CaldXsdXp02,
+ *                        src/OCPMixtureMethodComp.cpp:565-642, np*(nc+1)^2
+ *                        values per cell: 2,904 bytes at nc = 10) is not
+ *                        stored.  The flash keeps the two hydrocarbon
+ *                        phases' mole numbers instead (16 bytes per cell),
+ *                        and the Jacobian's connection blocks, GetSolution
+ *                        and the wells' perforation terms recompute it from
+ *                        the state the flash left (P, T, Ni, phase labels,
+ *                        x_ij) with the flash's own statements, so every
+ *                        result is bit-identical to the stored form's.  The
+ *                        compositional mixture only.  OCPX_F_DSEC_DPRI can
+ *                        still be read (recomputed on the fly: the flash's
+ *                        values until P, T or Ni change) but not written. */
+typedef struct ocpx_options {
+    size_t struct_size;
+    int recompute_flash_der;
+    int reserved[7];
+} ocpx_options;
+ocpx_status ocpx_create_ex(const ocpx_model_desc* model, const ocpx_grid_desc* grid, int device,
+                           const ocpx_options* options, ocpx_ctx** out);
 void ocpx_destroy(ocpx_ctx* ctx);
 const char* ocpx_last_error(void);
 int ocpx_abi_version(void);
@@ -311,7 +334,12 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *                 kernel 10.4 ms against 11.2 ms);
  *   POST_BLOCK    threads per block of the kernel that finishes the deferred
  *                 cells from their equilibrium (32, 64, 96 or 128; default
- *                 32: one warp per SM keeps its frames in L1). */
+ *                 32: one warp per SM keeps its frames in L1);
+ *   RECOMPUTE_FLASH_DER  (read only) 1 when the context was created with
+ *                 ocpx_options.recompute_flash_der;
+ *   DEVICE_BYTES  (read only) device memory the context holds: its arena,
+ *                 the linear system, the wells, the solver's and the
+ *                 adjoint's work space and the checkpoints. */
 typedef enum ocpx_param {
     OCPX_PARAM_FLASH_BUDGET = 0,
     OCPX_PARAM_COOP_BLOCKS = 1,
@@ -329,7 +357,9 @@ typedef enum ocpx_param {
     OCPX_PARAM_SMS = 13,
     OCPX_PARAM_FUSED_COOP_BLOCKS = 14,
     OCPX_PARAM_FUSED_EXCL = 15,
-    OCPX_PARAM_POST_BLOCK = 16
+    OCPX_PARAM_POST_BLOCK = 16,
+    OCPX_PARAM_RECOMPUTE_FLASH_DER = 17,
+    OCPX_PARAM_DEVICE_BYTES = 18
 } ocpx_param;
 ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value);
 ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value);

@@ -47,7 +47,10 @@ struct BulkView {
     double* kr;        // [np][nb]
     double* dKrdS;     // [np*np][nb]
     double* dPcdS;     // [np*np][nb]
-    double* dSec_dPri; // [np*(nc+1) * (nc+1)][nb], row-major rows (S_j, x_ij) x cols (P, N_k)
+    double* dSec_dPri; // [np*(nc+1) * (nc+1)][nb], row-major rows (S_j, x_ij) x cols (P, N_k);
+                       // NULL when the flash derivatives are recomputed where they are used
+    double* njhc;      // [2][nb] mole numbers of the hydrocarbon phases (label order, 0 if absent)
+                       // kept by the flash for that recomputation; NULL otherwise
     double* poro;
     double* poroP;
     double* rockVp;

@@ -356,7 +356,10 @@ OCPX_HD void krpc_rock_cell(const Model& M, const BulkView& b, int cell)
 // IsoT_FIM::GetSolution (src/IsoThermalMethod.cpp:1282-1418), one cell:
 // secondary update dtmp = dSec_dPri * u with the saturation chop, then S,
 // x_ij, P (unchopped) and Ni (chopped).  u holds (dP, dN_0..dN_nc-1) per cell.
-OCPX_HD void newton_update_cell(const BulkView& b, int cell, const double* u, double dSmax)
+// The cell's dSec_dPri is at ds[(row * (nc + 1) + col) * stride]: the stored
+// SoA rows, or a copy recomputed before the update.
+OCPX_HD void newton_update_cell(const BulkView& b, int cell, const double* u, double dSmax, const double* ds,
+                                size_t stride)
 {
     const int np = b.np, nc = b.nc, col = nc + 1, row = np * (nc + 1);
     double uc[NCT_MAX + 1];
@@ -365,7 +368,7 @@ OCPX_HD void newton_update_cell(const BulkView& b, int cell, const double* u, do
     double dS[NP];
     for (int j = 0; j < np; j++) {
         double dtmp = 0;
-        for (int k = 0; k < col; k++) dtmp += 1.0 * b.dSec_dPri[b.idx(j * col + k, cell)] * uc[k];
+        for (int k = 0; k < col; k++) dtmp += 1.0 * ds[(size_t)(j * col + k) * stride] * uc[k];
         dS[j] = dtmp;
         double choptmp = 1;
         const double Sj = b.S[b.idx(j, cell)];
@@ -376,11 +379,15 @@ OCPX_HD void newton_update_cell(const BulkView& b, int cell, const double* u, do
     for (int j = 0; j < np; j++) b.S[b.idx(j, cell)] += chopmin * dS[j];
     for (int r = np; r < row; r++) {
         double dtmp = 0;
-        for (int k = 0; k < col; k++) dtmp += 1.0 * b.dSec_dPri[b.idx(r * col + k, cell)] * uc[k];
+        for (int k = 0; k < col; k++) dtmp += 1.0 * ds[(size_t)(r * col + k) * stride] * uc[k];
         b.xij[b.idx(r - np, cell)] += chopmin * dtmp;
     }
     b.P[cell] += uc[0];
     for (int i = 0; i < nc; i++) b.Ni[b.idx(i, cell)] += chopmin * uc[1 + i];
+}
+OCPX_HD void newton_update_cell(const BulkView& b, int cell, const double* u, double dSmax)
+{
+    newton_update_cell(b, cell, u, dSmax, b.dSec_dPri + cell, (size_t)b.nb);
 }
 
 // Bulk::CheckNi (src/Bulk.cpp:178-213) and Bulk::CheckP (:116-131) for one

@@ -135,129 +135,150 @@ OCPX_HD void cell_residual(const BulkView& b, const ConnView& cv, int n, double 
 // the reference's operations.  In the compositional model the rows of
 // dSec_dPri for the water phase's composition are identically zero (the
 // water composition is fixed, CaldXsdXpW), so they are skipped.
+// the per-phase quantities of a connection that both sides' blocks use
+struct ConnPhase {
+    int bId, eId, jcomp_end;
+    double Akd, dGamma;
+    int up[NP];
+    bool act[NP];
+    double transJ[NP], xiU[NP], dPj[NP], muU[NP], wU[NP], wD[NP], muP[NP], xiP[NP], rhoPu[NP], rhoPd[NP];
+};
+
+OCPX_HD void conn_phase(const Model& M, const BulkView& b, const ConnView& cv, int c, ConnPhase& q)
+{
+    const int np = b.np, nconn = cv.nconn;
+    q.bId = (int)cv.bId[c];
+    q.eId = (int)cv.eId[c];
+    const int bId = q.bId, eId = q.eId;
+    q.Akd = cv.trans[c];
+    q.dGamma = M.units.gravity_factor * (b.depth[bId] - b.depth[eId]);
+    q.jcomp_end = (M.mixture == 1) ? np - 1 : np;  // phases whose composition rows of dSec are nonzero
+#pragma unroll
+    for (int j = 0; j < NP; j++) {
+        const int u = j < np ? (int)cv.upblock[j * nconn + c] : bId;
+        q.up[j] = u;
+        q.act[j] = j < np && b.phaseExist[b.idx(j, u)] != 0;
+        q.transJ[j] = 0; q.xiU[j] = 0; q.dPj[j] = 0; q.muU[j] = 1; q.wU[j] = 0; q.wD[j] = 0;
+        q.muP[j] = 0; q.xiP[j] = 0; q.rhoPu[j] = 0; q.rhoPd[j] = 0;
+        if (!q.act[j]) continue;
+        const int d = (u == bId) ? eId : bId;
+        const bool exD = b.phaseExist[b.idx(j, d)] != 0;
+        q.wU[j] = exD ? 0.5 : 1;
+        q.wD[j] = exD ? 0.5 : 0;
+        q.dPj[j] = cv.dP[j * nconn + c];
+        q.xiU[j] = b.xi[b.idx(j, u)];
+        q.muU[j] = b.mu[b.idx(j, u)];
+        q.transJ[j] = q.Akd * b.kr[b.idx(j, u)] / q.muU[j];
+        q.muP[j] = b.muP[b.idx(j, u)];
+        q.xiP[j] = b.xiP[b.idx(j, u)];
+        q.rhoPu[j] = b.rhoP[b.idx(j, u)];
+        q.rhoPd[j] = b.rhoP[b.idx(j, d)];
+    }
+}
+
+// The block of one side (0: bId, 1: eId) of a connection, with the side
+// cell's dSec_dPri at ds[(k * ncol + col) * stride] (the stored SoA rows, or
+// a recomputed copy).
+template <int NCT>
+OCPX_HD void conn_jac_side(const BulkView& b, const ConnPhase& q, int side, const double* ds, size_t stride,
+                           double dt, double* out)
+{
+    const int np = b.np, nc = b.nc;
+    const int ncol = nc + 1;
+    constexpr int NCOL = NCT + 1;
+    const int cell = side == 0 ? q.bId : q.eId;
+    const double sgn = side == 0 ? 1.0 : -1.0;
+    const double Akd = q.Akd, dGamma = q.dGamma;
+    const int jcomp_end = q.jcomp_end;
+    double W[NP][NCOL];
+#pragma unroll
+    for (int j = 0; j < NP; j++) {
+#pragma unroll
+        for (int col = 0; col < NCOL; col++) W[j][col] = 0;
+        if (!q.act[j]) continue;
+        const int u = q.up[j];
+        const bool isU = (u == cell);
+        const double xt = q.xiU[j] * q.transJ[j];
+        // saturation columns: sgn*xi*transJ*dPcdS(side cell) [+ Akd*dKrdS(U)/mu*xi*dP on the upwind side]
+        for (int k = 0; k < np; k++) {
+            double a = sgn * xt * b.dPcdS[b.idx(j * np + k, cell)];
+            if (isU) a += Akd * b.dKrdS[b.idx(j * np + k, u)] / q.muU[j] * q.xiU[j] * q.dPj[j];
+#pragma unroll
+            for (int col = 0; col < NCOL; col++)
+                if (col < ncol) W[j][col] = fma(a, ds[(size_t)(k * ncol + col) * stride], W[j][col]);
+        }
+        if (j >= jcomp_end) continue;
+        // composition columns of phase j
+        for (int m = 0; m < nc; m++) {
+            double g;
+            if (isU) {
+                const double rhox = b.rhox[b.idx(j * nc + m, u)];
+                const double xix = b.xix[b.idx(j * nc + m, u)];
+                const double mux = b.mux[b.idx(j * nc + m, u)];
+                g = -xt * q.wU[j] * rhox * dGamma;
+                g += q.transJ[j] * xix * q.dPj[j];
+                g += -xt * mux / q.muU[j] * q.dPj[j];
+            }
+            else {
+                if (q.wD[j] == 0) continue;
+                g = -xt * q.wD[j] * b.rhox[b.idx(j * nc + m, cell)] * dGamma;
+            }
+            const int k = np + j * nc + m;
+#pragma unroll
+            for (int col = 0; col < NCOL; col++)
+                if (col < ncol) W[j][col] = fma(g, ds[(size_t)(k * ncol + col) * stride], W[j][col]);
+        }
+    }
+    // row 0 has no flux term: dt * 0 + dt * 0
+    for (int col = 0; col < ncol; col++) out[col] = dt * 0.0 + dt * 0.0;
+    for (int i = 0; i < nc; i++) {
+        double acc[NCOL];
+#pragma unroll
+        for (int col = 0; col < NCOL; col++) acc[col] = 0;
+        double xp = 0;  // dFdXp[i + 1][0] of this side
+#pragma unroll
+        for (int j = 0; j < NP; j++) {
+            if (!q.act[j]) continue;
+            const double xij = b.xij[b.idx(j * nc + i, q.up[j])];
+            const double transIJ = xij * q.xiU[j] * q.transJ[j];
+            xp += sgn * transIJ;
+            if (q.up[j] == cell) {
+                double tmp = q.transJ[j] * q.xiP[j] * xij * q.dPj[j];
+                tmp += -transIJ * q.muP[j] / q.muU[j] * q.dPj[j];
+                xp += (tmp - transIJ * q.wU[j] * q.rhoPu[j] * dGamma);
+            }
+            else {
+                xp += -transIJ * q.wD[j] * q.rhoPd[j] * dGamma;
+            }
+#pragma unroll
+            for (int col = 0; col < NCOL; col++)
+                if (col < ncol) acc[col] = fma(xij, W[j][col], acc[col]);
+            if (q.up[j] == cell && j < jcomp_end) {
+                const double e = q.transJ[j] * q.xiU[j] * q.dPj[j];
+                const int k = np + j * nc + i;
+#pragma unroll
+                for (int col = 0; col < NCOL; col++)
+                    if (col < ncol) acc[col] = fma(e, ds[(size_t)(k * ncol + col) * stride], acc[col]);
+            }
+        }
+#pragma unroll
+        for (int col = 0; col < NCOL; col++) {
+            if (col >= ncol) break;
+            const double cv0 = (col == 0) ? xp : 0.0;
+            out[(i + 1) * ncol + col] = dt * acc[col] + dt * cv0;
+        }
+    }
+}
+
 template <int NCT>
 OCPX_HD void conn_jac_blocks(const Model& M, const BulkView& b, const ConnView& cv, int c, double dt,
                              double* bmatB, double* bmatE)
 {
-    const int np = b.np, nc = b.nc, nconn = cv.nconn;
-    const int ncol = nc + 1;
-    constexpr int NCOL = NCT + 1;
+    ConnPhase q;
+    conn_phase(M, b, cv, c, q);
     const size_t nb = (size_t)b.nb;
-    const int bId = (int)cv.bId[c], eId = (int)cv.eId[c];
-    const double Akd = cv.trans[c];
-    const double dGamma = M.units.gravity_factor * (b.depth[bId] - b.depth[eId]);
-    const int jcomp_end = (M.mixture == 1) ? np - 1 : np;  // phases whose composition rows of dSec are nonzero
-
-    // per-phase scalars of the connection
-    int up[NP];
-    bool act[NP];
-    double transJ[NP], xiU[NP], dPj[NP], muU[NP], wU[NP], wD[NP], muP[NP], xiP[NP], rhoPu[NP], rhoPd[NP];
-#pragma unroll
-    for (int j = 0; j < NP; j++) {
-        const int u = j < np ? (int)cv.upblock[j * nconn + c] : bId;
-        up[j] = u;
-        act[j] = j < np && b.phaseExist[b.idx(j, u)] != 0;
-        transJ[j] = 0; xiU[j] = 0; dPj[j] = 0; muU[j] = 1; wU[j] = 0; wD[j] = 0;
-        muP[j] = 0; xiP[j] = 0; rhoPu[j] = 0; rhoPd[j] = 0;
-        if (!act[j]) continue;
-        const int d = (u == bId) ? eId : bId;
-        const bool exD = b.phaseExist[b.idx(j, d)] != 0;
-        wU[j] = exD ? 0.5 : 1;
-        wD[j] = exD ? 0.5 : 0;
-        dPj[j] = cv.dP[j * nconn + c];
-        xiU[j] = b.xi[b.idx(j, u)];
-        muU[j] = b.mu[b.idx(j, u)];
-        transJ[j] = Akd * b.kr[b.idx(j, u)] / muU[j];
-        muP[j] = b.muP[b.idx(j, u)];
-        xiP[j] = b.xiP[b.idx(j, u)];
-        rhoPu[j] = b.rhoP[b.idx(j, u)];
-        rhoPd[j] = b.rhoP[b.idx(j, d)];
-    }
-
-    for (int side = 0; side < 2; side++) {
-        const int cell = side == 0 ? bId : eId;
-        const double sgn = side == 0 ? 1.0 : -1.0;
-        double* out = side == 0 ? bmatB : bmatE;
-        const double* ds = b.dSec_dPri + cell;  // ds[(k * ncol + col) * nb]
-        double W[NP][NCOL];
-#pragma unroll
-        for (int j = 0; j < NP; j++) {
-#pragma unroll
-            for (int col = 0; col < NCOL; col++) W[j][col] = 0;
-            if (!act[j]) continue;
-            const int u = up[j];
-            const bool isU = (u == cell);
-            const double xt = xiU[j] * transJ[j];
-            // saturation columns: sgn*xi*transJ*dPcdS(side cell) [+ Akd*dKrdS(U)/mu*xi*dP on the upwind side]
-            for (int k = 0; k < np; k++) {
-                double a = sgn * xt * b.dPcdS[b.idx(j * np + k, cell)];
-                if (isU) a += Akd * b.dKrdS[b.idx(j * np + k, u)] / muU[j] * xiU[j] * dPj[j];
-#pragma unroll
-                for (int col = 0; col < NCOL; col++)
-                    if (col < ncol) W[j][col] = fma(a, ds[(size_t)(k * ncol + col) * nb], W[j][col]);
-            }
-            if (j >= jcomp_end) continue;
-            // composition columns of phase j
-            for (int m = 0; m < nc; m++) {
-                double g;
-                if (isU) {
-                    const double rhox = b.rhox[b.idx(j * nc + m, u)];
-                    const double xix = b.xix[b.idx(j * nc + m, u)];
-                    const double mux = b.mux[b.idx(j * nc + m, u)];
-                    g = -xt * wU[j] * rhox * dGamma;
-                    g += transJ[j] * xix * dPj[j];
-                    g += -xt * mux / muU[j] * dPj[j];
-                }
-                else {
-                    if (wD[j] == 0) continue;
-                    g = -xt * wD[j] * b.rhox[b.idx(j * nc + m, cell)] * dGamma;
-                }
-                const int k = np + j * nc + m;
-#pragma unroll
-                for (int col = 0; col < NCOL; col++)
-                    if (col < ncol) W[j][col] = fma(g, ds[(size_t)(k * ncol + col) * nb], W[j][col]);
-            }
-        }
-        // row 0 has no flux term: dt * 0 + dt * 0
-        for (int col = 0; col < ncol; col++) out[col] = dt * 0.0 + dt * 0.0;
-        for (int i = 0; i < nc; i++) {
-            double acc[NCOL];
-#pragma unroll
-            for (int col = 0; col < NCOL; col++) acc[col] = 0;
-            double xp = 0;  // dFdXp[i + 1][0] of this side
-#pragma unroll
-            for (int j = 0; j < NP; j++) {
-                if (!act[j]) continue;
-                const double xij = b.xij[b.idx(j * nc + i, up[j])];
-                const double transIJ = xij * xiU[j] * transJ[j];
-                xp += sgn * transIJ;
-                if (up[j] == cell) {
-                    double tmp = transJ[j] * xiP[j] * xij * dPj[j];
-                    tmp += -transIJ * muP[j] / muU[j] * dPj[j];
-                    xp += (tmp - transIJ * wU[j] * rhoPu[j] * dGamma);
-                }
-                else {
-                    xp += -transIJ * wD[j] * rhoPd[j] * dGamma;
-                }
-#pragma unroll
-                for (int col = 0; col < NCOL; col++)
-                    if (col < ncol) acc[col] = fma(xij, W[j][col], acc[col]);
-                if (up[j] == cell && j < jcomp_end) {
-                    const double e = transJ[j] * xiU[j] * dPj[j];
-                    const int k = np + j * nc + i;
-#pragma unroll
-                    for (int col = 0; col < NCOL; col++)
-                        if (col < ncol) acc[col] = fma(e, ds[(size_t)(k * ncol + col) * nb], acc[col]);
-                }
-            }
-#pragma unroll
-            for (int col = 0; col < NCOL; col++) {
-                if (col >= ncol) break;
-                const double cv0 = (col == 0) ? xp : 0.0;
-                out[(i + 1) * ncol + col] = dt * acc[col] + dt * cv0;
-            }
-        }
-    }
+    conn_jac_side<NCT>(b, q, 0, b.dSec_dPri + q.bId, nb, dt, bmatB);
+    conn_jac_side<NCT>(b, q, 1, b.dSec_dPri + q.eId, nb, dt, bmatE);
 }
 
 // One block row of the Jacobian: the accumulation diagonal block

@@ -803,114 +803,21 @@ struct CompCellUpdate {
         }
         if (!label0_oil) swap_phases(NC);
 
-        // ---- CalPropertyW (:846-860): water always present
-        ex[2] = true;
-        xx[2][NC] = 1.0;
-        pvtw_rho_xi_mu_der(M.water, M.units.conv1, P, rho[2], xiv[2], mu[2], rhoPv[2], xiPv[2], muPv[2]);
-        nj[2] = Ni[NC];
-        vj[2] = nj[2] / xiv[2];
-        for (int i = 0; i < nct; i++) vji[2][i] = 0;
-        vji[2][NC] = 1 / xiv[2];
-        vjP[2] = -nj[2] * xiPv[2] / (xiv[2] * xiv[2]);
+        water_and_saturations(M, P, Ni[NC], NC);
+        volume_derivatives(NC, NPh);
 
-        // ---- OCPMixtureVarSet::CalVfS (include/OCPMixtureVarSet.hpp:143-155)
-        Vf = 0;
-        for (int j = 0; j < np; j++)
-            if (ex[j]) Vf += vj[j];
-        for (int j = 0; j < np; j++) S[j] = ex[j] ? vj[j] / Vf : 0;
-
-        // ---- CalVfiVfp_full02 + AddVfpVfiW (:462-524, 896-901)
-        for (int j = 0; j < 2; j++) vji[j][NC] = 0;
-        if (NPh == 1) {
-            const int j = ex[0] ? 0 : 1;
-            vjP[j] = nj[j] * vmP[j];
-            vfP = vjP[j];
-            for (int i = 0; i < NC; i++) {
-                vji[j][i] = vm[j] + vmx[j][i];
-                for (int k = 0; k < NC; k++) vji[j][i] -= vmx[j][k] * xx[j][k];
-                vfi[i] = vji[j][i];
-            }
+        // ---- CaldXsdXp02 + CaldXsdXpW (:565-642, 904-920), written straight to the SoA rows;
+        // when the flash derivatives are recomputed where they are used, the
+        // phase mole numbers are kept instead
+        if (b.dSec_dPri) {
+            dsec_rows(NC, NPh, Nt, Ni, [&](int r, int col) -> double& {
+                return b.dSec_dPri[b.idx(r * ncol + col, cell)];
+            });
         }
-        else {
-            double* lnN0 = f.lnf[0];
-            double* lnN1 = f.lnf[1];
-            double lnP0[NCM], lnP1[NCM];
-            f.eos.cal_lnfugN(xx[0], nj[0], lnN0);
-            f.eos.cal_lnfugP(xx[0], lnP0);
-            f.eos.cal_lnfugN(xx[1], nj[1], lnN1);
-            f.eos.cal_lnfugP(xx[1], lnP1);
-            double* Jd = f.J;
-            for (int i = 0; i < NC; i++)
-                for (int mm = 0; mm < NC; mm++) Jd[i * NC + mm] = lnN0[i * NC + mm] + lnN1[i * NC + mm];
-            for (int i = 0; i < NC; i++) rhs[i] = lnP1[i] - lnP0[i];
-            for (int k = 0; k < NC; k++)
-                for (int i = 0; i < NC; i++) rhs[(k + 1) * NC + i] = lnN1[k * NC + i];
-            if (!gen_solve_colmajor<NCM>(NC, Jd, rhs, NC + 1, f.W)) f.status |= ST_SINGULAR;
-            double tmp0 = 0, tmp1 = 0;
-            for (int i = 0; i < NC; i++) {
-                tmp0 -= vmx[0][i] * xx[0][i];
-                tmp1 -= vmx[1][i] * xx[1][i];
-            }
-            const double* dP = rhs;
-            vjP[0] = nj[0] * vmP[0];
-            vjP[1] = nj[1] * vmP[1];
-            for (int k = 0; k < NC; k++) {
-                vjP[0] += (vm[0] + tmp0 + vmx[0][k]) * dP[k];
-                vjP[1] -= (vm[1] + tmp1 + vmx[1][k]) * dP[k];
-            }
-            vfP = vjP[0] + vjP[1];
-            for (int i = 0; i < NC; i++) {
-                const double* dN = rhs + (i + 1) * NC;
-                vji[0][i] = 0;
-                vji[1][i] = 0;
-                for (int k = 0; k < NC; k++) {
-                    vji[0][i] += (vm[0] + tmp0 + vmx[0][k]) * dN[k];
-                    vji[1][i] += (vm[1] + tmp1 + vmx[1][k]) * ((i == k ? 1.0 : 0.0) - dN[k]);
-                }
-                vfi[i] = vji[0][i] + vji[1][i];
-            }
+        if (b.njhc) {
+            b.njhc[b.idx(0, cell)] = ex[0] ? nj[0] : 0.0;
+            b.njhc[b.idx(1, cell)] = ex[1] ? nj[1] : 0.0;
         }
-        vfP += vjP[2];
-        vfi[NC] = vji[2][NC];
-
-        // ---- CaldXsdXp02 + CaldXsdXpW (:565-642, 904-920), written straight to the SoA rows
-        const int nrow = np * nct + np;
-        auto dX = [&](int r, int col) -> double& { return b.dSec_dPri[b.idx(r * ncol + col, cell)]; };
-        for (int r = 0; r < nrow; r++)
-            for (int col = 0; col < ncol; col++) dX(r, col) = 0;
-        for (int j = 0; j < 2; j++) {
-            if (!ex[j]) continue;
-            dX(j, 0) = (vjP[j] - vfP * S[j]) / Vf;
-            for (int mm = 0; mm < NC; mm++) dX(j, 1 + mm) = (vji[j][mm] - vfi[mm] * S[j]) / Vf;
-        }
-        if (NPh == 1) {
-            const int j = ex[0] ? 0 : 1;
-            for (int i = 0; i < NC; i++)
-                for (int mm = 0; mm < NC; mm++)
-                    dX(np + j * nct + i, 1 + mm) = ((i == mm ? 1.0 : 0.0) * Nt - Ni[i]) / (Nt * Nt);
-        }
-        else {
-            double njDerSum = 0;
-            for (int i = 0; i < NC; i++) njDerSum += rhs[i];
-            for (int i = 0; i < NC; i++) {
-                dX(np + 0 * nct + i, 0) = (rhs[i] - njDerSum * xx[0][i]) / nj[0];
-                dX(np + 1 * nct + i, 0) = (-rhs[i] + njDerSum * xx[1][i]) / nj[1];
-            }
-            for (int mm = 0; mm < NC; mm++) {
-                const double* dN = rhs + (mm + 1) * NC;
-                njDerSum = 0;
-                for (int i = 0; i < NC; i++) njDerSum += dN[i];
-                for (int i = 0; i < NC; i++) {
-                    dX(np + 0 * nct + i, mm + 1) = (dN[i] - njDerSum * xx[0][i]) / nj[0];
-                    dX(np + 1 * nct + i, mm + 1) =
-                        (((i == mm ? 1.0 : 0.0) - dN[i]) - (1 - njDerSum) * xx[1][i]) / nj[1];
-                }
-            }
-        }
-        for (int j = 0; j < 2; j++)
-            if (ex[j]) dX(j, NC + 1) = (vji[j][NC] - vfi[NC] * S[j]) / Vf;
-        dX(2, 0) = (vjP[2] - vfP * S[2]) / Vf;
-        for (int i = 0; i < nct; i++) dX(2, 1 + i) = (vji[2][i] - vfi[i] * S[2]) / Vf;
 
         // ---- SkipPSAMethod01::CalSkipForNextStep (src/AcceleratePEC.cpp:127-170)
         if (m.skip_psa) {
@@ -970,6 +877,160 @@ struct CompCellUpdate {
         b.iters[b.idx(3, cell)] = f.it_nr_sp;
         b.iters[b.idx(4, cell)] = f.it_rr;
         return true;
+    }
+
+    // ---- CalPropertyW (src/OCPMixtureMethodComp.cpp:846-860): water always
+    // present; then OCPMixtureVarSet::CalVfS (include/OCPMixtureVarSet.hpp:143-155)
+    OCPX_HD void water_and_saturations(const Model& M, double P, double NiW, int NC)
+    {
+        const int np = 3, nct = NC + 1;
+        ex[2] = true;
+        xx[2][NC] = 1.0;
+        pvtw_rho_xi_mu_der(M.water, M.units.conv1, P, rho[2], xiv[2], mu[2], rhoPv[2], xiPv[2], muPv[2]);
+        nj[2] = NiW;
+        vj[2] = nj[2] / xiv[2];
+        for (int i = 0; i < nct; i++) vji[2][i] = 0;
+        vji[2][NC] = 1 / xiv[2];
+        vjP[2] = -nj[2] * xiPv[2] / (xiv[2] * xiv[2]);
+        Vf = 0;
+        for (int j = 0; j < np; j++)
+            if (ex[j]) Vf += vj[j];
+        for (int j = 0; j < np; j++) S[j] = ex[j] ? vj[j] / Vf : 0;
+    }
+
+    // ---- CalVfiVfp_full02 + AddVfpVfiW (src/OCPMixtureMethodComp.cpp:462-524, 896-901),
+    // phases in label order; leaves the derivative solve's solution in rhs
+    OCPX_HD void volume_derivatives(int NC, int NPh)
+    {
+        for (int j = 0; j < 2; j++) vji[j][NC] = 0;
+        if (NPh == 1) {
+            const int j = ex[0] ? 0 : 1;
+            vjP[j] = nj[j] * vmP[j];
+            vfP = vjP[j];
+            for (int i = 0; i < NC; i++) {
+                vji[j][i] = vm[j] + vmx[j][i];
+                for (int k = 0; k < NC; k++) vji[j][i] -= vmx[j][k] * xx[j][k];
+                vfi[i] = vji[j][i];
+            }
+        }
+        else {
+            double* lnN0 = f.lnf[0];
+            double* lnN1 = f.lnf[1];
+            double lnP0[NCM], lnP1[NCM];
+            f.eos.cal_lnfugN(xx[0], nj[0], lnN0);
+            f.eos.cal_lnfugP(xx[0], lnP0);
+            f.eos.cal_lnfugN(xx[1], nj[1], lnN1);
+            f.eos.cal_lnfugP(xx[1], lnP1);
+            double* Jd = f.J;
+            for (int i = 0; i < NC; i++)
+                for (int mm = 0; mm < NC; mm++) Jd[i * NC + mm] = lnN0[i * NC + mm] + lnN1[i * NC + mm];
+            for (int i = 0; i < NC; i++) rhs[i] = lnP1[i] - lnP0[i];
+            for (int k = 0; k < NC; k++)
+                for (int i = 0; i < NC; i++) rhs[(k + 1) * NC + i] = lnN1[k * NC + i];
+            if (!gen_solve_colmajor<NCM>(NC, Jd, rhs, NC + 1, f.W)) f.status |= ST_SINGULAR;
+            double tmp0 = 0, tmp1 = 0;
+            for (int i = 0; i < NC; i++) {
+                tmp0 -= vmx[0][i] * xx[0][i];
+                tmp1 -= vmx[1][i] * xx[1][i];
+            }
+            const double* dP = rhs;
+            vjP[0] = nj[0] * vmP[0];
+            vjP[1] = nj[1] * vmP[1];
+            for (int k = 0; k < NC; k++) {
+                vjP[0] += (vm[0] + tmp0 + vmx[0][k]) * dP[k];
+                vjP[1] -= (vm[1] + tmp1 + vmx[1][k]) * dP[k];
+            }
+            vfP = vjP[0] + vjP[1];
+            for (int i = 0; i < NC; i++) {
+                const double* dN = rhs + (i + 1) * NC;
+                vji[0][i] = 0;
+                vji[1][i] = 0;
+                for (int k = 0; k < NC; k++) {
+                    vji[0][i] += (vm[0] + tmp0 + vmx[0][k]) * dN[k];
+                    vji[1][i] += (vm[1] + tmp1 + vmx[1][k]) * ((i == k ? 1.0 : 0.0) - dN[k]);
+                }
+                vfi[i] = vji[0][i] + vji[1][i];
+            }
+        }
+        vfP += vjP[2];
+        vfi[NC] = vji[2][NC];
+    }
+
+    // ---- CaldXsdXp02 + CaldXsdXpW (src/OCPMixtureMethodComp.cpp:565-642, 904-920):
+    // dSec_dPri row by row through dX(row, column)
+    template <class F>
+    OCPX_HD void dsec_rows(int NC, int NPh, double Nt, const double* Ni, F dX)
+    {
+        const int np = 3, nct = NC + 1, ncol = nct + 1;
+        const int nrow = np * nct + np;
+        for (int r = 0; r < nrow; r++)
+            for (int col = 0; col < ncol; col++) dX(r, col) = 0;
+        for (int j = 0; j < 2; j++) {
+            if (!ex[j]) continue;
+            dX(j, 0) = (vjP[j] - vfP * S[j]) / Vf;
+            for (int mm = 0; mm < NC; mm++) dX(j, 1 + mm) = (vji[j][mm] - vfi[mm] * S[j]) / Vf;
+        }
+        if (NPh == 1) {
+            const int j = ex[0] ? 0 : 1;
+            for (int i = 0; i < NC; i++)
+                for (int mm = 0; mm < NC; mm++)
+                    dX(np + j * nct + i, 1 + mm) = ((i == mm ? 1.0 : 0.0) * Nt - Ni[i]) / (Nt * Nt);
+        }
+        else {
+            double njDerSum = 0;
+            for (int i = 0; i < NC; i++) njDerSum += rhs[i];
+            for (int i = 0; i < NC; i++) {
+                dX(np + 0 * nct + i, 0) = (rhs[i] - njDerSum * xx[0][i]) / nj[0];
+                dX(np + 1 * nct + i, 0) = (-rhs[i] + njDerSum * xx[1][i]) / nj[1];
+            }
+            for (int mm = 0; mm < NC; mm++) {
+                const double* dN = rhs + (mm + 1) * NC;
+                njDerSum = 0;
+                for (int i = 0; i < NC; i++) njDerSum += dN[i];
+                for (int i = 0; i < NC; i++) {
+                    dX(np + 0 * nct + i, mm + 1) = (dN[i] - njDerSum * xx[0][i]) / nj[0];
+                    dX(np + 1 * nct + i, mm + 1) =
+                        (((i == mm ? 1.0 : 0.0) - dN[i]) - (1 - njDerSum) * xx[1][i]) / nj[1];
+                }
+            }
+        }
+        for (int j = 0; j < 2; j++)
+            if (ex[j]) dX(j, NC + 1) = (vji[j][NC] - vfi[NC] * S[j]) / Vf;
+        dX(2, 0) = (vjP[2] - vfP * S[2]) / Vf;
+        for (int i = 0; i < nct; i++) dX(2, 1 + i) = (vji[2][i] - vfi[i] * S[2]) / Vf;
+    }
+
+    // dSec_dPri of a cell recomputed from the state its flash left (P, T, Ni,
+    // phase labels, x_ij and the hydrocarbon phases' mole numbers), with the
+    // flash's own statements in the same order, so the values are the ones
+    // the flash would have stored: out[(row * (nc + 1) + column) * stride].
+    OCPX_HD void recompute_dsec(const Model& M, const BulkView& b, int cell, double* out, size_t stride)
+    {
+        const CompModel& m = M.comp;
+        const int NC = m.nc, nct = NC + 1, ncol = nct + 1;
+        f.m = &m;
+        f.NC = NC;
+        f.status = 0;
+        const double P = b.P[cell];
+        const double T = b.T[cell] + M.units.conv4;
+        double Ni[NCM + 1];
+        for (int i = 0; i < nct; i++) Ni[i] = b.Ni[b.idx(i, cell)];
+        double Nt = 0;
+        for (int i = 0; i < NC; i++) Nt += Ni[i];
+        f.eos.setup(&m, M.units.gas_constant, P, T);
+        int NPh = 0;
+        for (int j = 0; j < 2; j++) {
+            ex[j] = b.phaseExist[b.idx(j, cell)] != 0;
+            if (!ex[j]) continue;
+            NPh++;
+            nj[j] = b.njhc[b.idx(j, cell)];
+            for (int i = 0; i < NC; i++) xx[j][i] = b.xij[b.idx(j * nct + i, cell)];
+            vm[j] = f.eos.cal_vm_der(xx[j], vmP[j], vmx[j]);
+            vj[j] = nj[j] * vm[j];
+        }
+        water_and_saturations(M, P, Ni[NC], NC);
+        volume_derivatives(NC, NPh);
+        dsec_rows(NC, NPh, Nt, Ni, [&](int r, int col) -> double& { return out[(size_t)(r * ncol + col) * stride]; });
     }
 
     OCPX_HD void swap_phases(int NC)

@@ -38,8 +38,9 @@ constexpr int WNCOL = NCT_MAX + 1;        // nc + 1 at most
 constexpr int WNCOL2 = 3 * (NCT_MAX + 1);  // np * nc + np at most (np = 3)
 
 // qi [nc], dqb [ncol] (row 0 zero), dqw [nc], S [ncol * ncol] of one perforation
+// (the perforated cell's dSec_dPri at ds[(row * ncol + col) * stride])
 __device__ void well_perf_terms(const BulkView& b, const WellPerf& f, double bhp, const double* __restrict__ zi,
-                                double* qi, double* dqb, double* dqw, double* S)
+                                const double* ds, size_t stride, double* qi, double* dqb, double* dqw, double* S)
 {
     const int np = b.np, nc = b.nc, n = f.cell;
     const int ncol = nc + 1, ncol2 = np * nc + np;
@@ -115,7 +116,7 @@ __device__ void well_perf_terms(const BulkView& b, const WellPerf& f, double bhp
     for (int r = 0; r < ncol; r++)
         for (int c = 0; c < ncol; c++) {
             double s = 0;
-            for (int k = 0; k < ncol2; k++) s += dqs[r][k] * b.dSec_dPri[b.idx(k * ncol + c, n)];
+            for (int k = 0; k < ncol2; k++) s += dqs[r][k] * ds[(size_t)(k * ncol + c) * stride];
             S[r * ncol + c] = s;
         }
 }
@@ -134,7 +135,7 @@ __global__ void k_well_perf_eval(BulkView b, const WellPerf* __restrict__ perf, 
     const int nc = b.nc, ncol = nc + 1;
     const double* fac = factor + (size_t)f.well * nc;
     double qi[WNCOL], dqb[WNCOL], dqw[WNCOL], S[WNCOL * WNCOL];
-    well_perf_terms(b, f, f.bhp, inj_zi + (size_t)f.well * nc, qi, dqb, dqw, S);
+    well_perf_terms(b, f, f.bhp, inj_zi + (size_t)f.well * nc, b.dSec_dPri + f.cell, (size_t)b.nb, qi, dqb, dqw, S);
     const size_t bs = (size_t)ncol * ncol;
     double* bb = out_bb + p * bs;
     double* wb = out_wb + p * bs;
@@ -159,7 +160,10 @@ __global__ void k_well_perf(BulkView b, WellSys w)
     if (p >= w.nperf) return;
     const WellPerf f = w.perf[p];
     const int nc = b.nc, ncol = nc + 1;
-    well_perf_terms(b, f, w.bhp[f.well], w.zi + (size_t)f.well * nc, w.qi + (size_t)p * nc,
+    // the stored dSec_dPri, or the copy recomputed for the perforated cells
+    const double* ds = w.dsec ? w.dsec + (size_t)w.perf_pc[p] * 3 * ncol * ncol : b.dSec_dPri + f.cell;
+    const size_t stride = w.dsec ? 1 : (size_t)b.nb;
+    well_perf_terms(b, f, w.bhp[f.well], w.zi + (size_t)f.well * nc, ds, stride, w.qi + (size_t)p * nc,
                     w.dqb + (size_t)p * ncol, w.dqw + (size_t)p * nc, w.S + (size_t)p * ncol * ncol);
 }
 

@@ -62,6 +62,44 @@ cudaError_t setup_flash_batched(int ncm, int* excl_smem)
     default: return cudaErrorInvalidValue;
     }
 }
+
+// the consumers of recomputed flash derivatives, one set per NCM
+#define OCPX_RECOMPUTE_DECL(N)                                                                                    \
+    cudaError_t launch_dsec_cells_##N(const Model*, const BulkView&, const int*, int, int, double*, cudaStream_t);  \
+    cudaError_t launch_jac_recompute_##N(const Model*, const BulkView&, const ConnView&, double, double*,          \
+                                         cudaStream_t);                                                            \
+    cudaError_t launch_newton_update_recompute_##N(const Model*, const BulkView&, const double*, double, cudaStream_t);
+OCPX_RECOMPUTE_DECL(4)
+OCPX_RECOMPUTE_DECL(6)
+OCPX_RECOMPUTE_DECL(8)
+OCPX_RECOMPUTE_DECL(10)
+OCPX_RECOMPUTE_DECL(12)
+#undef OCPX_RECOMPUTE_DECL
+#define OCPX_NCM_SWITCH(fn, ...)                      \
+    switch (ncm) {                                    \
+    case 4: return fn##4(__VA_ARGS__);                \
+    case 6: return fn##6(__VA_ARGS__);                \
+    case 8: return fn##8(__VA_ARGS__);                \
+    case 10: return fn##10(__VA_ARGS__);              \
+    case 12: return fn##12(__VA_ARGS__);              \
+    default: return cudaErrorInvalidValue;            \
+    }
+cudaError_t launch_dsec_cells(int ncm, const Model* dm, const BulkView& b, const int* list, int first, int n,
+                              double* out, cudaStream_t s)
+{
+    OCPX_NCM_SWITCH(launch_dsec_cells_, dm, b, list, first, n, out, s)
+}
+cudaError_t launch_jac_recompute(int ncm, const Model* dm, const BulkView& b, const ConnView& cv, double dt,
+                                 double* bmat, cudaStream_t s)
+{
+    OCPX_NCM_SWITCH(launch_jac_recompute_, dm, b, cv, dt, bmat, s)
+}
+cudaError_t launch_newton_update_recompute(int ncm, const Model* dm, const BulkView& b, const double* u,
+                                           double dSmax, cudaStream_t s)
+{
+    OCPX_NCM_SWITCH(launch_newton_update_recompute_, dm, b, u, dSmax, s)
+}
+#undef OCPX_NCM_SWITCH
 }  // namespace ocpx
 
 using namespace ocpx;
@@ -113,9 +151,13 @@ struct ocpx_ctx {
     Model* d_model = nullptr;
     int nb = 0, nbI = 0, np = 3, nc = 0, nconn = 0, NC = 0, ncm = 0, nct_cap = 0;
     int variant = 0;
+    // dSec_dPri recomputed where it is used instead of stored (ocpx_options)
+    bool recompute = false;
     // one arena for everything
     char* arena = nullptr;
     size_t arena_bytes = 0;
+    size_t sys_bytes = 0;           // the linear system's buffer (sys)
+    size_t wbuf_bytes = 0;          // the wells' buffer (wbuf)
     BulkView b{};
     ConnView cv{};
     double* res = nullptr;
@@ -282,7 +324,7 @@ FieldInfo ocpx_ctx::field(ocpx_field f) const
     case OCPX_F_KR: return {b.kr, nb, np, 8, true, true};
     case OCPX_F_DKRDS: return {b.dKrdS, nb, np * np, 8, true, true};
     case OCPX_F_DPCDS: return {b.dPcdS, nb, np * np, 8, true, true};
-    case OCPX_F_DSEC_DPRI: return {b.dSec_dPri, nb, lend, 8, true, true};
+    case OCPX_F_DSEC_DPRI: return {b.dSec_dPri, nb, lend, 8, true, !recompute};
     case OCPX_F_PORO: return {b.poro, nb, 1, 8, true, true};
     case OCPX_F_POROP: return {b.poroP, nb, 1, 8, true, true};
     case OCPX_F_ROCKVP: return {b.rockVp, nb, 1, 8, true, true};
@@ -393,8 +435,10 @@ ocpx_status build_system(ocpx_ctx* ctx, std::vector<uint32_t>* slot_bw, std::vec
     ctx->jac_slot = nullptr;
     ctx->jac_val = nullptr;
     ctx->res = ctx->u = ctx->adj = nullptr;
+    ctx->sys_bytes = 0;
     if (cudaMalloc(&ctx->sys, total) != cudaSuccess)
         return fail(OCPX_CUDA_ERROR, "cudaMalloc of " + std::to_string(total) + " bytes (the linear system) failed");
+    ctx->sys_bytes = total;
     ctx->jac_rowptr = (uint32_t*)(ctx->sys + o_row);
     ctx->jac_col = (uint32_t*)(ctx->sys + o_col);
     ctx->jac_slot = (uint32_t*)(ctx->sys + o_slot);
@@ -424,8 +468,19 @@ const char* ocpx_last_error(void) { return g_err.c_str(); }
 
 ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int device, ocpx_ctx** out)
 {
+    return ocpx_create_ex(md, gd, device, nullptr, out);
+}
+
+ocpx_status ocpx_create_ex(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int device, const ocpx_options* opt,
+                           ocpx_ctx** out)
+{
     if (!md || !gd || !out) return fail(OCPX_INVALID_ARG, "null argument");
     *out = nullptr;
+    if (opt && opt->struct_size != sizeof(ocpx_options))
+        return fail(OCPX_INVALID_ARG, "ocpx_options.struct_size must be sizeof(ocpx_options)");
+    const bool recompute = opt && opt->recompute_flash_der != 0;
+    if (recompute && md->mixture != 1)
+        return fail(OCPX_INVALID_ARG, "recompute_flash_der needs the compositional mixture");
     if (gd->nb <= 0 || gd->nconn < 0 || !gd->v || !gd->depth || !gd->poro_init ||
         (gd->nconn > 0 && (!gd->conn_b || !gd->conn_e || !gd->conn_trans)))
         return fail(OCPX_INVALID_ARG, "grid description incomplete");
@@ -457,6 +512,7 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     }
     ctx->nb = gd->nb;
     ctx->nbI = (int)nbI_;
+    ctx->recompute = recompute;
     ctx->nc = md->nc;
     ctx->np = 3;
     ctx->nconn = gd->nconn;
@@ -500,7 +556,11 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     add(&b.rhoP, D * np); add(&b.xiP, D * np); add(&b.muP, D * np);
     add(&b.rhox, D * np * nc); add(&b.xix, D * np * nc); add(&b.mux, D * np * nc);
     add(&b.kr, D * np); add(&b.dKrdS, D * np * np); add(&b.dPcdS, D * np * np);
-    add(&b.dSec_dPri, D * lend);
+    // dSec_dPri, or what recomputing it needs beyond the other fields: the
+    // hydrocarbon phases' mole numbers (both inside the state range, so the
+    // checkpoints keep them)
+    if (recompute) add(&b.njhc, D * 2);
+    else add(&b.dSec_dPri, D * lend);
     add(&b.poro, D); add(&b.poroP, D); add(&b.rockVp, D);
     add(&b.skip_flag, (size_t)nb); add(&b.skip_minEig, D); add(&b.skip_P, D); add(&b.skip_T, D);
     add(&b.skip_zi, D * (ctx->NC > 0 ? ctx->NC : 1));
@@ -532,8 +592,11 @@ ocpx_status ocpx_create(const ocpx_model_desc* md, const ocpx_grid_desc* gd, int
     add(&ctx->nr_res0, sizeof(double)); add(&ctx->nr_state, sizeof(int)); add(&ctx->nr_dt, sizeof(double) * 2);
     add(&ctx->bmat, sizeof(double) * C * 2 * bsize);
     add(&ctx->adj_conn, sizeof(double) * C);
-    size_t staging = D * lend;
+    // field transfers go through the staging buffer in chunks; stored
+    // dSec_dPri moves in one piece
+    size_t staging = recompute ? D * std::max({np * nc, np * np, 5}) : D * lend;
     staging = std::max(staging, sizeof(double) * C * nc);
+    staging = std::max(staging, sizeof(double) * lend);
     add(&ctx->staging, staging);
     ctx->staging_bytes = staging;
     size_t total = 0;
@@ -672,6 +735,25 @@ namespace {
 ocpx_status field_transfer(ocpx_ctx* ctx, ocpx_field f, size_t first, size_t n, void* host, bool to_device)
 {
     if (!ctx || (!host && n)) return fail(OCPX_INVALID_ARG, "null argument");
+    if (f == OCPX_F_DSEC_DPRI && ctx->recompute) {
+        // recomputed from the state the last flash left (P, T, Ni, phase labels,
+        // x_ij, phase mole numbers), chunk by chunk through the staging buffer
+        if (to_device) return fail(OCPX_INVALID_ARG, "dSec_dPri is recomputed, not stored: it cannot be set");
+        const size_t lend = (size_t)ctx->np * (ctx->nc + 1) * (ctx->nc + 1);
+        if (first > (size_t)ctx->nb || n > (size_t)ctx->nb - first)
+            return fail(OCPX_INVALID_ARG, "dSec_dPri: range outside the cells");
+        const size_t chunk = ctx->staging_bytes / (sizeof(double) * lend);
+        for (size_t k = 0; k < n; k += chunk) {
+            const size_t m = std::min(chunk, n - k);
+            OCPX_CUDA(launch_dsec_cells(ctx->ncm, ctx->d_model, ctx->b, nullptr, (int)(first + k), (int)m,
+                                        (double*)ctx->staging, ctx->stream));
+            ctx->launches++;
+            OCPX_CUDA(cudaMemcpyAsync((double*)host + k * lend, ctx->staging, sizeof(double) * m * lend,
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+            OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+        }
+        return OCPX_OK;
+    }
     const FieldInfo fi = ctx->field(f);
     if (!fi.dev) return fail(OCPX_INVALID_ARG, "unknown field " + std::to_string((int)f));
     if (to_device && !fi.writable) return fail(OCPX_INVALID_ARG, "field not writable: " + std::to_string((int)f));
@@ -680,24 +762,33 @@ ocpx_status field_transfer(ocpx_ctx* ctx, ocpx_field f, size_t first, size_t n, 
                                           std::to_string(first + n) + ") outside " + std::to_string(fi.n) + " entities");
     if (!n) return OCPX_OK;
     if (to_device) ctx->state_gen++;
-    const size_t bytes = n * fi.width * fi.elem;
+    const size_t ebytes = (size_t)fi.width * fi.elem;  // one entity
     const cudaMemcpyKind kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
     if (fi.width == 1 || !fi.soa) {
-        char* dev = (char*)fi.dev + first * fi.width * fi.elem;
-        OCPX_CUDA(cudaMemcpyAsync(to_device ? (void*)dev : host, to_device ? (const void*)host : (const void*)dev, bytes,
-                                  kind, ctx->stream));
+        char* dev = (char*)fi.dev + first * ebytes;
+        OCPX_CUDA(cudaMemcpyAsync(to_device ? (void*)dev : host, to_device ? (const void*)host : (const void*)dev,
+                                  n * ebytes, kind, ctx->stream));
+        OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
+        return OCPX_OK;
     }
-    else if (to_device) {
-        OCPX_CUDA(cudaMemcpyAsync(ctx->staging, host, bytes, kind, ctx->stream));
-        OCPX_CUDA(launch_transpose(fi.dev, ctx->staging, (int)n, fi.width, fi.elem, true, ctx->stream, fi.n, first));
+    // SoA fields through the staging buffer, as many entities at a time as it holds
+    const size_t chunk = ctx->staging_bytes / ebytes;
+    for (size_t k = 0; k < n; k += chunk) {
+        const size_t m = std::min(chunk, n - k);
+        char* h = (char*)host + k * ebytes;
+        if (to_device) {
+            OCPX_CUDA(cudaMemcpyAsync(ctx->staging, h, m * ebytes, kind, ctx->stream));
+            OCPX_CUDA(launch_transpose(fi.dev, ctx->staging, (int)m, fi.width, fi.elem, true, ctx->stream, fi.n,
+                                       first + k));
+        }
+        else {
+            OCPX_CUDA(launch_transpose(ctx->staging, fi.dev, (int)m, fi.width, fi.elem, false, ctx->stream, fi.n,
+                                       first + k));
+            OCPX_CUDA(cudaMemcpyAsync(h, ctx->staging, m * ebytes, kind, ctx->stream));
+        }
         ctx->launches++;
+        OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
     }
-    else {
-        OCPX_CUDA(launch_transpose(ctx->staging, fi.dev, (int)n, fi.width, fi.elem, false, ctx->stream, fi.n, first));
-        ctx->launches++;
-        OCPX_CUDA(cudaMemcpyAsync(host, ctx->staging, bytes, kind, ctx->stream));
-    }
-    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
     return OCPX_OK;
 }
 }  // namespace
@@ -884,6 +975,11 @@ ocpx_status enqueue_calres(ocpx_ctx* ctx, double dt)
                               wells ? nullptr : ctx->norm_out, ctx->block_cell, s));
     if (wells) {
         // CalResFIM of every well after the bulk rows, then the norms
+        if (ctx->recompute) {
+            OCPX_CUDA(launch_dsec_cells(ctx->ncm, ctx->d_model, ctx->b, ctx->ws.pc_cell, 0, ctx->ws.npc, ctx->ws.dsec,
+                                        s));
+            ctx->launches++;
+        }
         OCPX_CUDA(launch_wells_res(ctx->b, ctx->ws, dt, ctx->res, ctx->resRelV, ctx->resRelN, ctx->rownorm, s));
         OCPX_CUDA(launch_norm_reduce(ctx->rownorm, ctx->nbI, ctx->norm_out, s));
         ctx->launches += 3;
@@ -898,7 +994,10 @@ ocpx_status enqueue_assemble(ocpx_ctx* ctx, double dt)
 {
     cudaStream_t s = ctx->stream;
     int mk = ctx->stage_begin(6);
-    OCPX_CUDA(launch_jac_conn(ctx->nct_cap, ctx->d_model, ctx->b, ctx->cv, dt, ctx->bmat, ctx->block_conn, s));
+    if (ctx->recompute)
+        OCPX_CUDA(launch_jac_recompute(ctx->ncm, ctx->d_model, ctx->b, ctx->cv, dt, ctx->bmat, s));
+    else
+        OCPX_CUDA(launch_jac_conn(ctx->nct_cap, ctx->d_model, ctx->b, ctx->cv, dt, ctx->bmat, ctx->block_conn, s));
     ctx->stage_end(mk);
     mk = ctx->stage_begin(7);
     OCPX_CUDA(launch_jac_rows(ctx->b, ctx->cv, ctx->bmat, ctx->jac_rowptr, ctx->jac_val, ctx->block_cell, s));
@@ -983,11 +1082,20 @@ ocpx_status ocpx_linsolve(ocpx_ctx* ctx, double tol, int maxit, double* u_host, 
     return OCPX_OK;
 }
 
+namespace {
+// GetSolution of the cells, with dSec_dPri stored or recomputed
+cudaError_t newton_update(ocpx_ctx* ctx, double dSmax)
+{
+    if (ctx->recompute) return launch_newton_update_recompute(ctx->ncm, ctx->d_model, ctx->b, ctx->u, dSmax, ctx->stream);
+    return launch_newton_update(ctx->b, ctx->u, dSmax, ctx->block_cell, ctx->stream);
+}
+}  // namespace
+
 ocpx_status ocpx_newton_update_device(ocpx_ctx* ctx, double dSmax)
 {
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
     const int mk = ctx->stage_begin(8);
-    OCPX_CUDA(launch_newton_update(ctx->b, ctx->u, dSmax, ctx->block_cell, ctx->stream));
+    OCPX_CUDA(newton_update(ctx, dSmax));
     OCPX_CUDA(launch_wells_update(ctx->b, ctx->ws, ctx->u, ctx->stream));
     ctx->stage_end(mk);
     ctx->launches += ctx->ws.nw > 0 ? 2 : 1;
@@ -1001,7 +1109,7 @@ ocpx_status ocpx_newton_update(ocpx_ctx* ctx, const double* u_host, double dSmax
     const size_t bytes = sizeof(double) * ctx->nv();
     OCPX_CUDA(cudaMemcpyAsync(ctx->u, u_host, bytes, cudaMemcpyHostToDevice, ctx->stream));
     const int mk = ctx->stage_begin(8);
-    OCPX_CUDA(launch_newton_update(ctx->b, ctx->u, dSmax, ctx->block_cell, ctx->stream));
+    OCPX_CUDA(newton_update(ctx, dSmax));
     OCPX_CUDA(launch_wells_update(ctx->b, ctx->ws, ctx->u, ctx->stream));
     ctx->stage_end(mk);
     ctx->launches += ctx->ws.nw > 0 ? 2 : 1;
@@ -1255,6 +1363,7 @@ ocpx_status ocpx_set_wells(ocpx_ctx* ctx, int nwell, const ocpx_well* wells)
         OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
         if (ctx->wbuf) cudaFree(ctx->wbuf);
         ctx->wbuf = nullptr;
+        ctx->wbuf_bytes = 0;
         ctx->ws = WellSys{};
         ctx->well_cells = cells;
         ctx->well_nperf = nperf;
@@ -1309,8 +1418,14 @@ ocpx_status ocpx_set_wells(ocpx_ctx* ctx, int nwell, const ocpx_well* wells)
     const size_t o_qi = at(sizeof(double) * np_ * nc), o_dqb = at(sizeof(double) * np_ * ncol);
     const size_t o_dqw = at(sizeof(double) * np_ * nc), o_S = at(sizeof(double) * np_ * bs);
     const size_t o_wrel = at(sizeof(double) * nwell), o_max = at(sizeof(double));
+    const size_t o_ppc = at(sizeof(int) * np_);
+    const size_t o_dsec = ctx->recompute ? at(sizeof(double) * (size_t)npc * ctx->np * bs) : 0;
+    std::vector<int> perf_pc(np_);
+    for (int g = 0; g < npc; g++)
+        for (int k = pc_start[g]; k < pc_start[g + 1]; k++) perf_pc[order[k]] = g;
     if (!ctx->wbuf) {
         OCPX_CUDA(cudaMalloc(&ctx->wbuf, off));
+        ctx->wbuf_bytes = off;
         OCPX_CUDA(cudaMemset(ctx->wbuf, 0, off));
     }
     char* B = ctx->wbuf;
@@ -1334,6 +1449,8 @@ ocpx_status ocpx_set_wells(ocpx_ctx* ctx, int nwell, const ocpx_well* wells)
     ws.S = (double*)(B + o_S);
     ws.wrel = (double*)(B + o_wrel);
     ws.maxrel = (double*)(B + o_max);
+    ws.perf_pc = (const int*)(B + o_ppc);
+    ws.dsec = ctx->recompute ? (double*)(B + o_dsec) : nullptr;
     cudaStream_t s = ctx->stream;
     OCPX_CUDA(cudaMemcpyAsync(B + o_wd, wd.data(), sizeof(WellDev) * nwell, cudaMemcpyHostToDevice, s));
     OCPX_CUDA(cudaMemcpyAsync(B + o_bhp, bhp.data(), sizeof(double) * nwell, cudaMemcpyHostToDevice, s));
@@ -1346,6 +1463,7 @@ ocpx_status ocpx_set_wells(ocpx_ctx* ctx, int nwell, const ocpx_well* wells)
         OCPX_CUDA(cudaMemcpyAsync(B + o_pcc, pc_cell.data(), sizeof(int) * npc, cudaMemcpyHostToDevice, s));
         OCPX_CUDA(cudaMemcpyAsync(B + o_pcs, pc_start.data(), sizeof(int) * (npc + 1), cudaMemcpyHostToDevice, s));
         OCPX_CUDA(cudaMemcpyAsync(B + o_pcp, order.data(), sizeof(int) * np_, cudaMemcpyHostToDevice, s));
+        OCPX_CUDA(cudaMemcpyAsync(B + o_ppc, perf_pc.data(), sizeof(int) * np_, cudaMemcpyHostToDevice, s));
     }
     OCPX_CUDA(cudaStreamSynchronize(s));
     ctx->state_gen++;
@@ -1646,6 +1764,24 @@ ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value)
     }
 }
 
+}  // extern "C"
+
+namespace {
+// device memory the context holds: the arena, the linear system, the wells,
+// the linear solver's and the adjoint's work space, the checkpoints
+size_t device_bytes(const ocpx_ctx* ctx)
+{
+    size_t n = ctx->arena_bytes + ctx->sys_bytes + ctx->wbuf_bytes + ctx->weval_bytes;
+    if (ctx->ls_scratch) n += sizeof(double) * linsolve_scratch_doubles(ctx->nrow, ctx->nc + 1);
+    if (ctx->step_adj) n += sizeof(double) * (2 * ctx->nv() + ctx->nb + (size_t)ctx->nconn);
+    for (char* c : ctx->ckpt)
+        if (c) n += ctx->state_bytes;
+    return n;
+}
+}  // namespace
+
+extern "C" {
+
 ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value)
 {
     if (!ctx || !value) return fail(OCPX_INVALID_ARG, "null argument");
@@ -1664,6 +1800,8 @@ ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value)
     case OCPX_PARAM_FUSED_EXCL: *value = ctx->fused_excl; return OCPX_OK;
     case OCPX_PARAM_POST_BLOCK: *value = ctx->post_block; return OCPX_OK;
     case OCPX_PARAM_ROUND_GROWTH: *value = ctx->round_growth; return OCPX_OK;
+    case OCPX_PARAM_RECOMPUTE_FLASH_DER: *value = ctx->recompute ? 1 : 0; return OCPX_OK;
+    case OCPX_PARAM_DEVICE_BYTES: *value = (long long)device_bytes(ctx); return OCPX_OK;
     case OCPX_PARAM_DEFERRED: {
         unsigned n[2] = {0, 0};
         OCPX_CUDA(cudaMemcpyAsync(&n[0], ctx->defer_count + ctx->late_count, sizeof(unsigned),

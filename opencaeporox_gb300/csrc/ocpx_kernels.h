@@ -56,6 +56,16 @@ cudaError_t setup_flash_batched(int ncm, int* excl_smem);
 // SM-exclusive blocks when excl_blocks is nonzero)
 cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, const int* order,
                                  const FlashBatch& fb, int part, cudaStream_t s);
+// Flash derivatives recomputed where they are used (k_flash_comp.cu, part 7):
+// dSec_dPri of a list of cells (list NULL: first .. first + n - 1) into
+// out[t][np*(nc+1)^2]; the connection Jacobian blocks, each cell writing the
+// blocks of its side of its connections; GetSolution.
+cudaError_t launch_dsec_cells(int ncm, const Model* dm, const BulkView& b, const int* list, int first, int n,
+                              double* out, cudaStream_t s);
+cudaError_t launch_jac_recompute(int ncm, const Model* dm, const BulkView& b, const ConnView& cv, double dt,
+                                 double* bmat, cudaStream_t s);
+cudaError_t launch_newton_update_recompute(int ncm, const Model* dm, const BulkView& b, const double* u,
+                                           double dSmax, cudaStream_t s);
 // Cells grouped by flash path (two-phase, one-phase, skip-flagged) and, within
 // a group, in descending order of the work their last flash needed, by a
 // counting sort over COST_BUCKETS buckets.
@@ -123,6 +133,9 @@ struct WellSys {
     double* S = nullptr;             // [nperf*(nc+1)^2] dQ/dXs * dSec_dPri
     double* wrel = nullptr;          // [nw] |R_w / target rate|
     double* maxrel = nullptr;        // [1] maxWellRelRes_mol
+    const int* perf_pc = nullptr;    // [nperf] the perforated cell's index in pc_cell
+    double* dsec = nullptr;          // [npc][np*(nc+1)^2] the perforated cells' recomputed dSec_dPri
+                                     // (NULL: the stored one)
 };
 // after the bulk residual (before its norms are reduced): the perforations'
 // terms, the perforated rows and their relative residuals, the wells' rows

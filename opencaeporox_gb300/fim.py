@@ -88,6 +88,11 @@ class GridDesc(C.Structure):
                 ("conn_trans", C.POINTER(C.c_double)), ("nb_interior", C.c_int)]
 
 
+class Options(C.Structure):
+    """ocpx_options of ocpx_create_ex."""
+    _fields_ = [("struct_size", C.c_size_t), ("recompute_flash_der", C.c_int), ("reserved", C.c_int * 7)]
+
+
 class Report(C.Structure):
     _fields_ = [("status_or", C.c_uint32), ("n_two_phase", C.c_int), ("n_flagged", C.c_int)]
 
@@ -138,13 +143,13 @@ EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy",
            "ocpx_nr_init_step", "ocpx_nr_max_change", "ocpx_step_max_change", "ocpx_nr_check_converge",
            "ocpx_next_time_step", "ocpx_linsolve", "ocpx_newton_update_device", "ocpx_wells_eval",
            "ocpx_set_field_range", "ocpx_get_field_range", "ocpx_set_adjoint_seed", "ocpx_get_adjoint",
-           "ocpx_get_jacobian_rows", "ocpx_set_wells", "ocpx_get_wells"]
+           "ocpx_get_jacobian_rows", "ocpx_set_wells", "ocpx_get_wells", "ocpx_create_ex"]
 
 PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3, "predefer": 4, "coop_cells": 5,
           "predeferred": 6, "level": 7, "pre_blocks": 8,
           "cell_blocks": 9, "rounds": 10, "round_growth": 11,
           "fused_blocks": 12, "sms": 13, "fused_coop_blocks": 14,
-          "fused_excl": 15, "post_block": 16}
+          "fused_excl": 15, "post_block": 16, "recompute_flash_der": 17, "device_bytes": 18}
 
 _lib = None
 
@@ -161,6 +166,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.ocpx_abi_version.restype = C.c_int
     lib.ocpx_last_error.restype = C.c_char_p
     lib.ocpx_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(GridDesc), C.c_int, C.POINTER(P)]
+    lib.ocpx_create_ex.argtypes = [C.POINTER(ModelDesc), C.POINTER(GridDesc), C.c_int, C.POINTER(Options),
+                                   C.POINTER(P)]
     lib.ocpx_destroy.argtypes = [P]
     lib.ocpx_set_field.argtypes = [P, C.c_int, P, C.c_size_t]
     lib.ocpx_get_field.argtypes = [P, C.c_int, P, C.c_size_t]
@@ -344,7 +351,9 @@ def model_and_grid_from_dump(arrays: dict, prefix: str = "model/"):
 class FimContext:
     """One GPU context holding the bulk state of a grid."""
 
-    def __init__(self, model: Model, grid: Grid, device: int = -1, variant: int = 0):
+    def __init__(self, model: Model, grid: Grid, device: int = -1, variant: int = 0, recompute: bool = False):
+        """``recompute``: keep no dSec_dPri; the Jacobian, GetSolution and
+        the wells recompute it from the flash's results (ocpx_options)."""
         self.lib = load_library()
         self.model = model
         self.grid = grid
@@ -358,8 +367,10 @@ class FimContext:
         md, k1 = model.desc()
         gd, k2 = grid.desc()
         h = C.c_void_p()
-        _check(self.lib.ocpx_create(C.byref(md), C.byref(gd), device, C.byref(h)))
+        opt = Options(C.sizeof(Options), 1 if recompute else 0)
+        _check(self.lib.ocpx_create_ex(C.byref(md), C.byref(gd), device, C.byref(opt), C.byref(h)))
         self.h = h
+        self.recompute = bool(recompute)
         if variant:
             self.set_variant(variant)
 
@@ -458,6 +469,8 @@ class FimContext:
             v = np.asarray(state[ref_name])
             if fid == "SKIP_ZI" and self.NC == 0:
                 continue
+            if fid == "DSEC_DPRI" and getattr(self, "recompute", False):
+                continue  # not stored: recomputed from the flash's results
             if v.size != self.field_size(fid):
                 continue
             self.set(fid, v)

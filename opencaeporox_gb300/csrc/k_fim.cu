@@ -95,6 +95,26 @@ __global__ void __launch_bounds__(128) k_jac_conn(const Model* __restrict__ M, B
     conn_jac_blocks<NCT>(*M, b, cv, c, dt, bmat + (size_t)c * 2 * bsize, bmat + ((size_t)c * 2 + 1) * bsize);
 }
 
+// The side blocks of the connections incident to the cells [c0, c1): one
+// thread per incidence entry (row_conn[row_ptr[c0] .. row_ptr[c1])), each the
+// block k_jac_conn computes for that side, from a copy of the side cell's
+// dSec_dPri at ds[k * soa + (cell - c0)].
+template <int NCT>
+__global__ void __launch_bounds__(128) k_jac_side(const Model* __restrict__ M, BulkView b, ConnView cv, double dt,
+                                                  int c0, uint32_t e0, uint32_t e1, const double* __restrict__ ds,
+                                                  size_t soa, double* __restrict__ bmat)
+{
+    const uint32_t e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= e1) return;
+    const uint32_t entry = cv.row_conn[e];
+    const int c = (int)(entry >> 1), side = (int)(entry & 1u);
+    ConnPhase q;
+    conn_phase(*M, b, cv, c, q);
+    const int cell = side ? q.eId : q.bId;
+    const int bsize = (b.nc + 1) * (b.nc + 1);
+    conn_jac_side<NCT>(b, q, side, ds + (cell - c0), soa, dt, bmat + ((size_t)c * 2 + side) * bsize);
+}
+
 // one warp per Jacobian block row
 __global__ void k_jac_rows(BulkView b, ConnView cv, const double* __restrict__ bmat, const uint32_t* __restrict__ rowptr,
                            double* __restrict__ val)
@@ -195,6 +215,23 @@ cudaError_t launch_jac_conn(int nct, const Model* dm, const BulkView& b, const C
     case 9: k_jac_conn<9><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
     case 11: k_jac_conn<11><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
     case 13: k_jac_conn<13><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+cudaError_t launch_jac_side(int nct, const Model* dm, const BulkView& b, const ConnView& cv, double dt, int c0,
+                            uint32_t e0, uint32_t e1, const double* ds, size_t soa, double* bmat, int block,
+                            cudaStream_t s)
+{
+    if (e1 <= e0) return cudaSuccess;
+    const int g = grid_for((int)(e1 - e0), block);
+    switch (nct) {
+    case 3: k_jac_side<3><<<g, block, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
+    case 5: k_jac_side<5><<<g, block, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
+    case 7: k_jac_side<7><<<g, block, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
+    case 9: k_jac_side<9><<<g, block, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
+    case 11: k_jac_side<11><<<g, block, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
+    case 13: k_jac_side<13><<<g, block, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -302,41 +302,19 @@ __global__ void __launch_bounds__(128) k_flash_post(const Model* __restrict__ M,
 
 // ---- flash derivatives recomputed where they are used (no dSec_dPri stored)
 
-// dSec_dPri of the cells list[t] (or first + t) into out[t][row * (nc + 1) + col]
+// dSec_dPri of the cells list[t] (or first + t): with soa = 0 into
+// out[t][row * (nc + 1) + col], else into out[(row * (nc + 1) + col) * soa + t]
 template <int NCM>
 __global__ void __launch_bounds__(128) k_dsec_cells(const Model* __restrict__ M, BulkView b, const int* __restrict__ list,
-                                                    int first, int n, double* __restrict__ out)
+                                                    int first, int n, double* __restrict__ out, size_t soa)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int cell = list ? list[t] : first + t;
     const int ncol = b.nc + 1, lend = b.np * ncol * ncol;
     CompCellUpdate<NCM> u;
-    u.recompute_dsec(*M, b, cell, out + (size_t)t * lend, 1);
-}
-
-// The connection Jacobian blocks owned by each cell: the cell recomputes its
-// dSec_dPri once, then writes the block of its side of every incident
-// connection (the same side block the stored form computes per connection).
-template <int NCM>
-__global__ void __launch_bounds__(128) k_jac_recompute(const Model* __restrict__ M, BulkView b, ConnView cv, double dt,
-                                                       double* __restrict__ bmat)
-{
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= b.nb) return;
-    if (cv.row_ptr[cell] == cv.row_ptr[cell + 1]) return;
-    constexpr int NCT = NCM + 1;
-    double ds[3 * (NCT + 1) * (NCT + 1)];
-    CompCellUpdate<NCM> u;
-    u.recompute_dsec(*M, b, cell, ds, 1);
-    const int ncol = b.nc + 1, bsize = ncol * ncol;
-    for (uint32_t k = cv.row_ptr[cell]; k < cv.row_ptr[cell + 1]; k++) {
-        const uint32_t e = cv.row_conn[k];
-        const int c = (int)(e >> 1), side = (int)(e & 1u);
-        ConnPhase q;
-        conn_phase(*M, b, cv, c, q);
-        conn_jac_side<NCT>(b, q, side, ds, 1, dt, bmat + ((size_t)c * 2 + side) * bsize);
-    }
+    if (soa) u.recompute_dsec(*M, b, cell, out + t, soa);
+    else u.recompute_dsec(*M, b, cell, out + (size_t)t * lend, 1);
 }
 
 // GetSolution with the cell's dSec_dPri recomputed before its state changes
@@ -544,15 +522,9 @@ cudaError_t OCPX_NAME(setup_flash_coop_)(int dev, int optin, int* excl_smem)
 
 #if OCPX_FLASH_PART == 7
 cudaError_t OCPX_NAME(launch_dsec_cells_)(const Model* dm, const BulkView& b, const int* list, int first, int n,
-                                          double* out, cudaStream_t s)
+                                          double* out, size_t soa, cudaStream_t s)
 {
-    if (n > 0) k_dsec_cells<OCPX_NCM><<<(n + 127) / 128, 128, 0, s>>>(dm, b, list, first, n, out);
-    return cudaGetLastError();
-}
-cudaError_t OCPX_NAME(launch_jac_recompute_)(const Model* dm, const BulkView& b, const ConnView& cv, double dt,
-                                             double* bmat, cudaStream_t s)
-{
-    if (b.nb > 0) k_jac_recompute<OCPX_NCM><<<(b.nb + 127) / 128, 128, 0, s>>>(dm, b, cv, dt, bmat);
+    if (n > 0) k_dsec_cells<OCPX_NCM><<<(n + 127) / 128, 128, 0, s>>>(dm, b, list, first, n, out, soa);
     return cudaGetLastError();
 }
 cudaError_t OCPX_NAME(launch_newton_update_recompute_)(const Model* dm, const BulkView& b, const double* u,

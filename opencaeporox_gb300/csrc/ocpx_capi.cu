@@ -64,10 +64,9 @@ cudaError_t setup_flash_batched(int ncm, int* excl_smem)
 }
 
 // the consumers of recomputed flash derivatives, one set per NCM
-#define OCPX_RECOMPUTE_DECL(N)                                                                                    \
-    cudaError_t launch_dsec_cells_##N(const Model*, const BulkView&, const int*, int, int, double*, cudaStream_t);  \
-    cudaError_t launch_jac_recompute_##N(const Model*, const BulkView&, const ConnView&, double, double*,          \
-                                         cudaStream_t);                                                            \
+#define OCPX_RECOMPUTE_DECL(N)                                                                                     \
+    cudaError_t launch_dsec_cells_##N(const Model*, const BulkView&, const int*, int, int, double*, size_t,          \
+                                      cudaStream_t);                                                                 \
     cudaError_t launch_newton_update_recompute_##N(const Model*, const BulkView&, const double*, double, cudaStream_t);
 OCPX_RECOMPUTE_DECL(4)
 OCPX_RECOMPUTE_DECL(6)
@@ -85,14 +84,9 @@ OCPX_RECOMPUTE_DECL(12)
     default: return cudaErrorInvalidValue;            \
     }
 cudaError_t launch_dsec_cells(int ncm, const Model* dm, const BulkView& b, const int* list, int first, int n,
-                              double* out, cudaStream_t s)
+                              double* out, size_t soa, cudaStream_t s)
 {
-    OCPX_NCM_SWITCH(launch_dsec_cells_, dm, b, list, first, n, out, s)
-}
-cudaError_t launch_jac_recompute(int ncm, const Model* dm, const BulkView& b, const ConnView& cv, double dt,
-                                 double* bmat, cudaStream_t s)
-{
-    OCPX_NCM_SWITCH(launch_jac_recompute_, dm, b, cv, dt, bmat, s)
+    OCPX_NCM_SWITCH(launch_dsec_cells_, dm, b, list, first, n, out, soa, s)
 }
 cudaError_t launch_newton_update_recompute(int ncm, const Model* dm, const BulkView& b, const double* u,
                                            double dSmax, cudaStream_t s)
@@ -133,6 +127,11 @@ int cap_nct(int nct)
     return -1;
 }
 
+// cells per slab when dSec_dPri is recomputed for the Jacobian: 524,288 cells
+// hold 1.5 GB of it at nc = 10 (the whole grid's would be 11.6 GB at
+// 4,000,000 cells), eight slabs on that grid
+constexpr int RECOMPUTE_SLAB_CELLS = 1 << 19;
+
 struct FieldInfo {
     void* dev;       // device SoA base (or cell-major for AoS-native fields)
     int n;           // entities (cells or connections)
@@ -151,8 +150,11 @@ struct ocpx_ctx {
     Model* d_model = nullptr;
     int nb = 0, nbI = 0, np = 3, nc = 0, nconn = 0, NC = 0, ncm = 0, nct_cap = 0;
     int variant = 0;
-    // dSec_dPri recomputed where it is used instead of stored (ocpx_options)
+    // dSec_dPri recomputed where it is used instead of stored (ocpx_options):
+    // the Jacobian recomputes it slab by slab, dsec_slab cells at a time
     bool recompute = false;
+    int dsec_slab = 0;
+    double* dsec_scratch = nullptr;
     // one arena for everything
     char* arena = nullptr;
     size_t arena_bytes = 0;
@@ -324,7 +326,8 @@ FieldInfo ocpx_ctx::field(ocpx_field f) const
     case OCPX_F_KR: return {b.kr, nb, np, 8, true, true};
     case OCPX_F_DKRDS: return {b.dKrdS, nb, np * np, 8, true, true};
     case OCPX_F_DPCDS: return {b.dPcdS, nb, np * np, 8, true, true};
-    case OCPX_F_DSEC_DPRI: return {b.dSec_dPri, nb, lend, 8, true, !recompute};
+    // recomputed on reads when not stored (field_transfer); dev then only marks the field as known
+    case OCPX_F_DSEC_DPRI: return {recompute ? (void*)b.njhc : (void*)b.dSec_dPri, nb, lend, 8, true, !recompute};
     case OCPX_F_PORO: return {b.poro, nb, 1, 8, true, true};
     case OCPX_F_POROP: return {b.poroP, nb, 1, 8, true, true};
     case OCPX_F_ROCKVP: return {b.rockVp, nb, 1, 8, true, true};
@@ -561,6 +564,10 @@ ocpx_status ocpx_create_ex(const ocpx_model_desc* md, const ocpx_grid_desc* gd, 
     // checkpoints keep them)
     if (recompute) add(&b.njhc, D * 2);
     else add(&b.dSec_dPri, D * lend);
+    if (recompute) {
+        ctx->dsec_slab = std::min(nb, RECOMPUTE_SLAB_CELLS);
+        add(&ctx->dsec_scratch, sizeof(double) * (size_t)ctx->dsec_slab * lend);
+    }
     add(&b.poro, D); add(&b.poroP, D); add(&b.rockVp, D);
     add(&b.skip_flag, (size_t)nb); add(&b.skip_minEig, D); add(&b.skip_P, D); add(&b.skip_T, D);
     add(&b.skip_zi, D * (ctx->NC > 0 ? ctx->NC : 1));
@@ -706,6 +713,8 @@ uint64_t ocpx_launch_count(ocpx_ctx* ctx) { return ctx ? ctx->launches : 0; }
 ocpx_status ocpx_set_field(ocpx_ctx* ctx, ocpx_field f, const void* host, size_t count)
 {
     if (!ctx || !host) return fail(OCPX_INVALID_ARG, "null argument");
+    if (f == OCPX_F_DSEC_DPRI && ctx->recompute)
+        return fail(OCPX_INVALID_ARG, "dSec_dPri is recomputed, not stored: it cannot be set");
     const FieldInfo fi = ctx->field(f);
     if (!fi.dev || !fi.writable) return fail(OCPX_INVALID_ARG, "field not writable: " + std::to_string((int)f));
     const size_t expect = (size_t)fi.n * fi.width;
@@ -746,7 +755,7 @@ ocpx_status field_transfer(ocpx_ctx* ctx, ocpx_field f, size_t first, size_t n, 
         for (size_t k = 0; k < n; k += chunk) {
             const size_t m = std::min(chunk, n - k);
             OCPX_CUDA(launch_dsec_cells(ctx->ncm, ctx->d_model, ctx->b, nullptr, (int)(first + k), (int)m,
-                                        (double*)ctx->staging, ctx->stream));
+                                        (double*)ctx->staging, 0, ctx->stream));
             ctx->launches++;
             OCPX_CUDA(cudaMemcpyAsync((double*)host + k * lend, ctx->staging, sizeof(double) * m * lend,
                                       cudaMemcpyDeviceToHost, ctx->stream));
@@ -977,7 +986,7 @@ ocpx_status enqueue_calres(ocpx_ctx* ctx, double dt)
         // CalResFIM of every well after the bulk rows, then the norms
         if (ctx->recompute) {
             OCPX_CUDA(launch_dsec_cells(ctx->ncm, ctx->d_model, ctx->b, ctx->ws.pc_cell, 0, ctx->ws.npc, ctx->ws.dsec,
-                                        s));
+                                        0, s));
             ctx->launches++;
         }
         OCPX_CUDA(launch_wells_res(ctx->b, ctx->ws, dt, ctx->res, ctx->resRelV, ctx->resRelN, ctx->rownorm, s));
@@ -994,10 +1003,23 @@ ocpx_status enqueue_assemble(ocpx_ctx* ctx, double dt)
 {
     cudaStream_t s = ctx->stream;
     int mk = ctx->stage_begin(6);
-    if (ctx->recompute)
-        OCPX_CUDA(launch_jac_recompute(ctx->ncm, ctx->d_model, ctx->b, ctx->cv, dt, ctx->bmat, s));
-    else
+    if (ctx->recompute) {
+        // slab by slab: the slab's dSec_dPri into the scratch, then the side
+        // blocks of the slab's cells
+        for (int c0 = 0; c0 < ctx->nb; c0 += ctx->dsec_slab) {
+            const int n = std::min(ctx->dsec_slab, ctx->nb - c0);
+            OCPX_CUDA(launch_dsec_cells(ctx->ncm, ctx->d_model, ctx->b, nullptr, c0, n, ctx->dsec_scratch,
+                                        (size_t)n, s));
+            OCPX_CUDA(launch_jac_side(ctx->nct_cap, ctx->d_model, ctx->b, ctx->cv, dt, c0, ctx->h_row_ptr[c0],
+                                      ctx->h_row_ptr[c0 + n], ctx->dsec_scratch, (size_t)n, ctx->bmat,
+                                      ctx->block_conn, s));
+            ctx->launches += 2;
+        }
+        ctx->launches--;  // counted once below
+    }
+    else {
         OCPX_CUDA(launch_jac_conn(ctx->nct_cap, ctx->d_model, ctx->b, ctx->cv, dt, ctx->bmat, ctx->block_conn, s));
+    }
     ctx->stage_end(mk);
     mk = ctx->stage_begin(7);
     OCPX_CUDA(launch_jac_rows(ctx->b, ctx->cv, ctx->bmat, ctx->jac_rowptr, ctx->jac_val, ctx->block_cell, s));

@@ -58,12 +58,15 @@ cudaError_t launch_flash_batched(int ncm, const Model* dm, const BulkView& b, co
                                  const FlashBatch& fb, int part, cudaStream_t s);
 // Flash derivatives recomputed where they are used (k_flash_comp.cu, part 7):
 // dSec_dPri of a list of cells (list NULL: first .. first + n - 1) into
-// out[t][np*(nc+1)^2]; the connection Jacobian blocks, each cell writing the
-// blocks of its side of its connections; GetSolution.
+// out[t][np*(nc+1)^2] (soa = 0) or out[k * soa + t]; GetSolution.
 cudaError_t launch_dsec_cells(int ncm, const Model* dm, const BulkView& b, const int* list, int first, int n,
-                              double* out, cudaStream_t s);
-cudaError_t launch_jac_recompute(int ncm, const Model* dm, const BulkView& b, const ConnView& cv, double dt,
-                                 double* bmat, cudaStream_t s);
+                              double* out, size_t soa, cudaStream_t s);
+// The connection blocks of the sides whose cell lies in [c0, c1) (incidence
+// entries [e0, e1) = [row_ptr[c0], row_ptr[c1])), from those cells'
+// dSec_dPri at ds[k * soa + (cell - c0)] (k_fim.cu)
+cudaError_t launch_jac_side(int nct, const Model* dm, const BulkView& b, const ConnView& cv, double dt, int c0,
+                            uint32_t e0, uint32_t e1, const double* ds, size_t soa, double* bmat, int block,
+                            cudaStream_t s);
 cudaError_t launch_newton_update_recompute(int ncm, const Model* dm, const BulkView& b, const double* u,
                                            double dSmax, cudaStream_t s);
 // Cells grouped by flash path (two-phase, one-phase, skip-flagged) and, within

@@ -38,6 +38,7 @@ def lib(variant="exact"):
         L.oc_newton_update.argtypes = [P, P, P, C.c_double]
         if variant == "ulp":
             L.oc_set_nudge_seed.argtypes = [C.c_uint64]
+            L.oc_set_nudge_ulps.argtypes = [C.c_int]
         _libs[variant] = L
     return _libs[variant]
 
@@ -110,9 +111,11 @@ class OracleBulk:
         self.resRelN = np.zeros(self.nb)
         self.norms = np.zeros(4)
 
-    def set_nudge_seed(self, seed: int):
-        """Seed of the one-ulp perturbation pattern (variant "ulp" only)."""
+    def set_nudge_seed(self, seed: int, ulps: int = 1):
+        """Seed of the perturbation pattern and the ulps each transcendental
+        result moves (variant "ulp" only)."""
         self.lib.oc_set_nudge_seed(seed)
+        self.lib.oc_set_nudge_ulps(ulps)
 
     def load(self, state: dict):
         for k, v in state.items():

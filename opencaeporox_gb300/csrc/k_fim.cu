@@ -251,27 +251,57 @@ __device__ __forceinline__ int cost_level(long long w)
     return l < 0 ? 0 : (l > 63 ? 63 : l);
 }
 
-// Sort key of a cell for the batched flash: its class (skip-flagged cells,
-// which usually skip the equilibrium; two-phase cells, which run the split
-// and the two-phase derivatives; one-phase cells, which run the stability
-// test), then the work level its last flash used (iteration counters weighted
-// as the flash's budget charges them, Rachford-Rice iterations at a fifth), in
-// descending order.  Warps then hold cells on the same code path.
-__device__ __forceinline__ int cost_bucket(const BulkView& b, int cell)
+// The flash type a cell's flash starts from (SkipPSAMethod01::CalFtype02 /
+// IfSkip on the current state: 1 skips the equilibrium, 2 goes to the split,
+// 0 runs the stability test) and the work the cell is predicted to need: the
+// work its last flash used on the segments this type runs (none when it
+// skips, the split's when it goes to the split, all otherwise).  A cell whose
+// skip test fails now runs the equilibrium its flag promised to spare.
+__device__ long long predicted_work_now(const Model& M, const BulkView& b, int cell, int& ftype_in, unsigned& npPE)
 {
-    const int lvl = cost_level(predicted_work(b, cell));
-    const bool two = b.phaseExist[b.idx(0, cell)] && b.phaseExist[b.idx(1, cell)];
-    const int cls = b.skip_flag[cell] ? 2 : (two ? 0 : 1);
+    const CompModel& m = M.comp;
+    const int NC = m.nc, np = b.np;
+    double Ni[NC_MAX + 1], Sin[3];
+    for (int i = 0; i <= NC; i++) Ni[i] = b.Ni[b.idx(i, cell)];
+    unsigned phaseNum = 0;
+    for (int j = 0; j < np; j++) {
+        Sin[j] = b.S[b.idx(j, cell)];
+        if (b.phaseExist[b.idx(j, cell)]) phaseNum++;
+    }
+    double Nt = 0;
+    for (int i = 0; i < NC; i++) Nt += Ni[i];
+    const double P = b.P[cell], T = b.T[cell] + M.units.conv4;
+    npPE = phaseNum - 1u;
+    ftype_in = flash_type_in(m, b, cell, Ni, Nt, P, T, Sin, npPE);
+    if (ftype_in == 1) return 3;
+    const int32_t* it = b.iters;
+    if (ftype_in == 2)
+        return 3LL + WORK_SSM_SP * (long long)it[b.idx(2, cell)] + WORK_NR_SP * (long long)it[b.idx(3, cell)] +
+               it[b.idx(4, cell)] / 5;
+    return predicted_work(b, cell);
+}
+
+// Sort key of a cell for the batched flash: its class by the flash type it
+// starts from (cells that skip the equilibrium; cells that go to the split and
+// the two-phase derivatives; cells that run the stability test), then its
+// predicted work level (predicted_work_now), in descending order.  Warps then
+// hold cells on the same code path with similar work.
+__device__ __forceinline__ int cost_bucket(const Model& M, const BulkView& b, int cell)
+{
+    int ftype_in;
+    unsigned npPE;
+    const int lvl = cost_level(predicted_work_now(M, b, cell, ftype_in, npPE));
+    const int cls = ftype_in == 1 ? 2 : (ftype_in == 2 ? 0 : 1);
     return cls * 64 + (63 - lvl);
 }
 
-__global__ void k_cost_hist(BulkView b, unsigned* __restrict__ hist)
+__global__ void k_cost_hist(const Model* __restrict__ M, BulkView b, unsigned* __restrict__ hist)
 {
     __shared__ unsigned h[COST_BUCKETS];
     for (int k = threadIdx.x; k < COST_BUCKETS; k += blockDim.x) h[k] = 0;
     __syncthreads();
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell < b.nb) atomicAdd(&h[cost_bucket(b, cell)], 1u);
+    if (cell < b.nb) atomicAdd(&h[cost_bucket(*M, b, cell)], 1u);
     __syncthreads();
     for (int k = threadIdx.x; k < COST_BUCKETS; k += blockDim.x)
         if (h[k]) atomicAdd(&hist[k], h[k]);
@@ -319,32 +349,33 @@ __global__ void k_cost_scan(unsigned* __restrict__ hist, unsigned coop_cells, lo
     hist[t] = v[t] - hist[t];
 }
 
-__global__ void k_cost_scatter(BulkView b, unsigned* __restrict__ offs, int* __restrict__ order)
+__global__ void k_cost_scatter(const Model* __restrict__ M, BulkView b, unsigned* __restrict__ offs,
+                               int* __restrict__ order)
 {
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= b.nb) return;
-    const unsigned pos = atomicAdd(&offs[cost_bucket(b, cell)], 1u);
+    const unsigned pos = atomicAdd(&offs[cost_bucket(*M, b, cell)], 1u);
     order[pos] = cell;
 }
 
-cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, unsigned coop_cells, long long wt,
-                              int* level, cudaStream_t s)
+cudaError_t launch_cost_order(const Model* dm, const BulkView& b, unsigned* hist, int* order, unsigned coop_cells,
+                              long long wt, int* level, cudaStream_t s)
 {
     if (!b.nb) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned) * COST_BUCKETS, s);
     if (e != cudaSuccess) return e;
     const int block = 256;
-    k_cost_hist<<<grid_for(b.nb, block), block, 0, s>>>(b, hist);
+    k_cost_hist<<<grid_for(b.nb, block), block, 0, s>>>(dm, b, hist);
     k_cost_scan<<<1, COST_BUCKETS, 0, s>>>(hist, coop_cells, wt, level);
-    k_cost_scatter<<<grid_for(b.nb, block), block, 0, s>>>(b, hist, order);
+    k_cost_scatter<<<grid_for(b.nb, block), block, 0, s>>>(dm, b, hist, order);
     return cudaGetLastError();
 }
 
-// Cells whose last flash used more than `threshold` work units, and whose
-// work level is at or above the adaptive level, are handed to the cooperative
-// kernel before the per-cell kernel runs, so that both run at the same time
-// (pre[cell] = 1).  Cells that the skip test will let through
-// (flash type 1) stay with the per-cell kernel.  Thread q visits the q-th cell
+// Cells predicted to need more than `threshold` work units
+// (predicted_work_now), and whose work level is at or above the adaptive
+// level, are handed to the cooperative kernel before the per-cell kernel
+// runs, so that both run at the same time (pre[cell] = 1).  Cells that the
+// skip test will let through (flash type 1) stay with the per-cell kernel.  Thread q visits the q-th cell
 // of the cost order taken level by level (all classes of the highest level
 // first), so the list comes out roughly heaviest first whatever the class, and
 // the cooperative warps, which take list slots in order, start with the
@@ -387,22 +418,10 @@ __global__ void k_predefer(const Model* __restrict__ M, BulkView b, const int* _
     if (p < 0) return;  // not reached: the buckets hold every cell once
     const int cell = order[p];
     pre[cell] = 0;
-    const long long w = predicted_work(b, cell);
+    int ftype_in;
+    unsigned npPE;
+    const long long w = predicted_work_now(*M, b, cell, ftype_in, npPE);
     if (w <= threshold || cost_level(w) < level[0]) return;
-    const CompModel& m = M->comp;
-    const int NC = m.nc, np = b.np;
-    double Ni[NC_MAX + 1], Sin[3];
-    for (int i = 0; i <= NC; i++) Ni[i] = b.Ni[b.idx(i, cell)];
-    unsigned phaseNum = 0;
-    for (int j = 0; j < np; j++) {
-        Sin[j] = b.S[b.idx(j, cell)];
-        if (b.phaseExist[b.idx(j, cell)]) phaseNum++;
-    }
-    double Nt = 0;
-    for (int i = 0; i < NC; i++) Nt += Ni[i];
-    const double P = b.P[cell], T = b.T[cell] + M->units.conv4;
-    const unsigned npPE = phaseNum - 1u;
-    const int ftype_in = flash_type_in(m, b, cell, Ni, Nt, P, T, Sin, npPE);
     if (ftype_in == 1) return;
     if (sink.push(cell, ftype_in, npPE)) pre[cell] = 1;
 }

@@ -840,7 +840,7 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             // the count and position counter of re-budgeting round r; [32..34] the fused kernel's
             OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned) * 40, s));
             mk = ctx->stage_begin(9);
-            OCPX_CUDA(launch_cost_order(ctx->b, ctx->cost_hist, ctx->order, (unsigned)ctx->coop_cells,
+            OCPX_CUDA(launch_cost_order(ctx->d_model, ctx->b, ctx->cost_hist, ctx->order, (unsigned)ctx->coop_cells,
                                         pre ? ctx->predefer : (long long)ctx->flash_budget, ctx->adapt_level, s));
             ctx->launches += 3;
             if (pre) {

@@ -69,16 +69,17 @@ cudaError_t launch_jac_side(int nct, const Model* dm, const BulkView& b, const C
                             cudaStream_t s);
 cudaError_t launch_newton_update_recompute(int ncm, const Model* dm, const BulkView& b, const double* u,
                                            double dSmax, cudaStream_t s);
-// Cells grouped by flash path (two-phase, one-phase, skip-flagged) and, within
-// a group, in descending order of the work their last flash needed, by a
-// counting sort over COST_BUCKETS buckets.
+// Cells grouped by the flash type they start from (split, stability test,
+// skip) and, within a group, in descending order of their predicted work, by
+// a counting sort over COST_BUCKETS buckets.
 constexpr int COST_BUCKETS = 256;
 // level[0] receives the adaptive work level (see k_cost_scan); wt is the
 // deferral threshold in work units
-cudaError_t launch_cost_order(const BulkView& b, unsigned* hist, int* order, unsigned coop_cells, long long wt,
-                              int* level, cudaStream_t s);
-// hand the cells whose last flash used more than `threshold` work units, at or
-// above the adaptive level, to the cooperative kernel up front (pre[cell] = 1),
+cudaError_t launch_cost_order(const Model* dm, const BulkView& b, unsigned* hist, int* order, unsigned coop_cells,
+                              long long wt, int* level, cudaStream_t s);
+// hand the cells predicted to need more than `threshold` work units (the work
+// their last flash used on the segments this flash's type runs), at or above
+// the adaptive level, to the cooperative kernel up front (pre[cell] = 1),
 // visiting cells in `order`
 // bucket_end: launch_cost_order's bucket counts after it ran (the end of each
 // bucket in the order)

@@ -41,7 +41,12 @@ def outputs(ctx):
 
 def same(a, b, what):
     for k in a:
-        assert np.array_equal(a[k], b[k], equal_nan=True), f"{what}: {k} differs"
+        x, y = np.asarray(a[k]), np.asarray(b[k])
+        if np.array_equal(x, y, equal_nan=True):
+            continue
+        bad = np.nonzero(~((x == y) | (np.isnan(x) & np.isnan(y))))[0] if x.shape == y.shape else []
+        raise AssertionError(f"{what}: {k} differs at {len(bad)} of {x.size} entries {bad[:12]}: "
+                             f"{x[bad[:4]]} vs {y[bad[:4]]}")
 
 
 def first_it(fx):
@@ -191,8 +196,11 @@ def test_memory_and_refusals(gpu_lib):
     lend = 3 * (nc + 1) ** 2
     with fim.FimContext(model, grid) as st, fim.FimContext(model, grid, recompute=True) as rc:
         saved = st.get_param("device_bytes") - rc.get_param("device_bytes")
-        # dSec_dPri and its staging copy, less the phase mole numbers (256-byte alignment aside)
-        assert saved >= 2 * 8 * nb * lend - 8 * nb * max(3 * nc, 9, 5) - 2 * 8 * nb - 4096
+        # dSec_dPri and its staging copy, less the phase mole numbers, the
+        # smaller staging buffer and the slab scratch (here one slab: the whole
+        # grid), 256-byte alignment aside
+        slab = min(nb, 1 << 19)
+        assert saved >= 2 * 8 * nb * lend - 8 * nb * max(3 * nc, 9, 5) - 2 * 8 * nb - 8 * slab * lend - 4096
         with pytest.raises(RuntimeError, match="recomputed"):
             rc.set("DSEC_DPRI", np.zeros(nb * lend))
     bo = P.load_fixture("bo_10x10x3")

@@ -451,10 +451,14 @@ ocpx_status build_system(ocpx_ctx* ctx, std::vector<uint32_t>* slot_bw, std::vec
     ctx->jac_val = (double*)(ctx->sys + o_val);
     ctx->jac_nnz = nnz;
     ctx->nrow = nbI + nw;
-    OCPX_CUDA(cudaMemset(ctx->sys, 0, o_val));
-    OCPX_CUDA(cudaMemcpy(ctx->jac_rowptr, jrow.data(), sizeof(uint32_t) * jrow.size(), cudaMemcpyHostToDevice));
-    OCPX_CUDA(cudaMemcpy(ctx->jac_col, jcol.data(), sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice));
-    OCPX_CUDA(cudaMemcpy(ctx->jac_slot, jslot.data(), sizeof(uint32_t) * jslot.size(), cudaMemcpyHostToDevice));
+    // on the context's stream, which does not wait for the legacy stream
+    OCPX_CUDA(cudaMemsetAsync(ctx->sys, 0, o_val, ctx->stream));
+    OCPX_CUDA(cudaMemcpyAsync(ctx->jac_rowptr, jrow.data(), sizeof(uint32_t) * jrow.size(), cudaMemcpyHostToDevice,
+                              ctx->stream));
+    OCPX_CUDA(cudaMemcpyAsync(ctx->jac_col, jcol.data(), sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice, ctx->stream));
+    OCPX_CUDA(cudaMemcpyAsync(ctx->jac_slot, jslot.data(), sizeof(uint32_t) * jslot.size(), cudaMemcpyHostToDevice,
+                              ctx->stream));
+    OCPX_CUDA(cudaStreamSynchronize(ctx->stream));
     if (ctx->ls_scratch) {  // the solver's work space is sized by the rows
         cudaFree(ctx->ls_scratch);
         ctx->ls_scratch = nullptr;
@@ -1448,7 +1452,10 @@ ocpx_status ocpx_set_wells(ocpx_ctx* ctx, int nwell, const ocpx_well* wells)
     if (!ctx->wbuf) {
         OCPX_CUDA(cudaMalloc(&ctx->wbuf, off));
         ctx->wbuf_bytes = off;
-        OCPX_CUDA(cudaMemset(ctx->wbuf, 0, off));
+        // on the context's stream: a plain cudaMemset runs on the legacy
+        // stream, which the context's non-blocking stream does not wait for,
+        // and could clear the copies below after they land
+        OCPX_CUDA(cudaMemsetAsync(ctx->wbuf, 0, off, ctx->stream));
     }
     char* B = ctx->wbuf;
     WellSys& ws = ctx->ws;

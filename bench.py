@@ -865,19 +865,21 @@ def run_fim(args, wl, rt, local, rank, world):
     flush_bytes = 512 << 20
     flush = (rt.malloc(flush_bytes), flush_bytes)
     # plain form: fewer steps on the large grid, where one takes seconds
-    t0 = time.perf_counter()
     recompute = args.flash_der == "recompute"
-    ctx0, _ = prepare(wl, model, grid, 0, local, recompute)
-    log(f"{wl.key}: plain form set up in {time.perf_counter() - t0:.1f} s")
     p_steps, p_warm = (min(args.steps, 3), 1) if large else (args.steps, args.warmup)
-    ranks.barrier(rt)
-    t_plain, _ = time_device(ctx0, rt, p_steps, p_warm, flush)
-    ranks.barrier(rt)
-    plain_ms = ranks.max(statistics.median(t_plain))
-    plain_prof = stage_profile(ctx0, rt, flush)
-    log(f"{wl.key}: plain step {plain_ms:.1f} ms")
-    ctx0.close()
-    del ctx0
+    plain_ms, plain_prof = float("nan"), {}
+    if not args.no_plain:
+        t0 = time.perf_counter()
+        ctx0, _ = prepare(wl, model, grid, 0, local, recompute)
+        log(f"{wl.key}: plain form set up in {time.perf_counter() - t0:.1f} s")
+        ranks.barrier(rt)
+        t_plain, _ = time_device(ctx0, rt, p_steps, p_warm, flush)
+        ranks.barrier(rt)
+        plain_ms = ranks.max(statistics.median(t_plain))
+        plain_prof = stage_profile(ctx0, rt, flush)
+        log(f"{wl.key}: plain step {plain_ms:.1f} ms")
+        ctx0.close()
+        del ctx0
     # batched form
     t0 = time.perf_counter()
     ctx, u2 = prepare(wl, model, grid, 1, local, recompute)
@@ -998,6 +1000,8 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner (library defaults)")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the timed step")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain form's leg (to profile the batched step alone)")
     ap.add_argument("--parity-dump", default=None, help="write the cells above 1e-10 in the parity check to this .npz")
     ap.add_argument("--flash-der", default="store", choices=["store", "recompute"],
                     help="keep dSec_dPri, or recompute it where it is used (ocpx_options)")

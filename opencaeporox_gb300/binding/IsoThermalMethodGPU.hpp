@@ -169,8 +169,14 @@ public:
     void CreateContext(const Reservoir& rs, int device = -1)
     {
         desc.describe(rs);
-        ocpx_check(ocpx_create(&desc.model, &desc.grid, device, &ctx), "ocpx_create");
+        ocpx_options opt{};
+        opt.struct_size = sizeof(opt);
+        opt.recompute_flash_der = recompute_flash_der ? 1 : 0;
+        ocpx_check(ocpx_create_ex(&desc.model, &desc.grid, device, &opt, &ctx), "ocpx_create_ex");
     }
+    // before Setup: keep no dSec_dPri on the device, recompute it where it is
+    // used (compositional models; bit-identical results, less device memory)
+    void SetRecomputeFlashDer(bool on) { recompute_flash_der = on; }
     // the host's bulk state to the device (after InitReservoir, or whenever
     // the host changed it)
     void Upload(const BulkVarSet& b)
@@ -260,4 +266,5 @@ private:
     }
     OcpxDescription desc;
     ocpx_ctx* ctx = nullptr;
+    bool recompute_flash_der = false;
 };

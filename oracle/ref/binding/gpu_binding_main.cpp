@@ -8,7 +8,9 @@
 // runs one property update and residual on the device and compares the
 // residual with the reference's own CalRes on the same state.
 //
-//   ocp_gpu_binding <deck> [<deck>.ptn_ni]   exit 0: context created or OCPX_NO_DEVICE; 2: other status
+//   ocp_gpu_binding <deck> [--recompute]   exit 0: context created or OCPX_NO_DEVICE; 2: other status
+//   (PTN moles from "<deck>.ptn_ni" when present; --recompute: a context that
+//   recomputes the flash derivatives instead of storing them)
 #include "IsoThermalMethodGPU.hpp"
 
 #include "OCP.hpp"
@@ -34,6 +36,7 @@ int main(int argc, char* argv[])
     Reservoir& rs = sim.reservoir;
     IsoT_FIM& fim = sim.solver.IsoTSolver.fim;
     IsoT_FIM_GPU gpu;
+    if (argc > 2 && std::string(argv[2]) == "--recompute") gpu.SetRecomputeFlashDer(true);
     int rc = 0;
     try {
         gpu.CreateContext(rs);

@@ -43,3 +43,25 @@ def test_binding_describes_the_reference_model(tmp_path, case):
     assert f"description nb {nb} nbI {nb} nconn {nconn} nc {nc} mixture {mixture}" in r.stdout, r.stdout
     # this machine has no CUDA device: the descriptions passed the library's checks
     assert "status OCPX_NO_DEVICE" in r.stdout or "status OCPX_OK" in r.stdout, r.stdout
+
+
+@pytest.mark.parametrize("case", ["blackoil", "comp6"])
+def test_binding_recompute_option(tmp_path, case):
+    """IsoT_FIM_GPU::SetRecomputeFlashDer: a compositional deck passes the
+    library's checks with the option (OCPX_NO_DEVICE here), a black-oil deck
+    is refused (it has no flash to recompute from)."""
+    import decks
+    exe = _binding()
+    deck = tmp_path / "case.data"
+    if case == "blackoil":
+        deck.write_text(decks.blackoil_deck(seed=1))
+    else:
+        ni, text = decks.comp_deck(4, 3, 2, 6, seed=2)
+        deck.write_text(text)
+        ni.astype("<f8").tofile(str(deck) + ".ptn_ni")
+    r = subprocess.run([exe, str(deck), "--recompute"], capture_output=True, text=True, timeout=300, cwd=tmp_path)
+    if case == "blackoil":
+        assert r.returncode == 2 and "OCPX_INVALID_ARG" in r.stdout and "compositional" in r.stdout, r.stdout
+    else:
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "status OCPX_NO_DEVICE" in r.stdout or "status OCPX_OK" in r.stdout, r.stdout

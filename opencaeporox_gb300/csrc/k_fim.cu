@@ -85,14 +85,72 @@ __global__ void k_norm_reduce(const RowNorm* __restrict__ rn, int nb, RowNorm* _
     }
 }
 
+// The code path of a connection's blocks: per phase whether it flows (it
+// exists in its upwind cell), whether the bId side is upwind, and whether the
+// downwind cell holds the phase too (3 bits a phase).
+constexpr int CONN_CLASSES = 512;
+__device__ __forceinline__ int conn_class(const BulkView& b, const ConnView& cv, int c)
+{
+    const uint32_t bId = cv.bId[c], eId = cv.eId[c];
+    int key = 0;
+    for (int j = 0; j < b.np && j < 3; j++) {
+        const uint32_t u = cv.upblock[j * cv.nconn + c];
+        if (!b.phaseExist[b.idx(j, (int)u)]) continue;
+        const uint32_t d = (u == bId) ? eId : bId;
+        key |= (1 | ((u == bId) << 1) | ((b.phaseExist[b.idx(j, (int)d)] != 0) << 2)) << (3 * j);
+    }
+    return key;
+}
+
+// The connection blocks of a tile of JAC_TILE consecutive connections per
+// block of 128 threads: the tile is first sorted by code path (a counting
+// sort in shared memory), then each warp takes 32 consecutive connections of
+// the sorted tile, so its lanes take the same branches.  Every connection's
+// blocks are computed by conn_jac_blocks as before; only which thread computes
+// them changes.
+constexpr int JAC_TILE = 1024;
 template <int NCT>
 __global__ void __launch_bounds__(128) k_jac_conn(const Model* __restrict__ M, BulkView b, ConnView cv, double dt,
                                                   double* __restrict__ bmat)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= cv.nconn) return;
+    __shared__ unsigned cnt[CONN_CLASSES];
+    __shared__ unsigned short key_s[JAC_TILE];
+    __shared__ unsigned short idx_s[JAC_TILE];
+    const int t = threadIdx.x;
+    const int c0 = blockIdx.x * JAC_TILE;
+    const int n = min(JAC_TILE, cv.nconn - c0);
+    for (int k = t; k < CONN_CLASSES; k += blockDim.x) cnt[k] = 0;
+    __syncthreads();
+    for (int i = t; i < n; i += blockDim.x) {
+        const int key = conn_class(b, cv, c0 + i);
+        key_s[i] = (unsigned short)key;
+        atomicAdd(&cnt[key], 1u);
+    }
+    __syncthreads();
+    if (t < 32) {  // exclusive scan of the class counts, 16 per lane
+        constexpr int PER = CONN_CLASSES / 32;
+        unsigned part = 0;
+        for (int k = 0; k < PER; k++) part += cnt[t * PER + k];
+        unsigned incl = part;
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned v = __shfl_up_sync(0xffffffffu, incl, d);
+            if (t >= d) incl += v;
+        }
+        unsigned run = incl - part;
+        for (int k = 0; k < PER; k++) {
+            const unsigned v = cnt[t * PER + k];
+            cnt[t * PER + k] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    for (int i = t; i < n; i += blockDim.x) idx_s[atomicAdd(&cnt[key_s[i]], 1u)] = (unsigned short)i;
+    __syncthreads();
     const int bsize = (b.nc + 1) * (b.nc + 1);
-    conn_jac_blocks<NCT>(*M, b, cv, c, dt, bmat + (size_t)c * 2 * bsize, bmat + ((size_t)c * 2 + 1) * bsize);
+    for (int i = t; i < n; i += blockDim.x) {
+        const int c = c0 + idx_s[i];
+        conn_jac_blocks<NCT>(*M, b, cv, c, dt, bmat + (size_t)c * 2 * bsize, bmat + ((size_t)c * 2 + 1) * bsize);
+    }
 }
 
 // The side blocks of the connections incident to the cells [c0, c1): one
@@ -207,14 +265,15 @@ cudaError_t launch_jac_conn(int nct, const Model* dm, const BulkView& b, const C
                             int block, cudaStream_t s)
 {
     if (!cv.nconn) return cudaSuccess;
-    const int g = grid_for(cv.nconn, block);
+    (void)block;  // tiles of JAC_TILE connections on 128 threads
+    const int g = (cv.nconn + JAC_TILE - 1) / JAC_TILE;
     switch (nct) {
-    case 3: k_jac_conn<3><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
-    case 5: k_jac_conn<5><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
-    case 7: k_jac_conn<7><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
-    case 9: k_jac_conn<9><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
-    case 11: k_jac_conn<11><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
-    case 13: k_jac_conn<13><<<g, block, 0, s>>>(dm, b, cv, dt, bmat); break;
+    case 3: k_jac_conn<3><<<g, 128, 0, s>>>(dm, b, cv, dt, bmat); break;
+    case 5: k_jac_conn<5><<<g, 128, 0, s>>>(dm, b, cv, dt, bmat); break;
+    case 7: k_jac_conn<7><<<g, 128, 0, s>>>(dm, b, cv, dt, bmat); break;
+    case 9: k_jac_conn<9><<<g, 128, 0, s>>>(dm, b, cv, dt, bmat); break;
+    case 11: k_jac_conn<11><<<g, 128, 0, s>>>(dm, b, cv, dt, bmat); break;
+    case 13: k_jac_conn<13><<<g, 128, 0, s>>>(dm, b, cv, dt, bmat); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -4,6 +4,8 @@
 #include "conn_ops.cuh"
 #include "adjoint.cuh"
 
+#include <algorithm>
+
 namespace ocpx {
 
 __global__ void k_flash_bo(const Model* __restrict__ M, BulkView b)
@@ -48,19 +50,27 @@ __global__ void k_residual(BulkView b, ConnView cv, double dt, double* __restric
     if (n < b.nbI) cell_residual(b, cv, n, dt, res, resRelV, resRelN, rn + n);
 }
 
-// Global maxima with the reference's tie rule (first cell in index order wins),
-// one block; loops over all cells with a strided pattern.
+// Global maxima with the reference's tie rule (the first cell in index order
+// wins a tie: IsoT_FIM::CalRes keeps a maximum unless a later cell exceeds it).
+// Value first, then the smaller cell index, so any order of combination gives
+// the same result.
+__device__ __forceinline__ bool norm_better(double v, int i, double bestv, int besti)
+{
+    return i >= 0 && (besti < 0 || v > bestv || (v == bestv && i < besti));
+}
+
+// Pass 1 (gridDim.x blocks): each block's maxima over a grid-stride share of
+// the rows into out[blockIdx.x]; pass 2 (one block) over those partials.
 __global__ void k_norm_reduce(const RowNorm* __restrict__ rn, int nb, RowNorm* __restrict__ out)
 {
     __shared__ double sv[256], sn[256];
     __shared__ int iv[256], in_[256];
     double mv = 0, mN = 0;
     int bv = -1, bn = -1;
-    for (int n = threadIdx.x; n < nb; n += blockDim.x) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nb; n += gridDim.x * blockDim.x) {
         const RowNorm r = rn[n];
-        // strict ">" in index order as in IsoT_FIM::CalRes: ties keep the first cell
-        if (r.idV >= 0 && (bv < 0 || r.maxV > mv)) { mv = r.maxV; bv = r.idV; }
-        if (r.idN >= 0 && (bn < 0 || r.maxN > mN)) { mN = r.maxN; bn = r.idN; }
+        if (norm_better(r.maxV, r.idV, mv, bv)) { mv = r.maxV; bv = r.idV; }
+        if (norm_better(r.maxN, r.idN, mN, bn)) { mN = r.maxN; bn = r.idN; }
     }
     sv[threadIdx.x] = mv; iv[threadIdx.x] = bv;
     sn[threadIdx.x] = mN; in_[threadIdx.x] = bn;
@@ -68,20 +78,24 @@ __global__ void k_norm_reduce(const RowNorm* __restrict__ rn, int nb, RowNorm* _
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s) {
             const int o = threadIdx.x + s;
-            if (iv[o] >= 0 && (iv[threadIdx.x] < 0 || sv[o] > sv[threadIdx.x] ||
-                               (sv[o] == sv[threadIdx.x] && iv[o] < iv[threadIdx.x]))) {
+            if (norm_better(sv[o], iv[o], sv[threadIdx.x], iv[threadIdx.x])) {
                 sv[threadIdx.x] = sv[o]; iv[threadIdx.x] = iv[o];
             }
-            if (in_[o] >= 0 && (in_[threadIdx.x] < 0 || sn[o] > sn[threadIdx.x] ||
-                                (sn[o] == sn[threadIdx.x] && in_[o] < in_[threadIdx.x]))) {
+            if (norm_better(sn[o], in_[o], sn[threadIdx.x], in_[threadIdx.x])) {
                 sn[threadIdx.x] = sn[o]; in_[threadIdx.x] = in_[o];
             }
         }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        out->maxV = iv[0] >= 0 ? sv[0] : 0.0; out->idV = iv[0] >= 0 ? iv[0] : 0;
-        out->maxN = in_[0] >= 0 ? sn[0] : 0.0; out->idN = in_[0] >= 0 ? in_[0] : 0;
+        RowNorm& o = out[blockIdx.x];
+        if (gridDim.x > 1) {  // a partial: keep "none" as index -1
+            o.maxV = sv[0]; o.idV = iv[0]; o.maxN = sn[0]; o.idN = in_[0];
+        }
+        else {
+            o.maxV = iv[0] >= 0 ? sv[0] : 0.0; o.idV = iv[0] >= 0 ? iv[0] : 0;
+            o.maxN = in_[0] >= 0 ? sn[0] : 0.0; o.idN = in_[0] >= 0 ? in_[0] : 0;
+        }
     }
 }
 
@@ -249,16 +263,24 @@ cudaError_t launch_conn_flux(const Model* dm, const BulkView& b, const ConnView&
     return cudaGetLastError();
 }
 cudaError_t launch_residual(const BulkView& b, const ConnView& cv, double dt, double* res, double* resRelV,
-                            double* resRelN, RowNorm* rn, RowNorm* rn_out, int block, cudaStream_t s)
+                            double* resRelN, RowNorm* rn, RowNorm* rn_out, RowNorm* part, int block, cudaStream_t s)
 {
     if (!b.nbI) return cudaSuccess;
     k_residual<<<grid_for(b.nbI, block), block, 0, s>>>(b, cv, dt, res, resRelV, resRelN, rn);
-    if (rn_out) k_norm_reduce<<<1, 256, 0, s>>>(rn, b.nbI, rn_out);
+    if (rn_out) return launch_norm_reduce(rn, b.nbI, rn_out, part, s);
     return cudaGetLastError();
 }
-cudaError_t launch_norm_reduce(const RowNorm* rn, int nbI, RowNorm* rn_out, cudaStream_t s)
+cudaError_t launch_norm_reduce(const RowNorm* rn, int nbI, RowNorm* rn_out, RowNorm* part, cudaStream_t s)
 {
-    if (nbI) k_norm_reduce<<<1, 256, 0, s>>>(rn, nbI, rn_out);
+    if (!nbI) return cudaSuccess;
+    const int g = std::min(NORM_PARTS, (nbI + 255) / 256);
+    if (g > 1) {
+        k_norm_reduce<<<g, 256, 0, s>>>(rn, nbI, part);
+        k_norm_reduce<<<1, 256, 0, s>>>(part, g, rn_out);
+    }
+    else {
+        k_norm_reduce<<<1, 256, 0, s>>>(rn, nbI, rn_out);
+    }
     return cudaGetLastError();
 }
 cudaError_t launch_jac_conn(int nct, const Model* dm, const BulkView& b, const ConnView& cv, double dt, double* bmat,

@@ -167,6 +167,7 @@ struct ocpx_ctx {
     double* resRelN = nullptr;
     RowNorm* rownorm = nullptr;
     RowNorm* norm_out = nullptr;
+    RowNorm* norm_part = nullptr;   // partial maxima of the two-pass norm reduction
     uint32_t* flags = nullptr;      // [4]: check OR, report (OR, two-phase, flagged)
     // batched flash: cost order, deferral list, cooperative results
     int* order = nullptr;
@@ -586,6 +587,7 @@ ocpx_status ocpx_create_ex(const ocpx_model_desc* md, const ocpx_grid_desc* gd, 
     add(&cv.row_ptr, sizeof(uint32_t) * (nb + 1)); add(&cv.row_conn, sizeof(uint32_t) * (row_conn.size() + 1));
     add(&ctx->resRelV, D); add(&ctx->resRelN, D);
     add(&ctx->rownorm, sizeof(RowNorm) * (size_t)nb); add(&ctx->norm_out, sizeof(RowNorm));
+    add(&ctx->norm_part, sizeof(RowNorm) * NORM_PARTS);
     add(&ctx->flags, sizeof(uint32_t) * 4);
     ctx->defer_cap = std::max(1024, nb / 4);
     add(&ctx->order, sizeof(int) * (size_t)nb); add(&ctx->cost_hist, sizeof(unsigned) * COST_BUCKETS);
@@ -985,7 +987,7 @@ ocpx_status enqueue_calres(ocpx_ctx* ctx, double dt)
     mk = ctx->stage_begin(5);
     const bool wells = ctx->ws.nw > 0;
     OCPX_CUDA(launch_residual(ctx->b, ctx->cv, dt, ctx->res, ctx->resRelV, ctx->resRelN, ctx->rownorm,
-                              wells ? nullptr : ctx->norm_out, ctx->block_cell, s));
+                              wells ? nullptr : ctx->norm_out, ctx->norm_part, ctx->block_cell, s));
     if (wells) {
         // CalResFIM of every well after the bulk rows, then the norms
         if (ctx->recompute) {
@@ -994,7 +996,7 @@ ocpx_status enqueue_calres(ocpx_ctx* ctx, double dt)
             ctx->launches++;
         }
         OCPX_CUDA(launch_wells_res(ctx->b, ctx->ws, dt, ctx->res, ctx->resRelV, ctx->resRelN, ctx->rownorm, s));
-        OCPX_CUDA(launch_norm_reduce(ctx->rownorm, ctx->nbI, ctx->norm_out, s));
+        OCPX_CUDA(launch_norm_reduce(ctx->rownorm, ctx->nbI, ctx->norm_out, ctx->norm_part, s));
         ctx->launches += 3;
     }
     ctx->stage_end(mk);

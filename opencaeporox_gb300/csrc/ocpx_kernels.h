@@ -175,10 +175,12 @@ cudaError_t launch_check(const BulkView& b, uint32_t* flags, int block, cudaStre
 cudaError_t launch_newton_update(const BulkView& b, const double* u, double dSmax, int block, cudaStream_t s);
 cudaError_t launch_conn_flux(const Model* dm, const BulkView& b, const ConnView& cv, int block, cudaStream_t s);
 cudaError_t launch_residual(const BulkView& b, const ConnView& cv, double dt, double* res, double* resRelV,
-                            double* resRelN, RowNorm* rn, RowNorm* rn_out, int block, cudaStream_t s);
+                            double* resRelN, RowNorm* rn, RowNorm* rn_out, RowNorm* part, int block, cudaStream_t s);
 // the norm reduction of launch_residual alone (launch_residual with rn_out NULL
-// leaves it out, so that the wells' rows can be added first)
-cudaError_t launch_norm_reduce(const RowNorm* rn, int nbI, RowNorm* rn_out, cudaStream_t s);
+// leaves it out, so that the wells' rows can be added first); part: NORM_PARTS
+// partial maxima
+constexpr int NORM_PARTS = 1024;
+cudaError_t launch_norm_reduce(const RowNorm* rn, int nbI, RowNorm* rn_out, RowNorm* part, cudaStream_t s);
 cudaError_t launch_jac_conn(int nct, const Model* dm, const BulkView& b, const ConnView& cv, double dt,
                             double* bmat, int block, cudaStream_t s);
 cudaError_t launch_jac_rows(const BulkView& b, const ConnView& cv, const double* bmat, const uint32_t* rowptr,

@@ -884,6 +884,9 @@ def run_fim(args, wl, rt, local, rank, world):
     t0 = time.perf_counter()
     ctx, u2 = prepare(wl, model, grid, 1, local, recompute)
     log(f"{wl.key}: batched form set up in {time.perf_counter() - t0:.1f} s")
+    for kv in args.param:
+        k, v = kv.split("=")
+        ctx.set_param(k, int(v))
     tuned = None
     if not args.no_tune:
         from opencaeporox_gb300 import autotune
@@ -952,7 +955,7 @@ def run_fim(args, wl, rt, local, rank, world):
             "roofline": roof, "roofline_assembly": roof_asm, "fp64_peak_tflops": fp64,
             "batched": {k: ctx.get_param(k) for k in ("flash_budget", "coop_blocks", "block_cell", "predefer",
                                                       "coop_cells", "pre_blocks", "cell_blocks", "fused_blocks",
-                                                      "fused_coop_blocks")},
+                                                      "fused_coop_blocks", "split_refill")},
             "autotune": None if tuned is None else {k: v for k, v in tuned.items() if k != "trials"},
             "clocks": ck, "gpu_launches": launches,
             "e2e": {"value": nb / (e2e_ms * 1e-3) * world, "unit": "cells/s", "h2d_bytes_per_step": h2d,
@@ -1000,6 +1003,8 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner (library defaults)")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the timed step")
+    ap.add_argument("--param", action="append", default=[],
+                    help="name=value: a library parameter of the batched form, set before tuning (repeatable)")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain form's leg (to profile the batched step alone)")
     ap.add_argument("--parity-dump", default=None, help="write the cells above 1e-10 in the parity check to this .npz")

@@ -339,7 +339,14 @@ ocpx_status ocpx_set_variant(ocpx_ctx* ctx, int variant);
  *                 ocpx_options.recompute_flash_der;
  *   DEVICE_BYTES  (read only) device memory the context holds: its arena,
  *                 the linear system, the wells, the solver's and the
- *                 adjoint's work space and the checkpoints. */
+ *                 adjoint's work space and the checkpoints;
+ *   SPLIT_REFILL  1: in the fused form, the cells whose flash starts with
+ *                 the phase split run the split's first successive-
+ *                 substitution loop in a kernel whose lanes take a new cell
+ *                 as soon as theirs is done, then the rest of their flash
+ *                 from the saved state; results bit-identical.  Allocates
+ *                 one saved state per cell (704 bytes) when first set.
+ *                 0 (default): off. */
 typedef enum ocpx_param {
     OCPX_PARAM_FLASH_BUDGET = 0,
     OCPX_PARAM_COOP_BLOCKS = 1,
@@ -359,7 +366,8 @@ typedef enum ocpx_param {
     OCPX_PARAM_FUSED_EXCL = 15,
     OCPX_PARAM_POST_BLOCK = 16,
     OCPX_PARAM_RECOMPUTE_FLASH_DER = 17,
-    OCPX_PARAM_DEVICE_BYTES = 18
+    OCPX_PARAM_DEVICE_BYTES = 18,
+    OCPX_PARAM_SPLIT_REFILL = 19
 } ocpx_param;
 ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value);
 ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value);

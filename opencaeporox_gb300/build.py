@@ -29,8 +29,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libocpx_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NCM_CAPS = (4, 6, 8, 10, 12)
-FLASH_PARTS = 8  # plain + dispatch, budgeted, fused, round, cooperative, SM-exclusive cooperative, post,
-                 # the consumers of recomputed flash derivatives
+FLASH_PARTS = 9  # plain + dispatch, budgeted, fused, round, cooperative, SM-exclusive cooperative, post,
+                 # the consumers of recomputed flash derivatives, the split cells with lane refill
 
 
 def nvcc_path() -> str:

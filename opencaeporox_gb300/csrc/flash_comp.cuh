@@ -44,6 +44,17 @@ struct PERes {
     double x[2][NC_MAX];
 };
 
+// The state a cell's phase split leaves after its first successive-
+// substitution loop (split_ssm2 without restart), for the rest of the split
+// to resume from: what the loop writes and what comes after it reads.
+struct SplitState {
+    double Ks[NC_MAX], nu[2], x[2][NC_MAX], fug[2][NC_MAX], phi[2][NC_MAX];
+    int it_ssm_sp, it_rr, work;
+    uint32_t status;
+    uint8_t conv;   // ssm_sp_conv
+    uint8_t skip;   // 1: not a split cell, or left to the cooperative kernel
+};
+
 // A cell whose phase equilibrium ran over its work budget, with the inputs
 // the equilibrium needs besides the cell state.
 struct DeferRec {
@@ -395,40 +406,100 @@ struct CompFlash {
     }
 
     // OCPPhaseEquilibrium::SplitSSM2 (:586-647)
-    OCPX_HD_NOINLINE void split_ssm2(bool restart)
+    // the loop's controls: residual, tolerance, iteration cap and count
+    struct SsmLoop {
+        double Se, Stol;
+        int maxIt, iter;
+    };
+    OCPX_HD void split_ssm_init(bool restart, SsmLoop& L)
     {
         ssm_sp_conv = true;
-        double Se = 1;
-        double Stol = m->ssm_sp_tol2;
-        int maxIt = m->ssm_sp_maxit;
+        L.Se = 1;
+        L.Stol = m->ssm_sp_tol2;
+        L.maxIt = m->ssm_sp_maxit;
         if (!restart) {
             if (lNP == 2) for (int i = 0; i < NC; i++) Ks[i] = lKs[i];
             else          for (int i = 0; i < NC; i++) Ks[i] = Kw[0][i];
         }
         else {
-            Stol *= 1E-1;
-            maxIt *= 2;
+            L.Stol *= 1E-1;
+            L.maxIt *= 2;
         }
         if (Yt < 1.1) {
-            Stol *= 1E-1;
-            maxIt *= 2;
+            L.Stol *= 1E-1;
+            L.maxIt *= 2;
         }
-        int iter = 0;
-        while (Se > Stol) {
-            if (charge(WORK_SSM_SP)) return;
-            rachford_rice2();
-            update_x_rr();
-            eos.cal_fug_phi(x[0], fug[0], phi[0]);
-            eos.cal_fug_phi(x[1], fug[1], phi[1]);
-            Se = 0;
-            for (int i = 0; i < NC; i++) {
-                Se += sq(fug[1][i] / fug[0][i] - 1);
-                Ks[i] = phi[1][i] / phi[0][i];
+        L.iter = 0;
+    }
+    // one pass of the loop (its test first); true when the loop is over,
+    // with it_ssm_sp updated, or when the cell went over its budget (deferred)
+    OCPX_HD_NOINLINE bool split_ssm_step(SsmLoop& L)
+    {
+        if (!(L.Se > L.Stol)) {
+            it_ssm_sp += L.iter;
+            return true;
+        }
+        if (charge(WORK_SSM_SP)) return true;
+        rachford_rice2();
+        update_x_rr();
+        eos.cal_fug_phi(x[0], fug[0], phi[0]);
+        eos.cal_fug_phi(x[1], fug[1], phi[1]);
+        L.Se = 0;
+        for (int i = 0; i < NC; i++) {
+            L.Se += sq(fug[1][i] / fug[0][i] - 1);
+            Ks[i] = phi[1][i] / phi[0][i];
+        }
+        L.iter++;
+        if (L.iter > L.maxIt) {
+            ssm_sp_conv = false;
+            it_ssm_sp += L.iter;
+            return true;
+        }
+        return false;
+    }
+    OCPX_HD void split_ssm2(bool restart)
+    {
+        SsmLoop L;
+        split_ssm_init(restart, L);
+        while (!split_ssm_step(L)) {
+        }
+    }
+
+    OCPX_HD void split_save(SplitState& st) const
+    {
+        for (int i = 0; i < NC; i++) {
+            st.Ks[i] = Ks[i];
+            for (int j = 0; j < 2; j++) {
+                st.x[j][i] = x[j][i];
+                st.fug[j][i] = fug[j][i];
+                st.phi[j][i] = phi[j][i];
             }
-            iter++;
-            if (iter > maxIt) { ssm_sp_conv = false; break; }
         }
-        it_ssm_sp += iter;
+        st.nu[0] = nu[0];
+        st.nu[1] = nu[1];
+        st.it_ssm_sp = it_ssm_sp;
+        st.it_rr = it_rr;
+        st.work = work;
+        st.status = status;
+        st.conv = ssm_sp_conv ? 1 : 0;
+    }
+    OCPX_HD void split_load(const SplitState& st)
+    {
+        for (int i = 0; i < NC; i++) {
+            Ks[i] = st.Ks[i];
+            for (int j = 0; j < 2; j++) {
+                x[j][i] = st.x[j][i];
+                fug[j][i] = st.fug[j][i];
+                phi[j][i] = st.phi[j][i];
+            }
+        }
+        nu[0] = st.nu[0];
+        nu[1] = st.nu[1];
+        it_ssm_sp = st.it_ssm_sp;
+        it_rr = st.it_rr;
+        work = st.work;
+        status = st.status;
+        ssm_sp_conv = st.conv != 0;
     }
 
     // OCPPhaseEquilibrium::CalResSP (:899-907)
@@ -514,11 +585,13 @@ struct CompFlash {
     }
 
     // OCPPhaseEquilibrium::PhaseSplit (:549-573)
-    OCPX_HD_NOINLINE void phase_split()
+    OCPX_HD_NOINLINE void phase_split(const SplitState* resume = nullptr)
     {
         ssm_sp_conv = false;
         nr_sp_conv = false;
-        split_ssm2(false);
+        // the first successive-substitution loop, or its result computed elsewhere
+        if (resume) split_load(*resume);
+        else split_ssm2(false);
         if (deferred) return;
         split_nr();
         if (deferred) return;
@@ -541,7 +614,23 @@ struct CompFlash {
 
     // OCPPhaseEquilibrium::PhaseEquilibrium (:71-112) + SetInitalValue (:121-138).
     // lx points to the cell's previous oil composition; lx[i + lx_stride] is gas.
-    OCPX_HD_NOINLINE void phase_equilibrium(int ftype_in, unsigned lNP_in, const double* lx0, const double* lx1)
+    // split_begin: the prologue of flash type 2 up to the split's first loop
+    OCPX_HD void split_prologue(unsigned lNP_in, const double* lx0, const double* lx1)
+    {
+        ftype = 2;
+        lNP = lNP_in;
+        if (lNP == 2)
+            for (int i = 0; i < NC; i++) lKs[i] = lx0[i] / lx1[i];
+        NP = 2;
+        Yt = 1.01;
+        cal_kwilson();
+        ssm_sp_conv = false;
+        nr_sp_conv = false;
+    }
+
+    // resume (flash type 2 only): the split's first loop was run elsewhere
+    OCPX_HD_NOINLINE void phase_equilibrium(int ftype_in, unsigned lNP_in, const double* lx0, const double* lx1,
+                                            const SplitState* resume = nullptr)
     {
         ftype = ftype_in;
         lNP = lNP_in;
@@ -569,7 +658,7 @@ struct CompFlash {
             NP = 2;
             Yt = 1.01;
             cal_kwilson();
-            phase_split();
+            phase_split(resume);
             break;
         }
         if (deferred) return;
@@ -678,8 +767,10 @@ struct CompCellUpdate {
     // handed to `sink` (the plain kernel passes INT_MAX and no sink);
     // injected: a phase-equilibrium result computed elsewhere for this cell.
     // Returns false when the cell was deferred (nothing of it was written).
+    // resume: the state of the split's first loop, run elsewhere (flash type 2)
     OCPX_HD bool run(const Model& M, const BulkView& b, int cell, int budget = 0x7fffffff,
-                     const DeferSink* sink = nullptr, const PERes* injected = nullptr)
+                     const DeferSink* sink = nullptr, const PERes* injected = nullptr,
+                     const SplitState* resume = nullptr)
     {
         const CompModel& m = M.comp;
         const int NC = m.nc;
@@ -739,7 +830,8 @@ struct CompCellUpdate {
             }
         }
         else {
-            f.phase_equilibrium(ftype_in, npPE, xx[0], xx[1]);
+            f.phase_equilibrium(ftype_in, npPE, xx[0], xx[1],
+                                resume && !resume->skip && ftype_in == 2 ? resume : nullptr);
             if (f.deferred) {
                 if (sink && sink->push(cell, ftype_in, npPE)) return false;
                 // no room in the list: finish the equilibrium here from the start
@@ -998,6 +1090,47 @@ struct CompCellUpdate {
             if (ex[j]) dX(j, NC + 1) = (vji[j][NC] - vfi[NC] * S[j]) / Vf;
         dX(2, 0) = (vjP[2] - vfP * S[2]) / Vf;
         for (int i = 0; i < nct; i++) dX(2, 1 + i) = (vji[2][i] - vfi[i] * S[2]) / Vf;
+    }
+
+    // The prologue of run() for a cell whose flash starts with the phase split
+    // (flash type 2), up to the split's first successive-substitution loop,
+    // which L then drives one pass at a time (CompFlash::split_ssm_step).
+    // False, with nothing set up, for a cell of another flash type.
+    OCPX_HD bool split_begin(const Model& M, const BulkView& b, int cell, typename CompFlash<NCM>::SsmLoop& L)
+    {
+        const CompModel& m = M.comp;
+        const int NC = m.nc, nct = NC + 1, np = 3;
+        f.m = &m;
+        f.NC = NC;
+        f.status = 0;
+        f.it_ssm_sta = f.it_nr_sta = f.it_ssm_sp = f.it_nr_sp = f.it_rr = 0;
+        f.work = 0;
+        f.budget = 0x7fffffff;
+        f.deferred = false;
+        const double P = b.P[cell];
+        const double T = b.T[cell] + M.units.conv4;
+        double Ni[NCM + 1];
+        for (int i = 0; i < nct; i++) Ni[i] = b.Ni[b.idx(i, cell)];
+        double Sin[3];
+        unsigned phaseNum = 0;
+        for (int j = 0; j < np; j++) {
+            Sin[j] = b.S[b.idx(j, cell)];
+            if (b.phaseExist[b.idx(j, cell)] != 0) phaseNum++;
+        }
+        for (int j = 0; j < 2; j++)
+            for (int i = 0; i < nct; i++) xx[j][i] = b.xij[b.idx(j * nct + i, cell)];
+        double Nt = 0;
+        for (int i = 0; i < NC; i++) Nt += Ni[i];
+        for (int i = 0; i < NC; i++) f.zi[i] = Ni[i] / Nt;
+        f.Nt = Nt;
+        f.P = P;
+        f.T = T;
+        const unsigned npPE = phaseNum - 1u;
+        if (flash_type_in(m, b, cell, Ni, Nt, P, T, Sin, npPE) != 2) return false;
+        f.eos.setup(&m, M.units.gas_constant, P, T);
+        f.split_prologue(npPE, xx[0], xx[1]);
+        f.split_ssm_init(false, L);
+        return true;
     }
 
     // dSec_dPri of a cell recomputed from the state its flash left (P, T, Ni,

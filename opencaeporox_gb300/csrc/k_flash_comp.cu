@@ -8,7 +8,7 @@
 #error "compile with -DOCPX_NCM=<capacity>"
 #endif
 #ifndef OCPX_FLASH_PART
-#error "compile with -DOCPX_FLASH_PART=<0..7>"
+#error "compile with -DOCPX_FLASH_PART=<0..8>"
 #endif
 
 namespace ocpx {
@@ -331,6 +331,77 @@ __global__ void __launch_bounds__(128) k_newton_update_recompute(const Model* __
     newton_update_cell(b, cell, u, dSmax, ds, 1);
 }
 
+// ---- the split cells (flash type 2) with lane refill
+
+// The split's first successive-substitution loop of the cells at positions
+// [0, *n_split) of the cost order (the cells whose flash starts with the
+// split), one pass per trip through the loop below: a lane whose cell's loop
+// ends saves the cell's state and takes the next cell at once, so the lanes of
+// a warp keep running passes of the same loop whatever each cell's count.
+// Per lane, the arithmetic is the split's own (split_begin, split_ssm_step).
+// Pre-deferred cells (the cooperative kernel's) and cells that are not split
+// cells are marked skip.  next: a position counter, zero before the launch.
+template <int NCM>
+__global__ void __launch_bounds__(128) k_split_refill(const Model* __restrict__ M, BulkView b,
+                                                      const int* __restrict__ order,
+                                                      const unsigned* __restrict__ n_split,
+                                                      const uint8_t* __restrict__ pre, SplitState* __restrict__ st,
+                                                      unsigned* __restrict__ next)
+{
+    const unsigned n = *n_split;
+    CompCellUpdate<NCM> u;
+    typename CompFlash<NCM>::SsmLoop L;
+    unsigned p = 0;
+    bool active = false;
+    for (;;) {
+        while (!active) {
+            p = atomicAdd(next, 1u);
+            if (p >= n) break;
+            const int cell = order[p];
+            if ((pre && pre[cell]) || !u.split_begin(*M, b, cell, L)) {
+                st[p].skip = 1;
+                continue;
+            }
+            active = true;
+        }
+        if (!active) break;
+        if (u.f.split_ssm_step(L)) {
+            u.f.split_save(st[p]);
+            st[p].skip = 0;
+            active = false;
+        }
+    }
+}
+
+// The rest of those cells' flash, resumed from the saved state (run with
+// resume), 32 positions per warp from the counter next (zero before the
+// launch); pre-deferred cells are left to the cooperative kernel.
+template <int NCM>
+__global__ void __launch_bounds__(128) k_split_resume(const Model* __restrict__ M, BulkView b,
+                                                      const int* __restrict__ order,
+                                                      const unsigned* __restrict__ n_split,
+                                                      const uint8_t* __restrict__ pre,
+                                                      const SplitState* __restrict__ st, unsigned* __restrict__ next)
+{
+    const unsigned n = *n_split;
+    const unsigned lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(next, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const unsigned p = base + lane;
+        if (p < n) {
+            const int cell = order[p];
+            if (!(pre && pre[cell])) {
+                CompCellUpdate<NCM> u;
+                u.run(*M, b, cell, 0x7fffffff, nullptr, nullptr, &st[p]);
+            }
+        }
+        __syncwarp();
+    }
+}
+
 #define OCPX_CAT2(a, b) a##b
 #define OCPX_CAT(a, b) OCPX_CAT2(a, b)
 #define OCPX_NAME(base) OCPX_CAT(base, OCPX_NCM)
@@ -531,6 +602,23 @@ cudaError_t OCPX_NAME(launch_newton_update_recompute_)(const Model* dm, const Bu
                                                        double dSmax, cudaStream_t s)
 {
     if (b.nb > 0) k_newton_update_recompute<OCPX_NCM><<<(b.nb + 127) / 128, 128, 0, s>>>(dm, b, u, dSmax);
+    return cudaGetLastError();
+}
+#endif
+
+#if OCPX_FLASH_PART == 8
+cudaError_t OCPX_NAME(launch_split_refill_)(const Model* dm, const BulkView& b, const int* order,
+                                            const unsigned* n_split, const uint8_t* pre, SplitState* st,
+                                            unsigned* next, int blocks, cudaStream_t s)
+{
+    if (blocks > 0) k_split_refill<OCPX_NCM><<<blocks, 128, 0, s>>>(dm, b, order, n_split, pre, st, next);
+    return cudaGetLastError();
+}
+cudaError_t OCPX_NAME(launch_split_resume_)(const Model* dm, const BulkView& b, const int* order,
+                                            const unsigned* n_split, const uint8_t* pre, const SplitState* st,
+                                            unsigned* next, int blocks, cudaStream_t s)
+{
+    if (blocks > 0) k_split_resume<OCPX_NCM><<<blocks, 128, 0, s>>>(dm, b, order, n_split, pre, st, next);
     return cudaGetLastError();
 }
 #endif

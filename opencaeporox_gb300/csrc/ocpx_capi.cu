@@ -68,6 +68,17 @@ cudaError_t setup_flash_batched(int ncm, int* excl_smem)
     cudaError_t launch_dsec_cells_##N(const Model*, const BulkView&, const int*, int, int, double*, size_t,          \
                                       cudaStream_t);                                                                 \
     cudaError_t launch_newton_update_recompute_##N(const Model*, const BulkView&, const double*, double, cudaStream_t);
+#define OCPX_SPLIT_DECL(N)                                                                                         \
+    cudaError_t launch_split_refill_##N(const Model*, const BulkView&, const int*, const unsigned*, const uint8_t*,   \
+                                        SplitState*, unsigned*, int, cudaStream_t);                                   \
+    cudaError_t launch_split_resume_##N(const Model*, const BulkView&, const int*, const unsigned*, const uint8_t*,   \
+                                        const SplitState*, unsigned*, int, cudaStream_t);
+OCPX_SPLIT_DECL(4)
+OCPX_SPLIT_DECL(6)
+OCPX_SPLIT_DECL(8)
+OCPX_SPLIT_DECL(10)
+OCPX_SPLIT_DECL(12)
+#undef OCPX_SPLIT_DECL
 OCPX_RECOMPUTE_DECL(4)
 OCPX_RECOMPUTE_DECL(6)
 OCPX_RECOMPUTE_DECL(8)
@@ -92,6 +103,16 @@ cudaError_t launch_newton_update_recompute(int ncm, const Model* dm, const BulkV
                                            double dSmax, cudaStream_t s)
 {
     OCPX_NCM_SWITCH(launch_newton_update_recompute_, dm, b, u, dSmax, s)
+}
+cudaError_t launch_split_refill(int ncm, const Model* dm, const BulkView& b, const int* order, const unsigned* n_split,
+                                const uint8_t* pre, SplitState* st, unsigned* next, int blocks, cudaStream_t s)
+{
+    OCPX_NCM_SWITCH(launch_split_refill_, dm, b, order, n_split, pre, st, next, blocks, s)
+}
+cudaError_t launch_split_resume(int ncm, const Model* dm, const BulkView& b, const int* order, const unsigned* n_split,
+                                const uint8_t* pre, const SplitState* st, unsigned* next, int blocks, cudaStream_t s)
+{
+    OCPX_NCM_SWITCH(launch_split_resume_, dm, b, order, n_split, pre, st, next, blocks, s)
 }
 #undef OCPX_NCM_SWITCH
 }  // namespace ocpx
@@ -155,6 +176,9 @@ struct ocpx_ctx {
     bool recompute = false;
     int dsec_slab = 0;
     double* dsec_scratch = nullptr;
+    // the split cells' first loop with lane refill (OCPX_PARAM_SPLIT_REFILL)
+    int split_refill = 0;
+    SplitState* split_state = nullptr;  // [nb], allocated when the option is first set
     // one arena for everything
     char* arena = nullptr;
     size_t arena_bytes = 0;
@@ -699,6 +723,7 @@ void ocpx_destroy(ocpx_ctx* ctx)
     for (auto e : ctx->free_events) cudaEventDestroy(e);
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->ls_scratch) cudaFree(ctx->ls_scratch);
+    if (ctx->split_state) cudaFree(ctx->split_state);
     if (ctx->step_adj) cudaFree(ctx->step_adj);
     if (ctx->sys) cudaFree(ctx->sys);
     if (ctx->wbuf) cudaFree(ctx->wbuf);
@@ -843,7 +868,8 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
             const bool pre = ctx->predefer > 0;
             // list counts [0] late, [1] pre-deferred; [2], [3] the cooperative kernels' next-slot
             // counters; [4] the persistent per-cell kernel's position counter; [8 + r], [16 + r]
-            // the count and position counter of re-budgeting round r; [32..34] the fused kernel's
+            // the count and position counter of re-budgeting round r; [32..35] the fused kernel's;
+            // [36], [37] the split cells' refill and resume position counters
             OCPX_CUDA(cudaMemsetAsync(ctx->defer_count, 0, sizeof(unsigned) * 40, s));
             mk = ctx->stage_begin(9);
             OCPX_CUDA(launch_cost_order(ctx->d_model, ctx->b, ctx->cost_hist, ctx->order, (unsigned)ctx->coop_cells,
@@ -894,6 +920,19 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
                 ff.coop_only_blocks = coop_only;
                 ff.watchdog = ctx->flags + 1;
                 mk = ctx->stage_begin(10);
+                if (ctx->split_refill && ctx->split_state) {
+                    // the split cells (the order's first class) first: their first
+                    // loop with lane refill, then the rest of their flash; the fused
+                    // kernel then starts at the order's second class
+                    const unsigned* n_split = ctx->cost_hist + 63;
+                    const uint8_t* pf = pre ? ctx->pre_flag : nullptr;
+                    OCPX_CUDA(launch_split_refill(ctx->ncm, ctx->d_model, ctx->b, ctx->order, n_split, pf,
+                                                  ctx->split_state, cnt + 36, ctx->fused_blocks, s));
+                    OCPX_CUDA(launch_split_resume(ctx->ncm, ctx->d_model, ctx->b, ctx->order, n_split, pf,
+                                                  ctx->split_state, cnt + 37, ctx->fused_blocks, s));
+                    OCPX_CUDA(cudaMemcpyAsync(cnt + 33, n_split, sizeof(unsigned), cudaMemcpyDeviceToDevice, s));
+                    ctx->launches += 2;
+                }
                 OCPX_CUDA(launch_flash_batched(ctx->ncm, ctx->d_model, ctx->b, ctx->order, ff, 4, s));
                 ctx->stage_end(mk);
                 ctx->late_count = 0;
@@ -1790,6 +1829,16 @@ ocpx_status ocpx_set_param(ocpx_ctx* ctx, ocpx_param p, long long value)
         if (value < 2 || value > 64) return fail(OCPX_INVALID_ARG, "round growth must be 2..64");
         ctx->round_growth = (int)value;
         return OCPX_OK;
+    case OCPX_PARAM_SPLIT_REFILL:
+        if (value != 0 && value != 1) return fail(OCPX_INVALID_ARG, "split refill must be 0 or 1");
+        if (value && !ctx->split_state) {
+            if (cudaMalloc(&ctx->split_state, sizeof(SplitState) * (size_t)ctx->nb) != cudaSuccess) {
+                ctx->split_state = nullptr;
+                return fail(OCPX_CUDA_ERROR, "cudaMalloc of the split states failed");
+            }
+        }
+        ctx->split_refill = (int)value;
+        return OCPX_OK;
     default:
         return fail(OCPX_INVALID_ARG, "unknown or read-only parameter");
     }
@@ -1804,6 +1853,7 @@ size_t device_bytes(const ocpx_ctx* ctx)
 {
     size_t n = ctx->arena_bytes + ctx->sys_bytes + ctx->wbuf_bytes + ctx->weval_bytes;
     if (ctx->ls_scratch) n += sizeof(double) * linsolve_scratch_doubles(ctx->nrow, ctx->nc + 1);
+    if (ctx->split_state) n += sizeof(SplitState) * (size_t)ctx->nb;
     if (ctx->step_adj) n += sizeof(double) * (2 * ctx->nv() + ctx->nb + (size_t)ctx->nconn);
     for (char* c : ctx->ckpt)
         if (c) n += ctx->state_bytes;
@@ -1832,6 +1882,7 @@ ocpx_status ocpx_get_param(ocpx_ctx* ctx, ocpx_param p, long long* value)
     case OCPX_PARAM_POST_BLOCK: *value = ctx->post_block; return OCPX_OK;
     case OCPX_PARAM_ROUND_GROWTH: *value = ctx->round_growth; return OCPX_OK;
     case OCPX_PARAM_RECOMPUTE_FLASH_DER: *value = ctx->recompute ? 1 : 0; return OCPX_OK;
+    case OCPX_PARAM_SPLIT_REFILL: *value = ctx->split_refill; return OCPX_OK;
     case OCPX_PARAM_DEVICE_BYTES: *value = (long long)device_bytes(ctx); return OCPX_OK;
     case OCPX_PARAM_DEFERRED: {
         unsigned n[2] = {0, 0};

@@ -69,6 +69,14 @@ cudaError_t launch_jac_side(int nct, const Model* dm, const BulkView& b, const C
                             cudaStream_t s);
 cudaError_t launch_newton_update_recompute(int ncm, const Model* dm, const BulkView& b, const double* u,
                                            double dSmax, cudaStream_t s);
+// The cells at positions [0, *n_split) of the cost order (flash type 2):
+// the split's first loop with lane refill into st[position], then the rest
+// of their flash resumed from it (k_flash_comp.cu, part 8); next: position
+// counters, zero before the launch.
+cudaError_t launch_split_refill(int ncm, const Model* dm, const BulkView& b, const int* order, const unsigned* n_split,
+                                const uint8_t* pre, SplitState* st, unsigned* next, int blocks, cudaStream_t s);
+cudaError_t launch_split_resume(int ncm, const Model* dm, const BulkView& b, const int* order, const unsigned* n_split,
+                                const uint8_t* pre, const SplitState* st, unsigned* next, int blocks, cudaStream_t s);
 // Cells grouped by the flash type they start from (split, stability test,
 // skip) and, within a group, in descending order of their predicted work, by
 // a counting sort over COST_BUCKETS buckets.

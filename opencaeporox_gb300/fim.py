@@ -149,7 +149,8 @@ PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3, "
           "predeferred": 6, "level": 7, "pre_blocks": 8,
           "cell_blocks": 9, "rounds": 10, "round_growth": 11,
           "fused_blocks": 12, "sms": 13, "fused_coop_blocks": 14,
-          "fused_excl": 15, "post_block": 16, "recompute_flash_der": 17, "device_bytes": 18}
+          "fused_excl": 15, "post_block": 16, "recompute_flash_der": 17, "device_bytes": 18,
+          "split_refill": 19}
 
 _lib = None
 

@@ -33,6 +33,8 @@ FORMS = {
     "defaults": {},
     "fused-roles": dict(fused_blocks=3, fused_coop_blocks=1, flash_budget=3, coop_cells=0, predefer=1),
     "two-stream": dict(fused_blocks=0, flash_budget=3, coop_cells=0, predefer=1),
+    "split-refill": dict(split_refill=1),
+    "split-refill-predefer": dict(split_refill=1, flash_budget=3, coop_cells=0, predefer=1),
 }
 
 
@@ -294,3 +296,22 @@ def test_field_ranges(gpu_lib):
         assert np.array_equal(ctx.get("XIJ"), ref)
         with pytest.raises(fim.OcpxError, match="INVALID_ARG"):
             ctx.set_range("RES", 0, np.zeros(model.nc + 1))   # read-only field
+
+
+def test_bench_state_split_refill_matches_plain(bench_state):
+    """The split cells' first loop with lane refill (SPLIT_REFILL) on the
+    36,000-cell state: the replayed graph bit-identical to the plain step."""
+    model, grid, ctxs = bench_state
+    plain, batched = ctxs[0], ctxs[1]
+    plain.checkpoint(0, restore=True)
+    plain.update_property()
+    plain.cal_res(DT)
+    plain.assemble_mat(DT)
+    ref = outputs(plain)
+    batched.set_param("split_refill", 1)
+    try:
+        for rep in range(2):
+            batched.checkpoint(0, restore=True)
+            same(graph_step(batched, DT), ref, f"split refill, replay {rep}")
+    finally:
+        batched.set_param("split_refill", 0)

@@ -335,12 +335,15 @@ __global__ void __launch_bounds__(128) k_newton_update_recompute(const Model* __
 
 // The split's first successive-substitution loop of the cells at positions
 // [0, *n_split) of the cost order (the cells whose flash starts with the
-// split), one pass per trip through the loop below: a lane whose cell's loop
-// ends saves the cell's state and takes the next cell at once, so the lanes of
-// a warp keep running passes of the same loop whatever each cell's count.
-// Per lane, the arithmetic is the split's own (split_begin, split_ssm_step).
-// Pre-deferred cells (the cooperative kernel's) and cells that are not split
-// cells are marked skip.  next: a position counter, zero before the launch.
+// split), one pass per trip through the loop below.  A lane whose cell's
+// loop ends saves the cell's state and waits; once SPLIT_REFILL_MIN lanes of
+// the warp wait (or none runs), they take new cells together, so the passes
+// run with most lanes busy whatever each cell's count, and a cell's set-up
+// runs on many lanes at once.  Per lane, the arithmetic is the split's own
+// (split_begin, split_ssm_step).  Pre-deferred cells (the cooperative
+// kernel's) and cells that are not split cells are marked skip.  next: a
+// position counter, zero before the launch.
+constexpr int SPLIT_REFILL_MIN = 12;
 template <int NCM>
 __global__ void __launch_bounds__(128) k_split_refill(const Model* __restrict__ M, BulkView b,
                                                       const int* __restrict__ order,
@@ -352,20 +355,25 @@ __global__ void __launch_bounds__(128) k_split_refill(const Model* __restrict__ 
     CompCellUpdate<NCM> u;
     typename CompFlash<NCM>::SsmLoop L;
     unsigned p = 0;
-    bool active = false;
+    bool active = false, exhausted = false;
     for (;;) {
-        while (!active) {
-            p = atomicAdd(next, 1u);
-            if (p >= n) break;
-            const int cell = order[p];
-            if ((pre && pre[cell]) || !u.split_begin(*M, b, cell, L)) {
-                st[p].skip = 1;
-                continue;
+        const unsigned waiting = __ballot_sync(0xffffffffu, !active && !exhausted);
+        const unsigned running = __ballot_sync(0xffffffffu, active);
+        if (!running && !waiting) break;
+        if (waiting && (__popc(waiting) >= SPLIT_REFILL_MIN || !running) && !active && !exhausted) {
+            for (;;) {
+                p = atomicAdd(next, 1u);
+                if (p >= n) { exhausted = true; break; }
+                const int cell = order[p];
+                if ((pre && pre[cell]) || !u.split_begin(*M, b, cell, L)) {
+                    st[p].skip = 1;
+                    continue;
+                }
+                active = true;
+                break;
             }
-            active = true;
         }
-        if (!active) break;
-        if (u.f.split_ssm_step(L)) {
+        if (active && u.f.split_ssm_step(L)) {
             u.f.split_save(st[p]);
             st[p].skip = 0;
             active = false;

@@ -383,14 +383,22 @@ __global__ void __launch_bounds__(128) k_split_refill(const Model* __restrict__ 
 
 // The rest of those cells' flash, resumed from the saved state (run with
 // resume), 32 positions per warp from the counter next (zero before the
-// launch); pre-deferred cells are left to the cooperative kernel.
+// launch), under the per-lane work budget of the fused form: a cell over it
+// (the split's Newton loop failing into restarts) is published to the late
+// list, whose equilibria the fused kernel runs on whole warps.  Pre-deferred
+// cells are left to the cooperative kernel.
 template <int NCM>
 __global__ void __launch_bounds__(128) k_split_resume(const Model* __restrict__ M, BulkView b,
                                                       const int* __restrict__ order,
                                                       const unsigned* __restrict__ n_split,
                                                       const uint8_t* __restrict__ pre,
-                                                      const SplitState* __restrict__ st, unsigned* __restrict__ next)
+                                                      const SplitState* __restrict__ st, unsigned* __restrict__ next,
+                                                      int budget, const int* __restrict__ level, DeferSink late)
 {
+    if (level) {
+        const long long lw = (long long)exp2f(0.25f * (float)level[0]);
+        if (lw > budget) budget = lw > 0x7fffffffLL ? 0x7fffffff : (int)lw;
+    }
     const unsigned n = *n_split;
     const unsigned lane = threadIdx.x & 31;
     for (;;) {
@@ -403,7 +411,7 @@ __global__ void __launch_bounds__(128) k_split_resume(const Model* __restrict__ 
             const int cell = order[p];
             if (!(pre && pre[cell])) {
                 CompCellUpdate<NCM> u;
-                u.run(*M, b, cell, 0x7fffffff, nullptr, nullptr, &st[p]);
+                u.run(*M, b, cell, budget, &late, nullptr, &st[p]);
             }
         }
         __syncwarp();
@@ -624,9 +632,13 @@ cudaError_t OCPX_NAME(launch_split_refill_)(const Model* dm, const BulkView& b, 
 }
 cudaError_t OCPX_NAME(launch_split_resume_)(const Model* dm, const BulkView& b, const int* order,
                                             const unsigned* n_split, const uint8_t* pre, const SplitState* st,
-                                            unsigned* next, int blocks, cudaStream_t s)
+                                            unsigned* next, int blocks, const FlashBatch& fb, cudaStream_t s)
 {
-    if (blocks > 0) k_split_resume<OCPX_NCM><<<blocks, 128, 0, s>>>(dm, b, order, n_split, pre, st, next);
+    DeferSink late{fb.rec, fb.count, fb.cap};
+    late.seq = 1;
+    if (blocks > 0)
+        k_split_resume<OCPX_NCM><<<blocks, 128, 0, s>>>(dm, b, order, n_split, pre, st, next, fb.budget, fb.level,
+                                                        late);
     return cudaGetLastError();
 }
 #endif

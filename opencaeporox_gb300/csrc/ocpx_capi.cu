@@ -72,7 +72,7 @@ cudaError_t setup_flash_batched(int ncm, int* excl_smem)
     cudaError_t launch_split_refill_##N(const Model*, const BulkView&, const int*, const unsigned*, const uint8_t*,   \
                                         SplitState*, unsigned*, int, cudaStream_t);                                   \
     cudaError_t launch_split_resume_##N(const Model*, const BulkView&, const int*, const unsigned*, const uint8_t*,   \
-                                        const SplitState*, unsigned*, int, cudaStream_t);
+                                        const SplitState*, unsigned*, int, const FlashBatch&, cudaStream_t);
 OCPX_SPLIT_DECL(4)
 OCPX_SPLIT_DECL(6)
 OCPX_SPLIT_DECL(8)
@@ -110,9 +110,10 @@ cudaError_t launch_split_refill(int ncm, const Model* dm, const BulkView& b, con
     OCPX_NCM_SWITCH(launch_split_refill_, dm, b, order, n_split, pre, st, next, blocks, s)
 }
 cudaError_t launch_split_resume(int ncm, const Model* dm, const BulkView& b, const int* order, const unsigned* n_split,
-                                const uint8_t* pre, const SplitState* st, unsigned* next, int blocks, cudaStream_t s)
+                                const uint8_t* pre, const SplitState* st, unsigned* next, int blocks,
+                                const FlashBatch& fb, cudaStream_t s)
 {
-    OCPX_NCM_SWITCH(launch_split_resume_, dm, b, order, n_split, pre, st, next, blocks, s)
+    OCPX_NCM_SWITCH(launch_split_resume_, dm, b, order, n_split, pre, st, next, blocks, fb, s)
 }
 #undef OCPX_NCM_SWITCH
 }  // namespace ocpx
@@ -929,7 +930,7 @@ ocpx_status enqueue_properties(ocpx_ctx* ctx)
                     OCPX_CUDA(launch_split_refill(ctx->ncm, ctx->d_model, ctx->b, ctx->order, n_split, pf,
                                                   ctx->split_state, cnt + 36, ctx->fused_blocks, s));
                     OCPX_CUDA(launch_split_resume(ctx->ncm, ctx->d_model, ctx->b, ctx->order, n_split, pf,
-                                                  ctx->split_state, cnt + 37, ctx->fused_blocks, s));
+                                                  ctx->split_state, cnt + 37, ctx->fused_blocks, ff, s));
                     OCPX_CUDA(cudaMemcpyAsync(cnt + 33, n_split, sizeof(unsigned), cudaMemcpyDeviceToDevice, s));
                     ctx->launches += 2;
                 }

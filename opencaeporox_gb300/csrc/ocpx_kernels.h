@@ -75,8 +75,10 @@ cudaError_t launch_newton_update_recompute(int ncm, const Model* dm, const BulkV
 // counters, zero before the launch.
 cudaError_t launch_split_refill(int ncm, const Model* dm, const BulkView& b, const int* order, const unsigned* n_split,
                                 const uint8_t* pre, SplitState* st, unsigned* next, int blocks, cudaStream_t s);
+// fb: the fused form's batch (budget, adaptive level, late list)
 cudaError_t launch_split_resume(int ncm, const Model* dm, const BulkView& b, const int* order, const unsigned* n_split,
-                                const uint8_t* pre, const SplitState* st, unsigned* next, int blocks, cudaStream_t s);
+                                const uint8_t* pre, const SplitState* st, unsigned* next, int blocks,
+                                const FlashBatch& fb, cudaStream_t s);
 // Cells grouped by the flash type they start from (split, stability test,
 // skip) and, within a group, in descending order of their predicted work, by
 // a counting sort over COST_BUCKETS buckets.

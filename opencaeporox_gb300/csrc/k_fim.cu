@@ -122,7 +122,7 @@ __device__ __forceinline__ int conn_class(const BulkView& b, const ConnView& cv,
 // the sorted tile, so its lanes take the same branches.  Every connection's
 // blocks are computed by conn_jac_blocks as before; only which thread computes
 // them changes.
-constexpr int JAC_TILE = 1024;
+constexpr int JAC_TILE = 4096;
 template <int NCT>
 __global__ void __launch_bounds__(128) k_jac_conn(const Model* __restrict__ M, BulkView b, ConnView cv, double dt,
                                                   double* __restrict__ bmat)

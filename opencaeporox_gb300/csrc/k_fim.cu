@@ -117,9 +117,9 @@ __device__ __forceinline__ int conn_class(const BulkView& b, const ConnView& cv,
 }
 
 // The connection blocks of a tile of JAC_TILE consecutive connections per
-// block of 128 threads: the tile is first sorted by code path (a counting
-// sort in shared memory), then each warp takes 32 consecutive connections of
-// the sorted tile, so its lanes take the same branches.  Every connection's
+// block of 128 threads: the tile is first sorted by code path (a stable
+// counting sort in shared memory), then each warp takes 32 consecutive
+// connections of the sorted tile, so its lanes take the same branches.  Every connection's
 // blocks are computed by conn_jac_blocks as before; only which thread computes
 // them changes.
 constexpr int JAC_TILE = 4096;
@@ -158,7 +158,30 @@ __global__ void __launch_bounds__(128) k_jac_conn(const Model* __restrict__ M, B
         }
     }
     __syncthreads();
-    for (int i = t; i < n; i += blockDim.x) idx_s[atomicAdd(&cnt[key_s[i]], 1u)] = (unsigned short)i;
+    // stable placement: within a class the connections keep their order, so
+    // a warp's lanes read neighbouring cells' SoA rows together.  Chunks of
+    // blockDim.x in order; within a chunk, lanes of one key rank by lane
+    // (match_any) and warps take their offsets in turn.
+    {
+        const unsigned lane = t & 31, warp = t >> 5, nwarps = blockDim.x >> 5;
+        for (int base = 0; base < n; base += blockDim.x) {
+            const int i = base + t;
+            const bool valid = i < n;
+            const unsigned key = valid ? key_s[i] : 0xffffu;
+            const unsigned peers = __match_any_sync(0xffffffffu, key);
+            const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+            unsigned off = 0;
+            for (unsigned w = 0; w < nwarps; w++) {
+                if (w == warp && valid && rank == 0) {
+                    off = cnt[key];
+                    cnt[key] = off + __popc(peers);
+                }
+                __syncthreads();
+            }
+            off = __shfl_sync(0xffffffffu, off, __ffs(peers) - 1);
+            if (valid) idx_s[off + rank] = (unsigned short)i;
+        }
+    }
     __syncthreads();
     const int bsize = (b.nc + 1) * (b.nc + 1);
     for (int i = t; i < n; i += blockDim.x) {

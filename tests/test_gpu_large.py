@@ -11,8 +11,10 @@ reference at this size:
 * the adjoint (dR/dT)^T lambda matches central differences on 256 seeded
   connections, and J^T lambda matches the transpose of the assembled Jacobian.
 
-Wells of the configuration are host-side in this design and not part of the
-GPU step.
+and, with eight vertical Peaceman wells (two under a rate target) set on the
+device, the replayed graph of the batched form bit-identical to the plain
+path, the residual with the wells bit-identical to the oracle's wells added
+to the device's own bulk residual, and the Newton update of the wells' bhp.
 """
 import numpy as np
 import pytest
@@ -184,3 +186,53 @@ def test_large_adjoint(case):
         errs.append(abs(fd - g[c]) / max(abs(g[c]), abs(fd), 1e-9 * np.max(np.abs(g))))
     ctx.set("TRANS", T0)
     assert max(errs) <= 1e-6, max(errs)
+
+
+def test_large_wells_in_step(gpu_lib):
+    from oracle import wells as W
+    from opencaeporox_gb300 import wells as WL
+    model = synthetic.comp_model(NCOMP, SEED)
+    grid = synthetic.comp_grid_lognormal(NX, NY, NZ, median=200.0, sigma_ln=1.5, corr_cells=10, seed=SEED)
+    k = np.full(grid.nb, 200.0)
+    wl = WL.vertical_wells(NX, NY, NZ, 4, 4, 20.0, 5.0, k, 0.1 * k, grid.depth, NCOMP, SEED, n_rate=2)
+    nb, nc = grid.nb, model.nc
+    out = {}
+    for variant in (0, 1):
+        with fim.FimContext(model, grid, variant=variant) as ctx:
+            synthetic.ptn_workload(ctx, grid, NCOMP, SEED, dt=DT, dsmax=DSMAX)
+            ctx.set_wells(wl)
+            ctx.checkpoint(0)
+            for rep in range(2):  # a replay from the checkpoint repeats the first
+                ctx.checkpoint(0, restore=True)
+                ctx.enqueue_step(DT)
+                ctx.step_report()
+                got = dict(RES=ctx.get("RES"), JAC=ctx.jacobian()[2], WELLS=ctx.get_wells())
+                if rep:
+                    assert np.array_equal(got["RES"], first["RES"]) and np.array_equal(got["JAC"], first["JAC"])
+                first = got
+            state = {name: ctx.get(f) for name, f in (("P", "P"), ("Pj", "PJ"), ("kr", "KR"), ("mu", "MU"),
+                                                      ("xi", "XI"), ("xij", "XIJ"), ("phaseExist", "PHASE_EXIST"))}
+            u = np.zeros(ctx.nv)
+            u[nb * (nc + 1)::nc + 1] = np.arange(1, len(wl) + 1) * 0.25
+            bhp0 = got["WELLS"][0]
+            ctx.get_solution(u, DSMAX)
+            assert np.array_equal(ctx.get_wells()[0], bhp0 + np.arange(1, len(wl) + 1) * 0.25)
+            out[variant] = (got, state)
+    (a, _), (b, state) = out[0], out[1]
+    assert np.array_equal(a["RES"], b["RES"]) and np.array_equal(a["JAC"], b["JAC"])
+    assert np.array_equal(a["WELLS"][0], b["WELLS"][0]) and a["WELLS"][1] == b["WELLS"][1]
+    # the bulk residual of the same post-flash state without wells, plus the
+    # oracle's wells in the reference's order
+    with fim.FimContext(model, grid, variant=0) as bulk:
+        synthetic.ptn_workload(bulk, grid, NCOMP, SEED, dt=DT, dsmax=DSMAX)
+        bulk.update_property()
+        bulk.cal_res(DT)
+        res_bulk = bulk.get("RES")
+    wells_o = [dict(type=w["type"], mode=w["mode"], bhp=w["bhp"], tar_bhp=w["tar_bhp"], tar_rate=w["tar_rate"],
+                    factor=np.asarray(w["factor"]), inj_zi=np.asarray(w["inj_zi"]), loc=np.asarray(w["cell"]),
+                    WI=np.asarray(w["WI"]), mult=np.ones(len(w["cell"])), dG=np.asarray(w["dG"]),
+                    xi_inj=np.asarray(w["xi_inj"])) for w in wl]
+    ref, ref_mrel = W.residual_with_wells(res_bulk, wells_o, state, DT, nc, 3)
+    bad = np.nonzero(b["RES"] != np.asarray(ref))[0]
+    assert bad.size == 0, f"residual entries {bad[:10]}"
+    assert b["WELLS"][1] == ref_mrel

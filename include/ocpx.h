@@ -54,7 +54,8 @@
 extern "C" {
 #endif
 
-#define OCPX_ABI_VERSION 2
+/* 3: ocpx_create_ex / ocpx_options, parameters 17-19 */
+#define OCPX_ABI_VERSION 3
 
 typedef enum ocpx_status {
     OCPX_OK = 0,

@@ -716,8 +716,11 @@ def fp64_peak(device=0):
 FLASH_FP64_FLOP_PER_CELL = {"fim": (2 * 223408633 + 121682495 + 142721273) / 36000,
                             "large": (2 * 12605259882 + 6716773959 + 8614568226) / 1000000}
 # DRAM bytes (read + write) per cell of one fused-flash launch on the workload
-# (ncu dram__bytes_read.sum + dram__bytes_write.sum of k_flash_fused)
-FLASH_DRAM_BYTES_PER_CELL = {"fim": (155323904 + 250230016) / 36000, "large": None}
+# (ncu dram__bytes_read.sum + dram__bytes_write.sum of k_flash_fused); the large
+# workload's from its generator at 250,000 cells (the traffic, almost all of it
+# the thread frames' local memory, grows with the cells processed)
+FLASH_DRAM_BYTES_PER_CELL = {"fim": (155323904 + 250230016) / 36000,
+                             "large": (2463918000 + 3046760000) / 250000}
 
 
 def conn_jac_flops(nconn, nc):

@@ -3,6 +3,7 @@
 #include "cell_ops.cuh"
 #include "conn_ops.cuh"
 #include "adjoint.cuh"
+#include "tile_sort.cuh"
 
 #include <algorithm>
 
@@ -116,13 +117,14 @@ __device__ __forceinline__ int conn_class(const BulkView& b, const ConnView& cv,
     return key;
 }
 
-// The connection blocks of a tile of JAC_TILE consecutive connections per
-// block of 128 threads: the tile is first sorted by code path (a stable
-// counting sort in shared memory), then each warp takes 32 consecutive
-// connections of the sorted tile, so its lanes take the same branches.  Every connection's
-// blocks are computed by conn_jac_blocks as before; only which thread computes
-// them changes.
+// tiles of JAC_TILE connections (or incidence entries) per block, sorted by code path
 constexpr int JAC_TILE = 4096;
+
+// The connection blocks of a tile of JAC_TILE consecutive connections per
+// block of 128 threads: the tile is first sorted by code path (tile_sort),
+// then each warp takes 32 consecutive connections of the sorted tile, so its
+// lanes take the same branches.  Every connection's blocks are computed by
+// conn_jac_blocks as before; only which thread computes them changes.
 template <int NCT>
 __global__ void __launch_bounds__(128) k_jac_conn(const Model* __restrict__ M, BulkView b, ConnView cv, double dt,
                                                   double* __restrict__ bmat)
@@ -130,84 +132,48 @@ __global__ void __launch_bounds__(128) k_jac_conn(const Model* __restrict__ M, B
     __shared__ unsigned cnt[CONN_CLASSES];
     __shared__ unsigned short key_s[JAC_TILE];
     __shared__ unsigned short idx_s[JAC_TILE];
-    const int t = threadIdx.x;
     const int c0 = blockIdx.x * JAC_TILE;
     const int n = min(JAC_TILE, cv.nconn - c0);
-    for (int k = t; k < CONN_CLASSES; k += blockDim.x) cnt[k] = 0;
-    __syncthreads();
-    for (int i = t; i < n; i += blockDim.x) {
-        const int key = conn_class(b, cv, c0 + i);
-        key_s[i] = (unsigned short)key;
-        atomicAdd(&cnt[key], 1u);
-    }
-    __syncthreads();
-    if (t < 32) {  // exclusive scan of the class counts, 16 per lane
-        constexpr int PER = CONN_CLASSES / 32;
-        unsigned part = 0;
-        for (int k = 0; k < PER; k++) part += cnt[t * PER + k];
-        unsigned incl = part;
-        for (int d = 1; d < 32; d <<= 1) {
-            const unsigned v = __shfl_up_sync(0xffffffffu, incl, d);
-            if (t >= d) incl += v;
-        }
-        unsigned run = incl - part;
-        for (int k = 0; k < PER; k++) {
-            const unsigned v = cnt[t * PER + k];
-            cnt[t * PER + k] = run;
-            run += v;
-        }
-    }
-    __syncthreads();
-    // stable placement: within a class the connections keep their order, so
-    // a warp's lanes read neighbouring cells' SoA rows together.  Chunks of
-    // blockDim.x in order; within a chunk, lanes of one key rank by lane
-    // (match_any) and warps take their offsets in turn.
-    {
-        const unsigned lane = t & 31, warp = t >> 5, nwarps = blockDim.x >> 5;
-        for (int base = 0; base < n; base += blockDim.x) {
-            const int i = base + t;
-            const bool valid = i < n;
-            const unsigned key = valid ? key_s[i] : 0xffffu;
-            const unsigned peers = __match_any_sync(0xffffffffu, key);
-            const unsigned rank = __popc(peers & ((1u << lane) - 1u));
-            unsigned off = 0;
-            for (unsigned w = 0; w < nwarps; w++) {
-                if (w == warp && valid && rank == 0) {
-                    off = cnt[key];
-                    cnt[key] = off + __popc(peers);
-                }
-                __syncthreads();
-            }
-            off = __shfl_sync(0xffffffffu, off, __ffs(peers) - 1);
-            if (valid) idx_s[off + rank] = (unsigned short)i;
-        }
-    }
-    __syncthreads();
+    tile_sort<CONN_CLASSES>(
+        n, [&](int i) { return conn_class(b, cv, c0 + i); }, cnt, key_s, idx_s);
     const int bsize = (b.nc + 1) * (b.nc + 1);
-    for (int i = t; i < n; i += blockDim.x) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int c = c0 + idx_s[i];
         conn_jac_blocks<NCT>(*M, b, cv, c, dt, bmat + (size_t)c * 2 * bsize, bmat + ((size_t)c * 2 + 1) * bsize);
     }
 }
 
-// The side blocks of the connections incident to the cells [c0, c1): one
-// thread per incidence entry (row_conn[row_ptr[c0] .. row_ptr[c1])), each the
-// block k_jac_conn computes for that side, from a copy of the side cell's
-// dSec_dPri at ds[k * soa + (cell - c0)].
+// The side blocks of the connections incident to the cells [c0, c1): the
+// incidence entries row_conn[e0 .. e1) (e0 = row_ptr[c0], e1 = row_ptr[c1]),
+// each the block k_jac_conn computes for that side, from a copy of the side
+// cell's dSec_dPri at ds[k * soa + (cell - c0)].  Tiles of JAC_TILE entries,
+// sorted by code path and side as k_jac_conn's are.
 template <int NCT>
 __global__ void __launch_bounds__(128) k_jac_side(const Model* __restrict__ M, BulkView b, ConnView cv, double dt,
                                                   int c0, uint32_t e0, uint32_t e1, const double* __restrict__ ds,
                                                   size_t soa, double* __restrict__ bmat)
 {
-    const uint32_t e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= e1) return;
-    const uint32_t entry = cv.row_conn[e];
-    const int c = (int)(entry >> 1), side = (int)(entry & 1u);
-    ConnPhase q;
-    conn_phase(*M, b, cv, c, q);
-    const int cell = side ? q.eId : q.bId;
+    __shared__ unsigned cnt[2 * CONN_CLASSES];
+    __shared__ unsigned short key_s[JAC_TILE];
+    __shared__ unsigned short idx_s[JAC_TILE];
+    const uint32_t t0 = e0 + blockIdx.x * JAC_TILE;
+    const int n = (int)min((uint32_t)JAC_TILE, e1 - t0);
+    tile_sort<2 * CONN_CLASSES>(
+        n,
+        [&](int i) {
+            const uint32_t entry = cv.row_conn[t0 + i];
+            return conn_class(b, cv, (int)(entry >> 1)) | (int)((entry & 1u) << 9);
+        },
+        cnt, key_s, idx_s);
     const int bsize = (b.nc + 1) * (b.nc + 1);
-    conn_jac_side<NCT>(b, q, side, ds + (cell - c0), soa, dt, bmat + ((size_t)c * 2 + side) * bsize);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t entry = cv.row_conn[t0 + idx_s[i]];
+        const int c = (int)(entry >> 1), side = (int)(entry & 1u);
+        ConnPhase q;
+        conn_phase(*M, b, cv, c, q);
+        const int cell = side ? q.eId : q.bId;
+        conn_jac_side<NCT>(b, q, side, ds + (cell - c0), soa, dt, bmat + ((size_t)c * 2 + side) * bsize);
+    }
 }
 
 // one warp per Jacobian block row
@@ -328,14 +294,15 @@ cudaError_t launch_jac_side(int nct, const Model* dm, const BulkView& b, const C
                             cudaStream_t s)
 {
     if (e1 <= e0) return cudaSuccess;
-    const int g = grid_for((int)(e1 - e0), block);
+    (void)block;  // tiles of JAC_TILE entries on 128 threads
+    const int g = (int)((e1 - e0 + JAC_TILE - 1) / JAC_TILE);
     switch (nct) {
-    case 3: k_jac_side<3><<<g, block, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
-    case 5: k_jac_side<5><<<g, block, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
-    case 7: k_jac_side<7><<<g, block, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
-    case 9: k_jac_side<9><<<g, block, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
-    case 11: k_jac_side<11><<<g, block, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
-    case 13: k_jac_side<13><<<g, block, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
+    case 3: k_jac_side<3><<<g, 128, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
+    case 5: k_jac_side<5><<<g, 128, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
+    case 7: k_jac_side<7><<<g, 128, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
+    case 9: k_jac_side<9><<<g, 128, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
+    case 11: k_jac_side<11><<<g, 128, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
+    case 13: k_jac_side<13><<<g, 128, 0, s>>>(dm, b, cv, dt, c0, e0, e1, ds, soa, bmat); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -3,6 +3,7 @@
 #include "ocpx_kernels.h"
 #include "cell_ops.cuh"
 #include "flash_coop.cuh"
+#include "tile_sort.cuh"
 
 #ifndef OCPX_NCM
 #error "compile with -DOCPX_NCM=<capacity>"
@@ -317,6 +318,33 @@ __global__ void __launch_bounds__(128) k_dsec_cells(const Model* __restrict__ M,
     else u.recompute_dsec(*M, b, cell, out + (size_t)t * lend, 1);
 }
 
+// dSec_dPri of the cells [first, first + n) into out[k * soa + (cell - first)],
+// tiles of DSEC_TILE cells per block sorted by phase count first, so that the
+// two-phase cells' derivative solve runs on whole warps.
+constexpr int DSEC_TILE = 512;
+template <int NCM>
+__global__ void __launch_bounds__(128) k_dsec_slab(const Model* __restrict__ M, BulkView b, int first, int n,
+                                                   double* __restrict__ out, size_t soa)
+{
+    __shared__ unsigned cnt[32];
+    __shared__ unsigned short key_s[DSEC_TILE];
+    __shared__ unsigned short idx_s[DSEC_TILE];
+    const int c0 = first + blockIdx.x * DSEC_TILE;
+    const int m = min(DSEC_TILE, first + n - c0);
+    tile_sort<32>(
+        m,
+        [&](int i) {
+            const int cell = c0 + i;
+            return (b.phaseExist[b.idx(0, cell)] && b.phaseExist[b.idx(1, cell)]) ? 0 : 1;
+        },
+        cnt, key_s, idx_s);
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int cell = c0 + idx_s[i];
+        CompCellUpdate<NCM> u;
+        u.recompute_dsec(*M, b, cell, out + (cell - first), soa);
+    }
+}
+
 // GetSolution with the cell's dSec_dPri recomputed before its state changes
 template <int NCM>
 __global__ void __launch_bounds__(128) k_newton_update_recompute(const Model* __restrict__ M, BulkView b,
@@ -612,6 +640,12 @@ cudaError_t OCPX_NAME(launch_dsec_cells_)(const Model* dm, const BulkView& b, co
                                           double* out, size_t soa, cudaStream_t s)
 {
     if (n > 0) k_dsec_cells<OCPX_NCM><<<(n + 127) / 128, 128, 0, s>>>(dm, b, list, first, n, out, soa);
+    return cudaGetLastError();
+}
+cudaError_t OCPX_NAME(launch_dsec_slab_)(const Model* dm, const BulkView& b, int first, int n, double* out,
+                                         size_t soa, cudaStream_t s)
+{
+    if (n > 0) k_dsec_slab<OCPX_NCM><<<(n + DSEC_TILE - 1) / DSEC_TILE, 128, 0, s>>>(dm, b, first, n, out, soa);
     return cudaGetLastError();
 }
 cudaError_t OCPX_NAME(launch_newton_update_recompute_)(const Model* dm, const BulkView& b, const double* u,

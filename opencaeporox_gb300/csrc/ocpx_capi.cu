@@ -67,7 +67,8 @@ cudaError_t setup_flash_batched(int ncm, int* excl_smem)
 #define OCPX_RECOMPUTE_DECL(N)                                                                                     \
     cudaError_t launch_dsec_cells_##N(const Model*, const BulkView&, const int*, int, int, double*, size_t,          \
                                       cudaStream_t);                                                                 \
-    cudaError_t launch_newton_update_recompute_##N(const Model*, const BulkView&, const double*, double, cudaStream_t);
+    cudaError_t launch_newton_update_recompute_##N(const Model*, const BulkView&, const double*, double, cudaStream_t); \
+    cudaError_t launch_dsec_slab_##N(const Model*, const BulkView&, int, int, double*, size_t, cudaStream_t);
 #define OCPX_SPLIT_DECL(N)                                                                                         \
     cudaError_t launch_split_refill_##N(const Model*, const BulkView&, const int*, const unsigned*, const uint8_t*,   \
                                         SplitState*, unsigned*, int, cudaStream_t);                                   \
@@ -103,6 +104,11 @@ cudaError_t launch_newton_update_recompute(int ncm, const Model* dm, const BulkV
                                            double dSmax, cudaStream_t s)
 {
     OCPX_NCM_SWITCH(launch_newton_update_recompute_, dm, b, u, dSmax, s)
+}
+cudaError_t launch_dsec_slab(int ncm, const Model* dm, const BulkView& b, int first, int n, double* out, size_t soa,
+                             cudaStream_t s)
+{
+    OCPX_NCM_SWITCH(launch_dsec_slab_, dm, b, first, n, out, soa, s)
 }
 cudaError_t launch_split_refill(int ncm, const Model* dm, const BulkView& b, const int* order, const unsigned* n_split,
                                 const uint8_t* pre, SplitState* st, unsigned* next, int blocks, cudaStream_t s)
@@ -1054,8 +1060,7 @@ ocpx_status enqueue_assemble(ocpx_ctx* ctx, double dt)
         // blocks of the slab's cells
         for (int c0 = 0; c0 < ctx->nb; c0 += ctx->dsec_slab) {
             const int n = std::min(ctx->dsec_slab, ctx->nb - c0);
-            OCPX_CUDA(launch_dsec_cells(ctx->ncm, ctx->d_model, ctx->b, nullptr, c0, n, ctx->dsec_scratch,
-                                        (size_t)n, s));
+            OCPX_CUDA(launch_dsec_slab(ctx->ncm, ctx->d_model, ctx->b, c0, n, ctx->dsec_scratch, (size_t)n, s));
             OCPX_CUDA(launch_jac_side(ctx->nct_cap, ctx->d_model, ctx->b, ctx->cv, dt, c0, ctx->h_row_ptr[c0],
                                       ctx->h_row_ptr[c0 + n], ctx->dsec_scratch, (size_t)n, ctx->bmat,
                                       ctx->block_conn, s));

@@ -69,6 +69,10 @@ cudaError_t launch_jac_side(int nct, const Model* dm, const BulkView& b, const C
                             cudaStream_t s);
 cudaError_t launch_newton_update_recompute(int ncm, const Model* dm, const BulkView& b, const double* u,
                                            double dSmax, cudaStream_t s);
+// dSec_dPri of the cells [first, first + n) into out[k * soa + (cell - first)],
+// two-phase cells first within each tile
+cudaError_t launch_dsec_slab(int ncm, const Model* dm, const BulkView& b, int first, int n, double* out, size_t soa,
+                             cudaStream_t s);
 // The cells at positions [0, *n_split) of the cost order (flash type 2):
 // the split's first loop with lane refill into st[position], then the rest
 // of their flash resumed from it (k_flash_comp.cu, part 8); next: position

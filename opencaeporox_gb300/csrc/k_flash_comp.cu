@@ -345,18 +345,33 @@ __global__ void __launch_bounds__(128) k_dsec_slab(const Model* __restrict__ M, 
     }
 }
 
-// GetSolution with the cell's dSec_dPri recomputed before its state changes
+// GetSolution with the cell's dSec_dPri recomputed before its state changes;
+// tiles of DSEC_TILE cells with the two-phase cells first (their phase labels
+// read before any cell of the tile moves)
 template <int NCM>
 __global__ void __launch_bounds__(128) k_newton_update_recompute(const Model* __restrict__ M, BulkView b,
                                                                  const double* __restrict__ u, double dSmax)
 {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= b.nb) return;
+    __shared__ unsigned cnt[32];
+    __shared__ unsigned short key_s[DSEC_TILE];
+    __shared__ unsigned short idx_s[DSEC_TILE];
+    const int c0 = blockIdx.x * DSEC_TILE;
+    const int m = min(DSEC_TILE, b.nb - c0);
+    tile_sort<32>(
+        m,
+        [&](int i) {
+            const int cell = c0 + i;
+            return (b.phaseExist[b.idx(0, cell)] && b.phaseExist[b.idx(1, cell)]) ? 0 : 1;
+        },
+        cnt, key_s, idx_s);
     constexpr int NCT = NCM + 1;
-    double ds[3 * (NCT + 1) * (NCT + 1)];
-    CompCellUpdate<NCM> cu;
-    cu.recompute_dsec(*M, b, cell, ds, 1);
-    newton_update_cell(b, cell, u, dSmax, ds, 1);
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int cell = c0 + idx_s[i];
+        double ds[3 * (NCT + 1) * (NCT + 1)];
+        CompCellUpdate<NCM> cu;
+        cu.recompute_dsec(*M, b, cell, ds, 1);
+        newton_update_cell(b, cell, u, dSmax, ds, 1);
+    }
 }
 
 // ---- the split cells (flash type 2) with lane refill
@@ -651,7 +666,8 @@ cudaError_t OCPX_NAME(launch_dsec_slab_)(const Model* dm, const BulkView& b, int
 cudaError_t OCPX_NAME(launch_newton_update_recompute_)(const Model* dm, const BulkView& b, const double* u,
                                                        double dSmax, cudaStream_t s)
 {
-    if (b.nb > 0) k_newton_update_recompute<OCPX_NCM><<<(b.nb + 127) / 128, 128, 0, s>>>(dm, b, u, dSmax);
+    if (b.nb > 0)
+        k_newton_update_recompute<OCPX_NCM><<<(b.nb + DSEC_TILE - 1) / DSEC_TILE, 128, 0, s>>>(dm, b, u, dSmax);
     return cudaGetLastError();
 }
 #endif

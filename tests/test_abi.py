@@ -100,3 +100,29 @@ def test_python_structs_match_the_header(tmp_path):
         assert C.alignment(st) == got[(cname, "align")], cname
         for fname, _ in st._fields_:
             assert getattr(st, fname).offset == got[(cname, fname)], (cname, fname)
+
+
+def test_create_options_are_checked_before_the_device():
+    """ocpx_create_ex checks its options with the descriptions, before it
+    looks for a device: a wrong struct_size and the recompute option on a
+    black-oil model are refused (OCPX_INVALID_ARG); a compositional model
+    with the option passes the checks (OCPX_NO_DEVICE here)."""
+    from conftest import _cuda_available
+    if _cuda_available():
+        pytest.skip("a device is present")
+    bo = P.load_fixture("bo_10x10x3")
+    model, grid = fim.model_and_grid_from_dump(bo)
+    with pytest.raises(fim.OcpxError, match="INVALID_ARG.*compositional"):
+        fim.FimContext(model, grid, recompute=True)
+    comp = P.load_fixture("comp6_8x8x3")
+    m2, g2 = fim.model_and_grid_from_dump(comp)
+    with pytest.raises(fim.OcpxError, match="NO_DEVICE"):
+        fim.FimContext(m2, g2, recompute=True)
+    lib = fim.load_library()
+    md, keep1 = m2.desc()
+    gd, keep2 = g2.desc()
+    opt = fim.Options(C.sizeof(fim.Options) - 4, 1)
+    h = C.c_void_p()
+    st = lib.ocpx_create_ex(C.byref(md), C.byref(gd), -1, C.byref(opt), C.byref(h))
+    assert fim.STATUS_NAMES[st] == "INVALID_ARG"
+    assert b"struct_size" in lib.ocpx_last_error()

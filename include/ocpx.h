@@ -13,16 +13,21 @@
  *                           src/MixtureUnit.cpp:87-92), CalKrPc (:1073-1088),
  *                           CalRock (:19-30)
  *   ocpx_calres             IsoT_FIM::CalRes (src/IsoThermalMethod.cpp:1090-1185)
- *                           with OCPConvection01::CalFlux (src/OCPConvection.cpp:22-79),
- *                           bulk part (well terms are added by the host)
+ *                           with OCPConvection01::CalFlux (src/OCPConvection.cpp:22-79);
+ *                           the wells' terms too when they are set on the device
+ *                           (PeacemanWellIsoT::CalResFIM, src/WellPeaceman.cpp:1226),
+ *                           else the host adds them
  *   ocpx_assemble           IsoT_FIM::AssembleMatBulks (src/IsoThermalMethod.cpp:1187-1269)
  *                           with OCPConvection01::AssembleMatFIM (src/OCPConvection.cpp:82-187)
  *                           into LinearSystem::NewDiag/AddDiag/NewOffDiag
- *                           (include/LinearSystem.hpp:61-68)
- *   ocpx_newton_update      IsoT_FIM::GetSolution, bulk part
- *                           (src/IsoThermalMethod.cpp:1282-1418)
+ *                           (include/LinearSystem.hpp:61-68), then AssembleMatWells
+ *                           (:1272-1280) when the wells are on the device
+ *   ocpx_newton_update      IsoT_FIM::GetSolution (src/IsoThermalMethod.cpp:1282-1418),
+ *                           the wells' bhp too when they are on the device
  *   ocpx_update_last_step   IsoT_FIM::UpdateLastTimeStep, bulk part (:1473-1517)
- *   ocpx_linsolve           the linear solve of the Newton system (bulk rows)
+ *   ocpx_linsolve           the linear solve of the Newton system (the wells' rows
+ *                           included when they are on the device)
+ *   ocpx_set_wells          the Peaceman wells of the deck, kept on the device
  *   ocpx_nr_*, ocpx_step_max_change, ocpx_next_time_step
  *                           Newton and time-step control (OCPNRsuite,
  *                           ControlNR, ControlTime), bulk part; see below

@@ -600,10 +600,6 @@ ocpx_status ocpx_create_ex(const ocpx_model_desc* md, const ocpx_grid_desc* gd, 
     // checkpoints keep them)
     if (recompute) add(&b.njhc, D * 2);
     else add(&b.dSec_dPri, D * lend);
-    if (recompute) {
-        ctx->dsec_slab = std::min(nb, RECOMPUTE_SLAB_CELLS);
-        add(&ctx->dsec_scratch, sizeof(double) * (size_t)ctx->dsec_slab * lend);
-    }
     add(&b.poro, D); add(&b.poroP, D); add(&b.rockVp, D);
     add(&b.skip_flag, (size_t)nb); add(&b.skip_minEig, D); add(&b.skip_P, D); add(&b.skip_T, D);
     add(&b.skip_zi, D * (ctx->NC > 0 ? ctx->NC : 1));
@@ -635,6 +631,11 @@ ocpx_status ocpx_create_ex(const ocpx_model_desc* md, const ocpx_grid_desc* gd, 
     add(&ctx->nr_stats, sizeof(double) * 5); add(&ctx->ts_stats, sizeof(double) * 5);
     add(&ctx->nr_res0, sizeof(double)); add(&ctx->nr_state, sizeof(int)); add(&ctx->nr_dt, sizeof(double) * 2);
     add(&ctx->bmat, sizeof(double) * C * 2 * bsize);
+    // the recompute mode's slab scratch, outside the checkpointed state range
+    if (recompute) {
+        ctx->dsec_slab = std::min(nb, RECOMPUTE_SLAB_CELLS);
+        add(&ctx->dsec_scratch, sizeof(double) * (size_t)ctx->dsec_slab * lend);
+    }
     add(&ctx->adj_conn, sizeof(double) * C);
     // field transfers go through the staging buffer in chunks; stored
     // dSec_dPri moves in one piece

@@ -25,6 +25,8 @@ from __future__ import annotations
 
 import numpy as np
 
+PI = 3.141592653  # include/OCPConst.hpp:32: the reference's pi, which its well index uses
+
 
 def peaceman_wi(direction, dx, dy, dz, kx, ky, kz, ntg=1.0, radius=0.1, skin=0.0, conv_darcy=0.008527):
     """Well index of perforations along x (0), y (1) or z (2) (arrays or
@@ -44,7 +46,7 @@ def peaceman_wi(direction, dx, dy, dz, kx, ky, kz, ntg=1.0, radius=0.1, skin=0.0
     ro = 0.28 * np.sqrt(l1 * l1 * np.sqrt(1 / a_b) + l2 * l2 * np.sqrt(a_b))
     ro = ro / (a_b ** 0.25 + (1 / a_b) ** 0.25)
     kh = length * np.sqrt(ab)
-    return 2 * np.pi * kh / (np.log(ro / radius) + skin) * conv_darcy
+    return 2 * PI * kh / (np.log(ro / radius) + skin) * conv_darcy
 
 
 def vertical_wells(nx, ny, nz, n_inj, n_prod, dxy, dz, perm_x, perm_z, depth, ncomp, seed, temp_c=71.85,

@@ -280,3 +280,34 @@ def dipping_corner_point(nx, ny, nz, dxy, dz, top, dip_x_deg, dip_y_deg, pillar_
             for lr in range(2):
                 zc[:, tb, :, fb, :, lr] = zb[tb:nz + tb, fb:ny + fb, lr:nx + lr]
     return coord.ravel(), zc.ravel()
+
+
+def faulted_corner_point(nx, ny, nz, dxy, dz, top, dip_x_deg, dip_y_deg, faults, pillar_tilt=0.0, seed=0):
+    """The grid of dipping_corner_point cut by vertical faults on its pillar
+    lines.  Each fault is (axis, index, throw_start, throw_end[, stretch]):
+    for axis "x" the cells with I > index move down by a throw that varies
+    linearly along the fault, from throw_start at its first pillar (J = 0) to
+    throw_end at its last (J = ny), and their layers are `stretch` times as
+    thick (default 1); for axis "y" the cells with J > index, the throw
+    varying along I.  A throw that changes sign along the fault (a scissor
+    fault) or a change of thickness across it makes the faces on it overlap
+    in shapes other than quadrilaterals; a throw larger than dz makes
+    non-neighbour connections."""
+    coord, zc = dipping_corner_point(nx, ny, nz, dxy, dz, top, dip_x_deg, dip_y_deg, pillar_tilt, seed)
+    z = zc.reshape(nz, 2, ny, 2, nx, 2)              # [K][top/bottom][J][y-/y+][I][x-/x+]
+    for fault in faults:
+        axis, index, t0, t1 = fault[:4]
+        stretch = fault[4] if len(fault) > 4 else 1.0
+        if axis == "x":
+            pj = np.arange(ny)[:, None] + np.arange(2)[None, :]          # pillar J of each corner
+            side = (slice(None), slice(None), slice(None), slice(None), slice(index + 1, None), slice(None))
+            throw = (t0 + (t1 - t0) * pj / ny)[None, None, :, :, None, None]
+        elif axis == "y":
+            pi = np.arange(nx)[:, None] + np.arange(2)[None, :]
+            side = (slice(None), slice(None), slice(index + 1, None), slice(None), slice(None), slice(None))
+            throw = (t0 + (t1 - t0) * pi / nx)[None, None, None, None, :, :]
+        else:
+            raise ValueError("fault axis must be 'x' or 'y'")
+        zs = z[side]
+        z[side] = zs[:1, :1] + stretch * (zs - zs[:1, :1]) + throw
+    return coord, z.ravel()

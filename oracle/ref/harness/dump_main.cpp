@@ -630,6 +630,32 @@ int run_flash(const string& deck, const string& cells, size_t ncell)
     return 0;
 }
 
+/// The reference's overlap area of two faces on a vertical plane
+/// (CalAreaNotQuadr, src/UtilMesh.cpp) for n pairs read from a raw float64
+/// file: per pair face 1 then face 2, each four points (x, depth), the upper
+/// edge first; writes <outdir>/area.npy.
+int run_overlap(const string& pairs_file, size_t n)
+{
+    std::ifstream in(pairs_file, std::ios::binary);
+    vector<double> buf(n * 16);
+    in.read(reinterpret_cast<char*>(buf.data()), buf.size() * sizeof(double));
+    if (!in) { std::cerr << "short pairs file\n"; return 2; }
+    vector<double> area(n);
+    for (size_t m = 0; m < n; m++) {
+        HexahedronFace f[2];
+        for (int s = 0; s < 2; s++) {
+            const double* q = &buf[m * 16 + s * 8];
+            f[s].p0 = Point3D(q[0], q[1], 0);
+            f[s].p1 = Point3D(q[2], q[3], 0);
+            f[s].p2 = Point3D(q[4], q[5], 0);
+            f[s].p3 = Point3D(q[6], q[7], 0);
+        }
+        area[m] = CalAreaNotQuadr(f[0], f[1]);
+    }
+    put(g_out, "area", area);
+    return 0;
+}
+
 } // namespace
 
 int main(int argc, char* argv[])
@@ -638,7 +664,8 @@ int main(int argc, char* argv[])
     MPI_Comm_rank(MPI_COMM_WORLD, &CURRENT_RANK);
     if (argc < 5) {
         std::cerr << "usage: ocp_ref_dump fim <deck> <outdir> <max_iters>\n"
-                     "       ocp_ref_dump flash <deck> <cells.f64> <ncell> <outdir>\n";
+                     "       ocp_ref_dump flash <deck> <cells.f64> <ncell> <outdir>\n"
+                     "       ocp_ref_dump overlap <pairs.f64> <npairs> <outdir>\n";
         return 1;
     }
     const string mode = argv[1];
@@ -647,6 +674,11 @@ int main(int argc, char* argv[])
         g_out = argv[3];
         mkdir_p(g_out);
         rc = run_fim(argv[2], std::atoi(argv[4]));
+    }
+    else if (mode == "overlap") {
+        g_out = argv[4];
+        mkdir_p(g_out);
+        rc = run_overlap(argv[2], std::strtoull(argv[3], nullptr, 10));
     }
     else if (mode == "flash" && argc >= 6) {
         g_out = argv[5];

@@ -47,8 +47,11 @@ RES_KEYS = ["upblock", "dP", "flux_vj", "flux_ni", "res_bulk", "resRelV", "resRe
             "maxRelRes_N", "maxId_V", "maxId_N"]
 
 
+REFERENCE = os.environ.get("OCPX_REFERENCE_DIR", "/root/reference")
+
+
 def build_reference():
-    subprocess.run(["make", "-C", REF_DIR, "-j8"], check=True, stdout=subprocess.DEVNULL)
+    subprocess.run(["make", "-C", REF_DIR, "-j8", f"REF={REFERENCE}"], check=True, stdout=subprocess.DEVNULL)
 
 
 def load_dir(path, keys=None):
@@ -215,19 +218,52 @@ def _comp_fim(nx, ny, nz, ncomp, seed, name, max_iters, packer=pack_fim):
     return data
 
 
-def corner_fixture(nx=6, ny=5, nz=4, seed=7):
-    """The reference's corner-point ingest (COORD / ZCORN) on a dipping grid
-    with leaning pillars: the model dump (cells, connections, half areas,
-    transmissibilities) and the inputs that produced it."""
+# faults of the faulted corner-point fixture (axis, index, throw at the first
+# and last pillar, layer thickness factor of the moved side): a scissor fault
+# along x whose throw changes sign, with thicker layers beyond it; a scissor
+# fault along y with thinner layers; an x fault throwing two layers (NNCs
+# across two layers)
+CPG_FAULTS = [("x", 3, -4.5, 7.5, 1.5), ("y", 2, 1.2, -2.0, 0.6), ("x", 5, 6.0, 6.0, 0.7)]
+
+
+def corner_inputs(nx, ny, nz, seed, faults=None):
+    """COORD, ZCORN and rock arrays of a seeded dipping corner-point grid with
+    leaning pillars (cut by `faults`, see synthetic.faulted_corner_point)."""
     sys.path.insert(0, REPO)
     from opencaeporox_gb300 import synthetic
-    coord, zcorn = synthetic.dipping_corner_point(nx, ny, nz, 20.0, 3.0, 2000.0, 4.0, -3.0, 0.05, seed=seed)
+    if faults:
+        coord, zcorn = synthetic.faulted_corner_point(nx, ny, nz, 20.0, 3.0, 2000.0, 4.0, -3.0, faults, 0.05,
+                                                      seed=seed)
+    else:
+        coord, zcorn = synthetic.dipping_corner_point(nx, ny, nz, 20.0, 3.0, 2000.0, 4.0, -3.0, 0.05, seed=seed)
     n = nx * ny * nz
     rng = np.random.default_rng(seed)
     kx = np.exp(rng.normal(np.log(100.0), 1.0, n))
     ky = kx * rng.uniform(0.5, 1.5, n)
     kz = 0.1 * kx
     poro = rng.uniform(0.15, 0.3, n)
+    return coord, zcorn, kx, ky, kz, poro
+
+
+def fault_fim_fixture(nx=8, ny=6, nz=5, seed=11, ncomp=3, max_iters=3):
+    """Newton iterations of the reference on the faulted corner-point grid of
+    cpg_fault_8x6x5 (a compositional deck with two wells), dumped like the
+    other FIM fixtures, plus the grid inputs."""
+    coord, zcorn, kx, ky, kz, poro = corner_inputs(nx, ny, nz, seed, CPG_FAULTS)
+    text = decks.corner_grid_block(nx, ny, nz, coord, zcorn, poro, kx, ky, kz)
+    ni, deck_text = decks.comp_deck(nx, ny, nz, ncomp, seed, grid_text=text, tsteps=(0.02, 0.05, 0.1), smooth=True)
+    data = run_fim(deck_text, "fault", max_iters, ni=ni, calibrate=True)
+    data.update({"input/dims": np.array([nx, ny, nz]), "input/coord": coord, "input/zcorn": zcorn,
+                 "input/kx": kx, "input/ky": ky, "input/kz": kz, "input/poro": poro})
+    return data
+
+
+def corner_fixture(nx=6, ny=5, nz=4, seed=7, faults=None):
+    """The reference's corner-point ingest (COORD / ZCORN) on a dipping grid
+    with leaning pillars (cut by `faults`): the model dump (cells,
+    connections, half areas, transmissibilities) and the inputs that produced
+    it."""
+    coord, zcorn, kx, ky, kz, poro = corner_inputs(nx, ny, nz, seed, faults)
     text = decks.corner_grid_block(nx, ny, nz, coord, zcorn, poro, kx, ky, kz)
     ni, deck_text = decks.comp_deck(nx, ny, nz, 3, seed, grid_text=text)
     with tempfile.TemporaryDirectory() as tmp:
@@ -243,12 +279,52 @@ def corner_fixture(nx=6, ny=5, nz=4, seed=7):
     return data
 
 
+def overlap_pairs(n=1536, seed=5):
+    """Seeded pairs of faces on a vertical plane between two slightly leaning
+    pillars 20 m apart (points (x, depth): p0 upper and p3 lower on the right
+    pillar, p1 upper and p2 lower on the left), with independent tops and
+    thicknesses so that every crossing pattern of their edges occurs; the last
+    64 pairs have parallel upper edges."""
+    rng = np.random.default_rng(seed)
+    out = np.empty((n, 2, 4, 2))
+    for s in range(2):
+        top_r, top_l = rng.uniform(0, 10, n), rng.uniform(0, 10, n)
+        th_r, th_l = rng.uniform(0.5, 10, n), rng.uniform(0.5, 10, n)
+        lean = rng.uniform(-0.05, 0.05, (n, 2))
+        if s == 1:
+            top_r[-64:] = out[-64:, 0, 0, 1] + 1.5
+            top_l[-64:] = out[-64:, 0, 1, 1] + 1.5
+            lean[-64:] = 0.0
+        d = np.stack([top_r, top_l, top_l + th_l, top_r + th_r], 1)
+        if s == 0:
+            lean[-64:] = 0.0
+        x = np.stack([20.0 + lean[:, 0] * d[:, 0], lean[:, 1] * d[:, 1], lean[:, 1] * d[:, 2],
+                      20.0 + lean[:, 0] * d[:, 3]], 1)
+        out[:, s, :, 0], out[:, s, :, 1] = x, d
+    return out
+
+
+def overlap_fixture():
+    """The reference's CalAreaNotQuadr on overlap_pairs()."""
+    pairs = overlap_pairs()
+    with tempfile.TemporaryDirectory() as tmp:
+        f = os.path.join(tmp, "pairs.f64")
+        pairs.astype("<f8").tofile(f)
+        out = os.path.join(tmp, "out")
+        subprocess.run([DUMP, "overlap", f, str(len(pairs)), out], check=True, stdout=subprocess.DEVNULL)
+        area = np.load(os.path.join(out, "area.npy"))
+    return {"pairs": pairs, "area": area}
+
+
 FIXTURES = {
     "bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12),
     "comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4),
     "comp8_6x6x4": lambda: _comp_fim(6, 6, 4, 8, 4, "c8", 4),
     "flash10": lambda: run_flash(10, 1024, 3),
     "cpg_6x5x4": corner_fixture,
+    "cpg_fault_8x6x5": lambda: corner_fixture(8, 6, 5, 11, faults=CPG_FAULTS),
+    "overlap_area": overlap_fixture,
+    "fault_comp3_8x6x5": fault_fim_fixture,
     "wells_bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12, packer=pack_wells),
     "wells_comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4, packer=pack_wells),
 }

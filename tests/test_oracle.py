@@ -1,5 +1,6 @@
 """Pins the oracle's C restatement against the golden fixtures dumped from
-the reference itself (CPU only).
+the reference itself (CPU only), including Newton iterations on a faulted
+corner-point grid (fault_comp3_8x6x5: NNCs and partly overlapping faces).
 
 Tolerances as in the GPU parity tests: labels and upwind choices exact,
 values within REL_TOL, derivative-solve outputs per-cell normwise (the
@@ -11,7 +12,21 @@ import parity as P
 from opencaeporox_gb300 import fim
 from oracle.pyoracle import OracleBulk
 
-FIXTURES = ["bo_10x10x3", "comp6_8x8x3", "comp8_6x6x4"]
+FIXTURES = ["bo_10x10x3", "comp6_8x8x3", "comp8_6x6x4", "fault_comp3_8x6x5"]
+
+
+def _split_newton_count_is_rounding_decided(model, grid, fx, it, cell, seeds=6):
+    """Whether the oracle's split-Newton iteration count of `cell` changes
+    when every exp, log, pow, acos and cos result moves by one ulp (seeded)."""
+    counts = set()
+    for seed in range(seeds):
+        ob = OracleBulk(model, grid, variant="ulp")
+        ob.set_nudge_seed(seed, 1)
+        ob.load(P.jac_state(fx, it))
+        ob.load(P.group(fx, it + "/pre"))
+        ob.update_property()
+        counts.add(int(ob.a["iters"].reshape(-1, 5)[cell, 3]))
+    return len(counts) > 1
 
 
 @pytest.mark.parametrize("name", FIXTURES)
@@ -33,14 +48,18 @@ def test_oracle_property_update(name):
         if model.compositional:
             assert np.array_equal(got["ftype"], post["flash_ftype"]), it
             # iteration counts match except where the split Newton stalled at
-            # the rounding floor of its residual (it ran into its iteration
-            # cap): there the final |r| ~ tol comparison is decided by
-            # rounding (the reference's dnrm2 is OpenBLAS's), a
-            # threshold-adjacent cell; its converged state still matches.
+            # the rounding floor of its residual: there the final |r| ~ tol
+            # comparison (or the residual-growth exit) is decided by rounding
+            # (the reference's dnrm2 is OpenBLAS's), a threshold-adjacent
+            # cell; its converged state still matches.  Such a cell either ran
+            # into the iteration cap, or its split-Newton count moves when
+            # the oracle's transcendentals move by one ulp.
             gi, ri = got["iters"].reshape(-1, 5), post["flash_iters"].reshape(-1, 5)
             differ = np.any(gi != ri, axis=1)
             capped = (gi[:, 3] > 55) | (ri[:, 3] > 55)
-            assert not np.any(differ & ~capped), it
+            other = np.nonzero(differ & ~capped)[0]
+            assert np.array_equal(np.delete(gi[other], 3, axis=1), np.delete(ri[other], 3, axis=1)), it
+            assert all(_split_newton_count_is_rounding_decided(model, grid, fx, it, c) for c in other), it
             assert np.sum(differ) <= 2, it
             assert np.array_equal(got["skip_flag"], post["skip_flag"].astype(np.uint32)), it
         ob.cal_res(float(pre["dt"][0]))

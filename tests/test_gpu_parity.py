@@ -30,7 +30,7 @@ from opencaeporox_gb300 import fim
 
 pytestmark = pytest.mark.gpu
 
-FIXTURES = ["bo_10x10x3", "comp6_8x8x3", "comp8_6x6x4"]
+FIXTURES = ["bo_10x10x3", "comp6_8x8x3", "comp8_6x6x4", "fault_comp3_8x6x5"]
 REPORT = {}
 
 

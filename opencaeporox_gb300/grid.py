@@ -35,44 +35,96 @@ import numpy as np
 from .fim import Grid
 
 
-def orthogonal_grid(nx, ny, nz, dx, dy, dz, tops, kx, ky, kz, poro, ntg=None, conv_darcy=0.008527):
+def active_cells(v, poro, actnum=None, eps_v=1e-6, eps_poro=1e-6):
+    """Cells the reference keeps: pore fraction and volume at least 1e-6 and
+    ACTNUM not 0 (ActiveGridCheck::CheckActivityIsoT,
+    src/PreParamGridWell.cpp:856-872)."""
+    act = (poro >= eps_poro) & (v >= eps_v)
+    if actnum is not None:
+        act &= np.asarray(actnum).ravel() != 0
+    return act
+
+
+def _trans(mult, T1, T2, conv_darcy):
+    """BulkConnTransMethod01::CalTrans (src/BulkConnFunc.cpp:15-67)."""
+    return mult / (1 / T1 + 1 / T2) * conv_darcy
+
+
+def _compress(n, act, b, e, t, v, depth, poro, geo):
+    """The active cells' grid: cells renumbered in order, connections between
+    active cells (their order is kept)."""
+    a2 = np.full(n, -1, np.int64)
+    a2[act] = np.arange(int(act.sum()))
+    keep = act[b] & act[e]
+    g = Grid(v=v[act], depth=depth[act], poro_init=poro[act], conn_b=a2[b[keep]].astype(np.uint32),
+             conn_e=a2[e[keep]].astype(np.uint32), conn_trans=t[keep])
+    geo = {k: (x[act] if np.ndim(x) and len(x) == n else x) for k, x in geo.items()}
+    geo["act2all"] = np.nonzero(act)[0]
+    geo["conn_keep"] = keep
+    return g, geo
+
+
+def orthogonal_grid(nx, ny, nz, dx, dy, dz, tops, kx, ky, kz, poro, ntg=None, conv_darcy=0.008527, actnum=None,
+                    multz=None, return_geometry=False):
+    """Cells and connections of a block-centred grid in the reference's order
+    (see the module docstring).  As the reference: the pore fraction is
+    PORO * NTG when NTG is given, the volume dx dy dz, and NTG scales the
+    transmissibility across x and y; only active cells are kept (active_cells,
+    with ACTNUM); a cell whose neighbour across x (or y) is inactive gets no
+    connection in the later directions either (the loop's `continue`,
+    src/PreParamGridWell.cpp:1166-1167); MULTZ of the upper cell scales the
+    transmissibility across z.  return_geometry adds, per active cell, its
+    index among all cells, dx, dy, dz, NTG and the permeabilities."""
     n = nx * ny * nz
     f = lambda a: np.broadcast_to(np.asarray(a, np.float64), (n,)).copy() if np.ndim(a) == 0 else np.asarray(a, np.float64).ravel()
     dx, dy, dz, kx, ky, kz, poro = (f(a) for a in (dx, dy, dz, kx, ky, kz, poro))
-    ntg = np.ones(n) if ntg is None else f(ntg)
-    v = dx * dy * dz * ntg
-    # depth: cell centre, tops of the first layer plus accumulated thickness
-    top = np.empty(n)
+    ntg_given = ntg is not None
+    ntg = f(ntg) if ntg_given else np.ones(n)
+    if ntg_given:
+        poro = poro * ntg
+    v = dx * dy * dz
+    # depth of the cell centres: the top layer from TOPS, then each layer half
+    # a thickness below the centre of the one above plus half its own
+    # (CalDepthVOrthogonalGrid, src/PreParamGridWell.cpp:1036-1064)
     layer = nx * ny
-    top[:layer] = f(tops)[:layer] if np.ndim(tops) else tops
+    depth = np.empty(n)
+    t = np.broadcast_to(np.asarray(tops, np.float64), (layer,)) if np.ndim(tops) == 0 else np.asarray(tops, np.float64).ravel()[:layer]
+    depth[:layer] = t + dz[:layer] / 2
     for k in range(1, nz):
-        top[k * layer:(k + 1) * layer] = top[(k - 1) * layer:k * layer] + dz[(k - 1) * layer:k * layer]
-    depth = top + dz / 2
+        cur, prev = slice(k * layer, (k + 1) * layer), slice((k - 1) * layer, k * layer)
+        depth[cur] = depth[prev] + dz[prev] / 2 + dz[cur] / 2
+    act = active_cells(v, poro, actnum)
     idx = np.arange(n)
     i = idx % nx
     j = (idx // nx) % ny
     k = idx // layer
-    # per direction, vectorised; then ordered by (bId, direction x < y < z) as
-    # the reference's cell loop emits them
+    # per direction, vectorised; a cell stops at its first inactive neighbour
+    # (x, then y, then z); then ordered by (bId, direction x < y < z) as the
+    # reference's cell loop emits them
+    mz = np.ones(n) if multz is None else f(multz)
+    going = act.copy()
     bs, es, ts, keys = [], [], [], []
-    for d, (cond, step, area, perm) in enumerate((
-            (i < nx - 1, 1, 2 * dy * dz / dx, kx * ntg),
-            (j < ny - 1, nx, 2 * dz * dx / dy, ky * ntg),
-            (k < nz - 1, layer, 2 * dx * dy / dz, kz))):
-        bId = idx[cond]
+    for d, (cond, step, area, perm, mult) in enumerate((
+            (i < nx - 1, 1, 2 * dy * dz / dx, kx * ntg, np.ones(n)),
+            (j < ny - 1, nx, 2 * dz * dx / dy, ky * ntg, np.ones(n)),
+            (k < nz - 1, layer, 2 * dx * dy / dz, kz, mz))):
+        cand = going & cond
+        nb_ = np.minimum(idx + step, n - 1)
+        ok = cand & act[nb_]
+        going &= ~(cand & ~act[nb_])
+        bId = idx[ok]
         eId = bId + step
-        T1 = perm[bId] * area[bId]
-        T2 = perm[eId] * area[eId]
         bs.append(bId)
         es.append(eId)
-        ts.append(1.0 / (1 / T1 + 1 / T2) * conv_darcy)
+        ts.append(_trans(mult[bId], perm[bId] * area[bId], perm[eId] * area[eId], conv_darcy))
         keys.append(bId * 3 + d)
     order = np.argsort(np.concatenate(keys), kind="stable")
     b_list = np.concatenate(bs)[order]
     e_list = np.concatenate(es)[order]
     t_list = np.concatenate(ts)[order]
-    return Grid(v=v, depth=depth, poro_init=poro, conn_b=np.array(b_list, np.uint32),
-                conn_e=np.array(e_list, np.uint32), conn_trans=np.array(t_list))
+    grid, geo = _compress(n, act, b_list, e_list, t_list, v, depth, poro,
+                          dict(dx=dx, dy=dy, dz=dz, ntg=ntg, kx=kx, ky=ky, kz=kz))
+    return (grid, geo) if return_geometry else grid
 
 
 TINY = 1e-8     # include/OCPConst.hpp:30
@@ -316,13 +368,23 @@ def _projected_area(F, O, Fa, axis):
 
 
 def corner_point_grid(nx, ny, nz, coord, zcorn, kx, ky, kz, poro, ntg=None, conv_darcy=0.008527,
-                      return_geometry=False):
+                      return_geometry=False, actnum=None, multz=None):
     """Cells and connections of a corner-point grid (COORD, ZCORN in Eclipse
-    order), in the reference's order; see the module docstring."""
+    order), in the reference's order; see the module docstring.  As the
+    reference: the pore fraction is PORO * NTG when NTG is given, NTG scales
+    the transmissibility across x and y, MULTZ of the upper cell the one
+    across z; the connections are found among all cells, then only active
+    cells (active_cells, with ACTNUM) and the connections between them are
+    kept.  return_geometry adds the half areas, the axis of each connection,
+    and per active cell its index among all cells, dx, dy, dz (between the
+    centres of opposite faces), NTG and the permeabilities."""
     n = nx * ny * nz
     f = lambda a: np.broadcast_to(np.asarray(a, np.float64), (n,)).copy() if np.ndim(a) == 0 else np.asarray(a, np.float64).ravel()
     kx, ky, kz, poro = (f(a) for a in (kx, ky, kz, poro))
-    ntg = np.ones(n) if ntg is None else f(ntg)
+    ntg_given = ntg is not None
+    ntg = f(ntg) if ntg_given else np.ones(n)
+    if ntg_given:
+        poro = poro * ntg
     coord = np.asarray(coord, np.float64).ravel()
     z = np.asarray(zcorn, np.float64).reshape(nz, 2, ny, 2, nx, 2)   # [K][top/bottom][J][y-/y+][I][x-/x+]
     K, J, I = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
@@ -424,13 +486,25 @@ def corner_point_grid(nx, ny, nz, coord, zcorn, kx, ky, kz, poro, ntg=None, conv
     partner = first[pos]
     keep = found & (he > hb) & ~(Ad <= 0) & ~(Ad[partner] <= 0)
     b, e, aB, aE = hb[keep], he[keep], Ad[keep], Ad[partner][keep]
-    axis = np.array([0, 0, 1, 1, 2, 2])[hslot[keep] // span]
+    direction = hslot[keep] // span
+    axis = np.array([0, 0, 1, 1, 2, 2])[direction]
     perm = np.stack([kx, ky, kz])
     T1 = np.where(axis < 2, ntg[b], 1.0) * perm[axis, b] * aB
     T2 = np.where(axis < 2, ntg[e], 1.0) * perm[axis, e] * aE
-    trans = 1.0 / (1 / T1 + 1 / T2) * conv_darcy
-    grid = Grid(v=v, depth=depth, poro_init=poro, conn_b=np.array(b, np.uint32),
-                conn_e=np.array(e, np.uint32), conn_trans=trans)
+    mult = np.ones(b.size) if multz is None else np.where(direction == 5, f(multz)[b], 1.0)
+    trans = _trans(mult, T1, T2, conv_darcy)
+    # dx, dy, dz: between the centres of opposite faces, each taken from the
+    # cell centre as the reference forms them (src/CornerGrid.cpp:1085-1094)
+    half = [0.25 * (P[:, a] + P[:, b_] + P[:, c_] + P[:, d_]) - center for (a, b_, c_, d_) in FACE]
+    size = []
+    for lo, hi in ((0, 1), (2, 3), (4, 5)):
+        dp = half[hi] - half[lo]
+        size.append(np.sqrt(dp[:, 0] * dp[:, 0] + dp[:, 1] * dp[:, 1] + dp[:, 2] * dp[:, 2]))
+    act = active_cells(v, poro, actnum)
+    grid, geo = _compress(n, act, b, e, trans, v, depth, poro,
+                          dict(dx=size[0], dy=size[1], dz=size[2], ntg=ntg, kx=kx, ky=ky, kz=kz))
     if return_geometry:
-        return grid, dict(areaB=aB, areaE=aE, axis=axis, center=center, corners=P)
+        k = geo.pop("conn_keep")
+        geo.update(areaB=aB[k], areaE=aE[k], axis=axis[k], center=center[act], corners=P[act])
+        return grid, geo
     return grid

@@ -316,6 +316,84 @@ def overlap_fixture():
     return {"pairs": pairs, "area": area}
 
 
+def grid_deck_texts(kind, seed=21):
+    """GRID sections for the deck-reader fixtures: `kind` is "ortho" or
+    "corner" (the faulted grid of cpg_fault_8x6x5), then "_actnum" (inactive
+    cells by ACTNUM, by an EQUALS box of ACTNUM and by zero porosity, with
+    NTG) or "_multz" (all cells active, with NTG and MULTZ).  Arrays come as
+    plain values, `m*v` repeats, EQUALS / MULTIPLY / COPY boxes and one
+    INCLUDE file.  Returns (nx, ny, nz, grid_text, include_text)."""
+    rng = np.random.default_rng(seed)
+    corner = kind.startswith("corner")
+    nx, ny, nz = (8, 6, 5) if corner else (7, 5, 4)
+    n = nx * ny * nz
+    lines = [f"DIMENS\n{nx} {ny} {nz} /\n"]
+    if corner:
+        coord, zcorn, kx, ky, kz, poro = corner_inputs(nx, ny, nz, 11, CPG_FAULTS)
+        lines.append(f"COORD\n{decks._fmt(coord)}\n/\nZCORN\n{decks._fmt(zcorn)}\n/\n")
+    else:
+        dx = np.repeat(rng.uniform(15.0, 25.0, nx)[None, :], ny * nz, 0).ravel()
+        dy = np.tile(np.repeat(rng.uniform(15.0, 25.0, ny), nx), nz)
+        dz = np.repeat(rng.uniform(2.0, 6.0, nz), nx * ny) * rng.uniform(0.9, 1.1, n)
+        tops = 2000.0 + rng.uniform(-3.0, 3.0, nx * ny)
+        lines.append(f"DX\n{decks._fmt(dx)}\n/\nDY\n{decks._fmt(dy)}\n/\n"
+                     f"-- layer thicknesses vary cell by cell\nDZ\n{decks._fmt(dz)}\n/\n"
+                     f"TOPS\n{decks._fmt(tops)}\n/\n")
+        kx = np.exp(rng.normal(np.log(100.0), 1.0, n))
+        poro = rng.uniform(0.15, 0.3, n)
+    ntg = rng.uniform(0.5, 1.0, n)
+    if kind.endswith("_actnum"):
+        poro = poro.copy()
+        poro[[5, 17, n - 9]] = 0.0                       # inactive by the pore-volume cut
+    include = f"PORO\n{decks._fmt(poro)}\n/\n"
+    lines.append("INCLUDE\n'grid_poro.inc' /\n")
+    lines.append(f"PERMX\n{decks._fmt(kx)}\n/\n")
+    lines.append(f"NTG\n{decks._fmt(ntg)}\n/\n")
+    # PERMY from PERMX, scaled in a box; PERMZ a tenth of PERMX
+    lines.append("COPY\nPERMX PERMY 6* /\nPERMX PERMZ 6* /\n/\n")
+    lines.append(f"MULTIPLY\nPERMY 0.7 2 {nx - 1} 1* {ny} 2* /\nPERMZ 0.1 6* /\n/\n")
+    lines.append(f"EQUALS\nPERMY 55.5 1 2 1 1 1 {nz} /\n/\n")
+    if kind.endswith("_actnum"):
+        act = np.ones(n, np.int64)
+        off = [3 + nx * 2, 4 + nx * 2 + nx * ny, 2 + nx * (ny - 2) + 2 * nx * ny, 1 + nx + nx * ny]
+        act[off] = 0
+        # one run of repeats, as decks write long runs
+        body = " ".join(f"{v}" for v in act[:nx * ny]) + "\n" + f"{n - nx * ny - 1}*1 1"
+        tail = act[nx * ny:]
+        if np.all(tail == 1):
+            text = body
+        else:
+            text = " ".join(f"{v}" for v in act[:nx * ny]) + "\n" + " ".join(f"{v}" for v in tail)
+        lines.append(f"ACTNUM\n{text}\n/\n")
+        # and a box of inactive cells away from the wells' columns
+        lines.append(f"EQUALS\nACTNUM 0 {nx - 2} {nx - 2} 2 3 2 2 /\n/\n")
+    else:
+        multz = rng.uniform(0.05, 1.0, n)
+        lines.append(f"MULTZ\n{decks._fmt(multz)}\n/\n")
+    return nx, ny, nz, "".join(lines), include
+
+
+def deck_grid_fixture(kind):
+    """The reference's grid from a GRID section of grid_deck_texts(kind)
+    inside a compositional deck with two wells: the model dump and the deck
+    texts (the test reads them with opencaeporox_gb300.deck)."""
+    nx, ny, nz, grid_text, include = grid_deck_texts(kind)
+    ni, deck_text = decks.comp_deck(nx, ny, nz, 3, 21, grid_text=grid_text)
+    with tempfile.TemporaryDirectory() as tmp:
+        deck = os.path.join(tmp, "grid.data")
+        with open(deck, "w") as f:
+            f.write(deck_text)
+        with open(os.path.join(tmp, "grid_poro.inc"), "w") as f:
+            f.write(include)
+        ni.astype("<f8").tofile(deck + ".ptn_ni")
+        out = os.path.join(tmp, "out")
+        subprocess.run([DUMP, "fim", deck, out, "0"], check=True, stdout=subprocess.DEVNULL)
+        data = {f"model/{k}": v for k, v in load_dir(os.path.join(out, "model")).items()}
+    data["deck/main"] = np.array(deck_text)
+    data["deck/include"] = np.array(include)
+    return data
+
+
 FIXTURES = {
     "bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12),
     "comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4),
@@ -325,6 +403,10 @@ FIXTURES = {
     "cpg_fault_8x6x5": lambda: corner_fixture(8, 6, 5, 11, faults=CPG_FAULTS),
     "overlap_area": overlap_fixture,
     "fault_comp3_8x6x5": fault_fim_fixture,
+    "deck_ortho_actnum": lambda: deck_grid_fixture("ortho_actnum"),
+    "deck_ortho_multz": lambda: deck_grid_fixture("ortho_multz"),
+    "deck_corner_actnum": lambda: deck_grid_fixture("corner_actnum"),
+    "deck_corner_multz": lambda: deck_grid_fixture("corner_multz"),
     "wells_bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12, packer=pack_wells),
     "wells_comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4, packer=pack_wells),
 }

@@ -1,0 +1,169 @@
+"""The GRID-section deck reader (opencaeporox_gb300.deck) against the
+reference's own reading and grid set-up: four decks made by
+tests/golden/gen_fixtures.py (grid_deck_texts) were read by the reference,
+whose harness dumped the grid it built (deck_*.npz).  Block-centred and
+faulted corner-point grids, with inactive cells (ACTNUM, an EQUALS box of
+ACTNUM, zero porosity) and NTG, or with NTG and MULTZ; arrays given as plain
+values, m*v repeats, COPY / MULTIPLY / EQUALS boxes and an INCLUDE file.
+Host only."""
+import numpy as np
+import pytest
+
+import parity as P
+from opencaeporox_gb300 import deck as D
+
+DECKS = ["deck_ortho_actnum", "deck_ortho_multz", "deck_corner_actnum", "deck_corner_multz"]
+
+
+def _read(fx, tmp_path):
+    (tmp_path / "grid.data").write_text(str(fx["deck/main"]))
+    (tmp_path / "grid_poro.inc").write_text(str(fx["deck/include"]))
+    return D.read_grid_deck(str(tmp_path / "grid.data"))
+
+
+@pytest.mark.parametrize("name", DECKS)
+def test_grid_from_deck_against_reference(name, tmp_path):
+    fx = P.load_fixture(name)
+    deck = _read(fx, tmp_path)
+    g, geo = D.grid_from_deck(deck, float(fx["model/CONV_DARCY"].ravel()[0]))
+    m = lambda k: fx["model/" + k]
+    assert g.nb == int(m("nb").ravel()[0])
+    assert np.array_equal(g.conn_b, m("conn_bId")) and np.array_equal(g.conn_e, m("conn_eId"))
+    assert np.array_equal(g.conn_trans, m("conn_trans"))
+    assert np.array_equal(g.depth, m("depth")) and np.array_equal(g.poro_init, m("poroInit"))
+    for k, mk in (("dx", "dx"), ("dy", "dy"), ("dz", "dz"), ("ntg", "ntg"), ("kx", "rockKx"), ("ky", "rockKy"),
+                  ("kz", "rockKz")):
+        assert np.array_equal(geo[k], m(mk)), k
+    if deck.corner:
+        # Gauss quadrature against the reference's expanded polynomial
+        assert np.max(np.abs(g.v - m("v")) / m("v")) < 1e-13
+    else:
+        assert np.array_equal(g.v, m("v"))
+    if name.endswith("_actnum"):
+        assert g.nb < deck.n
+
+
+def test_inactive_x_neighbour_ends_the_cells_connections(tmp_path):
+    """A cell whose +x neighbour is inactive gets no +y or +z connection
+    either (the reference's loop leaves the cell at the first inactive
+    neighbour), and the reference's own grid agrees (previous test)."""
+    fx = P.load_fixture("deck_ortho_actnum")
+    deck = _read(fx, tmp_path)
+    g, geo = D.grid_from_deck(deck)
+    nx, ny, n = deck.nx, deck.ny, deck.n
+    a2 = np.full(n, -1)
+    a2[geo["act2all"]] = np.arange(g.nb)
+    pairs = set(zip(g.conn_b.tolist(), g.conn_e.tolist()))
+    seen = 0
+    for c in geo["act2all"]:
+        i, j = c % nx, (c // nx) % ny
+        if i < nx - 1 and a2[c + 1] < 0 and j < ny - 1 and a2[c + nx] >= 0:
+            assert (a2[c], a2[c + nx]) not in pairs
+            seen += 1
+    assert seen >= 1
+
+
+def _write(tmp_path, text, name="d.data"):
+    p = tmp_path / name
+    p.write_text(text)
+    return str(p)
+
+
+def test_reader_syntax(tmp_path):
+    text = """-- a comment
+# another
+DIMENS
+2 2 2 /
+DX 99 99
+8*10.0
+/
+DY
+4*5.0 4*6.0 /
+DZ
+1, 2, 3, 4 -- trailing words are not values
+/
+-- the data above stops at the first '/', the rest of the line is dropped
+TOPS
+'100' 100 101 101
+/
+PORO
+8*0.25
+/
+EQUALS
+PORO 0.1 1 1 1 1 1 2 /
+TOPS 50 2 2 2* 2 2 /
+/
+MULTIPLY
+DX 2 1 1 6* /
+/
+SOMEKEY
+1 2 3 /
+/
+"""
+    with pytest.raises(ValueError):
+        # "--" is not a value: the reference stops on it too
+        D.read_grid_deck(_write(tmp_path, text))
+    text = text.replace(" -- trailing words are not values", " /")
+    d = D.read_grid_deck(_write(tmp_path, text))
+    A = d.arrays
+    assert (d.nx, d.ny, d.nz) == (2, 2, 2)
+    # MULTIPLY DX 2 over i = 1 (all j, k): cells with i == 0 doubled
+    assert np.array_equal(A["DX"], np.where(np.arange(8) % 2 == 0, 20.0, 10.0))
+    assert np.array_equal(A["DY"], np.r_[[5.0] * 4, [6.0] * 4])
+    assert np.array_equal(A["DZ"], [1.0, 2.0, 3.0, 4.0])
+    # TOPS: the EQUALS box (i = 2, every j, k = 2) is cut to the top layer
+    assert np.array_equal(A["TOPS"], [100.0, 50.0, 101.0, 50.0])
+    # EQUALS PORO over i = 1, j = 1, k = 1..2
+    assert np.array_equal(A["PORO"], np.where(np.arange(8) % 4 == 0, 0.1, 0.25))
+
+
+def test_include_copy_and_errors(tmp_path):
+    (tmp_path / "perm.inc").write_text("PERMX\n4*100 4*200\n/\n")
+    main = _write(tmp_path, """DIMENS
+2 2 2 /
+INCLUDE
+'perm.inc' /
+COPY
+PERMX PERMY 6* /
+PERMX PERMZ 1 1 1 2 1 2 /
+/
+""")
+    d = D.read_grid_deck(main)
+    A = d.arrays
+    assert np.array_equal(A["PERMY"], A["PERMX"])
+    assert np.array_equal(A["PERMZ"], np.where(np.arange(8) % 2 == 0, A["PERMX"], 0.0))
+    with pytest.raises(ValueError, match="not given"):
+        D.read_grid_deck(_write(tmp_path, "DIMENS\n2 2 2 /\nMULTIPLY\nPORO 2 6* /\n/\n", "m.data"))
+    with pytest.raises(ValueError, match="PORO"):
+        D.grid_from_deck(d)
+    # a '/' ends the line, in the reference's reader as in this one
+    with pytest.raises(ValueError, match="INCLUDE"):
+        D.read_grid_deck(_write(tmp_path, "DIMENS\n2 2 2 /\nINCLUDE\n'sub/perm.inc' /\n", "i.data"))
+
+
+def test_ntg_and_actnum_of_the_wrong_length_are_dropped(tmp_path):
+    base = """DIMENS
+2 1 1 /
+DX
+2*10 /
+DY
+2*10 /
+DZ
+2*2 /
+TOPS
+2*1000 /
+PORO
+2*0.2 /
+PERMX
+2*100 /
+PERMY
+2*100 /
+PERMZ
+2*10 /
+"""
+    g0, _ = D.grid_from_deck(D.read_grid_deck(_write(tmp_path, base, "a.data")))
+    g1, geo = D.grid_from_deck(D.read_grid_deck(_write(tmp_path, base + "NTG\n3*0.5 /\nACTNUM\n0 /\n", "b.data")))
+    assert g1.nb == 2 and np.array_equal(g1.poro_init, g0.poro_init) and np.array_equal(geo["ntg"], [1.0, 1.0])
+    assert np.array_equal(g1.conn_trans, g0.conn_trans)
+    g2, _ = D.grid_from_deck(D.read_grid_deck(_write(tmp_path, base + "NTG\n0.5 1 /\nACTNUM\n1 0 /\n", "c.data")))
+    assert g2.nb == 1 and g2.poro_init[0] == 0.2 * 0.5 and g2.conn_b.size == 0

@@ -594,7 +594,7 @@ ocpx_status ocpx_get_wells(ocpx_ctx* ctx, double* bhp, double* max_rel);
  * hands this system to an external package (FASP, PETSc or PARDISO,
  * src/LinearSystem.cpp:35-89); here BiCGStab with right block-Jacobi
  * preconditioning, from u = 0, until |rhs - J u| <= tol |rhs| or maxit
- * iterations (the norm is checked every 10).  The system holds the wells'
+ * iterations (the norm is tested on the device every 10).  The system holds the wells'
  * rows when ocpx_set_wells gave them; a host that keeps its own well code
  * solves the full system itself.  Single domain only.  The solution stays on
  * the device for ocpx_newton_update_device and is copied to u_host
@@ -607,6 +607,17 @@ typedef struct ocpx_solve_report {
     int breakdown;   /* 1: BiCGStab breakdown, 2: a singular diagonal block */
 } ocpx_solve_report;
 ocpx_status ocpx_linsolve(ocpx_ctx* ctx, double tol, int maxit, double* u_host, ocpx_solve_report* rep);
+/* The same solve, enqueued on the context stream without waiting: the
+ * convergence test runs on the device every 10 iterations and, once the
+ * solve has converged or broken down, the rest of the maxit iterations'
+ * kernels return at once.  No host synchronization, allocation or host
+ * memory access once the work space exists (the first solve of either form
+ * allocates it and must not run inside a stream capture), so the call can be
+ * captured in a CUDA graph on the context stream (ocpx_stream).  The solution
+ * and the report are the same as ocpx_linsolve's. */
+ocpx_status ocpx_linsolve_async(ocpx_ctx* ctx, double tol, int maxit);
+/* Waits for the context stream and reads the report of the last solve. */
+ocpx_status ocpx_linsolve_report(ocpx_ctx* ctx, ocpx_solve_report* rep);
 /* IsoT_FIM::GetSolution, bulk part, with the update the last ocpx_linsolve
  * left on the device. */
 ocpx_status ocpx_newton_update_device(ocpx_ctx* ctx, double dSmax);

@@ -1137,14 +1137,49 @@ ocpx_status ocpx_assemble(ocpx_ctx* ctx, double dt)
     return enqueue_assemble(ctx, dt);
 }
 
-ocpx_status ocpx_linsolve(ocpx_ctx* ctx, double tol, int maxit, double* u_host, ocpx_solve_report* rep)
+namespace {
+// checks shared by the two forms of the solve; allocates the work space on
+// the first call, which must not be inside a stream capture
+ocpx_status linsolve_prepare(ocpx_ctx* ctx, double tol, int maxit)
 {
     if (!ctx) return fail(OCPX_INVALID_ARG, "null context");
     if (!(tol > 0) || maxit < 1) return fail(OCPX_INVALID_ARG, "tol must be > 0 and maxit >= 1");
     if (ctx->nbI < ctx->nb) return fail(OCPX_INVALID_ARG, "the device solve needs a single domain (no ghost cells)");
+    if (!ctx->ls_scratch) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        OCPX_CUDA(cudaStreamIsCapturing(ctx->stream, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+            return fail(OCPX_INVALID_ARG, "the solver's work space is allocated by the first solve, outside a capture");
+        OCPX_CUDA(cudaMalloc(&ctx->ls_scratch, sizeof(double) * linsolve_scratch_doubles(ctx->nrow, ctx->nc + 1)));
+    }
+    return OCPX_OK;
+}
+}  // namespace
+
+ocpx_status ocpx_linsolve_async(ocpx_ctx* ctx, double tol, int maxit)
+{
+    const ocpx_status st = linsolve_prepare(ctx, tol, maxit);
+    if (st != OCPX_OK) return st;
+    OCPX_CUDA(linsolve_async(ctx->jac_rowptr, ctx->jac_col, ctx->jac_val, ctx->nrow, ctx->nc + 1, ctx->res, ctx->u,
+                             ctx->ls_scratch, tol, maxit, 10, &ctx->launches, ctx->stream));
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_linsolve_report(ocpx_ctx* ctx, ocpx_solve_report* rep)
+{
+    if (!ctx || !rep) return fail(OCPX_INVALID_ARG, "null argument");
+    if (!ctx->ls_scratch) return fail(OCPX_INVALID_ARG, "no solve has run on this context");
+    LinsolveResult r{};
+    OCPX_CUDA(linsolve_read(ctx->ls_scratch, ctx->nrow, ctx->nc + 1, &r, ctx->stream));
+    *rep = ocpx_solve_report{r.iterations, r.relres, r.converged, r.breakdown};
+    return OCPX_OK;
+}
+
+ocpx_status ocpx_linsolve(ocpx_ctx* ctx, double tol, int maxit, double* u_host, ocpx_solve_report* rep)
+{
+    const ocpx_status st = linsolve_prepare(ctx, tol, maxit);
+    if (st != OCPX_OK) return st;
     const int dim = ctx->nc + 1;
-    if (!ctx->ls_scratch)
-        OCPX_CUDA(cudaMalloc(&ctx->ls_scratch, sizeof(double) * linsolve_scratch_doubles(ctx->nrow, dim)));
     LinsolveResult r{};
     OCPX_CUDA(linsolve(ctx->jac_rowptr, ctx->jac_col, ctx->jac_val, ctx->nrow, dim, ctx->res, ctx->u,
                        ctx->ls_scratch, tol, maxit, 10, &r, &ctx->launches, ctx->stream));

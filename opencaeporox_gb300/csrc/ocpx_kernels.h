@@ -170,8 +170,11 @@ cudaError_t launch_wells_jt(const BulkView& b, const WellSys& w, const uint32_t*
 
 // Linear solve of J u = rhs on the device (k_linsolve.cu): BiCGStab with right
 // block-Jacobi preconditioning, x from zero; scratch holds
-// linsolve_scratch_doubles(nb, dim) doubles.  The residual norm is read every
-// check_every iterations.
+// linsolve_scratch_doubles(nb, dim) doubles.  The residual norm is tested on
+// the device every check_every iterations.  linsolve waits for each test and
+// returns the result; linsolve_async enqueues the whole solve without waiting
+// (capturable in a graph), and linsolve_read waits for the stream and reads
+// the result of the last solve in `scratch`.
 struct LinsolveResult {
     int iterations;
     double relres;   // |rhs - J x| / |rhs| of the recursively updated residual
@@ -182,6 +185,10 @@ size_t linsolve_scratch_doubles(int nb, int dim);
 cudaError_t linsolve(const uint32_t* rowptr, const uint32_t* col, const double* val, int nb, int dim,
                      const double* rhs, double* x, double* scratch, double tol, int maxit, int check_every,
                      LinsolveResult* res, uint64_t* launches, cudaStream_t s);
+cudaError_t linsolve_async(const uint32_t* rowptr, const uint32_t* col, const double* val, int nb, int dim,
+                           const double* rhs, double* x, double* scratch, double tol, int maxit, int check_every,
+                           uint64_t* launches, cudaStream_t s);
+cudaError_t linsolve_read(const double* scratch, int nb, int dim, LinsolveResult* res, cudaStream_t s);
 
 cudaError_t launch_flash_bo(const Model* dm, const BulkView& b, int block, cudaStream_t s);
 cudaError_t launch_krpc_rock(const Model* dm, const BulkView& b, int block, cudaStream_t s);

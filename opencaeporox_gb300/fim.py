@@ -143,7 +143,8 @@ EXPORTS = ["ocpx_abi_version", "ocpx_last_error", "ocpx_create", "ocpx_destroy",
            "ocpx_nr_init_step", "ocpx_nr_max_change", "ocpx_step_max_change", "ocpx_nr_check_converge",
            "ocpx_next_time_step", "ocpx_linsolve", "ocpx_newton_update_device", "ocpx_wells_eval",
            "ocpx_set_field_range", "ocpx_get_field_range", "ocpx_set_adjoint_seed", "ocpx_get_adjoint",
-           "ocpx_get_jacobian_rows", "ocpx_set_wells", "ocpx_get_wells", "ocpx_create_ex"]
+           "ocpx_get_jacobian_rows", "ocpx_set_wells", "ocpx_get_wells", "ocpx_create_ex", "ocpx_linsolve_async",
+           "ocpx_linsolve_report"]
 
 PARAMS = {"flash_budget": 0, "coop_blocks": 1, "block_cell": 2, "deferred": 3, "predefer": 4, "coop_cells": 5,
           "predeferred": 6, "level": 7, "pre_blocks": 8,
@@ -193,6 +194,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.ocpx_set_param.argtypes = [P, C.c_int, C.c_longlong]
     lib.ocpx_nr_init_step.argtypes = [P]
     lib.ocpx_linsolve.argtypes = [P, C.c_double, C.c_int, P, C.POINTER(SolveReport)]
+    lib.ocpx_linsolve_async.argtypes = [P, C.c_double, C.c_int]
+    lib.ocpx_linsolve_report.argtypes = [P, C.POINTER(SolveReport)]
     lib.ocpx_newton_update_device.argtypes = [P, C.c_double]
     lib.ocpx_nr_max_change.argtypes = [P, C.POINTER(ChangeMax)]
     lib.ocpx_step_max_change.argtypes = [P, C.POINTER(ChangeMax)]
@@ -582,6 +585,18 @@ class FimContext:
         _check(self.lib.ocpx_linsolve(self.h, float(tol), int(maxit),
                                       None if u is None else u.ctypes.data_as(C.c_void_p), C.byref(rep)))
         return u, {k: getattr(rep, k) for k, _ in rep._fields_}
+
+    def linsolve_async(self, tol: float = 1e-10, maxit: int = 2000):
+        """The same solve enqueued on the context stream without waiting
+        (capturable in a CUDA graph on `stream`); read it with
+        linsolve_report."""
+        _check(self.lib.ocpx_linsolve_async(self.h, float(tol), int(maxit)))
+
+    def linsolve_report(self):
+        """Waits for the context stream; the report of the last solve."""
+        rep = SolveReport()
+        _check(self.lib.ocpx_linsolve_report(self.h, C.byref(rep)))
+        return {k: getattr(rep, k) for k, _ in rep._fields_}
 
     def newton_update_device(self, dSmax: float):
         """GetSolution with the update the last linsolve left on the device."""

@@ -62,3 +62,43 @@ def test_linsolve_bench_system_and_device_update(gpu_lib):
         ctx.get_solution(u, 0.2)
         for k, v in dev.items():
             assert np.array_equal(v, ctx.get(k)), k
+
+
+def test_linsolve_async_and_graph_replay(gpu_lib):
+    """The enqueue-only solve (ocpx_linsolve_async) gives the synchronous
+    solve's report and update bit for bit, also when it is captured in a CUDA
+    graph on the context stream and replayed."""
+    torch = pytest.importorskip("torch")
+    fx = P.load_fixture("comp6_8x8x3")
+    model, grid = fim.model_and_grid_from_dump(fx)
+    keys = ("P", "NI", "S", "XIJ")
+    with fim.FimContext(model, grid) as ctx:
+        js = P.jac_state(fx, P.iterations(fx)[0])
+        dt = float(js["dt"][0])
+        ctx.load_state(js)
+        ctx.cal_res(dt)
+        ctx.assemble_mat(dt)
+        ctx.checkpoint(0)
+        _, rep = ctx.linsolve(tol=1e-12, maxit=300, copy_out=False)
+        assert rep["converged"] and rep["iterations"] > 0
+        ctx.newton_update_device(0.2)
+        ref = {k: ctx.get(k) for k in keys}
+
+        ctx.checkpoint(0, restore=True)
+        ctx.linsolve_async(tol=1e-12, maxit=300)
+        assert ctx.linsolve_report() == rep
+        ctx.newton_update_device(0.2)
+        for k in keys:
+            assert np.array_equal(ctx.get(k), ref[k]), k
+
+        ctx.checkpoint(0, restore=True)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=torch.cuda.ExternalStream(ctx.stream)):
+            ctx.linsolve_async(tol=1e-12, maxit=300)
+        for _ in range(2):
+            g.replay()
+            torch.cuda.synchronize()
+            assert ctx.linsolve_report() == rep
+        ctx.newton_update_device(0.2)
+        for k in keys:
+            assert np.array_equal(ctx.get(k), ref[k]), k

@@ -1482,13 +1482,36 @@ long oc_assemble(const oc_model* m, const oc_bulk* b, const oc_conn* c, double d
         for (int side = 0; side < 2; side++) {
             const double* s = side ? sE : sB;
             const double* sec = b->dSec_dPri + (size_t)(side ? eId : bId) * lend;
-            /* DaABpbC (src/DenseMat.cpp:61-85): bmat = dt*dFdXs*dSec + dt*dFdXp */
-            for (int r = 0; r < n1; r++)
-                for (int q = 0; q < n1; q++) {
-                    double acc = 0;
-                    for (int t = 0; t < n2; t++) acc += s[r * n2 + t] * sec[t * n1 + q];
-                    bm[r * n1 + q] = dt * acc + dt * (side ? pE : pB)[r * n1 + q];
+            /* DaABpbC (src/DenseMat.cpp:61-85): bmat = dt*dFdXs*dSec + dt*dFdXp.
+             * Each element sums its products in t order.  Rows go four at a
+             * time, so that each row of dSec is read once per four rows, and
+             * the inner loop runs over the contiguous columns q. */
+            for (int q = 0; q < bs; q++) bm[q] = 0;
+            int r = 0;
+            for (; r + 4 <= n1; r += 4) {
+                double *a0 = bm + r * n1, *a1 = a0 + n1, *a2 = a1 + n1, *a3 = a2 + n1;
+                const double *s0 = s + r * n2, *s1 = s0 + n2, *s2 = s1 + n2, *s3 = s2 + n2;
+                for (int t = 0; t < n2; t++) {
+                    const double* srow = sec + t * n1;
+                    const double f0 = s0[t], f1 = s1[t], f2 = s2[t], f3 = s3[t];
+                    for (int q = 0; q < n1; q++) {
+                        const double x = srow[q];
+                        a0[q] += f0 * x; a1[q] += f1 * x; a2[q] += f2 * x; a3[q] += f3 * x;
+                    }
                 }
+            }
+            for (; r < n1; r++) {
+                double* acc = bm + r * n1;
+                for (int t = 0; t < n2; t++) {
+                    const double a = s[r * n2 + t];
+                    const double* srow = sec + t * n1;
+                    for (int q = 0; q < n1; q++) acc[q] += a * srow[q];
+                }
+            }
+            {
+                const double* pp = side ? pE : pB;
+                for (int q = 0; q < bs; q++) bm[q] = dt * bm[q] + dt * pp[q];
+            }
             if (side == 0) {
                 double* dg = val + (size_t)rowptr[bId] * bs;
                 for (int q = 0; q < bs; q++) dg[q] += bm[q];                    /* AddDiag(bId) */

@@ -11,15 +11,20 @@ start, :33-94), and reduces the residual norms over the ranks (MPI_Allreduce,
 :1176).  Here the subdomains of a structured grid are slabs of whole layers,
 which need no graph partitioner:
 
-* ``zslab_partition`` cuts cells (k, j, i), i fastest, into R slabs of
-  consecutive layers.  Subdomain r owns the layers [k0, k1) and has up to one
-  ghost layer below and one above.  Its local cell numbers are the owned
-  cells first, in the global order, then the ghost cells, in the global
-  order (so the context's nb_interior is the owned count).  Its connections
-  are the global connections with at least one owned end, in the global
-  order, each end keeping its role (bId, eId): the owned rows of the
-  subdomain's residual and Jacobian are then bit-identical to the same rows
-  of the whole grid.
+* ``partition`` builds the subdomains from an owner rank per cell (from any
+  partitioner).  A rank's ghost cells are all the other ranks' cells
+  connected to one of its own, as the reference's one layer of ghost cells
+  is defined by the grid's connections; a fault's non-neighbour connections
+  can reach a second layer away, and such a cell is a ghost too.  Its local
+  cell numbers are the owned cells first, in the global order, then the
+  ghost cells, in the global order (so the context's nb_interior is the owned
+  count).  Its connections are the global connections with at least one
+  owned end, in the global order, each end keeping its role (bId, eId): the
+  owned rows of the subdomain's residual and Jacobian are then bit-identical
+  to the same rows of the whole grid.
+* ``zslab_partition`` owns cells (k, j, i), i fastest, by slabs of R runs of
+  consecutive layers; for a grid of the active cells of a larger one it
+  takes each active cell's index in that grid.
 * ``pack`` / ``unpack`` give each neighbour the owned values it holds as
   ghosts and write received values into the ghost cells (the Newton update,
   or any cell array in the reference's layout).  ``HaloExchange`` moves them
@@ -41,7 +46,7 @@ from .fim import Grid
 @dataclass
 class Subdomain:
     rank: int
-    layers: tuple            # owned layers [k0, k1)
+    layers: tuple            # owned layers [k0, k1) (None for an owner map not by layer)
     cells: np.ndarray        # global cell number of each local cell (owned, then ghost)
     n_owned: int
     grid: Grid               # local grid (nb_interior = n_owned)
@@ -85,34 +90,63 @@ def layer_bounds(nz: int, nranks: int):
     return [(k[r], k[r + 1]) for r in range(nranks)]
 
 
-def zslab_partition(grid: Grid, nx: int, ny: int, nz: int, nranks: int):
-    """Subdomains of a grid of nx * ny * nz cells (order k, j, i; every cell
-    active) in slabs of whole layers, one ghost layer on each inner side.
-    Needs at least one layer per rank."""
-    if nranks < 1 or nranks > nz:
-        raise ValueError(f"{nranks} ranks for {nz} layers")
-    if grid.nb != nx * ny * nz:
-        raise ValueError("grid size does not match nx * ny * nz")
-    layer = nx * ny
-    bounds = layer_bounds(nz, nranks)
+def partition(grid: Grid, owner, nranks: int, layers=None):
+    """Subdomains of `grid` from the owner rank of each cell: rank r owns the
+    cells with owner r and holds as ghosts every other cell connected to one
+    of them.  send[q] / recv[q] list, in the global order, the owned cells
+    rank q holds as ghosts and the ghosts rank q owns (local numbers), so
+    that the two sides of each exchange agree.  `layers` gives each rank's
+    owned layers, for the record."""
+    owner = np.asarray(owner, np.int64)
+    if owner.shape != (grid.nb,) or owner.min() < 0 or owner.max() >= nranks:
+        raise ValueError("owner must give a rank in [0, nranks) for every cell")
+    b = np.asarray(grid.conn_b, np.int64)
+    e = np.asarray(grid.conn_e, np.int64)
+    cross = owner[b] != owner[e]
+    # a crossing connection makes each end a ghost of the other end's owner
+    g_rank = np.concatenate([owner[b[cross]], owner[e[cross]]])
+    g_cell = np.concatenate([e[cross], b[cross]])
+    ghosts = [np.unique(g_cell[g_rank == r]) for r in range(nranks)]
     subs = []
-    for r, (k0, k1) in enumerate(bounds):
-        owned = np.arange(k0 * layer, k1 * layer)
-        below = np.arange((k0 - 1) * layer, k0 * layer) if r > 0 else np.zeros(0, np.int64)
-        above = np.arange(k1 * layer, (k1 + 1) * layer) if r < nranks - 1 else np.zeros(0, np.int64)
-        ghost = np.concatenate([below, above])
+    for r in range(nranks):
+        owned = np.nonzero(owner == r)[0]
+        if not owned.size:
+            raise ValueError(f"rank {r} owns no cell")
+        ghost = ghosts[r]
         g, cells, conns = subdomain(grid, owned, ghost)
         n = owned.size
         send, recv = {}, {}
-        if r > 0:
-            send[r - 1] = np.arange(0, layer)                  # my lowest owned layer
-            recv[r - 1] = np.arange(n, n + layer)              # the ghost layer below
-        if r < nranks - 1:
-            send[r + 1] = np.arange(n - layer, n)              # my highest owned layer
-            off = n + (layer if r > 0 else 0)
-            recv[r + 1] = np.arange(off, off + layer)          # the ghost layer above
-        subs.append(Subdomain(r, (k0, k1), cells, n, g, conns, send, recv))
+        for q in range(nranks):
+            if q == r:
+                continue
+            mine = ghosts[q][owner[ghosts[q]] == r]
+            if mine.size:
+                send[q] = np.searchsorted(owned, mine)
+            theirs = ghost[owner[ghost] == q]
+            if theirs.size:
+                recv[q] = n + np.searchsorted(ghost, theirs)
+        subs.append(Subdomain(r, layers[r] if layers is not None else None, cells, n, g, conns, send, recv))
     return subs
+
+
+def zslab_partition(grid: Grid, nx: int, ny: int, nz: int, nranks: int, cell_index=None):
+    """Subdomains of a grid of nx * ny * nz cells (order k, j, i) in slabs of
+    whole layers (partition by layer).  cell_index: for a grid of the active
+    cells of that grid, each cell's index in it (the geometry's act2all from
+    deck.grid_from_deck or the grid ingest); None when every cell is
+    present.  Needs at least one layer per rank."""
+    if nranks < 1 or nranks > nz:
+        raise ValueError(f"{nranks} ranks for {nz} layers")
+    if cell_index is None:
+        if grid.nb != nx * ny * nz:
+            raise ValueError("grid size does not match nx * ny * nz")
+        cell_index = np.arange(grid.nb)
+    cell_index = np.asarray(cell_index, np.int64)
+    if cell_index.shape != (grid.nb,):
+        raise ValueError("cell_index must give one index per cell")
+    bounds = layer_bounds(nz, nranks)
+    rank_of_layer = np.repeat(np.arange(nranks), [k1 - k0 for k0, k1 in bounds])
+    return partition(grid, rank_of_layer[cell_index // (nx * ny)], nranks, layers=bounds)
 
 
 def pack(sub: Subdomain, values: np.ndarray, width: int) -> dict:

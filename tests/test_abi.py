@@ -126,3 +126,16 @@ def test_create_options_are_checked_before_the_device():
     st = lib.ocpx_create_ex(C.byref(md), C.byref(gd), -1, C.byref(opt), C.byref(h))
     assert fim.STATUS_NAMES[st] == "INVALID_ARG"
     assert b"struct_size" in lib.ocpx_last_error()
+
+
+def test_solve_entry_points_refuse_a_null_context(lib):
+    """The enqueue-only solve and its report check their arguments before
+    any device work."""
+    lib.ocpx_linsolve_async.argtypes = [C.c_void_p, C.c_double, C.c_int]
+    lib.ocpx_linsolve_report.argtypes = [C.c_void_p, C.POINTER(fim.SolveReport)]
+    lib.ocpx_last_error.restype = C.c_char_p
+    rep = fim.SolveReport()
+    assert lib.ocpx_linsolve_async(None, 1e-10, 10) != 0
+    assert b"null context" in lib.ocpx_last_error()
+    assert lib.ocpx_linsolve_report(None, C.byref(rep)) != 0
+    assert b"null argument" in lib.ocpx_last_error()

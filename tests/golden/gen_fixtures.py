@@ -394,6 +394,81 @@ def deck_grid_fixture(kind):
     return data
 
 
+def corpus_case(seed):
+    """One seeded small grid for the grid corpus: (nx, ny, nz, GRID text).
+    Even seeds: corner-point with one to three random faults (throws up to
+    two layers, scissor faults, thickness changes) and leaning pillars; odd
+    seeds: block-centred with per-cell sizes.  Random inactive cells
+    (ACTNUM or zero porosity) in half the cases, NTG in half, MULTZ where
+    every cell is active."""
+    sys.path.insert(0, REPO)
+    from opencaeporox_gb300 import synthetic
+    rng = np.random.default_rng(1000 + seed)
+    nx, ny, nz = int(rng.integers(3, 8)), int(rng.integers(3, 7)), int(rng.integers(2, 6))
+    n = nx * ny * nz
+    dz = float(rng.uniform(2.0, 5.0))
+    lines = [f"DIMENS\n{nx} {ny} {nz} /\n"]
+    if seed % 2 == 0:
+        faults = []
+        for _ in range(int(rng.integers(1, 4))):
+            axis = "x" if rng.random() < 0.5 else "y"
+            index = int(rng.integers(0, (nx if axis == "x" else ny) - 1))
+            t0, t1 = rng.uniform(-2.2, 2.2, 2) * dz
+            faults.append((axis, index, float(t0), float(t1), float(rng.uniform(0.5, 1.8))))
+        coord, zcorn = synthetic.faulted_corner_point(nx, ny, nz, float(rng.uniform(10, 30)), dz, 2000.0,
+                                                      float(rng.uniform(-6, 6)), float(rng.uniform(-6, 6)),
+                                                      faults, float(rng.uniform(0, 0.08)), seed=seed)
+        lines.append(f"COORD\n{decks._fmt(coord)}\n/\nZCORN\n{decks._fmt(zcorn)}\n/\n")
+    else:
+        lines.append(f"DX\n{decks._fmt(rng.uniform(10, 30, n))}\n/\nDY\n{decks._fmt(rng.uniform(10, 30, n))}\n/\n"
+                     f"DZ\n{decks._fmt(rng.uniform(1, 6, n))}\n/\nTOPS\n{decks._fmt(2000 + rng.uniform(-5, 5, nx * ny))}\n/\n")
+    poro = rng.uniform(0.1, 0.3, n)
+    inactive = rng.random() < 0.5
+    if inactive:
+        poro[rng.choice(n, size=max(1, n // 15), replace=False)] = 0.0
+    lines.append(f"PORO\n{decks._fmt(poro)}\n/\n")
+    kx = np.exp(rng.normal(np.log(100.0), 1.0, n))
+    lines.append(f"PERMX\n{decks._fmt(kx)}\n/\nPERMY\n{decks._fmt(kx * rng.uniform(0.5, 1.5, n))}\n/\n"
+                 f"PERMZ\n{decks._fmt(0.1 * kx)}\n/\n")
+    if rng.random() < 0.5:
+        lines.append(f"NTG\n{decks._fmt(rng.uniform(0.5, 1.0, n))}\n/\n")
+    if inactive:
+        act = (rng.random(n) > 0.1).astype(int)
+        # keep the two wells' columns (first and last) active
+        col = np.arange(n) % (nx * ny)
+        act[(col == 0) | (col == nx * ny - 1)] = 1
+        lines.append("ACTNUM\n" + " ".join(str(a) for a in act) + "\n/\n")
+    else:
+        lines.append(f"MULTZ\n{decks._fmt(rng.uniform(0.05, 1.0, n))}\n/\n")
+    return nx, ny, nz, "".join(lines)
+
+
+def grid_corpus(ncase=40):
+    """The reference's grid (model dump) for each corpus_case, with the GRID
+    texts; cases the reference refuses are recorded as refused."""
+    data = {}
+    for seed in range(ncase):
+        nx, ny, nz, grid_text = corpus_case(seed)
+        col = np.arange(nx * ny * nz) % (nx * ny)
+        ni, deck_text = decks.comp_deck(nx, ny, nz, 3, 7, grid_text=grid_text)
+        with tempfile.TemporaryDirectory() as tmp:
+            deck = os.path.join(tmp, "case.data")
+            with open(deck, "w") as f:
+                f.write(deck_text)
+            ni.astype("<f8").tofile(deck + ".ptn_ni")
+            out = os.path.join(tmp, "out")
+            r = subprocess.run([DUMP, "fim", deck, out, "0"], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            data[f"case{seed:03d}/grid"] = np.array(grid_text)
+            if r.returncode != 0:
+                data[f"case{seed:03d}/refused"] = np.array(r.returncode)
+                continue
+            m = load_dir(os.path.join(out, "model"))
+            for k in ("nb", "conn_bId", "conn_eId", "conn_trans", "conn_areaB", "conn_areaE", "v", "depth",
+                      "poroInit", "ntg", "rockKx", "rockKy", "rockKz", "dx", "dy", "dz", "CONV_DARCY"):
+                data[f"case{seed:03d}/{k}"] = m[k]
+    return data
+
+
 FIXTURES = {
     "bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12),
     "comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4),
@@ -407,6 +482,7 @@ FIXTURES = {
     "deck_ortho_multz": lambda: deck_grid_fixture("ortho_multz"),
     "deck_corner_actnum": lambda: deck_grid_fixture("corner_actnum"),
     "deck_corner_multz": lambda: deck_grid_fixture("corner_multz"),
+    "grid_corpus": grid_corpus,
     "wells_bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12, packer=pack_wells),
     "wells_comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4, packer=pack_wells),
 }

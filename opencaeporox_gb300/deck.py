@@ -42,6 +42,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import grid as G
+from . import wells as W
 
 REAL_ARRAYS = ("DX", "DY", "DZ", "TOPS", "COORD", "ZCORN", "NTG", "PORO", "PERMX", "PERMY", "PERMZ", "MULTZ")
 INT_ARRAYS = ("ACTNUM",)
@@ -239,3 +240,122 @@ def grid_from_deck(deck: GridDeck, conv_darcy: float = 0.008527):
         raise ValueError(f"TOPS must give {deck.nx * deck.ny} values")
     return G.orthogonal_grid(deck.nx, deck.ny, deck.nz, A["DX"], A["DY"], A["DZ"], A["TOPS"], A["PERMX"],
                              A["PERMY"], A["PERMZ"], A["PORO"], **common)
+
+
+# ------------------------------------------------------------------ wells ---
+@dataclass
+class WellSpec:
+    """A structured well of WELSPECS with its COMPDAT perforations, one per
+    layer: (I, J, K, WI, diameter, kh, skin, direction), 1-based cells, -1 for
+    a WI or kh not given."""
+    name: str
+    I: int
+    J: int
+    perfs: list = field(default_factory=list)
+
+
+def _defaults(tokens):
+    """DealDefault: m* as m DEFAULT entries, m*v as m copies of v."""
+    out = []
+    for t in tokens:
+        star = t.find("*")
+        num = int(t[:star]) if star > 0 and t[:star].isdigit() else 0
+        if num == 0:
+            out.append(t)
+        else:
+            out += ["DEFAULT" if star == len(t) - 1 else t[star + 1:]] * num
+    return out
+
+
+def read_wells(path: str, workdir: str | None = None, wells: list | None = None) -> list:
+    """WELSPECS and COMPDAT of a deck (and the files it includes), as
+    PreParamGridWell::InputWELSPECS / InputCOMPDAT and WellParam read them
+    (src/PreParamGridWell.cpp:554-600, src/ParamWell.cpp:50-128): a COMPDAT
+    record names a well, or with a trailing `*` every well whose name starts
+    so; I J default to the well's; K1..K2 give one perforation per layer;
+    then WI, diameter (default 1), kh, skin (default 0) and direction (x, y,
+    z; default z).  Wells given by coordinates are not read."""
+    wells = [] if wells is None else wells
+    workdir = workdir if workdir is not None else os.path.dirname(os.path.abspath(path))
+    lines = _lines(path)
+    for toks in lines:
+        key = toks[0]
+        if key == "WELSPECS":
+            for t in lines:
+                if t[0] == "/":
+                    break
+                v = _defaults(t)
+                if "COORDINATE" in v[-2:]:
+                    raise ValueError(f"well {v[0]}: wells given by coordinates are not read")
+                wells.append(WellSpec(v[0], int(v[2]), int(v[3])))
+        elif key == "COMPDAT":
+            for t in lines:
+                if t[0] == "/":
+                    break
+                v = _defaults(t)
+                v = v[:-1] if v[-1] == "/" else v
+                v += ["DEFAULT"] * (10 - len(v))
+                name = v[0]
+                star = name.find("*")
+                match = (lambda w: w.name[:star] == name[:star]) if star >= 0 else (lambda w: w.name == name)
+                for w in wells:
+                    if not match(w):
+                        continue
+                    I, J = (w.I, w.J) if "DEFAULT" in (v[1], v[2]) else (int(v[1]), int(v[2]))
+                    for k in range(int(v[3]), int(v[4]) + 1):
+                        d = v[9].lower() if v[9] != "DEFAULT" else "z"
+                        if d not in ("x", "y", "z"):
+                            raise ValueError(f"well {w.name}: perforation direction {v[9]!r}")
+                        w.perfs.append((I, J, k, -1.0 if v[5] == "DEFAULT" else float(v[5]),
+                                        1.0 if v[6] == "DEFAULT" else float(v[6]),
+                                        -1.0 if v[7] == "DEFAULT" else float(v[7]),
+                                        0.0 if v[8] == "DEFAULT" else float(v[8]), "xyz".index(d)))
+        elif key == "INCLUDE":
+            name = next(lines)[0]
+            if name.endswith("/"):
+                raise ValueError(f"INCLUDE {name!r}: a '/' ends the line, so the file name cannot hold one")
+            read_wells(os.path.join(workdir, name), workdir, wells)
+    return wells
+
+
+def well_perforations(wells: list, deck: GridDeck, grid, geo, conv_darcy: float = 0.008527, conv1: float = 1.0):
+    """Per well the perforations the reference keeps and their indices, ready
+    for the device's well set (ocpx_set_wells): a perforation whose cell is
+    inactive or holds no pore space (pore fraction not above 1e-6) is dropped
+    (ActiveGridCheck::IfFluid, src/PreParamGridWell.cpp:874-878); WI as
+    PeacemanWell::CalWI forms it (src/WellPeaceman.cpp:277-361), including
+    that a WI given in the deck is scaled by CONV1 at the well's first such
+    perforation and the well's later perforations are left as read.
+    Returns dicts with cell (active numbering), WI, kh, radius, skin and
+    direction (0 x, 1 y, 2 z)."""
+    n, A = deck.n, deck.arrays
+    a2 = np.full(n, -1, np.int64)
+    a2[geo["act2all"]] = np.arange(grid.nb)
+    ntg = A.get("NTG")
+    poro = np.asarray(A["PORO"], np.float64)
+    if ntg is not None and len(ntg) == n:
+        poro = poro * ntg
+    out = []
+    for w in wells:
+        cells, perfs = [], []
+        for (I, J, K, wi, diam, kh, skin, d) in w.perfs:
+            c = (K - 1) * deck.nx * deck.ny + (J - 1) * deck.nx + (I - 1)
+            if not (0 <= c < n) or a2[c] < 0 or not poro[c] > 1e-6:
+                continue
+            cells.append(int(a2[c]))
+            perfs.append([wi, diam / 2.0, kh, skin, d])
+        if not cells:
+            raise ValueError(f"every perforation of well {w.name} is in an inactive cell")
+        WI = np.array([p[0] for p in perfs])
+        KH = np.array([p[2] for p in perfs])
+        for q, (wi, radius, kh, skin, d) in enumerate(perfs):
+            if wi > 0:
+                WI[q] = wi * conv1
+                break
+            c = cells[q]
+            WI[q], KH[q] = W.peaceman_index(d, geo["dx"][c], geo["dy"][c], geo["dz"][c], geo["ntg"][c], geo["kx"][c],
+                                            geo["ky"][c], geo["kz"][c], radius, skin, kh, conv_darcy)
+        out.append(dict(name=w.name, cell=np.array(cells, np.int32), WI=WI, kh=KH,
+                        radius=np.array([p[1] for p in perfs]), skin=np.array([p[3] for p in perfs]),
+                        direction=np.array([p[4] for p in perfs], np.int32)))
+    return out

@@ -23,16 +23,19 @@ pressure with Z = 0.9.
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 PI = 3.141592653  # include/OCPConst.hpp:32: the reference's pi, which its well index uses
 
 
-def peaceman_wi(direction, dx, dy, dz, kx, ky, kz, ntg=1.0, radius=0.1, skin=0.0, conv_darcy=0.008527):
-    """Well index of perforations along x (0), y (1) or z (2) (arrays or
-    scalars; kh derived from the cell)."""
-    dx, dy, dz = (np.asarray(v, np.float64) for v in (dx, dy, dz))
-    kx, ky, kz = (np.asarray(v, np.float64) for v in (kx, ky, kz))
+def peaceman_index(direction, dx, dy, dz, ntg, kx, ky, kz, radius, skin=0.0, kh=-1.0, conv_darcy=0.008527):
+    """Well index and kh of one perforation along x (0), y (1) or z (2) whose
+    WI is not given, as PeacemanWell::CalWI forms them
+    (src/WellPeaceman.cpp:277-361): the layer thickness dz * NTG, kh from the
+    cell when kh < 0, pow and log from the C library (math), in the
+    reference's order of operations.  Returns (WI, kh)."""
     dz = dz * ntg
     if direction == 0:
         a, b, l1, l2, length = ky, kz, dy, dz, dx
@@ -43,10 +46,26 @@ def peaceman_wi(direction, dx, dy, dz, kx, ky, kz, ntg=1.0, radius=0.1, skin=0.0
     else:
         raise ValueError("direction must be 0, 1 or 2")
     ab, a_b = a * b, a / b
-    ro = 0.28 * np.sqrt(l1 * l1 * np.sqrt(1 / a_b) + l2 * l2 * np.sqrt(a_b))
-    ro = ro / (a_b ** 0.25 + (1 / a_b) ** 0.25)
-    kh = length * np.sqrt(ab)
-    return 2 * PI * kh / (np.log(ro / radius) + skin) * conv_darcy
+    ro = 0.28 * math.pow(l1 * l1 * math.pow(1 / a_b, 0.5) + l2 * l2 * math.pow(a_b, 0.5), 0.5)
+    ro /= math.pow(a_b, 0.25) + math.pow(1 / a_b, 0.25)
+    if kh < 0:
+        kh = length * math.pow(ab, 0.5)
+    wi = (2 * PI) * kh / (math.log(ro / radius) + skin)
+    return wi * conv_darcy, kh
+
+
+def peaceman_wi(direction, dx, dy, dz, kx, ky, kz, ntg=1.0, radius=0.1, skin=0.0, conv_darcy=0.008527):
+    """Well index of perforations along x (0), y (1) or z (2) (arrays or
+    scalars; kh derived from the cell), perforation by perforation with
+    peaceman_index."""
+    if direction not in (0, 1, 2):
+        raise ValueError("direction must be 0, 1 or 2")
+    args = np.broadcast_arrays(*(np.asarray(v, np.float64) for v in (dx, dy, dz, ntg, kx, ky, kz, radius, skin)))
+    out = np.empty(args[0].shape)
+    for i in np.ndindex(out.shape):
+        v = [float(a[i]) for a in args]
+        out[i] = peaceman_index(direction, *v[:8], skin=v[8], conv_darcy=conv_darcy)[0]
+    return out[()] if out.ndim == 0 else out
 
 
 def vertical_wells(nx, ny, nz, n_inj, n_prod, dxy, dz, perm_x, perm_z, depth, ncomp, seed, temp_c=71.85,

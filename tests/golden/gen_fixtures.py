@@ -469,6 +469,45 @@ def grid_corpus(ncase=40):
     return data
 
 
+def deck_wells_fixture():
+    """The reference's perforations and well indices from WELSPECS/COMPDAT
+    on the faulted grid with inactive cells (grid_deck_texts("corner_actnum")):
+    default and explicit directions, a given kh, a skin, a given WI, a record
+    naming its wells by a prefix and one in an inactive cell.  One Newton
+    iteration, for the well dump."""
+    nx, ny, nz, grid_text, include = grid_deck_texts("corner_actnum")
+    ni, deck_text = decks.comp_deck(nx, ny, nz, 3, 21, grid_text=grid_text)
+    compdat = f"""COMPDAT
+'INJE1'   2*   1   2     1*   0.2   3*   /
+'INJE1'   4   3   1   1   1*   0.2   3*   /
+'INJE1'   2   1   3   {nz}   1*   0.25   1*   1.5   'X'   /
+'PROD*'   2*   1   2   1*   0.3   40.0   1*   'Y'   /
+'PROD1'   {nx - 1}   {ny}   3   3   1*   0.2   3*   /
+'PROD1'   2*   4   {nz}   25.0   0.2   3*   /
+/
+"""
+    i = deck_text.index("COMPDAT")
+    j = deck_text.index("/\n/\n", i) + 4
+    deck_text = deck_text[:i] + compdat + deck_text[j:]
+    with tempfile.TemporaryDirectory() as tmp:
+        deck = os.path.join(tmp, "grid.data")
+        with open(deck, "w") as f:
+            f.write(deck_text)
+        with open(os.path.join(tmp, "grid_poro.inc"), "w") as f:
+            f.write(include)
+        ni.astype("<f8").tofile(deck + ".ptn_ni")
+        out = os.path.join(tmp, "out")
+        subprocess.run([DUMP, "fim", deck, out, "1"], check=True, stdout=subprocess.DEVNULL)
+        data = {f"model/{k}": v for k, v in load_dir(os.path.join(out, "model")).items()
+                if k in ("nb", "CONV_DARCY", "CONV1")}
+        for k, v in load_dir(os.path.join(out, "it000", "jac_state")).items():
+            if k.startswith("perf_") or k.startswith("well_"):
+                data[f"wells/{k}"] = v
+    data["deck/main"] = np.array(deck_text)
+    data["deck/include"] = np.array(include)
+    return data
+
+
 FIXTURES = {
     "bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12),
     "comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4),
@@ -483,6 +522,7 @@ FIXTURES = {
     "deck_corner_actnum": lambda: deck_grid_fixture("corner_actnum"),
     "deck_corner_multz": lambda: deck_grid_fixture("corner_multz"),
     "grid_corpus": grid_corpus,
+    "deck_wells": deck_wells_fixture,
     "wells_bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12, packer=pack_wells),
     "wells_comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4, packer=pack_wells),
 }

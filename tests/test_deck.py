@@ -198,3 +198,46 @@ def test_grid_corpus_against_reference(tmp_path):
             assert np.max(np.abs(g.v - m["v"]) / m["v"]) < 1e-13, c
         else:
             assert np.array_equal(g.v, m["v"]), c
+
+
+def test_well_perforations_against_reference(tmp_path):
+    """WELSPECS/COMPDAT on the faulted grid with inactive cells, read by the
+    reference (deck_wells.npz): the perforations it keeps (one in an inactive
+    cell is dropped), their cells, well indices, kh, radius, skin and
+    direction, bit for bit.  The records cover x, y and z perforations, a
+    given kh, a skin, a given WI and a well name given by its prefix."""
+    fx = P.load_fixture("deck_wells")
+    w, m = P.group(fx, "wells"), P.group(fx, "model")
+    deck = _read(fx, tmp_path)
+    wells = D.read_wells(str(tmp_path / "grid.data"))
+    g, geo = D.grid_from_deck(deck, float(m["CONV_DARCY"].ravel()[0]))
+    perfs = D.well_perforations(wells, deck, g, geo, float(m["CONV_DARCY"].ravel()[0]), float(m["CONV1"].ravel()[0]))
+    assert [p["name"] for p in perfs] == ["INJE1", "PROD1"]
+    assert [p["cell"].size for p in perfs] == list(np.asarray(w["well_nperf"]).ravel())
+    cat = lambda k: np.concatenate([p[k] for p in perfs])
+    for k, rk in (("cell", "perf_loc"), ("WI", "perf_WI"), ("kh", "perf_kh"), ("radius", "perf_radius"),
+                  ("skin", "perf_skin"), ("direction", "perf_dir")):
+        assert np.array_equal(cat(k), np.asarray(w[rk]).ravel()), k
+    assert sum(len(x.perfs) for x in wells) == int(np.sum(w["well_nperf"])) + 1
+
+
+def test_read_wells_records(tmp_path):
+    text = """WELSPECS
+'A1' 'G' 2 3 1* 'OIL' /
+'A2' 'G' 1 1 1* 'OIL' /
+'B1' 'G' 4 4 1* 'GAS' /
+/
+COMPDAT
+'A*' 2* 1 2 1* 0.5 3* /
+'B1' 3 3 2 2 7.5 0.2 100 2.0 'x' /
+/
+"""
+    wells = D.read_wells(_write(tmp_path, text))
+    a1, a2, b1 = wells
+    assert [p[:3] for p in a1.perfs] == [(2, 3, 1), (2, 3, 2)]
+    assert [p[:3] for p in a2.perfs] == [(1, 1, 1), (1, 1, 2)]
+    assert a1.perfs[0][3:] == (-1.0, 0.5, -1.0, 0.0, 2)
+    assert b1.perfs == [(3, 3, 2, 7.5, 0.2, 100.0, 2.0, 0)]
+    with pytest.raises(ValueError, match="direction"):
+        D.read_wells(_write(tmp_path, "WELSPECS\n'C' 'G' 1 1 1* 'OIL' /\n/\nCOMPDAT\n'C' 2* 1 1 1* 0.2 2* 'q' /\n/\n",
+                            "bad.data"))

@@ -20,7 +20,7 @@ def test_peaceman_wi_matches_the_reference_formula(direction):
     got = W.peaceman_wi(direction, dx, dy, dz, kx, ky, kz, ntg, radius, skin)
     ref = np.array([OW.well_index(direction, dx[i], dy[i], dz[i], ntg[i], kx[i], ky[i], kz[i],
                                   radius, skin, 0.008527)[0] for i in range(n)])
-    np.testing.assert_allclose(got, ref, rtol=1e-14, atol=0)
+    np.testing.assert_array_equal(got, ref)
 
 
 def test_peaceman_wi_rejects_an_unknown_direction():

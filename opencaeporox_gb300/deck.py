@@ -359,3 +359,221 @@ def well_perforations(wells: list, deck: GridDeck, grid, geo, conv_darcy: float 
                         radius=np.array([p[1] for p in perfs]), skin=np.array([p[3] for p in perfs]),
                         direction=np.array([p[4] for p in perfs], np.int32)))
     return out
+
+
+# ------------------------------------------------------------------ PROPS ---
+UNITS = {
+    # src/OCPUnits.cpp:17-56, include/OCPUnits.hpp:46-103 (CONV3 and CONV4 as the reference sets them)
+    "METRIC": dict(GRAVITY_FACTOR=0.0000980665, CONV_DARCY=0.008527, GAS_CONSTANT=0.083143, CONV1=1.0, CONV3=1.0,
+                   CONV4=273.15, RHOW_STD=999.014, RHOAIR_STD=1.2232),
+    "FIELD": dict(GRAVITY_FACTOR=0.00694444, CONV_DARCY=0.001127 * 5.61458, GAS_CONSTANT=10.73159, CONV1=5.61458,
+                  CONV3=1000 / 5.61458, CONV4=459.67, RHOW_STD=62.3664, RHOAIR_STD=0.076362),
+}
+TABLE_COLUMNS = {"SWOF": 4, "SGOF": 4, "PVCO": 6, "PVDG": 3, "PVTW": 5}
+COMPONENT_ARRAYS = ("TCRIT", "PCRIT", "VCRIT", "ZCRIT", "MW", "ACF", "OMEGAA", "OMEGAB", "SSHIFT", "VCRITVIS")
+LBC_DEFAULT = (0.1023, 0.023364, 0.058533, -0.040758, 0.0093324)   # ComponentParam::Init
+
+
+def _stod(tok: str) -> float:
+    """The leading number of a token, as std::stod reads it."""
+    import re
+    m = re.match(r"\s*[+-]?(\d+\.?\d*([eEdD][+-]?\d+)?|\.\d+([eEdD][+-]?\d+)?)", tok)
+    if not m:
+        raise ValueError(f"not a number: {tok!r}")
+    return float(m.group(0).replace("d", "e").replace("D", "e"))
+
+
+def read_props(path: str, p: dict | None = None, workdir: str | None = None) -> dict:
+    """The keywords of a deck that the device's Model needs, read as the
+    reference's ParamRead::ReadFile dispatches them
+    (src/ParamRead.cpp:60-360): units, the model (BLACKOIL / COMPS), the
+    tables (ParamReservoir::InputTABLE), ROCK, DENSITY / GRAVITY, and the
+    component data (ComponentParam: TCRIT ... VCRITVIS, LBCCOEF, BIC and the
+    flash controls SSMSTA NRSTA SSMSP NRSP RR).  One PVT / saturation region."""
+    p = dict(units="FIELD", blackoil=False, ncomp=0, tables={}, rock=None, density=None, gravity=None,
+             comp={}, bic=None, lbc=list(LBC_DEFAULT), flash={}) if p is None else p
+    workdir = workdir if workdir is not None else os.path.dirname(os.path.abspath(path))
+    lines = _lines(path)
+    for toks in lines:
+        key = toks[0]
+        if key in ("FIELD", "METRIC"):
+            p["units"] = key
+        elif key in ("SPE11A", "SPE11Amg"):
+            raise ValueError(f"unit system {key} is not read")
+        elif key == "BLACKOIL":
+            p["blackoil"] = True
+        elif key in ("COMPS", "NCOMPS"):
+            p["ncomp"] = int(next(lines)[0])
+        elif key in TABLE_COLUMNS:
+            ncol, rows, regions = TABLE_COLUMNS[key], [], []
+            for t in lines:
+                if t[0] == "/":
+                    break
+                rows.append([_stod(t[i]) for i in range(ncol)])
+                if t[-1] == "/":
+                    regions.append(rows)
+                    rows = []
+            if rows:
+                regions.append(rows)
+            if len(regions) != 1:
+                raise ValueError(f"{key}: {len(regions)} regions; one region is read")
+            p["tables"][key] = np.array(regions[0], np.float64)
+        elif key == "ROCK":
+            for t in lines:
+                if t[0] == "/":
+                    break
+                if p["rock"] is not None:
+                    raise ValueError("ROCK: more than one rock region")
+                kind = t[0]
+                if kind not in ("LINEAR01", "LINEAR02"):
+                    raise ValueError(f"ROCK {kind}: only the linear rock models are read")
+                cp1 = _stod(t[2])
+                cp2 = 0.0
+                if kind == "LINEAR02":
+                    cp2 = _stod(t[3]) if len(t) > 3 and t[3] != "/" else cp1
+                p["rock"] = (_stod(t[1]), cp1, cp2)
+        elif key in ("DENSITY", "GRAVITY"):
+            t = next(lines)
+            if key == "GRAVITY":
+                p["gravity"] = [45.5, 1.0, 0.7773]          # ParamReservoir::Init, active once the keyword appears
+            if t[0] == "/":
+                continue
+            v = _defaults(t)
+            v = v[:-1] if v[-1] == "/" else v
+            if len(v) != 3:
+                raise ValueError(f"{key} takes three values")
+            if key == "GRAVITY":
+                p["gravity"] = [p["gravity"][i] if v[i] == "DEFAULT" else _stod(v[i]) for i in range(3)]
+            elif any(x != "DEFAULT" for x in v):
+                base = p["density"] or [37.457, 62.366416, 0.062428]
+                p["density"] = [base[i] if v[i] == "DEFAULT" else _stod(v[i]) for i in range(3)]
+        elif key in COMPONENT_ARRAYS:
+            vals = []
+            for t in lines:
+                if t[0] == "/":
+                    break
+                vals += [_stod(x) for x in t if x != "/"]
+                if t[-1] == "/":
+                    break
+            n = p["ncomp"]
+            if n <= 0:
+                raise ValueError(f"{key} before the number of components")
+            p["comp"][key] = np.array((vals + [0.0] * n)[:n], np.float64)
+        elif key == "LBCCOEF":
+            v = _defaults(next(lines))
+            for i in range(5):
+                if i < len(v) and v[i] not in ("DEFAULT", "/"):
+                    p["lbc"][i] = _stod(v[i])
+        elif key == "BIC":
+            vals = []
+            for t in lines:
+                if t[0] == "/":
+                    break
+                vals += [_stod(x) for x in t if x != "/"]
+                if t[-1] == "/":
+                    break
+            p["bic"] = np.array(vals, np.float64)
+        elif key in ("SSMSTA", "NRSTA", "SSMSP", "NRSP", "RR"):
+            p["flash"][key] = next(lines)
+        elif key == "INCLUDE":
+            name = next(lines)[0]
+            if name.endswith("/"):
+                raise ValueError(f"INCLUDE {name!r}: a '/' ends the line, so the file name cannot hold one")
+            read_props(os.path.join(workdir, name), p, workdir)
+    return p
+
+
+def model_from_props(p: dict):
+    """The device's Model as the reference sets it up from the read keywords
+    (OCPMixtureMethodComp01 with EoS_PR, OCPPhaseEquilibrium::Setup and
+    ViscosityMethod03, src/OCPMixtureMethodComp.cpp:650-668,
+    src/OCPEoS.cpp:19-66, src/OCPPhaseEquilibrium.cpp:15-69,
+    src/OCPFuncPVT.cpp:414-446; or the black-oil OGW01 mixture,
+    src/OCPMixtureMethodK.cpp:418-436), in the arrays of a model dump."""
+    from .fim import Model
+    u = UNITS[p["units"]]
+    R = u["GAS_CONSTANT"]
+    a = {k: np.array([v]) for k, v in u.items() if k not in ("RHOW_STD", "RHOAIR_STD")}
+    T = p["tables"]
+    for name in ("SWOF", "SGOF", "PVTW"):
+        if name not in T:
+            raise ValueError(f"{name} is not given")
+        a[name] = T[name].T.ravel().copy()
+        a[name + "_nrow"] = np.array([T[name].shape[0]])
+    pref, cp1, cp2 = p["rock"] if p["rock"] is not None else (14.7, 3.406e-6, 0.0)
+    a.update(rock_Pref=np.array([pref]), rock_cp1=np.array([cp1]), rock_cp2=np.array([cp2]))
+    if p["blackoil"]:
+        for name in ("PVCO", "PVDG"):
+            if name not in T:
+                raise ValueError(f"{name} is not given (only the live-oil OGW black-oil model is read)")
+            a[name] = T[name].T.ravel().copy()
+            a[name + "_nrow"] = np.array([T[name].shape[0]])
+        if p["density"] is not None:
+            ro, rw, rg = p["density"]
+        else:
+            g = p["gravity"] or [45.5, 1.0, 0.7773]
+            ro = (141.5 * u["RHOW_STD"]) / (g[0] + 131.5)
+            rw = u["RHOW_STD"] * g[1]
+            rg = u["RHOAIR_STD"] * g[2]
+        a.update(mixture_comp=np.array([0]), nc=np.array([3]), stdRhoO=np.array([ro]), stdRhoG=np.array([rg]),
+                 stdRhoW=np.array([rw]), stdVo=np.array([1.0]), stdVg=np.array([1.0]), stdVw=np.array([1.0]))
+        return Model(a)
+    n = p["ncomp"]
+    C = p["comp"]
+    for name in ("TCRIT", "PCRIT", "MW", "ACF"):
+        if name not in C:
+            raise ValueError(f"{name} is not given")
+    Tc, Pc = C["TCRIT"], C["PCRIT"]
+    if "VCRIT" in C:
+        Vc = C["VCRIT"]
+    elif "ZCRIT" in C:
+        Vc = np.array([R * C["ZCRIT"][i] * Tc[i] / Pc[i] for i in range(n)])
+    else:
+        raise ValueError("VCRIT or ZCRIT is not given")
+    oa = C.get("OMEGAA", np.full(n, 0.457235529))
+    ob = C.get("OMEGAB", np.full(n, 0.077796074))
+    bic = np.zeros(n * n)
+    b = p["bic"] if p["bic"] is not None else np.zeros(0)
+    if b.size == n * n:
+        bic = b.copy()
+    else:
+        it = 0
+        for i in range(1, n):
+            for j in range(i):
+                bic[i * n + j] = bic[j * n + i] = b[it] if it < b.size else 0.0
+                it += 1
+    if "SSHIFT" in C:
+        vshift = np.array([C["SSHIFT"][i] * (R * ob[i] * Tc[i] / Pc[i]) for i in range(n)])
+    else:
+        vshift = np.zeros(n)
+    if "VCRITVIS" in C:
+        vcvis = C["VCRITVIS"]
+    elif "VCRIT" in C:
+        vcvis = C["VCRIT"]
+    else:
+        vcvis = np.array([10.73159 * C["ZCRIT"][i] * Tc[i] / Pc[i] for i in range(n)])
+    F = p["flash"]
+    for name in ("SSMSTA", "NRSTA", "SSMSP", "NRSP", "RR"):
+        if name not in F:
+            raise ValueError(f"flash control {name} is not given")
+    ssm = F["SSMSTA"]
+    flash = [int(ssm[0]), _stod(ssm[1]), _stod(ssm[2]), 1e-4, 1e-6,
+             int(F["NRSTA"][0]), _stod(F["NRSTA"][1]), int(F["SSMSP"][0]), _stod(F["SSMSP"][1]),
+             int(F["NRSP"][0]), _stod(F["NRSP"][1]), int(F["RR"][0]), _stod(F["RR"][1])]
+    if p["gravity"] is not None:
+        rhow = u["RHOW_STD"] * p["gravity"][1]
+    if p["density"] is not None:
+        rhow = u["RHOW_STD"]          # the reference's choice whenever DENSITY is given
+    if p["gravity"] is None and p["density"] is None:
+        raise ValueError("DENSITY or GRAVITY is not given")
+    a.update(mixture_comp=np.array([1]), nc=np.array([n + 1]), NC=np.array([n]), Tc=Tc.copy(), Pc=Pc.copy(),
+             Vc=np.asarray(Vc, np.float64), MWC=C["MW"].copy(), acf=C["ACF"].copy(), OmegaA=np.asarray(oa, np.float64),
+             OmegaB=np.asarray(ob, np.float64), BIC=bic, Vshift=vshift, Vcvis=np.asarray(vcvis, np.float64),
+             LBCcoef=np.array(p["lbc"]) * 10, flash_ctrl=np.array(flash, np.float64), stdRhoW=np.array([rhow]),
+             stdVw=np.array([1.0]), skipPSA=np.array([1]))
+    return Model(a)
+
+
+def read_model(path: str):
+    """The device's Model from a deck file (read_props, model_from_props)."""
+    return model_from_props(read_props(path))

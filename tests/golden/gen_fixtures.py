@@ -508,6 +508,60 @@ def deck_wells_fixture():
     return data
 
 
+def props_variant_texts():
+    """Decks for the PROPS reader that take the branches the other fixtures
+    do not: FIELD units, GRAVITY, VCRIT, OMEGAA / OMEGAB, SSHIFT, VCRITVIS,
+    LBCCOEF with defaults, a full BIC matrix, LINEAR02 rock, and a black-oil
+    deck with GRAVITY.  Returns {name: deck text}."""
+    out = {}
+    ncomp = 4
+    comp = decks.seeded_components(ncomp, 13)
+    ni, base = decks.comp_deck(4, 3, 2, ncomp, seed=13)
+    rng = np.random.default_rng(13)
+    vc = comp["Zc"] * 10.73159 * comp["Tc"] / comp["Pc"] * 0.08
+    extra = (f"VCRIT\n{decks._fmt(vc, 1)}\n/\nOMEGAA\n{decks._fmt(0.457235529 * rng.uniform(0.98, 1.02, ncomp), 1)}\n/\n"
+             f"OMEGAB\n{decks._fmt(0.077796074 * rng.uniform(0.98, 1.02, ncomp), 1)}\n/\n"
+             f"SSHIFT\n{decks._fmt(rng.uniform(-0.1, 0.1, ncomp), 1)}\n/\n"
+             f"VCRITVIS\n{decks._fmt(vc * 1.1, 1)}\n/\nLBCCOEF\n0.1025 2* -0.0408 1* /\n")
+    t = base.replace("ZCRIT", "ZCRIT_UNUSED").replace("NCOMPS", extra + "NCOMPS", 1)
+    t = t.replace("METRIC", "FIELD").replace("DENSITY\n850.0 1000.0 0.9 /", "GRAVITY\n40.0 1.02 0.75 /")
+    t = t.replace("LINEAR01 200.0 4.5E-5", "LINEAR02 3000.0 3.0E-6 1.0E-7")
+    out["comp_field_gravity"] = (t, ni)
+    full = " ".join(f"{v:.17g}" for v in comp["BIC"].ravel())
+    i = base.index("BIC")
+    j = base.index("/", i)
+    t2 = base[:i] + "BIC\n" + full + " " + base[j:]
+    out["comp_fullbic"] = (t2, ni)
+    bo = decks.blackoil_deck(seed=3)
+    bo = bo.replace("DENSITY\n850.0 1000.0 0.9 /", "GRAVITY\n35.0 1.01 0.7 /").replace("METRIC", "FIELD")
+    out["bo_field_gravity"] = (bo, None)
+    return out
+
+
+def props_fixture():
+    """The reference's model dump for each props_variant_texts deck, with the
+    deck text."""
+    data = {}
+    for name, (text, ni) in props_variant_texts().items():
+        with tempfile.TemporaryDirectory() as tmp:
+            deck = os.path.join(tmp, "props.data")
+            with open(deck, "w") as f:
+                f.write(text)
+            if ni is not None:
+                ni.astype("<f8").tofile(deck + ".ptn_ni")
+            out = os.path.join(tmp, "out")
+            r = subprocess.run([DUMP, "fim", deck, out, "0"], stdout=subprocess.DEVNULL, stderr=subprocess.PIPE,
+                               text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"{name}: the reference refused the deck: {r.stderr[-400:]}")
+            for k, v in load_dir(os.path.join(out, "model")).items():
+                if not k.startswith("conn_") and k not in ("v", "depth", "poroInit", "ntg", "rockKx", "rockKy",
+                                                            "rockKz", "dx", "dy", "dz"):
+                    data[f"{name}/{k}"] = v
+        data[f"{name}/deck"] = np.array(text)
+    return data
+
+
 FIXTURES = {
     "bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12),
     "comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4),
@@ -523,6 +577,7 @@ FIXTURES = {
     "deck_corner_multz": lambda: deck_grid_fixture("corner_multz"),
     "grid_corpus": grid_corpus,
     "deck_wells": deck_wells_fixture,
+    "props_variants": props_fixture,
     "wells_bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12, packer=pack_wells),
     "wells_comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4, packer=pack_wells),
 }

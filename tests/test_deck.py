@@ -241,3 +241,85 @@ COMPDAT
     with pytest.raises(ValueError, match="direction"):
         D.read_wells(_write(tmp_path, "WELSPECS\n'C' 'G' 1 1 1* 'OIL' /\n/\nCOMPDAT\n'C' 2* 1 1 1* 0.2 2* 'q' /\n/\n",
                             "bad.data"))
+
+
+def _decks_module():
+    import importlib.util
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "decks.py")
+    spec = importlib.util.spec_from_file_location("golden_decks", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+# the decks the FIM fixtures were made from (tests/golden/gen_fixtures.py)
+FIXTURE_DECKS = {
+    "comp6_8x8x3": lambda d: d.comp_deck(8, 8, 3, 6, seed=2, tsteps=(0.02, 0.05, 0.1), smooth=True)[1],
+    "comp8_6x6x4": lambda d: d.comp_deck(6, 6, 4, 8, seed=4, tsteps=(0.02, 0.05, 0.1), smooth=True)[1],
+    "bo_10x10x3": lambda d: d.blackoil_deck(seed=1),
+}
+
+
+def _model_equal(model, ref):
+    for k, v in model.arrays.items():
+        assert k in ref, k
+        a, b = np.asarray(v, float).ravel(), np.asarray(ref[k], float).ravel()
+        assert a.shape == b.shape and np.array_equal(a, b), k
+
+
+@pytest.mark.parametrize("name", sorted(FIXTURE_DECKS))
+def test_model_from_deck_against_reference(name, tmp_path):
+    """The device's Model read from a deck equals the reference's model dump
+    of the same deck, every array bit for bit."""
+    text = FIXTURE_DECKS[name](_decks_module())
+    model = D.read_model(_write(tmp_path, text))
+    _model_equal(model, P.group(P.load_fixture(name), "model"))
+
+
+def test_model_variants_against_reference(tmp_path):
+    """FIELD units, GRAVITY, VCRIT, OMEGAA / OMEGAB, SSHIFT, VCRITVIS, LBCCOEF
+    with defaults, a full BIC matrix, LINEAR02 rock and a black-oil deck with
+    GRAVITY (props_variants.npz, read by the reference)."""
+    fx = P.load_fixture("props_variants")
+    names = sorted({k.split("/")[0] for k in fx})
+    assert names == ["bo_field_gravity", "comp_field_gravity", "comp_fullbic"]
+    for name in names:
+        ref = P.group(fx, name)
+        _model_equal(D.read_model(_write(tmp_path, str(ref["deck"]), name + ".data")), ref)
+
+
+def test_deck_drives_the_reference_algorithm(tmp_path):
+    """Grid and Model read from the deck of comp6_8x8x3, with the reference's
+    states of its Newton iterations: the oracle's residual and Jacobian equal
+    the reference's (rows within 1e-10), so a deck reaches the device path
+    without the reference."""
+    from oracle.pyoracle import OracleBulk
+    path = _write(tmp_path, FIXTURE_DECKS["comp6_8x8x3"](_decks_module()))
+    model = D.read_model(path)
+    grid, _ = D.grid_from_deck(D.read_grid_deck(path), float(model.arrays["CONV_DARCY"][0]))
+    fx = P.load_fixture("comp6_8x8x3")
+    ref = P.group(fx, "model")
+    assert np.array_equal(grid.conn_trans, ref["conn_trans"]) and np.array_equal(grid.v, ref["v"])
+    bs = (model.nc + 1) ** 2
+    for it in P.iterations(fx):
+        js = P.jac_state(fx, it)
+        ob = OracleBulk(model, grid)
+        ob.load(js)
+        ob.cal_res(float(js["dt"][0]))
+        assert P.res_err(ob.res, js["res_bulk"], js["rockVp"], js["Nt"], model.nc) <= P.REL_TOL
+        rp, col, val = ob.assemble(float(js["dt"][0]))
+        assert np.array_equal(rp, js["jac_rowptr"]) and np.array_equal(col, js["jac_col"])
+        v, r = val, js["jac_val"]
+        e = max(np.linalg.norm(v[rp[i] * bs:rp[i + 1] * bs] - r[rp[i] * bs:rp[i + 1] * bs]) /
+                max(np.linalg.norm(r[rp[i] * bs:rp[i + 1] * bs]), 1e-300) for i in range(grid.nb))
+        assert e <= P.REL_TOL, (it, e)
+
+
+def test_props_errors(tmp_path):
+    with pytest.raises(ValueError, match="SWOF"):
+        D.read_model(_write(tmp_path, "METRIC\nCOMPS\n2 /\n", "e1.data"))
+    with pytest.raises(ValueError, match="regions"):
+        D.read_props(_write(tmp_path, "SWOF\n0.2 0 1 0 /\n0.3 0.1 0.8 0 /\n/\n", "e2.data"))
+    with pytest.raises(ValueError, match="linear"):
+        D.read_props(_write(tmp_path, "ROCK\nEXPONENT 200 1e-5 /\n/\n", "e3.data"))

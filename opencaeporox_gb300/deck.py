@@ -1,8 +1,15 @@
-"""The GRID section of an ECL-style input deck, read as the reference reads it
-(PreParamGridWell::InputFile, src/PreParamGridWell.cpp:25-150), and the grid
-the reference builds from it (PreParamGridWell::Setup, :876-1020): the cells
-that stay active, their geometry and the connections between them, ready for
-ocpx_create.
+"""An ECL-style input deck, as far as the device path needs it, read as the
+reference reads it, and what the reference builds from it:
+
+- the GRID section (PreParamGridWell::InputFile,
+  src/PreParamGridWell.cpp:25-150) and the grid (PreParamGridWell::Setup,
+  :876-1020): the cells that stay active, their geometry and the connections
+  between them (read_grid_deck, grid_from_deck);
+- the wells' perforations and Peaceman indices from WELSPECS / COMPDAT
+  (read_wells, well_perforations);
+- the fluid, rock and tables of the device's Model (read_model).
+
+The GRID section in detail:
 
 Read as the reference reads it:
 
@@ -117,12 +124,12 @@ def _box(tokens, nx, ny, nz):
     return box
 
 
-def _box_index(box, nx, ny, tops=False):
+def _box_index(box, nx, ny, nz, tops=False):
     i0, i1, j0, j1, k0, k1 = box
     if tops:
         k0 = k1 = 0
-    if min(i0, j0, k0) < 0:
-        raise ValueError(f"box {box} out of range")
+    if min(i0, j0, k0) < 0 or i1 >= nx or j1 >= ny or k1 >= nz:
+        raise ValueError(f"box {[b + 1 for b in box]} out of range")
     k, j, i = np.meshgrid(np.arange(k0, k1 + 1), np.arange(j0, j1 + 1), np.arange(i0, i1 + 1), indexing="ij")
     return (k * nx * ny + j * nx + i).ravel()
 
@@ -156,7 +163,8 @@ def read_grid_deck(path: str, deck: GridDeck | None = None, workdir: str | None 
             dims = next(lines)
             deck.nx, deck.ny, deck.nz = (int(x) for x in dims[:3])
         elif key in REAL_ARRAYS or key in INT_ARRAYS:
-            cast = int if key in INT_ARRAYS else float
+            # integer arrays are read as numbers and truncated, as the reference stores them
+            cast = (lambda x: int(float(x))) if key in INT_ARRAYS else float
             vals = []
             for t in lines:
                 if t[0] == "/":
@@ -173,7 +181,7 @@ def read_grid_deck(path: str, deck: GridDeck | None = None, workdir: str | None 
                 if t[0] == "/":
                     break
                 name, val = t[0], float(t[1])
-                idx = _box_index(_box(t[2:], deck.nx, deck.ny, deck.nz), deck.nx, deck.ny, name == "TOPS")
+                idx = _box_index(_box(t[2:], deck.nx, deck.ny, deck.nz), deck.nx, deck.ny, deck.nz, name == "TOPS")
                 if key == "EQUALS":
                     a = target(name)
                     a[idx] = int(val) if name in INT_ARRAYS else val
@@ -192,7 +200,7 @@ def read_grid_deck(path: str, deck: GridDeck | None = None, workdir: str | None 
                     raise ValueError(f"COPY from {src}, which is not given")
                 if (src in INT_ARRAYS) != (dst in INT_ARRAYS):
                     raise ValueError(f"COPY between {src} and {dst} of different types")
-                idx = _box_index(_box(t[2:], deck.nx, deck.ny, deck.nz), deck.nx, deck.ny)
+                idx = _box_index(_box(t[2:], deck.nx, deck.ny, deck.nz), deck.nx, deck.ny, deck.nz)
                 a = A.get(dst)
                 if a is None or len(a) != len(A[src]):
                     b = np.zeros(len(A[src]), A[src].dtype)

@@ -323,3 +323,10 @@ def test_props_errors(tmp_path):
         D.read_props(_write(tmp_path, "SWOF\n0.2 0 1 0 /\n0.3 0.1 0.8 0 /\n/\n", "e2.data"))
     with pytest.raises(ValueError, match="linear"):
         D.read_props(_write(tmp_path, "ROCK\nEXPONENT 200 1e-5 /\n/\n", "e3.data"))
+
+
+def test_box_out_of_range_is_refused(tmp_path):
+    with pytest.raises(ValueError, match="out of range"):
+        D.read_grid_deck(_write(tmp_path, "DIMENS\n2 2 2 /\nEQUALS\nPORO 0.1 1 3 1 1 1 1 /\n/\n", "r.data"))
+    d = D.read_grid_deck(_write(tmp_path, "DIMENS\n2 1 1 /\nACTNUM\n1.0 0 /\n", "a.data"))
+    assert np.array_equal(d.arrays["ACTNUM"], [1, 0])

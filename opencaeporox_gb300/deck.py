@@ -51,7 +51,9 @@ import numpy as np
 from . import grid as G
 from . import wells as W
 
-REAL_ARRAYS = ("DX", "DY", "DZ", "TOPS", "COORD", "ZCORN", "NTG", "PORO", "PERMX", "PERMY", "PERMZ", "MULTZ")
+REAL_ARRAYS = ("DX", "DY", "DZ", "TOPS", "COORD", "ZCORN", "NTG", "PORO", "PERMX", "PERMY", "PERMZ", "MULTZ",
+               # the PTN start (read by the same reader in the reference)
+               "PRESSURE", "TEMPER", "PHASEP-0", "PHASEP-1", "PHASEP-2") + tuple(f"COMPM-{i}" for i in range(10))
 INT_ARRAYS = ("ACTNUM",)
 
 
@@ -63,6 +65,7 @@ class GridDeck:
     ny: int = 0
     nz: int = 0
     arrays: dict = field(default_factory=dict)
+    init: str = ""           # INITPTN0 (arrays of every cell) or INITPTN1 (of the active cells)
 
     @property
     def n(self) -> int:
@@ -162,6 +165,8 @@ def read_grid_deck(path: str, deck: GridDeck | None = None, workdir: str | None 
         if key == "DIMENS":
             dims = next(lines)
             deck.nx, deck.ny, deck.nz = (int(x) for x in dims[:3])
+        elif key in ("INITPTN0", "INITPTN1"):
+            deck.init = key
         elif key in REAL_ARRAYS or key in INT_ARRAYS:
             # integer arrays are read as numbers and truncated, as the reference stores them
             cast = (lambda x: int(float(x))) if key in INT_ARRAYS else float
@@ -397,9 +402,10 @@ def read_props(path: str, p: dict | None = None, workdir: str | None = None) -> 
     (src/ParamRead.cpp:60-360): units, the model (BLACKOIL / COMPS), the
     tables (ParamReservoir::InputTABLE), ROCK, DENSITY / GRAVITY, and the
     component data (ComponentParam: TCRIT ... VCRITVIS, LBCCOEF, BIC and the
-    flash controls SSMSTA NRSTA SSMSP NRSP RR).  One PVT / saturation region."""
+    flash controls SSMSTA NRSTA SSMSP NRSP RR), and RTEMP for a PTN start.
+    One PVT / saturation region."""
     p = dict(units="FIELD", blackoil=False, ncomp=0, tables={}, rock=None, density=None, gravity=None,
-             comp={}, bic=None, lbc=list(LBC_DEFAULT), flash={}) if p is None else p
+             comp={}, bic=None, lbc=list(LBC_DEFAULT), flash={}, rtemp=60.0) if p is None else p
     workdir = workdir if workdir is not None else os.path.dirname(os.path.abspath(path))
     lines = _lines(path)
     for toks in lines:
@@ -483,6 +489,10 @@ def read_props(path: str, p: dict | None = None, workdir: str | None = None) -> 
             p["bic"] = np.array(vals, np.float64)
         elif key in ("SSMSTA", "NRSTA", "SSMSP", "NRSP", "RR"):
             p["flash"][key] = next(lines)
+        elif key == "RTEMP":
+            t = next(lines)              # ParamReservoir::InputRTEMP; 60 when not given
+            if t[0] != "/":
+                p["rtemp"] = _stod(t[0])
         elif key == "INCLUDE":
             name = next(lines)[0]
             if name.endswith("/"):
@@ -585,3 +595,35 @@ def model_from_props(p: dict):
 def read_model(path: str):
     """The device's Model from a deck file (read_props, model_from_props)."""
     return model_from_props(read_props(path))
+
+
+# ---------------------------------------------------------- initial state ---
+def initial_state(deck: GridDeck, geo, model, rtemp: float = 60.0) -> dict:
+    """The state a PTN start gives the active cells, as
+    BulkInitializer::InitPTNi sets it (src/BulkInitializer.cpp:104-144):
+    pressure, temperature (TEMPER, else RTEMP), the moles of each component
+    from COMPM-0.. (water last) and the phase pressures from PHASEP-0..2,
+    every phase absent.  With INITPTN1 the arrays list the active cells only
+    (InitialReservoir::PostProcess).  The dict is ready for
+    FimContext.load_state."""
+    if deck.init not in ("INITPTN0", "INITPTN1"):
+        raise ValueError("the deck has no PTN start (INITPTN0 or INITPTN1)")
+    A, nb, nc = deck.arrays, len(geo["act2all"]), model.nc
+    take = (lambda a: np.asarray(a, np.float64)[geo["act2all"]]) if deck.init == "INITPTN0" \
+        else (lambda a: np.asarray(a, np.float64)[:nb])
+    need = deck.n if deck.init == "INITPTN0" else nb
+
+    def arr(name):
+        a = A.get(name)
+        if a is None or len(a) < need:
+            raise ValueError(f"{name} must give {need} values")
+        return take(a)
+
+    comps = [f"COMPM-{i}" for i in range(10) if f"COMPM-{i}" in A]
+    if len(comps) != nc:
+        raise ValueError(f"{len(comps)} COMPM arrays for {nc} components")
+    P = arr("PRESSURE")
+    T = arr("TEMPER") if "TEMPER" in A else np.full(nb, float(rtemp))
+    Ni = np.stack([arr(f"COMPM-{i}") for i in range(nc)], axis=1).ravel()
+    Pj = np.stack([arr(f"PHASEP-{j}") for j in range(3)], axis=1).ravel()
+    return dict(P=P, T=T, Ni=Ni, Pj=Pj, phaseExist=np.zeros(nb * 3, np.uint8))

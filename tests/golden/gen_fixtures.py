@@ -562,6 +562,41 @@ def props_fixture():
     return data
 
 
+def deck_ptn_fixture(kind="INITPTN0"):
+    """The reference's state after a PTN start whose arrays are all in the
+    deck (three hydrocarbon components and water, so every COMPM array fits
+    the reference's limit of 30 per-cell arrays; no side file): PRESSURE,
+    TEMPER, PHASEP-0..2 and COMPM-0..3 per cell, on the block-centred grid
+    with inactive cells of deck_ortho_actnum.  The model's initial dump."""
+    nx, ny, nz, grid_text, include = grid_deck_texts("ortho_actnum")
+    n = nx * ny * nz
+    ni, text = decks.comp_deck(nx, ny, nz, 3, 21, grid_text=grid_text)
+    rng = np.random.default_rng(77)
+    p = rng.uniform(100.0, 300.0, n)
+    t = 70.0 + rng.uniform(-2.0, 2.0, n)
+    i = text.index("INITPTN0")
+    j = text.index("PROPS")
+    init = ["INITPTN0", "PRESSURE", decks._fmt(p), "/", "TEMPER", decks._fmt(t), "/"]
+    for k in range(3):
+        init += [f"PHASEP-{k}", decks._fmt(p + k), "/"]
+    for c in range(ni.shape[1]):
+        init += [f"COMPM-{c}", decks._fmt(ni[:, c]), "/"]
+    text = text[:i] + "\n".join(init) + "\n\n" + text[j:]
+    with tempfile.TemporaryDirectory() as tmp:
+        deck = os.path.join(tmp, "grid.data")
+        with open(deck, "w") as f:
+            f.write(text)
+        with open(os.path.join(tmp, "grid_poro.inc"), "w") as f:
+            f.write(include)
+        out = os.path.join(tmp, "out")
+        subprocess.run([DUMP, "fim", deck, out, "0"], check=True, stdout=subprocess.DEVNULL)
+        data = {f"init/{k}": v for k, v in load_dir(os.path.join(out, "init"), {"P", "T", "Ni", "Pj"}).items()}
+        data["model/nb"] = np.load(os.path.join(out, "model", "nb.npy"))
+    data["deck/main"] = np.array(text)
+    data["deck/include"] = np.array(include)
+    return data
+
+
 FIXTURES = {
     "bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12),
     "comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4),
@@ -578,6 +613,7 @@ FIXTURES = {
     "grid_corpus": grid_corpus,
     "deck_wells": deck_wells_fixture,
     "props_variants": props_fixture,
+    "deck_ptn": deck_ptn_fixture,
     "wells_bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12, packer=pack_wells),
     "wells_comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4, packer=pack_wells),
 }

@@ -330,3 +330,23 @@ def test_box_out_of_range_is_refused(tmp_path):
         D.read_grid_deck(_write(tmp_path, "DIMENS\n2 2 2 /\nEQUALS\nPORO 0.1 1 3 1 1 1 1 /\n/\n", "r.data"))
     d = D.read_grid_deck(_write(tmp_path, "DIMENS\n2 1 1 /\nACTNUM\n1.0 0 /\n", "a.data"))
     assert np.array_equal(d.arrays["ACTNUM"], [1, 0])
+
+
+def test_initial_state_against_reference(tmp_path):
+    """A PTN start with every array in the deck (PRESSURE, TEMPER, PHASEP,
+    COMPM-0..3) on a grid with inactive cells (deck_ptn.npz): pressure,
+    temperature and moles of the active cells equal the reference's initial
+    state.  (The reference's initial flash and CalKrPc then set Pj from the
+    capillary pressures, as the device's property update does, so the
+    dumped Pj is not the deck's.)"""
+    fx = P.load_fixture("deck_ptn")
+    deck = _read(fx, tmp_path)
+    props = D.read_props(str(tmp_path / "grid.data"))
+    model = D.model_from_props(props)
+    grid, geo = D.grid_from_deck(deck, float(model.arrays["CONV_DARCY"][0]))
+    assert grid.nb == int(fx["model/nb"].ravel()[0]) < deck.n
+    st = D.initial_state(deck, geo, model, props["rtemp"])
+    for k in ("P", "T", "Ni"):
+        assert np.array_equal(st[k], np.asarray(fx["init/" + k]).ravel()), k
+    assert np.array_equal(st["Pj"].reshape(-1, 3)[:, 1], np.asarray(deck.arrays["PHASEP-1"])[geo["act2all"]])
+    assert not st["phaseExist"].any()

@@ -597,6 +597,17 @@ def deck_ptn_fixture(kind="INITPTN0"):
     return data
 
 
+def field_fim_fixture():
+    """Newton iterations of the reference on a compositional deck in FIELD
+    units with GRAVITY (the other FIM fixtures are METRIC with DENSITY): the
+    unit constants (CONV1, the gas constant, the gravity factor, the Darcy
+    factor) and the standard water density from GRAVITY enter every
+    property, residual and Jacobian."""
+    ni, text = decks.comp_deck(6, 5, 3, 4, seed=9, tsteps=(0.02, 0.05, 0.1), smooth=True)
+    text = text.replace("METRIC", "FIELD").replace("DENSITY\n850.0 1000.0 0.9 /", "GRAVITY\n40.0 1.02 0.75 /")
+    return run_fim(text, "field", 3, ni=ni, calibrate=True)
+
+
 FIXTURES = {
     "bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12),
     "comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4),
@@ -614,6 +625,9 @@ FIXTURES = {
     "deck_wells": deck_wells_fixture,
     "props_variants": props_fixture,
     "deck_ptn": deck_ptn_fixture,
+    "comp4_field_6x5x3": field_fim_fixture,
+    "bo_field_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1).replace("METRIC", "FIELD").replace(
+        "DENSITY\n850.0 1000.0 0.9 /", "GRAVITY\n35.0 1.01 0.7 /"), "bof", 6),
     "wells_bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12, packer=pack_wells),
     "wells_comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4, packer=pack_wells),
 }

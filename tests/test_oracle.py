@@ -12,7 +12,8 @@ import parity as P
 from opencaeporox_gb300 import fim
 from oracle.pyoracle import OracleBulk
 
-FIXTURES = ["bo_10x10x3", "comp6_8x8x3", "comp8_6x6x4", "fault_comp3_8x6x5"]
+FIXTURES = ["bo_10x10x3", "comp6_8x8x3", "comp8_6x6x4", "fault_comp3_8x6x5", "comp4_field_6x5x3",
+            "bo_field_10x10x3"]
 
 
 def _split_newton_count_is_rounding_decided(model, grid, fx, it, cell, seeds=6):

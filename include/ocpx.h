@@ -26,7 +26,8 @@
  *                           the wells' bhp too when they are on the device
  *   ocpx_update_last_step   IsoT_FIM::UpdateLastTimeStep, bulk part (:1473-1517)
  *   ocpx_linsolve           the linear solve of the Newton system (the wells' rows
- *                           included when they are on the device)
+ *                           included when they are on the device); ocpx_linsolve_async
+ *                           enqueues it without waiting (capturable in a CUDA graph)
  *   ocpx_set_wells          the Peaceman wells of the deck, kept on the device
  *   ocpx_nr_*, ocpx_step_max_change, ocpx_next_time_step
  *                           Newton and time-step control (OCPNRsuite,

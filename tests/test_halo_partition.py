@@ -101,3 +101,55 @@ def test_partition_refuses_bad_owner_maps():
         halo.partition(grid, np.zeros(grid.nb - 1, int), 2)
     with pytest.raises(ValueError, match="owns no cell"):
         halo.partition(grid, np.zeros(grid.nb, int), 2)
+
+
+def _faulted_grid():
+    nx, ny, nz = 8, 6, 5
+    faults = [("x", 3, -4.5, 7.5, 1.5), ("y", 2, 1.2, -2.0, 0.6), ("x", 5, 6.0, 6.0, 0.7)]
+    coord, zcorn = synthetic.faulted_corner_point(nx, ny, nz, 20.0, 3.0, 2000.0, 4.0, -3.0, faults, 0.05, seed=11)
+    return G.corner_point_grid(nx, ny, nz, coord, zcorn, 100.0, 100.0, 10.0, 0.2), (nx, ny, nz)
+
+
+def _rank_exchange(rank, world, port, q):
+    import os
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    import torch.distributed as dist
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        grid, dims = _faulted_grid()
+        sub = halo.zslab_partition(grid, *dims, world)[rank]
+        vals = np.arange(grid.nb * 3, dtype=np.float64).reshape(grid.nb, 3)
+        local = np.where(np.arange(sub.grid.nb)[:, None] < sub.n_owned, vals[sub.cells], -1.0)
+        got = halo.HaloExchange(sub).exchange(local, 3)
+        norms = halo.HaloExchange(sub).max_norms((float(rank), -float(rank)))
+        q.put((rank, bool(np.array_equal(got, vals[sub.cells])), sorted(sub.recv), norms))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_rank_exchange_on_the_faulted_grid():
+    """Three gloo ranks exchange a cell array over the faulted grid's
+    partition, whose ghost sets are irregular (NNC ghosts two layers away):
+    every ghost receives its owner's value, and the norms reduce to the
+    maximum over the ranks."""
+    import socket
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    world = 3
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_rank_exchange, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    got = sorted(q.get(timeout=300) for _ in range(world))
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    for rank, ok, peers, norms in got:
+        assert ok, rank
+        assert norms == (2.0, 0.0)
+    assert got[1][2] == [0, 2]

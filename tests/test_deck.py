@@ -350,3 +350,44 @@ def test_initial_state_against_reference(tmp_path):
         assert np.array_equal(st[k], np.asarray(fx["init/" + k]).ravel()), k
     assert np.array_equal(st["Pj"].reshape(-1, 3)[:, 1], np.asarray(deck.arrays["PHASEP-1"])[geo["act2all"]])
     assert not st["phaseExist"].any()
+
+
+def test_ptn1_arrays_list_the_active_cells(tmp_path):
+    """With INITPTN1 the PTN arrays give the active cells only, in order
+    (InitialReservoir::PostProcess); with INITPTN0 every cell."""
+    base = """DIMENS
+3 1 1 /
+DX
+3*10 /
+DY
+3*10 /
+DZ
+3*2 /
+TOPS
+3*1000 /
+PORO
+0.2 0.2 0.2 /
+PERMX
+3*100 /
+PERMY
+3*100 /
+PERMZ
+3*10 /
+ACTNUM
+1 0 1 /
+"""
+    from opencaeporox_gb300 import synthetic
+    model = synthetic.comp_model(2, 3)          # three components with water
+    ptn1 = base + "INITPTN1\nPRESSURE\n100 300 /\nPHASEP-0\n100 300 /\nPHASEP-1\n100 300 /\nPHASEP-2\n100 300 /\n" \
+                  "COMPM-0\n1 2 /\nCOMPM-1\n3 4 /\nCOMPM-2\n5 6 /\n"
+    deck = D.read_grid_deck(_write(tmp_path, ptn1, "p1.data"))
+    grid, geo = D.grid_from_deck(deck)
+    st = D.initial_state(deck, geo, model, rtemp=70.0)
+    assert grid.nb == 2 and np.array_equal(st["P"], [100.0, 300.0]) and np.array_equal(st["T"], [70.0, 70.0])
+    assert np.array_equal(st["Ni"], [1.0, 3.0, 5.0, 2.0, 4.0, 6.0])
+    ptn0 = ptn1.replace("INITPTN1", "INITPTN0").replace("100 300 /", "100 200 300 /").replace(
+        "1 2 /", "1 9 2 /").replace("3 4 /", "3 9 4 /").replace("5 6 /", "5 9 6 /")
+    deck0 = D.read_grid_deck(_write(tmp_path, ptn0, "p0.data"))
+    st0 = D.initial_state(deck0, D.grid_from_deck(deck0)[1], model, rtemp=70.0)
+    for k in ("P", "T", "Ni", "Pj"):
+        assert np.array_equal(st0[k], st[k]), k

@@ -608,6 +608,31 @@ def field_fim_fixture():
     return run_fim(text, "field", 3, ni=ni, calibrate=True)
 
 
+def fim_corpus(ncase=6):
+    """Two Newton iterations of the reference on each of `ncase` seeded small
+    decks: the grids of corpus_case (faulted corner-point or block-centred,
+    inactive cells, NTG, MULTZ) with 3 to 5 components and the two wells of
+    the compositional deck.  Packed per case under case<NNN>/."""
+    data = {}
+    for seed in range(ncase):
+        nx, ny, nz, grid_text = corpus_case(seed)
+        ncomp = 3 + seed % 3
+        ni, text = decks.comp_deck(nx, ny, nz, ncomp, seed=50 + seed, grid_text=grid_text,
+                                   tsteps=(0.02, 0.05), smooth=True)
+        # the harness reads the side file's moles per active cell
+        sys.path.insert(0, REPO)
+        from opencaeporox_gb300 import deck as D
+        with tempfile.TemporaryDirectory() as tmp:
+            g = os.path.join(tmp, "g.data")
+            with open(g, "w") as f:
+                f.write(grid_text)
+            _, geo = D.grid_from_deck(D.read_grid_deck(g))
+        d = run_fim(text, f"corpus{seed}", 2, ni=ni[geo["act2all"]], calibrate=True)
+        for k, v in d.items():
+            data[f"case{seed:03d}/{k}"] = v
+    return data
+
+
 FIXTURES = {
     "bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12),
     "comp6_8x8x3": lambda: _comp_fim(8, 8, 3, 6, 2, "c6", 4),
@@ -626,6 +651,7 @@ FIXTURES = {
     "props_variants": props_fixture,
     "deck_ptn": deck_ptn_fixture,
     "comp4_field_6x5x3": field_fim_fixture,
+    "fim_corpus": fim_corpus,
     "bo_field_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1).replace("METRIC", "FIELD").replace(
         "DENSITY\n850.0 1000.0 0.9 /", "GRAVITY\n35.0 1.01 0.7 /"), "bof", 6),
     "wells_bo_10x10x3": lambda: run_fim(decks.blackoil_deck(seed=1), "bo", 12, packer=pack_wells),
